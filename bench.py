@@ -1,0 +1,328 @@
+"""Throughput benchmark of the GPU particle step (particle-steps/s).
+
+Workload (default): LSM1 2D with k-epsilon diffusivity-gradient drift at
+scale -- 4 km x 1 km jittered mesh (1001x251 vertices, 500,000 triangles),
+node fields interpolated in time between records 600 s apart, 1e7 particles
+uniform in the domain, dt = 0.5 s.  One step = one Solver.forward over all
+particles (time interpolation of the fields + the fused particle kernel).
+Inputs are synthetic (cylag_gb300.synth, seeded); the particle state
+(~360 MB) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # the CPU implementation, host cores
+
+Prints one JSON line (rank 0).  Under torchrun each rank advances its own
+1e7-particle shard (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s on 1 GB300 (mixed vs plain FP64); p50/p99 request latency"
+UNIT = "particle-steps/s"
+WORKLOAD = "lsm1_2d_keps_drift_500k_tri_1e7_particles"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--npart", type=int, default=10_000_000)
+    ap.add_argument("--nx", type=int, default=1001)
+    ap.add_argument("--ny", type=int, default=251)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(args, rank=0):
+    from cylag_gb300 import synth
+    c = synth.keps_drift_channel(npart=args.npart, nx=args.nx, ny=args.ny, seed=0)
+    if rank:
+        rng = np.random.default_rng(1000 + rank)
+        c["position"] = np.stack([rng.uniform(0, 4000.0, args.npart),
+                                  rng.uniform(0, 1000.0, args.npart)], 1)
+    return c
+
+
+def bytes_per_particle_step(precision):
+    """Algorithmic (compulsory) DRAM bytes per particle-step of the fused
+    step: position r+w 32, tri r+w 8, PCG32 state r+w 16, tag r 4."""
+    return 32 + 8 + 16 + 4
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU implementation (oracle port, all host threads) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_rate(c, params, nsample, nsteps, threads):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from cylag_gb300.mesh import TriangularMesh
+    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+    fields = dict(dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
+                  velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
+                  opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
+    o = oracle.OracleSolver(mesh, fields, params, c["position"][:nsample], nthreads=threads)
+    o.forward()  # warm
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        o.forward()
+    dt = time.perf_counter() - t0
+    return nsample * nsteps / dt, dt
+
+
+def run_reference_arm(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        print(json.dumps({"impl": "reference", "rank": rank, "skipped": True}), file=sys.stderr)
+        return
+    c = make_workload(args)
+    params = dict(c["parameters"])
+    threads = os.cpu_count() or 1
+    nsample = int(os.environ.get("CYLAG_REF_SAMPLE", "200000"))
+    rates = []
+    for _ in range(args.warmup):
+        cpu_rate(c, params, nsample, 1, threads)
+    t_all = 0.
+    for _ in range(args.steps):
+        r, dt = cpu_rate(c, params, nsample, 1, threads)
+        rates.append(r)
+        t_all += dt
+    value = float(nsample * args.steps / t_all)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_particles": nsample,
+                   "note": "each step advances a bounded sample of the particles on all host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{nsample} particles of the workload, 1 step per timed step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args):
+    import torch
+    import cylag_gb300 as cg
+    from cylag_gb300 import _lib
+    rank, world, local = dist_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    c = make_workload(args, rank)
+    params = dict(c["parameters"])
+    total_steps = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
+    if total_steps * params["time_step"] > 1200.0:
+        raise SystemExit("warmup + 2*steps must stay within the 1,200 s field records")
+    from cylag_gb300.mesh import TriangularMesh
+    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+    fs = cg.EulerianFieldSet(mesh, dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
+                             velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
+                             opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
+    ps = cg.LagrangianParticleSet(c["position"], dim=2)
+    solver = cg.Solver(fs, ps, params, precision=args.precision, seed=rank, device=local)
+    L = solver.L
+    stream = torch.cuda.ExternalStream(L.cg_ctx_stream(solver._ctx), device=local)
+    n = ps.npart
+
+    # warm-up
+    solver.forward(nsteps=args.warmup)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    solver.forward(nsteps=args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    kern_ms, launches = solver.last_kernel_ms()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1e3)
+
+    # end to end: host state (pinned) -> device, one step through the C ABI,
+    # device -> host, every step
+    e2e = None
+    if not args.no_e2e:
+        d = ps._dev
+        keys_in = ("position", "tri", "tag", "rng_state")
+        keys_out = ("position", "tri", "rng_state")
+        host = {k: torch.empty_like(d[k], device="cpu").pin_memory() for k in keys_in}
+        for k in keys_in:
+            host[k].copy_(d[k])
+        h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
+        d2h = sum(host[k].numel() * host[k].element_size() for k in keys_out)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                for k in keys_in:
+                    d[k].copy_(host[k], non_blocking=True)
+                rc = L.cg_run_step(solver._run, 1, None)
+                _lib.check(solver._ctx, rc)
+                for k in keys_out:
+                    host[k].copy_(d[k], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ems = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ems], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": world * n * args.steps / (ems / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "wall_s": wall}
+
+    if rank != 0:
+        return
+    bpp = bytes_per_particle_step(args.precision)
+    peak, peak_kind = peaks()
+    achieved = bpp * n / (kern_ms / 1e3) / 1e9
+    traffic = os.environ.get("CYLAG_NCU_TRAFFIC_PER_LAUNCH")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles_per_gpu": n, "triangles": int(mesh.nt),
+                   "precision": args.precision, "dt": params["time_step"],
+                   "l2": "state larger than L2 (no flush)", "model": "LSM1 Euler, k-eps drift"},
+        "gpu_launches": int(launches) + args.steps,  # step kernels + field blends
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": float(traffic) if traffic else None,
+                     "peak_kind": peak_kind, "kernel_ms": kern_ms,
+                     "bytes_per_particle_step": bpp},
+        "clocks": clk,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        nsample = int(os.environ.get("CYLAG_CPU_SAMPLE", "200000"))
+        rate, dt = cpu_rate(c, params, nsample, 4, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{nsample} particles x 4 steps of the workload"}
+    print(json.dumps(line))
+    solver.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,78 @@
+"""Build libcylag_gpu.so in-tree with nvcc for sm_103a (no torch extension
+machinery, no cmake).  Translation units compile in parallel; the plain-form
+kernels use -fmad=false so that FP64 arithmetic rounds exactly like the
+reference's C.
+
+Usage: ``python -m cylag_gb300.build [--force]``
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+OUT_DIR = PKG / "_native"
+LIB = OUT_DIR / "libcylag_gpu.so"
+INCLUDE = PKG.parent / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          f"-I{INCLUDE}", f"-I{CSRC}"]
+
+# translation unit -> extra flags
+UNITS = {
+    "cg_api.cu": ["-fmad=false"],
+    "cg_kernels_plain.cu": ["-fmad=false"],
+}
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcylag_gpu.so")
+    return exe
+
+
+def _sources_newest() -> float:
+    files = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+    files += list(INCLUDE.glob("*.h")) + [Path(__file__)]
+    return max(f.stat().st_mtime for f in files)
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    if not force and LIB.exists() and LIB.stat().st_mtime >= _sources_newest():
+        return LIB
+    OUT_DIR.mkdir(exist_ok=True)
+    objs = []
+    exe = nvcc()
+
+    def one(item):
+        src, extra = item
+        obj = OUT_DIR / (Path(src).stem + ".o")
+        cmd = [exe, *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(r.stdout, r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(one, UNITS.items()))
+    tmp = LIB.with_suffix(f".so.{os.getpid()}")
+    cmd = [exe, *ARCH, "-shared", *map(str, objs), "-o", str(tmp), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(LIB)

@@ -1,0 +1,523 @@
+"""Host mirror of cylag.core: EulerianFieldSet, LagrangianParticleSet, Solver.
+
+Same constructor signatures and public attributes as the reference
+(cylag/core/eulerian_field_set.pyx:125-256,
+cylag/core/lagrangian_particle_set.pyx:158-261, cylag/core/solver.pyx:74-236),
+so that scripts written for cylag run unchanged.  The particle loop of
+``Solver.forward`` (solver.pyx:459-549) runs as one fused CUDA launch per
+step through libcylag_gpu.so; particle state lives in HBM in torch tensors
+(plumbing only) in the reference's layout (``double[npart, dim]`` rows), and
+reading a public array (``pset.position`` ...) copies it to the host.
+
+Per-particle random streams: particle with tag t draws from
+pcg32_seed(seed, t) (cylag/lsm/random_utils.pyx:30-37), so that results do
+not depend on particle order or batch composition.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time as _time
+
+import numpy as np
+
+from . import _lib
+from .mesh import TriangularMesh
+from .parameters import Parameters
+
+EPSILON = 1.0e-16
+DEFAULT_INITIAL_POOL_SIZE = 10000
+_OPT_NAMES = {
+    "turbulent_energy": ("TURBULENT ENERG.", "TURBULENT ENERGY", "ENERGIE TURBUL."),
+    "dissipation": ("DISSIPATION",),
+    "bottom": ("BOTTOM", "FOND"),
+}
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("cylag_gb300 needs a CUDA device (no CPU fallback)")
+    return torch
+
+
+class SimuTime:
+    """cylag/core/simutime.pyx:25-125 (time bookkeeping on the host)."""
+
+    def __init__(self, print_progress, initial_time=0., final_time=0., time_step=0.):
+        if final_time <= initial_time:
+            raise ValueError("final_time must be greater than initial_time")
+        if time_step <= 0.:
+            raise ValueError("time_step must be greater than 0")
+        if final_time - initial_time < time_step:
+            raise ValueError("final_time - initial_time must be greater than time_step")
+        self.time = initial_time
+        self.initial_time = initial_time
+        self.time_step = time_step
+        self.final_time = final_time
+        self.nt = int((final_time - initial_time) / time_step)
+        self.times = np.linspace(initial_time, final_time, self.nt + 1)
+        self.iteration = 0
+        self.is_finished = False
+        self.print_progress = print_progress
+
+    def increment(self):
+        self.time += self.time_step
+        self.iteration += 1
+        if self.time >= self.final_time:
+            self.is_finished = True
+
+
+class EulerianFieldSet:
+    """Mirror of cylag.EulerianFieldSet (eulerian_field_set.pyx:125-256)."""
+
+    def __init__(self, triangular_mesh, dim=2, nlayers=1, times=None, elevation=None,
+                 velocity_x=None, velocity_y=None, velocity_z=None, opt_fields=None,
+                 opt_fields_names=None, trifinder=None, friction_model=1,
+                 friction_coefficient=40.):
+        if not isinstance(triangular_mesh, TriangularMesh):
+            triangular_mesh = TriangularMesh(
+                np.asarray(triangular_mesh.x), np.asarray(triangular_mesh.y),
+                np.asarray(triangular_mesh.triangles), nopen=getattr(triangular_mesh, "nopen", 0))
+        self.triangular_mesh = triangular_mesh
+        self.npoints = triangular_mesh.nv
+        self.nlayers = int(nlayers)
+        self.dim = int(dim)
+        self.trifinder = trifinder
+        self.times = np.ascontiguousarray(times, dtype=np.float64)
+        self.ntimes = len(self.times)
+        self.record = 0
+        self.frozen_hydro = self.ntimes == 1
+        for i in range(self.ntimes - 1):
+            dt = self.times[i + 1] - self.times[i]
+            if dt <= EPSILON:
+                raise ValueError(
+                    f"Invalid times array: times must be strictly increasing. Found "
+                    f"times[{i}]={self.times[i]:.6e} and times[{i+1}]={self.times[i+1]:.6e}")
+        ref = (self.ntimes, self.npoints) if self.dim == 2 else (self.ntimes, self.npoints * self.nlayers)
+        for name, f in (("elevation", elevation), ("velocity_x", velocity_x),
+                        ("velocity_y", velocity_y)) + ((("velocity_z", velocity_z),) if self.dim == 3 else ()):
+            if np.shape(f) != ref:
+                raise ValueError(f"Field have wrong dimension, expected {ref}, found {np.shape(f)}")
+        self.elevation = np.ascontiguousarray(elevation, dtype=np.float64)
+        self.velocity_x = np.ascontiguousarray(velocity_x, dtype=np.float64)
+        self.velocity_y = np.ascontiguousarray(velocity_y, dtype=np.float64)
+        self.velocity_z = None if velocity_z is None else np.ascontiguousarray(velocity_z, dtype=np.float64)
+        if self.dim == 3:
+            self.check_regular_layers()
+        self.nopt = 0 if opt_fields is None else len(opt_fields_names)
+        self.opt_fields = None if opt_fields is None else np.ascontiguousarray(opt_fields, dtype=np.float64)
+        self.opt_fields_names = opt_fields_names
+        self.field_names = ["ELEVATION", "VELOCITY U", "VELOCITY V", "VELOCITY W"]
+        self.fid_zs, self.fid_ux, self.fid_uy, self.fid_uz = 0, 1, 2, 3
+        self.fid_turbeng = self.fid_dissip = self.fid_zb = -1
+        self._opt = {}
+        if opt_fields_names is not None:
+            names = list(opt_fields_names)
+            for key, alts in _OPT_NAMES.items():
+                for nm in alts:
+                    if nm in names:
+                        j = names.index(nm)
+                        self._opt[key] = np.ascontiguousarray(self.opt_fields[j])
+                        if key == "turbulent_energy":
+                            self.fid_turbeng = 4 + j
+                        elif key == "dissipation":
+                            self.fid_dissip = 4 + j
+                        else:
+                            self.fid_zb = 4 + j
+                        break
+        self.friction_model = friction_model
+        self.friction_coefficient = friction_coefficient
+
+    def check_regular_layers(self, rtol=1e-3):
+        """eulerian_field_set.pyx:258-294 (uniform sigma layers)."""
+        nl = self.nlayers
+        if self.dim != 3 or nl < 2:
+            return
+        frac = (np.arange(nl) / (nl - 1.))[:, None]
+        z = np.asarray(self.elevation)[0].reshape(nl, self.npoints)
+        zb = z[0]
+        hl = (z[-1] - zb) / (nl - 1.)
+        expected = zb[None, :] + frac * (z[-1] - zb)[None, :]
+        tol = rtol * np.abs(hl) + 1e-6 * (1. + np.abs(zb))
+        err = np.abs(z - expected) - tol[None, :]
+        if np.any(err > 0.):
+            raise ValueError("Vertical layers are not regularly spaced (CyLag requires uniform sigma layers)")
+
+
+class LagrangianParticleSet:
+    """Mirror of cylag.LagrangianParticleSet (lagrangian_particle_set.pyx:158-261).
+
+    Before a Solver attaches, arrays live on the host; afterwards the device
+    copy is authoritative and attribute reads return fresh host copies.
+    """
+
+    _STATE = ("position", "velocity", "fluid_velocity_seen", "last_position", "last_velocity",
+              "tri", "last_tri", "lowerlayer", "tag", "diameter")
+
+    def __init__(self, position=None, velocity=None, fluid_velocity_seen=None, dim=2,
+                 initial_pool_size=None, min_pool_size_update=1000, particle_density=1000.,
+                 particle_diameter=0.01, particle_diameter_distribution=None,
+                 drag_coefficient_model=1, drag_coefficient=0.44, added_mass_force=False,
+                 added_mass_coef=0.5, buoyancy_velocity_model=0, buoyancy_velocity=0.0,
+                 compute_depth=False, max_stranded=None):
+        if position is not None and initial_pool_size is None:
+            npart = np.shape(position)[0]
+        else:
+            npart = initial_pool_size if initial_pool_size is not None else DEFAULT_INITIAL_POOL_SIZE
+        self.npart = int(npart)
+        self.dim = int(dim)
+        self.min_pool_size_update = min_pool_size_update
+        self.rho0 = 1000.
+        self.density = particle_density
+        self.particle_diameter = particle_diameter
+        self.particle_volume = np.pi * (particle_diameter ** 3) / 6.
+        if particle_diameter_distribution is not None:
+            raise NotImplementedError(
+                "particle_diameter_distribution: draw diameters on the host and set "
+                "pset.diameter before creating the Solver")
+        self.diameter_distribution = "monodisperse"
+        self.drag_coef_model = drag_coefficient_model
+        self.drag_coef = drag_coefficient
+        self.added_mass_force = added_mass_force
+        self.added_mass_coef = added_mass_coef
+        self.buoyancy_velocity_model = buoyancy_velocity_model
+        self.buoyancy_velocity_value = buoyancy_velocity
+        self.additional_velocity = False
+        self.additional_force = False
+        self.compute_depth = compute_depth
+        if compute_depth:
+            raise NotImplementedError("compute_depth is not built in the GPU step")
+        self.max_stranded = max_stranded if max_stranded is not None else self.npart
+        self.stranded_count = 0
+        n, d = self.npart, self.dim
+        h = {}
+        h["position"] = np.zeros((n, d))
+        h["velocity"] = np.zeros((n, d))
+        h["fluid_velocity_seen"] = np.zeros((n, d))
+        inactive = np.ones(n, dtype=np.int32)
+        if position is not None:
+            pos = np.asarray(position, dtype=np.float64)
+            if pos.shape[0] > n:
+                raise ValueError("size of position > initial_pool_size")
+            if pos.shape[1] != d:
+                raise ValueError("dim of position != LagrangianParticleSet.dim")
+            h["position"][: pos.shape[0]] = pos
+            inactive[: pos.shape[0]] = 0
+            if velocity is not None:
+                vel = np.asarray(velocity, dtype=np.float64)
+                if vel.shape != pos.shape:
+                    raise ValueError("size of velocity != size of position")
+                h["velocity"][: pos.shape[0]] = vel
+            if fluid_velocity_seen is not None:
+                if velocity is None:
+                    raise ValueError("velocity must be != None")
+                fvs = np.asarray(fluid_velocity_seen, dtype=np.float64)
+                if fvs.shape != pos.shape:
+                    raise ValueError("size of fluid_velocity_seen != size of velocity")
+                h["fluid_velocity_seen"][: pos.shape[0]] = fvs
+        elif velocity is not None or fluid_velocity_seen is not None:
+            raise ValueError("position must be != None")
+        h["last_position"] = h["position"].copy()
+        h["last_velocity"] = h["velocity"].copy()
+        # -2: active, awaiting Solver.initialize_particle_state; -1: inactive
+        h["tri"] = np.where(inactive == 0, -2, -1).astype(np.int32)
+        h["last_tri"] = -np.ones(n, dtype=np.int32)
+        h["lowerlayer"] = np.zeros(n, dtype=np.int32)
+        h["tag"] = np.arange(n, dtype=np.int32)
+        h["diameter"] = np.full(n, float(particle_diameter))
+        self.maxtag = n - 1
+        self._host = h
+        self._dev = None
+        self._ctx = None
+
+    # ---- device attachment -----------------------------------------------------
+    def _attach(self, ctx, device):
+        torch = _torch()
+        dev = torch.device("cuda", device)
+        self._dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in self._host.items()}
+        self._dev["rng_state"] = torch.zeros(self.npart, dtype=torch.int64, device=dev)
+        self._host = None
+        self._ctx = ctx
+
+    def _state_desc(self):
+        d = self._dev
+        p = lambda k: d[k].data_ptr()
+        return _lib.StateDesc(self.npart, p("position"), p("velocity"), p("fluid_velocity_seen"),
+                              p("last_position"), p("last_velocity"), p("tri"), p("last_tri"),
+                              p("lowerlayer"), p("tag"), p("diameter"), p("rng_state"))
+
+    def _sync(self):
+        if self._ctx is not None:
+            _lib.check(self._ctx, _lib.load().cg_ctx_sync(self._ctx))
+
+    def _get(self, key):
+        if self._dev is None:
+            return self._host[key]
+        self._sync()
+        return self._dev[key].cpu().numpy()
+
+    def _set(self, key, value):
+        value = np.ascontiguousarray(value, dtype=np.float64 if key in
+                                     ("position", "velocity", "fluid_velocity_seen",
+                                      "last_position", "last_velocity", "diameter") else np.int32)
+        if self._dev is None:
+            self._host[key][...] = value
+        else:
+            self._sync()
+            self._dev[key].copy_(_torch().from_numpy(value))
+            _torch().cuda.synchronize()
+
+    def _retag(self):
+        """Deleted particles carry a negative marker (-1: deleted while being
+        initialized, -2-it: deleted during iteration it); give them
+        maxtag+1, maxtag+2, ... in deletion order then index order, as
+        delete_single does (lagrangian_particle_set.pyx:786-788)."""
+        if self._dev is None:
+            return
+        self._sync()
+        tag = self._dev["tag"]
+        neg = (tag < 0).nonzero().flatten()
+        if neg.numel() == 0:
+            return
+        idx = neg.cpu().numpy()
+        mark = tag[neg].cpu().numpy()
+        order = np.lexsort((idx, -mark))
+        new = np.empty(len(idx), dtype=np.int32)
+        new[order] = self.maxtag + 1 + np.arange(len(idx), dtype=np.int32)
+        self.maxtag += len(idx)
+        torch = _torch()
+        tag[neg] = torch.from_numpy(new).to(tag.device)
+        torch.cuda.synchronize()
+
+    # ---- public arrays --------------------------------------------------------
+    position = property(lambda s: s._get("position"), lambda s, v: s._set("position", v))
+    velocity = property(lambda s: s._get("velocity"), lambda s, v: s._set("velocity", v))
+    fluid_velocity_seen = property(lambda s: s._get("fluid_velocity_seen"),
+                                   lambda s, v: s._set("fluid_velocity_seen", v))
+    last_position = property(lambda s: s._get("last_position"))
+    last_velocity = property(lambda s: s._get("last_velocity"))
+    tri = property(lambda s: s._get("tri"))
+    last_tri = property(lambda s: s._get("last_tri"))
+    lowerlayer = property(lambda s: s._get("lowerlayer"))
+    diameter = property(lambda s: s._get("diameter"), lambda s, v: s._set("diameter", v))
+
+    @property
+    def volume(self):
+        d = self.diameter
+        return np.pi * (d ** 3) / 6.
+
+    @property
+    def tag(self):
+        self._retag()
+        return self._get("tag")
+
+    @property
+    def inactive(self):
+        return (self._get("tri") == -1).astype(np.int32)
+
+    @property
+    def npart_active(self):
+        return int((self._get("tri") != -1).sum())
+
+    def get_state(self):
+        """lagrangian_particle_set.pyx:398-423: sorts active particles first,
+        returns their position, velocity, fluid velocity seen."""
+        self._sort_active_particles()
+        na = self.npart_active
+        return self.position[:na], self.velocity[:na], self.fluid_velocity_seen[:na]
+
+    def get_particle_properties(self):
+        self._sort_active_particles()
+        na = self.npart_active
+        d = self.diameter[:na]
+        return d, np.pi * (d ** 3) / 6.
+
+    def _sort_active_particles(self):
+        """lagrangian_particle_set.pyx:584-618 (same np.argsort permutation)."""
+        self._retag()
+        idx = np.argsort(self.inactive)
+        if np.array_equal(idx, np.arange(self.npart)):
+            return
+        if self._dev is None:
+            for k in self._host:
+                self._host[k] = self._host[k][idx]
+            return
+        torch = _torch()
+        self._sync()
+        ti = torch.from_numpy(idx).to(self._dev["tri"].device)
+        for k in self._dev:  # in place: the run keeps pointing at these buffers
+            self._dev[k].copy_(self._dev[k].index_select(0, ti))
+        torch.cuda.synchronize()
+
+    def delete_single(self, i):
+        """lagrangian_particle_set.pyx:754-788"""
+        if self._get("tri")[i] == -1:
+            return
+        for k in ("position", "velocity", "fluid_velocity_seen", "last_position", "last_velocity"):
+            a = self._get(k)
+            a[i] = 0.
+            self._set(k, a)
+        for k, v in (("tri", -1), ("last_tri", -1), ("lowerlayer", 0)):
+            a = self._get(k)
+            a[i] = v
+            self._set(k, a)
+        d = self._get("diameter")
+        d[i] = 0.
+        self._set("diameter", d)
+        t = self._get("tag")
+        self.maxtag += 1
+        t[i] = self.maxtag
+        self._set("tag", t)
+
+
+class Solver:
+    """Mirror of cylag.Solver (solver.pyx:42-236) running the GPU step.
+
+    Extra keyword arguments (not in the reference): ``precision``
+    ('fp64' plain form or 'mixed'), ``seed`` (PCG32 seed of every particle
+    stream), ``device`` (CUDA ordinal), ``hbm_budget`` (bytes, 0 = none).
+    """
+
+    def __init__(self, field_set, particle_set, parameters={}, sources=None,
+                 control_sections=None, precision="fp64", seed=0, device=0, hbm_budget=0):
+        self.parameters = Parameters(parameters)
+        self.parameters.check_values()
+        P = self.parameters
+        self.simutime = SimuTime(P.listing, P.initial_time, P.final_time, P.time_step)
+        if sources:
+            raise NotImplementedError("particle sources are not built in the GPU step")
+        if control_sections:
+            raise NotImplementedError("control sections are not built in the GPU step")
+        self.sources = sources
+        self.control_sections = control_sections
+        self.particle_set = particle_set
+        self.field_set = field_set
+        fs, ps = field_set, particle_set
+        if fs.dim != ps.dim:
+            if fs.dim == 2 and ps.dim == 3:
+                raise NotImplementedError("pseudo-3D (2D fields, 3D particles) is not built in the GPU step")
+            raise ValueError(f"EulerianFieldSet dimension ({fs.dim}) does not match "
+                             f"LagrangianParticleSet set dimension ({ps.dim})")
+        if P.frozen_eulerian_fields != 1 and P.final_time > fs.times[-1]:
+            raise ValueError("final_time > EulerianFieldSet maximum time")
+        fs.frozen_hydro = bool(P.frozen_eulerian_fields)
+        if fs.ntimes == 1 and not fs.frozen_hydro:
+            raise ValueError("EulerianFieldSet has only one time step, use frozen_eulerian_fields=True")
+        if P.diffusion_model in (2, 3) and (fs.fid_turbeng == -1 or fs.fid_dissip == -1):
+            raise ValueError(f"LSM: diffusion_model={P.diffusion_model} requires 'TURBULENT ENERG.' "
+                             "and 'DISSIPATION' fields in EulerianFieldSet")
+        prec = {"fp64": _lib.CG_PRECISION_FP64, "plain": _lib.CG_PRECISION_FP64,
+                "mixed": _lib.CG_PRECISION_MIXED}.get(precision)
+        if prec is None:
+            raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
+        ps.rho0 = P.water_density
+        self.L = _lib.load()
+        self.device = device
+        self.seed = int(seed)
+        self._ctx = C.c_void_p()
+        _lib.check(None, self.L.cg_ctx_create(device, int(hbm_budget), C.byref(self._ctx)))
+        self._upload_mesh_fields()
+        ps._attach(self._ctx, device)
+        ps._solver = self
+        self._prm = _lib.Params(
+            P.model, P.time_scheme, P.rng_method, P.diffusion_model, P.diffusion_lsm2_option,
+            P.lsm3_edge_opt, int(bool(P.boundary_conditions)), P.boundary_conditions_type,
+            P.max_wall_rebounds, int(bool(P.bnd_statistics)), P.particle_velocity_init,
+            int(bool(P.frozen_eulerian_fields)), P.initial_time, P.final_time, P.time_step,
+            P.horizontal_diffusivity, P.vertical_diffusivity, P.schmidt_number,
+            P.diffusion_lsm3_tl_horizontal, P.diffusion_lsm3_tl_vertical,
+            P.rebound_damping_coef, P.wall_roughness_angle, P.stranding_probability,
+            P.water_density, ps.dim, ps.density, ps.drag_coef_model, ps.drag_coef,
+            int(bool(ps.added_mass_force)), ps.added_mass_coef, ps.buoyancy_velocity_model,
+            ps.buoyancy_velocity_value, prec, self.seed)
+        self._run = C.c_void_p()
+        self._create_run()
+        _lib.check(self._ctx, self.L.cg_run_seed(self._run))
+        self.initialize_particle_state()
+        nopen = fs.triangular_mesh.nopen
+        self._bnd_stats_times = []
+        self._bnd_stats_data = []
+        self.nopen = nopen
+
+    def _upload_mesh_fields(self):
+        m = self.field_set.triangular_mesh
+        g = m.locator_grid()
+        self._keep = [m.x, m.y, m.triangles, m.gradx, m.grady, m.det, m.edges, m.triedge_map,
+                      m.edgetri_map, m.edges_labels, g[5], g[6]]
+        md = _lib.MeshDesc(m.nv, m.nt, m.ne, m.nopen, m.x.ctypes.data, m.y.ctypes.data,
+                           m.triangles.ctypes.data, m.gradx.ctypes.data, m.grady.ctypes.data,
+                           m.det.ctypes.data, m.edges.ctypes.data, m.triedge_map.ctypes.data,
+                           m.edgetri_map.ctypes.data, m.edges_labels.ctypes.data,
+                           g[0], g[1], g[2], g[3], g[4], g[5].ctypes.data, g[6].ctypes.data)
+        _lib.check(self._ctx, self.L.cg_mesh_upload(self._ctx, C.byref(md)))
+        fs = self.field_set
+        ptr = lambda a: None if a is None else a.ctypes.data
+        fd = _lib.FieldsDesc(fs.dim, fs.nlayers, fs.npoints, fs.ntimes, ptr(fs.times),
+                             ptr(fs.elevation), ptr(fs.velocity_x), ptr(fs.velocity_y),
+                             ptr(fs.velocity_z), ptr(fs._opt.get("turbulent_energy")),
+                             ptr(fs._opt.get("dissipation")), ptr(fs._opt.get("bottom")))
+        _lib.check(self._ctx, self.L.cg_fields_upload(self._ctx, C.byref(fd)))
+
+    def _create_run(self):
+        sd = self.particle_set._state_desc()
+        _lib.check(self._ctx, self.L.cg_run_create(self._ctx, C.byref(self._prm), C.byref(sd),
+                                                   C.byref(self._run)))
+
+    def initialize_particle_state(self, i=None):
+        """solver.pyx:238-379, for every particle awaiting initialization."""
+        _lib.check(self._ctx, self.L.cg_run_init(self._run))
+
+    def forward(self, time_step=None, nsteps=1):
+        """solver.pyx:413-585: advances the run by one step (nsteps > 1
+        batches several forward calls into one library call)."""
+        if time_step is not None and time_step != self.simutime.time_step:
+            raise ValueError("forward(time_step) must equal parameters['time_step']")
+        nopen = max(1, self.nopen)
+        stats = np.zeros((nsteps, nopen), dtype=np.int32)
+        t0 = self.simutime.time
+        rc = self.L.cg_run_step(self._run, nsteps, stats.ctypes.data)
+        _lib.check(self._ctx, rc)
+        for s in range(nsteps):
+            if self.parameters.bnd_statistics:
+                self._bnd_stats_times.append(self.simutime.time)
+                self._bnd_stats_data.append(stats[s, : self.nopen].copy())
+            self.simutime.increment()
+        self._last_forward = (t0, nsteps)
+
+    def solve(self):
+        """solver.pyx:382-411"""
+        start = _time.time()
+        remaining = self.simutime.nt - self.simutime.iteration
+        if remaining > 0 and not self.simutime.is_finished:
+            self.forward(nsteps=remaining)
+        self.wall_time = _time.time() - start
+        self.flush_statistics()
+
+    def flush_statistics(self):
+        """solver.pyx:587-630 (kept in memory: see bnd_statistics())."""
+        return None
+
+    def bnd_statistics(self):
+        """Per-step open-boundary exit counts, [nsteps, nopen]."""
+        if not self._bnd_stats_data:
+            return np.zeros((0, self.nopen), dtype=np.int32)
+        return np.stack(self._bnd_stats_data)
+
+    def last_kernel_ms(self):
+        ms, n = C.c_double(), C.c_int32()
+        self.L.cg_run_last_kernel_ms(self._run, C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
+    def close(self):
+        if getattr(self, "_run", None):
+            self.L.cg_run_destroy(self._run)
+            self._run = None
+        if getattr(self, "_ctx", None):
+            self.L.cg_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,575 @@
+// cg_api.cu -- the C ABI of libcylag_gpu.so (declared in include/cylag_gpu.h).
+//
+// Host side of the GB300 particle step: context and stream, one-time mesh
+// and field uploads into packed device layouts, per-run time stepping
+// (SimuTime and the field time-interpolation record, cylag/core/simutime.pyx
+// and cylag/core/eulerian_field_set.pyx:845-938), kernel launches and error
+// reporting.  No exception leaves this file.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cylag_gpu.h"
+#include "cg_internal.h"
+
+using namespace cg;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct cg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;
+    uint64_t used = 0;
+    std::string err;
+    // mesh
+    bool have_mesh = false;
+    DevMesh mesh{};
+    int nopen = 0;
+    std::vector<DevBuf> mesh_bufs;
+    // fields
+    bool have_fields = false;
+    DevFrames frames{};
+    DevBuf frames_buf;
+    std::vector<double> times;
+    int fdim = 2, nlayers = 1, npoints = 0;
+    bool has_keps = false;
+};
+
+struct cg_run {
+    cg_ctx* ctx = nullptr;
+    cg_params prm{};
+    DevParams dp{};
+    DevState st{};
+    double time = 0.;
+    int64_t iteration = 0;
+    int64_t nt = 0;
+    bool frozen = false;
+    int record = 0;
+    bool interp_done = false;
+    bool prev_valid = false;
+    bool fields_ready = false;
+    DevBuf cur, prev;
+    DevBuf stats;
+    int stats_rows = 0;
+    DevBuf errw;
+    uint64_t bytes = 0;
+    std::vector<cudaEvent_t> ev;
+    int last_launches = 0;
+    double last_ms = 0.;
+};
+
+static int set_err(cg_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+#define CUDA_TRY(c, call)                                                                    \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return set_err((c), CG_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+static int dalloc(cg_ctx* c, DevBuf& b, size_t bytes) {
+    b.bytes = bytes;
+    if (bytes == 0) { b.p = nullptr; return CG_OK; }
+    CUDA_TRY(c, cudaMalloc(&b.p, bytes));
+    return CG_OK;
+}
+
+static void dfree(DevBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+template <typename T>
+static int upload(cg_ctx* c, const std::vector<T>& h, const T*& out) {
+    c->mesh_bufs.emplace_back();
+    DevBuf& b = c->mesh_bufs.back();
+    int rc = dalloc(c, b, h.size() * sizeof(T));
+    if (rc) return rc;
+    if (!h.empty()) CUDA_TRY(c, cudaMemcpy(b.p, h.data(), b.bytes, cudaMemcpyHostToDevice));
+    out = (const T*)b.p;
+    c->used += b.bytes;
+    return CG_OK;
+}
+
+
+extern "C" {
+
+int cg_ctx_create(int32_t device, uint64_t hbm_budget_bytes, cg_ctx** out) {
+    if (!out) return CG_EINVAL;
+    *out = nullptr;
+    cg_ctx* c = new (std::nothrow) cg_ctx();
+    if (!c) return CG_EINVAL;
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return CG_ECUDA;
+    }
+    *out = c;
+    return CG_OK;
+}
+
+int cg_ctx_destroy(cg_ctx* c) {
+    if (!c) return CG_EINVAL;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& b : c->mesh_bufs) dfree(b);
+    dfree(c->frames_buf);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return CG_OK;
+}
+
+int cg_last_error(const cg_ctx* c, char* buf, uint64_t len) {
+    if (!c || !buf || len == 0) return CG_EINVAL;
+    snprintf(buf, (size_t)len, "%s", c->err.c_str());
+    return CG_OK;
+}
+
+uint64_t cg_ctx_stream(const cg_ctx* c) { return c ? (uint64_t)(uintptr_t)c->stream : 0; }
+
+int cg_ctx_sync(cg_ctx* c) {
+    if (!c) return CG_EINVAL;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mesh (cylag/geom/triangular_mesh.pyx:75-179)
+// ---------------------------------------------------------------------------
+int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
+    if (!c || !d) return CG_EINVAL;
+    if (d->nv <= 0 || d->nt <= 0 || d->ne <= 0 || !d->x || !d->y || !d->triangles || !d->gradx ||
+        !d->grady || !d->det || !d->edges || !d->triedge_map || !d->edgetri_map ||
+        !d->edges_labels || !d->grid_start || !d->grid_tris || d->grid_nx <= 0 || d->grid_ny <= 0)
+        return set_err(c, CG_EINVAL, "cg_mesh_upload: incomplete mesh description");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    for (auto& b : c->mesh_bufs) dfree(b);
+    c->mesh_bufs.clear();
+    int nv = d->nv, nt = d->nt, ne = d->ne;
+    // range checks: every index the kernels follow must stay in bounds
+    for (int64_t k = 0; k < 3LL * nt; ++k) {
+        if (d->triangles[k] < 0 || d->triangles[k] >= nv)
+            return set_err(c, CG_EINVAL, "triangle vertex out of range at %lld", (long long)k);
+        if (d->triedge_map[k] < 0 || d->triedge_map[k] >= ne)
+            return set_err(c, CG_EINVAL, "triedge_map out of range at %lld", (long long)k);
+    }
+    for (int64_t j = 0; j < ne; ++j) {
+        int a = d->edges[2 * j], b = d->edges[2 * j + 1];
+        int t0 = d->edgetri_map[2 * j], t1 = d->edgetri_map[2 * j + 1];
+        if (a < 0 || a >= nv || b < 0 || b >= nv || t0 < 0 || t0 >= nt || t1 < -1 || t1 >= nt)
+            return set_err(c, CG_EINVAL, "edge %lld out of range", (long long)j);
+    }
+    int64_t ncell = (int64_t)d->grid_nx * d->grid_ny;
+    int64_t ngt = d->grid_start[ncell];
+    for (int64_t q = 0; q < ncell; ++q)
+        if (d->grid_start[q] < 0 || d->grid_start[q] > d->grid_start[q + 1])
+            return set_err(c, CG_EINVAL, "grid_start not monotonic");
+    for (int64_t q = 0; q < ngt; ++q)
+        if (d->grid_tris[q] < 0 || d->grid_tris[q] >= nt)
+            return set_err(c, CG_EINVAL, "grid triangle out of range");
+    for (int64_t v = 0; v < nv; ++v)
+        if (!std::isfinite(d->x[v]) || !std::isfinite(d->y[v]))
+            return set_err(c, CG_EINVAL, "non-finite vertex coordinate at %lld", (long long)v);
+
+    std::vector<double2> xy(nv);
+    for (int v = 0; v < nv; ++v) xy[v] = make_double2(d->x[v], d->y[v]);
+    std::vector<int4> tv(2 * (size_t)nt);
+    std::vector<double2> basis(5 * (size_t)nt);
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        const int32_t* e = d->triedge_map + 3 * k;
+        tv[2 * k] = make_int4(t[0], t[1], t[2], e[0]);
+        tv[2 * k + 1] = make_int4(e[1], e[2], 0, 0);
+        const double *de = d->det + 3 * k, *gx = d->gradx + 3 * k, *gy = d->grady + 3 * k;
+        basis[5 * k + 0] = make_double2(de[0], de[1]);
+        basis[5 * k + 1] = make_double2(de[2], gx[0]);
+        basis[5 * k + 2] = make_double2(gx[1], gx[2]);
+        basis[5 * k + 3] = make_double2(gy[0], gy[1]);
+        basis[5 * k + 4] = make_double2(gy[2], 0.0);
+    }
+    std::vector<int4> edge(ne);
+    std::vector<int> lab(ne);
+    for (int j = 0; j < ne; ++j) {
+        edge[j] = make_int4(d->edges[2 * j], d->edges[2 * j + 1], d->edgetri_map[2 * j],
+                            d->edgetri_map[2 * j + 1]);
+        lab[j] = d->edges_labels[j];
+    }
+    std::vector<int> gstart(d->grid_start, d->grid_start + ncell + 1);
+    std::vector<int> gtris(d->grid_tris, d->grid_tris + ngt);
+    DevMesh m{};
+    m.nv = nv; m.nt = nt; m.ne = ne;
+    int rc;
+    const double2 *p_xy, *p_basis;
+    const int4 *p_tv, *p_edge;
+    const int *p_lab, *p_gs, *p_gt;
+    if ((rc = upload(c, xy, p_xy))) return rc;
+    if ((rc = upload(c, tv, p_tv))) return rc;
+    if ((rc = upload(c, basis, p_basis))) return rc;
+    if ((rc = upload(c, edge, p_edge))) return rc;
+    if ((rc = upload(c, lab, p_lab))) return rc;
+    if ((rc = upload(c, gstart, p_gs))) return rc;
+    if ((rc = upload(c, gtris, p_gt))) return rc;
+    m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
+    m.gstart = p_gs; m.gtris = p_gt;
+    m.gx0 = d->grid_x0;
+    m.gy0 = d->grid_y0;
+    m.ginv = d->grid_inv_cell;
+    m.gnx = d->grid_nx;
+    m.gny = d->grid_ny;
+    c->mesh = m;
+    c->nopen = d->nopen;
+    c->have_mesh = true;
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fields (cylag/core/eulerian_field_set.pyx:125-256)
+// ---------------------------------------------------------------------------
+int cg_fields_upload(cg_ctx* c, const cg_fields_desc* d) {
+    if (!c || !d) return CG_EINVAL;
+    if (!c->have_mesh) return set_err(c, CG_ESTATE, "cg_fields_upload before cg_mesh_upload");
+    if (d->dim != 2 && d->dim != 3)
+        return set_err(c, CG_EINVAL, "field dim must be 2 or 3");
+    if (d->npoints != c->mesh.nv)
+        return set_err(c, CG_EINVAL, "npoints (%d) != mesh nv (%d)", d->npoints, c->mesh.nv);
+    if (d->nlayers < 1 || d->ntimes < 1 || !d->times || !d->elevation || !d->velocity_x ||
+        !d->velocity_y || (d->dim == 3 && !d->velocity_z))
+        return set_err(c, CG_EINVAL, "incomplete field description");
+    if (d->dim == 2 && d->nlayers != 1) return set_err(c, CG_EINVAL, "2D fields need nlayers == 1");
+    for (int t = 0; t + 1 < d->ntimes; ++t)
+        if (!(d->times[t + 1] - d->times[t] > EPSILON))
+            return set_err(c, CG_EINVAL, "times must be strictly increasing (at %d)", t);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const double* src[RF_COUNT] = {d->elevation, d->velocity_x, d->velocity_y,
+                                   d->dim == 3 ? d->velocity_z : nullptr,
+                                   d->turbulent_energy, d->dissipation, d->bottom};
+    DevFrames fr{};
+    fr.nraw = 0;
+    for (int f = 0; f < RF_COUNT; ++f) fr.raw_slot[f] = src[f] ? fr.nraw++ : -1;
+    fr.nnodes = (int64_t)d->npoints * d->nlayers;
+    fr.dim = d->dim;
+    int64_t per = fr.nnodes;
+    std::vector<double> h((size_t)d->ntimes * fr.nraw * per);
+    for (int t = 0; t < d->ntimes; ++t)
+        for (int f = 0; f < RF_COUNT; ++f) {
+            if (!src[f]) continue;
+            memcpy(&h[((size_t)t * fr.nraw + fr.raw_slot[f]) * per], src[f] + (size_t)t * per,
+                   per * sizeof(double));
+        }
+    dfree(c->frames_buf);
+    int rc = dalloc(c, c->frames_buf, h.size() * sizeof(double));
+    if (rc) return rc;
+    CUDA_TRY(c, cudaMemcpy(c->frames_buf.p, h.data(), c->frames_buf.bytes, cudaMemcpyHostToDevice));
+    c->used += c->frames_buf.bytes;
+    fr.frames = (const double*)c->frames_buf.p;
+    c->frames = fr;
+    c->times.assign(d->times, d->times + d->ntimes);
+    c->fdim = d->dim;
+    c->nlayers = d->nlayers;
+    c->npoints = d->npoints;
+    c->has_keps = d->turbulent_energy && d->dissipation;
+    c->have_fields = true;
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// runs (cylag/core/solver.pyx:74-236)
+// ---------------------------------------------------------------------------
+// zlocalizer.pyx:125-151
+static int lower_index(const std::vector<double>& t, double value, int last) {
+    int ni = (int)t.size();
+    for (int i = last; i < ni - 1; ++i)
+        if (value >= t[i] && value < t[i + 1]) return i;
+    if (ni > 1 && value >= t[ni - 1]) return ni - 2;
+    return 0;
+}
+
+int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run** out) {
+    if (!c || !p || !s || !out) return CG_EINVAL;
+    *out = nullptr;
+    if (!c->have_mesh || !c->have_fields)
+        return set_err(c, CG_ESTATE, "cg_run_create before mesh/field upload");
+    if (p->precision != CG_PRECISION_FP64)
+        return set_err(c, CG_EINVAL, "precision %d is not built", p->precision);
+    if (p->model != 1)
+        return set_err(c, CG_EINVAL, "model %d is not built in this library", p->model);
+    if (p->dim != c->fdim)
+        return set_err(c, CG_EINVAL, "particle dim %d != field dim %d (pseudo-3D not built)",
+                       p->dim, c->fdim);
+    if (p->time_scheme < 1 || p->time_scheme > 4)
+        return set_err(c, CG_EINVAL, "LSM1 time_scheme must be 1..4");
+    if (p->rng_method < 1 || p->rng_method > 3) return set_err(c, CG_EINVAL, "bad rng_method");
+    if ((p->diffusion_model == 2 || p->diffusion_model == 3) && !c->has_keps)
+        return set_err(c, CG_EINVAL,
+                       "diffusion_model=%d requires 'TURBULENT ENERG.' and 'DISSIPATION' fields",
+                       p->diffusion_model);
+    if (!(p->time_step > 0.) || !(p->final_time > p->initial_time))
+        return set_err(c, CG_EINVAL, "bad time interval");
+    if (s->n < 0 || (s->n > 0 && (!s->position || !s->velocity || !s->fluid_velocity_seen ||
+                                  !s->last_position || !s->last_velocity || !s->tri ||
+                                  !s->last_tri || !s->lowerlayer || !s->tag || !s->diameter ||
+                                  !s->rng_state)))
+        return set_err(c, CG_EINVAL, "incomplete particle state description");
+    bool frozen = p->frozen_eulerian_fields || c->times.size() == 1;
+    if (c->times.size() == 1 && !p->frozen_eulerian_fields)
+        return set_err(c, CG_EINVAL,
+                       "EulerianFieldSet has only one time step, use frozen_eulerian_fields=True");
+    if (!p->frozen_eulerian_fields && p->final_time > c->times.back())
+        return set_err(c, CG_EINVAL, "final_time > EulerianFieldSet maximum time");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+
+    int rv = record_values(c->fdim);
+    size_t rec_bytes = (size_t)rv * sizeof(double) * c->frames.nnodes;
+    uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
+    uint64_t need = state_bytes + 2 * rec_bytes + 64;
+    if (c->budget && c->used + need > c->budget)
+        return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
+                       (unsigned long long)need, (unsigned long long)c->used,
+                       (unsigned long long)c->budget);
+
+    cg_run* r = new (std::nothrow) cg_run();
+    if (!r) return set_err(c, CG_EINVAL, "out of host memory");
+    r->ctx = c;
+    r->prm = *p;
+    int rc;
+    if ((rc = dalloc(c, r->cur, rec_bytes)) || (rc = dalloc(c, r->prev, rec_bytes)) ||
+        (rc = dalloc(c, r->errw, 64))) {
+        dfree(r->cur); dfree(r->prev); dfree(r->errw);
+        delete r;
+        return rc;
+    }
+    cudaMemsetAsync(r->errw.p, 0, 64, c->stream);
+    r->bytes = need;
+    c->used += need;
+
+    DevParams& d = r->dp;
+    d.model = p->model;
+    d.time_scheme = p->time_scheme;
+    d.rng_method = p->rng_method;
+    d.diffmod = p->diffusion_model;
+    d.bc_on = p->boundary_conditions != 0;
+    d.bc_type = p->boundary_conditions_type;
+    d.max_rebounds = p->max_wall_rebounds;
+    d.bnd_statistics = p->bnd_statistics != 0;
+    d.nopen = c->nopen;
+    d.pdim = p->dim;
+    d.dt = p->time_step;
+    d.sqrtdt = std::sqrt(p->time_step);
+    d.nux = p->horizontal_diffusivity;
+    d.nuz = p->vertical_diffusivity;
+    // update_state_lsm1.pyx:708-713
+    d.diffx_const = std::sqrt(2. * d.nux) * d.sqrtdt;
+    d.diffz_const = std::sqrt(2. * d.nuz) * d.sqrtdt;
+    d.damp = std::fmin(p->rebound_damping_coef, 1.0 - EPSILON_REBOUND);  // compute_bc.pyx:76
+    d.strand = p->stranding_probability;
+    d.roughness = p->wall_roughness_angle * DEG_TO_RAD;
+    d.buoy_model = p->buoyancy_velocity_model;
+    d.buoy_wb = p->buoyancy_velocity;
+    d.density = p->particle_density;
+    d.rho0 = p->water_density;
+    d.drag_coef = p->drag_coefficient;
+
+    DevState& st = r->st;
+    st.n = s->n;
+    st.pos = s->position;
+    st.vel = s->velocity;
+    st.fvs = s->fluid_velocity_seen;
+    st.last_pos = s->last_position;
+    st.last_vel = s->last_velocity;
+    st.tri = s->tri;
+    st.last_tri = s->last_tri;
+    st.lowerlayer = s->lowerlayer;
+    st.tag = s->tag;
+    st.diameter = s->diameter;
+    st.rng = s->rng_state;
+
+    // simutime.pyx:46-75
+    r->time = p->initial_time;
+    r->nt = (int64_t)((p->final_time - p->initial_time) / p->time_step);
+    r->frozen = frozen;
+    // solver.pyx:144-152 and 188-191
+    r->record = frozen ? 0 : lower_index(c->times, p->initial_time, 0);
+    r->interp_done = false;
+    r->prev_valid = false;
+    *out = r;
+    return CG_OK;
+}
+
+int cg_run_destroy(cg_run* r) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    dfree(r->cur);
+    dfree(r->prev);
+    dfree(r->stats);
+    dfree(r->errw);
+    for (auto e : r->ev) cudaEventDestroy(e);
+    c->used -= r->bytes;
+    delete r;
+    return CG_OK;
+}
+
+int cg_run_seed(cg_run* r) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_seed(r->st.tag, r->st.rng, r->st.n, r->prm.seed, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    return CG_OK;
+}
+
+static double keps_fac(const cg_run* r) { return CMU / r->prm.schmidt_number; }
+
+// eulerian_field_set.pyx:866-938: saves the previous temps (pointer swap)
+// and interpolates at `time` into the current ones.
+static int time_interpolation(cg_run* r, double time) {
+    cg_ctx* c = r->ctx;
+    if (r->frozen) {
+        if (!r->fields_ready) {
+            launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, 0, c->stream);
+            CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes,
+                                        cudaMemcpyDeviceToDevice, c->stream));
+            r->fields_ready = true;
+        }
+        return CG_OK;
+    }
+    std::swap(r->cur, r->prev);
+    r->prev_valid = r->interp_done;
+    r->interp_done = true;
+    r->record = lower_index(c->times, time, r->record);
+    int rec = r->record;
+    double dt = c->times[rec] - c->times[rec + 1];
+    if (std::fabs(dt) < EPSILON)
+        return set_err(c, CG_EINVAL, "Time interpolation failed: duplicate times at record %d", rec);
+    double tf = (time - c->times[rec + 1]) / dt;
+    launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, 0, c->stream);
+    r->fields_ready = true;
+    CUDA_TRY(c, cudaGetLastError());
+    return CG_OK;
+}
+
+static int ensure_fields(cg_run* r) {
+    if (r->fields_ready) return CG_OK;
+    cg_ctx* c = r->ctx;
+    if (r->frozen) return time_interpolation(r, r->time);
+    // EulerianFieldSet._init_tmp (743-776): both temps hold record 0, then
+    // Solver.__init__ interpolates at initial_time (solver.pyx:190-191).
+    launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, 0, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes, cudaMemcpyDeviceToDevice,
+                                c->stream));
+    return time_interpolation(r, r->prm.initial_time);
+}
+
+int cg_run_init(cg_run* r) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = ensure_fields(r);
+    if (rc) return rc;
+    launch_init_plain(c->fdim, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st,
+                      r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    return CG_OK;
+}
+
+int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
+    if (!r || nsteps < 0) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (nsteps == 0) return CG_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = ensure_fields(r);
+    if (rc) return rc;
+    int nopen = c->nopen > 0 ? c->nopen : 1;
+    if (r->stats_rows < nsteps) {
+        dfree(r->stats);
+        if ((rc = dalloc(c, r->stats, (size_t)nsteps * nopen * sizeof(int)))) return rc;
+        r->stats_rows = nsteps;
+    }
+    CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * nopen * sizeof(int), c->stream));
+    int nev = 2 * nsteps;
+    while ((int)r->ev.size() < nev) {
+        cudaEvent_t e;
+        CUDA_TRY(c, cudaEventCreate(&e));
+        r->ev.push_back(e);
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        // solver.pyx:440: fields at the step-start time
+        if ((rc = time_interpolation(r, r->time))) return rc;
+        int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
+        int* stats = (int*)r->stats.p + (size_t)s * nopen;
+        CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
+        launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
+                          r->prev_valid, r->dp, r->st, aux, (int)(r->iteration),
+                          stats, (uint32_t*)r->errw.p, c->stream);
+        CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
+        CUDA_TRY(c, cudaGetLastError());
+        // simutime.pyx:77-84
+        r->time += r->prm.time_step;
+        r->iteration += 1;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    double tot = 0.;
+    for (int s = 0; s < nsteps; ++s) {
+        float ms = 0.f;
+        CUDA_TRY(c, cudaEventElapsedTime(&ms, r->ev[2 * s], r->ev[2 * s + 1]));
+        tot += ms;
+    }
+    r->last_ms = tot / nsteps;
+    r->last_launches = nsteps;
+    if (bnd_stats_host && c->nopen > 0)
+        CUDA_TRY(c, cudaMemcpy(bnd_stats_host, r->stats.p, (size_t)nsteps * c->nopen * sizeof(int),
+                               cudaMemcpyDeviceToHost));
+    uint32_t flags = 0;
+    CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
+    return CG_OK;
+}
+
+int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
+    if (!r) return CG_EINVAL;
+    if (time) *time = r->time;
+    if (iteration) *iteration = r->iteration;
+    return CG_OK;
+}
+
+int cg_run_errors(cg_run* r, uint32_t* flags) {
+    if (!r || !flags) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    CUDA_TRY(c, cudaMemcpy(flags, r->errw.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemset(r->errw.p, 0, sizeof(uint32_t)));
+    return CG_OK;
+}
+
+int cg_run_last_kernel_ms(const cg_run* r, double* ms, int32_t* launches) {
+    if (!r) return CG_EINVAL;
+    if (ms) *ms = r->last_ms;
+    if (launches) *launches = r->last_launches;
+    return CG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,378 @@
+// cg_device.cuh -- device-side building blocks of the fused particle step.
+//
+// Every function restates one piece of CyLag's per-particle step (the file
+// and lines are cited at each function) in the same floating-point
+// expression order, so that the plain form, compiled with -fmad=false,
+// rounds exactly as the reference's C does.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "ziggurat_tables.h"
+
+namespace cg {
+
+// cylag/core/constants.pyx:1-75
+constexpr double EPSILON = 1.e-16;
+constexpr double EPSILON_LSM2 = 1.e-8;
+constexpr double EPSILON_LSM3 = 1.e-8;
+constexpr double EPSILON_REBOUND = 1.e-8;
+constexpr double DEG_TO_RAD = 0.017453292519943295;
+constexpr double TWO_SQRT3 = 3.4641016151377544;
+constexpr double GRAV = 9.80665;
+constexpr double NU0 = 1.3e-6;
+constexpr double C0KOLM = 1.2;
+constexpr double CMU = 0.09;
+constexpr double KAPPA = 0.41;
+constexpr int BND_WALL_REF = 0;
+constexpr int BND_OPEN_REF = 1;
+constexpr int PART_LOC_O = -1;
+constexpr int PART_LOC_B = -2;
+constexpr int PART_LOC_A = -3;
+constexpr int NITER_MAX = 50;            // xylocalizer.pyx:362
+constexpr int RNG_MAX_TRIES = 1 << 16;   // bound on every rejection loop
+
+// error flags (mirror CG_ERR_* in cylag_gpu.h)
+constexpr uint32_t ERR_INTERP_OUTSIDE = 1;
+constexpr uint32_t ERR_DEGENERATE_LAYER = 2;
+constexpr uint32_t ERR_RNG_LIMIT = 4;
+constexpr uint32_t ERR_UNSUPPORTED = 8;
+
+// ---------------------------------------------------------------------------
+// device views
+// ---------------------------------------------------------------------------
+struct DevMesh {
+    int nv, nt, ne;
+    const double2* __restrict__ xy;     // [nv]
+    const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
+    const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
+    const int4* __restrict__ edge;      // [ne]: {n0, n1, t0, t1}
+    const int* __restrict__ elabel;     // [ne]
+    double gx0, gy0, ginv;
+    int gnx, gny;
+    const int* __restrict__ gstart;     // [gnx*gny+1]
+    const int* __restrict__ gtris;
+};
+
+// Time-interpolated node fields for one step, packed per node.
+// 2D: 4 values {ux, uy, K, zs};  3D: 8 values {zs, ux, uy, uz, K, -, -, -}
+// where K = (Cmu/sigc) k^2 / max(eps, EPSILON) is the nodal k-epsilon
+// diffusivity (eulerian_field_set.pyx:1995-1997), exactly what the
+// reference evaluates per node inside _interpolate_diffusivity_gradient_c.
+template <typename FT>
+struct DevFields {
+    const FT* __restrict__ cur;
+    const FT* __restrict__ prev;
+    int npoints, nlayers, dim;
+    int prev_valid;
+};
+
+struct DevParams {
+    int model, time_scheme, rng_method, diffmod;
+    int bc_on, bc_type, max_rebounds, bnd_statistics, nopen;
+    int pdim;
+    double dt, sqrtdt, nux, nuz;
+    double diffx_const, diffz_const;     // sqrt(2 nu) * sqrt(dt)
+    double damp, strand, roughness;
+    double buoy_wb;                      // constant buoyancy velocity (model 0)
+    int buoy_model;
+    double density, rho0, drag_coef;
+};
+
+struct DevState {
+    int n;
+    double* __restrict__ pos;
+    double* __restrict__ vel;
+    double* __restrict__ fvs;
+    double* __restrict__ last_pos;
+    double* __restrict__ last_vel;
+    int* __restrict__ tri;
+    int* __restrict__ last_tri;
+    int* __restrict__ lowerlayer;
+    int* __restrict__ tag;
+    double* __restrict__ diameter;
+    uint64_t* __restrict__ rng;
+};
+
+// ---------------------------------------------------------------------------
+// PCG32 + normal variates (cylag/lsm/random_utils.pyx)
+// ---------------------------------------------------------------------------
+struct Rng {
+    uint64_t state, inc;
+    uint32_t err;
+};
+
+struct ZigTables {
+    uint32_t kn[128];
+    double wn[128];
+    double fn[128];
+};
+
+// random_utils.pyx:22-28
+__device__ __forceinline__ uint32_t pcg_next(Rng& r) {
+    uint64_t old = r.state;
+    r.state = old * 6364136223846793005ULL + r.inc;
+    uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+
+// random_utils.pyx:30-37
+__host__ __device__ inline void pcg_seed(uint64_t seed, uint64_t stream, uint64_t& state,
+                                         uint64_t& inc) {
+    uint64_t m = 6364136223846793005ULL;
+    inc = (stream << 1) | 1ULL;
+    state = 0ULL * m + inc;
+    state += seed;
+    state = state * m + inc;
+}
+
+// random_utils.pyx:55-67
+__device__ __forceinline__ double rng_uniform(Rng& r) {
+    uint32_t u = pcg_next(r);
+    return u * (1.0 / 4294967296.0);
+}
+
+// random_utils.pyx:154-194
+__device__ inline double rng_ziggurat(Rng& r, const ZigTables& z) {
+    for (int tries = 0; tries < RNG_MAX_TRIES; ++tries) {
+        int32_t hz = (int32_t)pcg_next(r);
+        uint32_t iz = (uint32_t)hz & 127u;
+        uint32_t ahz = hz < 0 ? 0u - (uint32_t)hz : (uint32_t)hz;  // c_abs(INT_MIN) == INT_MIN
+        if (ahz < z.kn[iz]) return hz * z.wn[iz];
+        if (iz == 0) {
+            for (int t2 = 0; t2 < RNG_MAX_TRIES; ++t2) {
+                double x = -log(rng_uniform(r)) * 0.2904764;
+                double y = -log(rng_uniform(r));
+                if (y + y >= x * x) return hz > 0 ? 3.442619855899 + x : -3.442619855899 - x;
+            }
+            r.err |= ERR_RNG_LIMIT;
+            return 0.0;
+        }
+        double x = hz * z.wn[iz];
+        if (z.fn[iz] + rng_uniform(r) * (z.fn[iz - 1] - z.fn[iz]) < exp(-0.5 * x * x)) return x;
+    }
+    r.err |= ERR_RNG_LIMIT;
+    return 0.0;
+}
+
+// random_utils.pyx:72-108 (pair == true returns both coordinates)
+__device__ inline void rng_polar(Rng& r, double& a, double& b) {
+    double x1 = 0., x2 = 0., w = 2.0;
+    int tries = 0;
+    while ((w >= 1.0 || w == 0.0) && tries < RNG_MAX_TRIES) {
+        x1 = 2.0 * rng_uniform(r) - 1.0;
+        x2 = 2.0 * rng_uniform(r) - 1.0;
+        w = x1 * x1 + x2 * x2;
+        ++tries;
+    }
+    if (tries == RNG_MAX_TRIES) { r.err |= ERR_RNG_LIMIT; a = b = 0.; return; }
+    w = sqrt((-2.0 * log(w)) / w);
+    a = x1 * w;
+    b = x2 * w;
+}
+
+// random_utils.pyx:202-233
+__device__ inline void rng_pair(Rng& r, int method, const ZigTables& z, double& a, double& b) {
+    if (method == 1) {
+        a = (rng_uniform(r) - 0.5) * TWO_SQRT3;
+        b = (rng_uniform(r) - 0.5) * TWO_SQRT3;
+    } else if (method == 2) {
+        a = rng_ziggurat(r, z);
+        b = rng_ziggurat(r, z);
+    } else {
+        rng_polar(r, a, b);
+    }
+}
+
+// random_utils.pyx:235-263
+__device__ inline double rng_single(Rng& r, int method, const ZigTables& z) {
+    if (method == 1) return (rng_uniform(r) - 0.5) * TWO_SQRT3;
+    if (method == 2) return rng_ziggurat(r, z);
+    double a, b;
+    rng_polar(r, a, b);
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// geometry (cylag/geom/utils.pyx, intersections.pyx, xylocalizer.pyx)
+// ---------------------------------------------------------------------------
+
+// utils.pyx:332-361
+__device__ __forceinline__ double pintri(double x, double y, double xa, double ya, double xb,
+                                         double yb, double xc, double yc) {
+    return ((xb - xa) * (y - ya) - (x - xa) * (yb - ya)) *
+           ((x - xa) * (yc - ya) - (xc - xa) * (y - ya));
+}
+
+// utils.pyx:363-385 with xylocalizer.pyx:126-167
+__device__ __forceinline__ bool in_tri(const DevMesh& m, int k, double x, double y) {
+    int4 t = __ldg(&m.tv[2 * k]);
+    double2 a = __ldg(&m.xy[t.x]), b = __ldg(&m.xy[t.y]), c = __ldg(&m.xy[t.z]);
+    return pintri(x, y, a.x, a.y, b.x, b.y, c.x, c.y) >= 0 &&
+           pintri(x, y, b.x, b.y, c.x, c.y, a.x, a.y) >= 0 &&
+           pintri(x, y, c.x, c.y, a.x, a.y, b.x, b.y) >= 0;
+}
+
+// utils.pyx:228-252
+__device__ __forceinline__ int orientation(double v0x, double v0y, double v1x, double v1y,
+                                           double v2x, double v2y) {
+    double delta = (v0y - v1y) * (v2x - v0x) - (v0x - v1x) * (v2y - v0y);
+    if (delta == 0.) return 0;
+    if (delta > 0.) return 1;
+    return 2;
+}
+
+// utils.pyx:282-303
+__device__ __forceinline__ bool on_segment(double v0x, double v0y, double v1x, double v1y,
+                                           double v2x, double v2y) {
+    return v2x <= fmax(v1x, v0x) && v2x >= fmin(v1x, v0x) && v2y <= fmax(v1y, v0y) &&
+           v2y >= fmin(v1y, v0y);
+}
+
+// intersections.pyx:106-148
+__device__ inline bool intersec2d(double p0x, double p0y, double p1x, double p1y, double s0x,
+                                  double s0y, double s1x, double s1y) {
+    int o1 = orientation(p0x, p0y, p1x, p1y, s0x, s0y);
+    int o2 = orientation(p0x, p0y, p1x, p1y, s1x, s1y);
+    int o3 = orientation(s0x, s0y, s1x, s1y, p0x, p0y);
+    int o4 = orientation(s0x, s0y, s1x, s1y, p1x, p1y);
+    if (o1 != o2 && o3 != o4) return true;
+    if (o1 == 0 && on_segment(p0x, p0y, p1x, p1y, s0x, s0y)) return true;
+    if (o2 == 0 && on_segment(p0x, p0y, p1x, p1y, s1x, s1y)) return true;
+    if (o3 == 0 && on_segment(s0x, s0y, s1x, s1y, p0x, p0y)) return true;
+    if (o4 == 0 && on_segment(s0x, s0y, s1x, s1y, p1x, p1y)) return true;
+    return false;
+}
+
+// Global point location: first triangle (lowest id) in the point's grid
+// bucket that contains it.  Stands in for the KD-tree fallback of
+// xylocalizer.pyx:200-286; same result unless the point lies exactly on an
+// edge shared by two triangles.
+__device__ inline int grid_locate(const DevMesh& m, double x, double y) {
+    double fx = floor((x - m.gx0) * m.ginv);
+    double fy = floor((y - m.gy0) * m.ginv);
+    if (!(fx >= 0.)) fx = 0.;
+    if (!(fy >= 0.)) fy = 0.;
+    int cx = fx > (double)(m.gnx - 1) ? m.gnx - 1 : (int)fx;
+    int cy = fy > (double)(m.gny - 1) ? m.gny - 1 : (int)fy;
+    int c = cy * m.gnx + cx;
+    int b = __ldg(&m.gstart[c]), e = __ldg(&m.gstart[c + 1]);
+    for (int j = b; j < e; ++j) {
+        int k = __ldg(&m.gtris[j]);
+        if (in_tri(m, k, x, y)) return k;
+    }
+    return -1;
+}
+
+// xylocalizer.pyx:338-435
+__device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y, double x,
+                                 double y, int& new_k, int& bnd) {
+    int intersected_edge = -1;
+    for (int niter = 0; niter <= NITER_MAX; ++niter) {
+        int4 ta = __ldg(&m.tv[2 * k]);
+        int4 tb = __ldg(&m.tv[2 * k + 1]);
+        int ed[3] = {ta.w, tb.x, tb.y};
+        bool intersects = false;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int j = ed[i];
+            if (j == intersected_edge) continue;
+            int4 e = __ldg(&m.edge[j]);
+            double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+            if (intersec2d(p0x, p0y, x, y, a.x, a.y, b.x, b.y)) {
+                intersects = true;
+                int kn = (e.z == k) ? e.w : e.z;
+                if (kn == -1) { new_k = -1; bnd = j; return; }
+                if (in_tri(m, kn, x, y)) { new_k = kn; bnd = -1; return; }
+                k = kn;
+                intersected_edge = j;
+                break;
+            }
+        }
+        if (!intersects) {
+            new_k = in_tri(m, k, x, y) ? k : -1;
+            bnd = -1;
+            return;
+        }
+    }
+    new_k = -1;
+    bnd = -1;
+}
+
+// xylocalizer.pyx:27-124, method 3
+__device__ inline void xy_localize(const DevMesh& m, int k, double p0x, double p0y, double x,
+                                   double y, int& new_k, int& bnd) {
+    bnd = -1;
+    if (in_tri(m, k, x, y)) { new_k = k; return; }
+    path_walk(m, k, p0x, p0y, x, y, new_k, bnd);
+    if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
+}
+
+// zlocalizer.pyx:51-71
+__device__ __forceinline__ int lower_layer_index(int nl, double zs, double zb, double z) {
+    if (nl == 1) return 0;
+    double hl = (zs - zb) / (nl - 1);
+    if (!(hl > 0.)) return 0;
+    double findex = floor((z - zb) / hl);
+    if (!(findex >= 0.)) return 0;
+    if (!(findex <= (double)(nl - 2))) return nl - 2;
+    return (int)findex;
+}
+
+// ---------------------------------------------------------------------------
+// P1 interpolation (cylag/core/eulerian_field_set.pyx)
+// ---------------------------------------------------------------------------
+struct P1 {
+    int i0, i1, i2;
+    double f0, f1, f2;
+    double gx0, gx1, gx2, gy0, gy1, gy2;
+};
+
+// eulerian_field_set.pyx:1043-1052 (factors) + the vertex ids
+__device__ __forceinline__ P1 p1_at(const DevMesh& m, int k, double x, double y) {
+    P1 p;
+    int4 t = __ldg(&m.tv[2 * k]);
+    p.i0 = t.x; p.i1 = t.y; p.i2 = t.z;
+    double2 b0 = __ldg(&m.basis[5 * k]), b1 = __ldg(&m.basis[5 * k + 1]),
+            b2 = __ldg(&m.basis[5 * k + 2]), b3 = __ldg(&m.basis[5 * k + 3]),
+            b4 = __ldg(&m.basis[5 * k + 4]);
+    // basis layout: det0 det1 | det2 gx0 | gx1 gx2 | gy0 gy1 | gy2 pad
+    p.gx0 = b1.y; p.gx1 = b2.x; p.gx2 = b2.y;
+    p.gy0 = b3.x; p.gy1 = b3.y; p.gy2 = b4.x;
+    p.f0 = b0.x + x * p.gx0 + y * p.gy0;
+    p.f1 = b0.y + x * p.gx1 + y * p.gy1;
+    p.f2 = b1.x + x * p.gx2 + y * p.gy2;
+    return p;
+}
+
+// node record accessors --------------------------------------------------------
+template <int DIM> struct Slots;
+template <> struct Slots<2> { static constexpr int NF = 4, UX = 0, UY = 1, K = 2, ZS = 3, UZ = -1; };
+template <> struct Slots<3> { static constexpr int NF = 8, ZS = 0, UX = 1, UY = 2, UZ = 3, K = 4; };
+
+template <int DIM, typename FT>
+__device__ __forceinline__ double nodev(const FT* __restrict__ f, int node, int slot) {
+    return (double)__ldg(&f[(size_t)node * Slots<DIM>::NF + slot]);
+}
+
+template <int DIM, typename FT>
+__device__ __forceinline__ double p1_eval(const FT* __restrict__ f, int off, const P1& p, int slot) {
+    return nodev<DIM>(f, off + p.i0, slot) * p.f0 + nodev<DIM>(f, off + p.i1, slot) * p.f1 +
+           nodev<DIM>(f, off + p.i2, slot) * p.f2;
+}
+
+template <int DIM, typename FT>
+__device__ __forceinline__ double p1_gx(const FT* __restrict__ f, int off, const P1& p, int slot) {
+    return nodev<DIM>(f, off + p.i0, slot) * p.gx0 + nodev<DIM>(f, off + p.i1, slot) * p.gx1 +
+           nodev<DIM>(f, off + p.i2, slot) * p.gx2;
+}
+
+template <int DIM, typename FT>
+__device__ __forceinline__ double p1_gy(const FT* __restrict__ f, int off, const P1& p, int slot) {
+    return nodev<DIM>(f, off + p.i0, slot) * p.gy0 + nodev<DIM>(f, off + p.i1, slot) * p.gy1 +
+           nodev<DIM>(f, off + p.i2, slot) * p.gy2;
+}
+
+}  // namespace cg

@@ -1,0 +1,45 @@
+// cg_internal.h -- launchers shared between the C-ABI layer (cg_api.cu) and
+// the kernel translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cg_device.cuh"
+
+namespace cg {
+
+// Raw node fields on the device, planar: frames[t][f][node] for the raw
+// field ids below (absent fields are not stored; raw_slot[f] == -1).
+enum RawField { RF_ZS = 0, RF_UX, RF_UY, RF_UZ, RF_KT, RF_EP, RF_ZB, RF_COUNT };
+
+struct DevFrames {
+    const double* frames;   // [ntimes][nraw][nnodes]
+    int nraw;
+    int raw_slot[RF_COUNT]; // position of each raw field in a frame, -1 if absent
+    int64_t nnodes;         // npoints * nlayers
+    int dim;
+};
+
+// Time interpolation + nodal diffusivity into the packed per-node record
+// (eulerian_field_set.pyx:866-938 and 1995-1997).  frozen: copy record 0.
+void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac_keps,
+                  void* cur, int precision, cudaStream_t st);
+
+// One fused step over every particle of a run (plain FP64 form).
+void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
+                       int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
+                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+
+// Solver.initialize_particle_state for particles with tri == -2.
+void launch_init_plain(int dim, const DevMesh& m, const void* cur, int npoints, int nlayers,
+                       const DevParams& p, const DevState& s, int velocity_init, uint32_t* err,
+                       cudaStream_t st);
+
+// rng[i] = pcg32_seed(seed, tag[i])
+void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);
+
+// bytes of one packed node record
+inline int record_values(int dim) { return dim == 2 ? Slots<2>::NF : Slots<3>::NF; }
+
+}  // namespace cg

@@ -1,0 +1,481 @@
+// cg_step.cuh -- the fused per-particle step (one thread per particle).
+//
+// One launch replaces the body of the particle loop of Solver.forward
+// (cylag/core/solver.pyx:459-524): the LSM update (advection scheme,
+// diffusion with k-epsilon drift, buoyancy), re-localization by path walk,
+// and the boundary conditions (wall rebound, open exit, bed/surface
+// reflection, deletion).  Everything for one particle stays in registers;
+// the only global traffic is the particle's own state and the gathers of
+// its element's mesh and node data (L2-resident for meshes up to ~1e6
+// triangles).
+#pragma once
+
+#include "cg_device.cuh"
+
+namespace cg {
+
+__constant__ ZigTables c_zig = {CG_ZIG_KN_INIT, CG_ZIG_WN_INIT, CG_ZIG_FN_INIT};
+
+template <int DIM, typename FT>
+struct Particle {
+    const DevMesh& m;
+    const DevFields<FT>& f;
+    const DevParams& p;
+    const ZigTables& z;
+    Rng rng;
+    double x[3];      // position
+    double x0[3];     // position at step start (last_position)
+    double up[3];     // velocity
+    double us[3];     // fluid velocity seen
+    int tri, tri0, ltri, ll, ll0;
+    uint32_t err;
+    bool deleted;
+
+    __device__ Particle(const DevMesh& m_, const DevFields<FT>& f_, const DevParams& p_,
+                        const ZigTables& z_)
+        : m(m_), f(f_), p(p_), z(z_), err(0), deleted(false) {}
+
+    // ---- field interpolation -------------------------------------------------
+    // eulerian_field_set.pyx:1057-1115 (2D) and 1289-1394 (3D, zlocalize=0)
+    __device__ void velocity(int k, int l, double px, double py, double pz, double& ux,
+                             double& uy, double& uz) {
+        using S = Slots<DIM>;
+        P1 q = p1_at(m, k, px, py);
+        if (DIM == 2) {
+            ux = p1_eval<DIM>(f.cur, 0, q, S::UX);
+            uy = p1_eval<DIM>(f.cur, 0, q, S::UY);
+            uz = 0.;
+        } else {
+            if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ux = uy = uz = 0.; return; }
+            int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+            double zlp = p1_eval<DIM>(f.cur, jl, q, S::ZS);
+            double zup = p1_eval<DIM>(f.cur, ju, q, S::ZS);
+            double dz = zlp - zup;
+            if (fabs(dz) < EPSILON) { err |= ERR_DEGENERATE_LAYER; ux = uy = uz = 0.; return; }
+            double zf0 = (pz - zup) / dz;
+            double zf1 = (zlp - pz) / dz;
+            ux = zf0 * p1_eval<DIM>(f.cur, jl, q, S::UX) + zf1 * p1_eval<DIM>(f.cur, ju, q, S::UX);
+            uy = zf0 * p1_eval<DIM>(f.cur, jl, q, S::UY) + zf1 * p1_eval<DIM>(f.cur, ju, q, S::UY);
+            uz = zf0 * p1_eval<DIM>(f.cur, jl, q, Slots<3>::UZ) +
+                 zf1 * p1_eval<DIM>(f.cur, ju, q, Slots<3>::UZ);
+        }
+    }
+
+    // eulerian_field_set.pyx:1117-1182 (3D fields)
+    __device__ int z_localize(int k, double px, double py, double pz) {
+        if (k == -1) return PART_LOC_O;
+        P1 q = p1_at(m, k, px, py);
+        int nl = f.nlayers;
+        double zbp = p1_eval<DIM>(f.cur, 0, q, Slots<DIM>::ZS);
+        double zsp = p1_eval<DIM>(f.cur, (nl - 1) * f.npoints, q, Slots<DIM>::ZS);
+        int l = lower_layer_index(nl, zsp, zbp, pz);
+        if (pz < zbp) l = PART_LOC_B;
+        else if (pz > zsp) l = PART_LOC_A;
+        return l;
+    }
+
+    // eulerian_field_set.pyx:994-1055 (zs at layer l)
+    __device__ double zs_at(int k, int l, double px, double py) {
+        P1 q = p1_at(m, k, px, py);
+        return p1_eval<DIM>(f.cur, l * f.npoints, q, Slots<DIM>::ZS);
+    }
+
+    // eulerian_field_set.pyx:1644-1763
+    __device__ void diffusivity(int k, int l, double px, double py, double pz, double& K,
+                                double& dKdx, double& dKdy, double& dKdz) {
+        using S = Slots<DIM>;
+        P1 q = p1_at(m, k, px, py);
+        if (DIM == 2) {
+            double kn0 = nodev<DIM>(f.cur, q.i0, S::K), kn1 = nodev<DIM>(f.cur, q.i1, S::K),
+                   kn2 = nodev<DIM>(f.cur, q.i2, S::K);
+            double Kp = kn0 * q.f0 + kn1 * q.f1 + kn2 * q.f2;
+            dKdx = kn0 * q.gx0 + kn1 * q.gx1 + kn2 * q.gx2;
+            dKdy = kn0 * q.gy0 + kn1 * q.gy1 + kn2 * q.gy2;
+            dKdz = 0.;
+            K = fmax(0., Kp);
+            return;
+        }
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; K = dKdx = dKdy = dKdz = 0.; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        double Kl = p1_eval<DIM>(f.cur, jl, q, S::K);
+        double gxl = p1_gx<DIM>(f.cur, jl, q, S::K);
+        double gyl = p1_gy<DIM>(f.cur, jl, q, S::K);
+        double zlp = p1_eval<DIM>(f.cur, jl, q, S::ZS);
+        double zlx = p1_gx<DIM>(f.cur, jl, q, S::ZS);
+        double zly = p1_gy<DIM>(f.cur, jl, q, S::ZS);
+        double Ku = p1_eval<DIM>(f.cur, ju, q, S::K);
+        double gxu = p1_gx<DIM>(f.cur, ju, q, S::K);
+        double gyu = p1_gy<DIM>(f.cur, ju, q, S::K);
+        double zup = p1_eval<DIM>(f.cur, ju, q, S::ZS);
+        double zux = p1_gx<DIM>(f.cur, ju, q, S::ZS);
+        double zuy = p1_gy<DIM>(f.cur, ju, q, S::ZS);
+        double dz = zup - zlp;
+        if (fabs(dz) < EPSILON) { err |= ERR_DEGENERATE_LAYER; K = dKdx = dKdy = dKdz = 0.; return; }
+        double s = (pz - zlp) / dz;
+        double Kp = (1. - s) * Kl + s * Ku;
+        dKdz = (Ku - Kl) / dz;
+        dKdx = (1. - s) * gxl + s * gxu - dKdz * ((1. - s) * zlx + s * zux);
+        dKdy = (1. - s) * gyl + s * gyu - dKdz * ((1. - s) * zly + s * zuy);
+        K = fmax(0., Kp);
+    }
+
+    // lagrangian_particle_set.pyx:834-890 (model_hr = 0)
+    __device__ double buoyancy_velocity(double dp) {
+        if (p.buoy_model == 0) return p.buoy_wb;
+        double s = p.density / p.rho0, wb;
+        if (dp < 1.e-4) {
+            wb = fabs(s - 1.) * (GRAV * (dp * dp)) / (18. * NU0);
+        } else if (dp > 1.e-3) {
+            wb = sqrt(fabs(s - 1.) * (4. * dp * GRAV) / (3. * p.drag_coef));
+        } else {
+            wb = (10. * NU0 / dp) * (sqrt(1. + fabs(s - 1.) * GRAV * pow(dp, 3.0) / (100. * (NU0 * NU0))) - 1.);
+        }
+        if (s > 1.) wb *= -1.;
+        return wb;
+    }
+
+    // ---- LSM1 (cylag/lsm/update_state_lsm1.pyx) ----------------------------------
+    __device__ void set_up_us(double ux, double uy, double uz) {
+        up[0] = ux; up[1] = uy; us[0] = ux; us[1] = uy;
+        if (DIM == 3) { up[2] = uz; us[2] = uz; }
+    }
+
+    // update_state_lsm1.pyx:228-248; true when the scheme stops at this stage
+    __device__ bool stage_locate(double xt, double yt, double zt, int& tt, int& tl, int& bnd) {
+        ltri = tri;
+        xy_localize(m, ltri, x0[0], x0[1], xt, yt, tt, bnd);
+        tl = 0;
+        if (DIM == 3) tl = z_localize(tt, xt, yt, zt);
+        if (bnd != -1 || (DIM == 3 && (tl == -2 || tl == -3))) {
+            tri = tt;
+            if (DIM == 3) ll = tl;
+            x[0] += up[0] * p.dt;
+            x[1] += up[1] * p.dt;
+            if (DIM == 3) x[2] += up[2] * p.dt;
+            return true;
+        }
+        return false;
+    }
+
+    // update_state_lsm1.pyx:135-656
+    __device__ int advect_lsm1() {
+        double dt = p.dt, ux, uy, uz;
+        velocity(tri, ll, x[0], x[1], DIM == 3 ? x[2] : 0., ux, uy, uz);
+        set_up_us(ux, uy, uz);
+        if (p.time_scheme == 1) {  // 135-177
+            x[0] += ux * dt;
+            x[1] += uy * dt;
+            if (DIM == 3) x[2] += uz * dt;
+            return -1;
+        }
+        int tt, tl, bnd;
+        double xt, yt, zt = 0.;
+        if (p.time_scheme == 2) {  // 179-274
+            xt = x[0] + 0.5 * ux * dt;
+            yt = x[1] + 0.5 * uy * dt;
+            if (DIM == 3) zt = x[2] + 0.5 * uz * dt;
+            if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+            velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+            x[0] += ux * dt;
+            x[1] += uy * dt;
+            if (DIM == 3) x[2] += uz * dt;
+            return -1;
+        }
+        double k1x = ux * dt, k1y = uy * dt, k1z = DIM == 3 ? uz * dt : 0.;
+        if (p.time_scheme == 3) {  // 276-432
+            xt = x[0] + (1. / 3.) * k1x;
+            yt = x[1] + (1. / 3.) * k1y;
+            zt = DIM == 3 ? x[2] + (1. / 3.) * k1z : 0.;
+            if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+            velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+            double k2x = ux * dt, k2y = uy * dt, k2z = DIM == 3 ? uz * dt : 0.;
+            xt = x[0] + (2. / 3.) * k2x;
+            yt = x[1] + (2. / 3.) * k2y;
+            zt = DIM == 3 ? x[2] + (2. / 3.) * k2z : 0.;
+            if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+            velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+            double k3x = ux * dt, k3y = uy * dt, k3z = DIM == 3 ? uz * dt : 0.;
+            x[0] += (0.25 * k1x + 0.75 * k3x);
+            x[1] += (0.25 * k1y + 0.75 * k3y);
+            if (DIM == 3) x[2] += (0.25 * k1z + 0.75 * k3z);
+            return -1;
+        }
+        // time_scheme 4, 434-656
+        xt = x[0] + 0.5 * k1x;
+        yt = x[1] + 0.5 * k1y;
+        zt = DIM == 3 ? x[2] + 0.5 * k1z : 0.;
+        if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+        velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+        double k2x = ux * dt, k2y = uy * dt, k2z = DIM == 3 ? uz * dt : 0.;
+        xt = x[0] + 0.5 * k2x;
+        yt = x[1] + 0.5 * k2y;
+        zt = DIM == 3 ? x[2] + 0.5 * k2z : 0.;
+        if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+        velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+        double k3x = ux * dt, k3y = uy * dt, k3z = DIM == 3 ? uz * dt : 0.;
+        xt = x[0] + k3x;
+        yt = x[1] + k3y;
+        zt = DIM == 3 ? x[2] + k3z : 0.;
+        if (stage_locate(xt, yt, zt, tt, tl, bnd)) return bnd;
+        velocity(tt, tl, xt, yt, zt, ux, uy, uz);
+        double k4x = ux * dt, k4y = uy * dt, k4z = DIM == 3 ? uz * dt : 0.;
+        x[0] += (k1x + 2. * k2x + 2. * k3x + k4x) / 6.;
+        x[1] += (k1y + 2. * k2y + 2. * k3y + k4y) / 6.;
+        if (DIM == 3) x[2] += (k1z + 2. * k2z + 2. * k3z + k4z) / 6.;
+        return -1;
+    }
+
+    // update_state_lsm1.pyx:658-726
+    __device__ void diffusion_lsm1() {
+        double dt = p.dt;
+        double xix = 0., xiy = 0., xiz = 0.;
+        double diffx, diffy, diffz = 0.;
+        double driftx = 0., drifty = 0., driftz = 0.;
+        if (p.diffmod == 2 || p.diffmod == 3) {
+            double Kp, dKdx, dKdy, dKdz;
+            diffusivity(tri0, ll0, x0[0], x0[1], DIM == 3 ? x0[2] : 0., Kp, dKdx, dKdy, dKdz);
+            diffx = sqrt(2. * Kp) * p.sqrtdt;
+            diffy = diffx;
+            driftx = dKdx * dt;
+            drifty = dKdy * dt;
+            if (DIM == 3) {
+                if (p.diffmod == 2) {
+                    diffz = p.diffz_const;
+                } else {
+                    diffz = diffx;
+                    driftz = dKdz * dt;
+                }
+            }
+        } else {
+            diffx = p.diffx_const;
+            diffy = diffx;
+            if (DIM == 3) diffz = p.diffz_const;
+        }
+        if (diffx != 0.) rng_pair(rng, p.rng_method, z, xix, xiy);
+        if (DIM == 3 && diffz != 0.) xiz = rng_single(rng, p.rng_method, z);
+        x[0] += driftx + diffx * xix;
+        x[1] += drifty + diffy * xiy;
+        if (DIM == 3) x[2] += driftz + diffz * xiz;
+    }
+
+    // update_state_lsm1.pyx:30-133
+    __device__ int update_lsm1(double dp) {
+        int bnd_j = advect_lsm1();
+        if (p.diffmod != 0) diffusion_lsm1();
+        if (DIM == 3) {
+            double wb = buoyancy_velocity(dp);
+            x[2] += wb * p.dt;
+            up[2] += wb;
+        }
+        if (bnd_j == -1) {
+            ltri = tri;
+            xy_localize(m, ltri, x0[0], x0[1], x[0], x[1], tri, bnd_j);
+            if (DIM == 3) ll = z_localize(tri, x[0], x[1], x[2]);
+        }
+        return bnd_j;
+    }
+
+    // ---- boundary conditions (compute_bc.pyx:35-395) ----------------------------
+    // compute_bc.pyx:190-240 (normal2u utils.pyx:99-119)
+    __device__ void reflect(double* v, double ex0, double ey0, double ex1, double ey1,
+                            bool damp_vel) {
+        double norm = sqrt((ex1 - ex0) * (ex1 - ex0) + (ey1 - ey0) * (ey1 - ey0));
+        double nx = (ey0 - ey1) / norm;
+        double ny = (ex1 - ex0) / norm;
+        if (p.bc_type == 2 && p.roughness > 0.) {
+            double max_theta = 85.0 * DEG_TO_RAD;
+            double theta = rng_single(rng, p.rng_method, z) * p.roughness;
+            theta = fmax(-max_theta, fmin(max_theta, theta));
+            double ct = cos(theta), st = sin(theta);
+            double nnx = nx * ct - ny * st;
+            double nny = nx * st + ny * ct;
+            nx = nnx; ny = nny;
+        }
+        double u0 = v[0];
+        v[0] = u0 * nx + v[1] * ny;
+        v[1] = -u0 * ny + v[1] * nx;
+        v[0] = -1. * v[0];
+        u0 = v[0];
+        v[0] = u0 * nx - v[1] * ny;
+        v[1] = u0 * ny + v[1] * nx;
+        if (damp_vel) {
+            v[0] *= 1. - p.damp;
+            v[1] *= 1. - p.damp;
+            if (DIM == 3) v[2] *= 1. - p.damp;
+        }
+    }
+
+    __device__ void count_open(int* stats, int label) {
+        if (p.bnd_statistics && stats) atomicAdd(&stats[label - 1], 1);
+    }
+
+    __device__ void compute_bc(int bnd_j, int* stats) {
+        double damp = p.damp;
+        bool strand_condition = false;
+        if (bnd_j != -1) {
+            int lab = __ldg(&m.elabel[bnd_j]);
+            if (lab == BND_WALL_REF && p.strand > 0.) strand_condition = rng_uniform(rng) < p.strand;
+            if (lab == BND_WALL_REF && !strand_condition) {
+                int bnd_jj = bnd_j;
+                for (int rc = 0; tri == PART_LOC_O && rc < p.max_rebounds; ++rc) {
+                    int4 e = __ldg(&m.edge[bnd_jj]);
+                    double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+                    // intersections.pyx:27-62
+                    double coef = 1. - damp / 2.;
+                    double nx = a.y - b.y, ny = b.x - a.x;
+                    double norm2 = nx * nx + ny * ny;
+                    double dist = (x[0] - a.x) * nx + (x[1] - a.y) * ny;
+                    double px = x[0] - 2. * ((dist * coef) / norm2) * nx;
+                    double py = x[1] - 2. * ((dist * coef) / norm2) * ny;
+                    x[0] = px;
+                    x[1] = py;
+                    xy_localize(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
+                    if (tri == PART_LOC_O && bnd_jj != -1) {
+                        int lj = __ldg(&m.elabel[bnd_jj]);
+                        if (lj >= BND_OPEN_REF) {
+                            count_open(stats, lj);
+                            deleted = true;
+                            break;
+                        }
+                    }
+                    if (p.model == 0 || p.model >= 2) reflect(up, a.x, a.y, b.x, b.y, true);
+                    if (p.model == 3) reflect(us, a.x, a.y, b.x, b.y, false);
+                    if (tri == PART_LOC_O && bnd_jj == -1) break;
+                }
+                if (DIM == 3 && !deleted && tri != PART_LOC_O) ll = z_localize(tri, x[0], x[1], x[2]);
+            }
+            if (lab >= BND_OPEN_REF) {
+                if (!deleted) count_open(stats, lab);
+                deleted = true;
+            }
+        }
+        if (deleted) return;
+        // compute_bc.pyx:287-374
+        if (DIM == 3) {
+            for (int side = 0; side < 2; ++side) {
+                int want = side == 0 ? PART_LOC_B : PART_LOC_A;
+                if (!(ll == want && tri != PART_LOC_O)) continue;
+                double zbp = zs_at(tri, 0, x[0], x[1]);
+                double zsp = zs_at(tri, f.nlayers - 1, x[0], x[1]);
+                double hp = fmax(0., zsp - zbp);
+                if (side == 0) {
+                    double dz = fabs(zbp - x[2]);
+                    x[2] = fmin(zbp + (1. - damp) * dz, zbp + 0.5 * hp);
+                } else {
+                    double dz = fabs(x[2] - zsp);
+                    x[2] = fmax(zsp - (1. - damp) * dz, zsp - 0.5 * hp);
+                }
+                ll = lower_layer_index(f.nlayers, zsp, zbp, x[2]);
+                double sg = side == 0 ? 1. : -1.;
+                if (p.model >= 2) up[2] = sg * fabs(up[2]) * (1. - damp);
+                if (p.model == 3) us[2] = sg * fabs(us[2]) * (1. - damp);
+            }
+        }
+        // compute_bc.pyx:378-395
+        if (tri == PART_LOC_O || ll == PART_LOC_B || ll == PART_LOC_A) deleted = true;
+    }
+};
+
+// aux: 0 = state only; 1 = also write velocity / fluid velocity seen;
+//      2 = also write last_position / last_velocity / last_tri (the last
+//      step of a batch, so that every public array is current afterwards).
+template <int DIM, typename FT>
+__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+                                                   DevState s, int aux, int step_index,
+                                                   int* __restrict__ stats,
+                                                   uint32_t* __restrict__ err_word) {
+    __shared__ ZigTables zt;
+    for (int t = threadIdx.x; t < 128; t += blockDim.x) {
+        zt.kn[t] = c_zig.kn[t];
+        zt.wn[t] = c_zig.wn[t];
+        zt.fn[t] = c_zig.fn[t];
+    }
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    int tri = s.tri[i];
+    if (tri < 0) return;  // inactive (-1) or awaiting initialization (-2)
+
+    Particle<DIM, FT> q(m, f, p, zt);
+    q.tri = tri;
+    q.tri0 = tri;
+    q.ltri = tri;
+    q.ll = DIM == 3 ? s.lowerlayer[i] : 0;
+    q.ll0 = q.ll;
+    const int D = DIM;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        q.x[d] = s.pos[(size_t)i * D + d];
+        q.x0[d] = q.x[d];
+    }
+    bool need_vel = (p.model >= 2) || aux >= 2;
+    if (need_vel) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)i * D + d];
+    }
+    double lastv[3] = {q.up[0], q.up[1], DIM == 3 ? q.up[2] : 0.};
+    if (p.model == 3) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)i * D + d];
+    }
+    q.rng.state = s.rng[i];
+    q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
+    q.rng.err = 0;
+    double dp = DIM == 3 ? s.diameter[i] : 0.;
+
+    int bnd_j = -1;
+    if (p.model == 1) bnd_j = q.update_lsm1(dp);
+    else q.err |= ERR_UNSUPPORTED;
+
+    if (p.bc_on) {
+        q.compute_bc(bnd_j, stats);
+    } else if (q.tri == PART_LOC_O || q.ll == PART_LOC_B || q.ll == PART_LOC_A) {
+        q.deleted = true;
+    }
+
+    uint32_t e = q.err | q.rng.err;
+    if (e) atomicOr(err_word, e);
+
+    if (q.deleted) {
+        // lagrangian_particle_set.pyx:766-788; the tag records the step for
+        // the host-side retag (maxtag+1, ... in step then index order)
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            s.pos[(size_t)i * D + d] = 0.;
+            s.vel[(size_t)i * D + d] = 0.;
+            s.fvs[(size_t)i * D + d] = 0.;
+            s.last_pos[(size_t)i * D + d] = 0.;
+            s.last_vel[(size_t)i * D + d] = 0.;
+        }
+        s.diameter[i] = 0.;
+        s.tri[i] = -1;
+        s.last_tri[i] = -1;
+        s.lowerlayer[i] = 0;
+        s.tag[i] = -2 - step_index;
+        s.rng[i] = q.rng.state;
+        return;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = q.x[d];
+    s.tri[i] = q.tri;
+    if (DIM == 3) s.lowerlayer[i] = q.ll;
+    s.rng[i] = q.rng.state;
+    if (p.model >= 2 || aux >= 1) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) s.vel[(size_t)i * D + d] = q.up[d];
+    }
+    if (p.model == 3 || aux >= 1) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) s.fvs[(size_t)i * D + d] = q.us[d];
+    }
+    if (aux >= 2) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            s.last_pos[(size_t)i * D + d] = q.x0[d];
+            s.last_vel[(size_t)i * D + d] = lastv[d];
+        }
+        s.last_tri[i] = q.ltri;
+    }
+}
+
+}  // namespace cg

@@ -1,0 +1,174 @@
+/*
+ * cylag_gpu.h -- C ABI of libcylag_gpu.so, the GB300 (sm_103a) particle step.
+ *
+ * Plain C types only: sizes, host pointers for one-time uploads, device
+ * pointers for the particle state (the caller allocates and owns them, e.g.
+ * as torch tensors; the library never frees caller memory).  Every call
+ * returns an int status: CG_OK (0) or a negative CG_E* code, with the message
+ * available from cg_last_error().  No C++ exception crosses this boundary.
+ * One host thread per context; work is issued on the context's own CUDA
+ * stream (cg_ctx_stream) and is asynchronous unless stated otherwise.
+ *
+ * Each entry point names the reference interface it replaces (CyLag, paths
+ * relative to the CyLag source tree).
+ */
+#ifndef CYLAG_GPU_H
+#define CYLAG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_OK 0
+#define CG_EINVAL (-1)        /* bad argument (reference: ValueError) */
+#define CG_ECUDA (-2)         /* CUDA runtime error */
+#define CG_ENOMEM_BUDGET (-3) /* admission refused: HBM budget exceeded */
+#define CG_EDEVICE (-4)       /* device-side error flag (see cg_run_errors) */
+#define CG_ESTATE (-5)        /* call out of order (mesh/fields not uploaded) */
+
+/* device error flags, OR-ed into the run's error word */
+#define CG_ERR_INTERP_OUTSIDE 1   /* interpolation below bed / above surface
+                                     (eulerian_field_set.pyx:1270-1276) */
+#define CG_ERR_DEGENERATE_LAYER 2 /* |dz| < EPSILON between layers (1356-1363) */
+#define CG_ERR_RNG_LIMIT 4        /* a rejection loop hit its iteration cap */
+#define CG_ERR_UNSUPPORTED 8      /* option combination not built */
+
+#define CG_PRECISION_FP64 0       /* plain form: FP64 end to end */
+#define CG_PRECISION_MIXED 1      /* FP32 fields/updates, FP64 position + localization */
+
+typedef struct cg_ctx cg_ctx;
+typedef struct cg_run cg_run;
+
+/* Mesh arrays exactly as cylag.TriangularMesh holds them
+ * (cylag/geom/triangular_mesh.pyx:28-629), plus the point-location grid
+ * that replaces its KD-tree (triangular_mesh.pyx:602-629). Host pointers. */
+typedef struct {
+    int32_t nv, nt, ne, nopen;
+    const double *x, *y;             /* [nv] */
+    const int32_t *triangles;        /* [nt][3] */
+    const double *gradx, *grady, *det; /* [nt][3] */
+    const int32_t *edges;            /* [ne][2] */
+    const int32_t *triedge_map;      /* [nt][3] */
+    const int32_t *edgetri_map;      /* [ne][2] */
+    const int32_t *edges_labels;     /* [ne] */
+    double grid_x0, grid_y0, grid_inv_cell;
+    int32_t grid_nx, grid_ny;
+    const int32_t *grid_start;       /* [grid_nx*grid_ny + 1] */
+    const int32_t *grid_tris;        /* [grid_start[last]] */
+} cg_mesh_desc;
+
+/* Node fields as cylag.EulerianFieldSet holds them
+ * (cylag/core/eulerian_field_set.pyx:125-256): each [ntimes][npoints*nlayers],
+ * layer l at [l*npoints, (l+1)*npoints).  NULL for an absent field. Host. */
+typedef struct {
+    int32_t dim, nlayers, npoints, ntimes;
+    const double *times;             /* [ntimes] */
+    const double *elevation;         /* field id 0 */
+    const double *velocity_x, *velocity_y, *velocity_z; /* ids 1-3 */
+    const double *turbulent_energy;  /* 'TURBULENT ENERG.' */
+    const double *dissipation;       /* 'DISSIPATION' */
+    const double *bottom;            /* 'BOTTOM' */
+} cg_fields_desc;
+
+/* Parameters (cylag/cylag_dico.py:9-51, cylag/core/parameters.pyx:116-195)
+ * and the particle-set scalars (cylag/core/lagrangian_particle_set.pyx:158-261). */
+typedef struct {
+    int32_t model, time_scheme, rng_method, diffusion_model;
+    int32_t diffusion_lsm2_option, lsm3_edge_opt;
+    int32_t boundary_conditions, boundary_conditions_type, max_wall_rebounds;
+    int32_t bnd_statistics, particle_velocity_init, frozen_eulerian_fields;
+    double initial_time, final_time, time_step;
+    double horizontal_diffusivity, vertical_diffusivity, schmidt_number;
+    double tl_horizontal, tl_vertical;
+    double rebound_damping_coef, wall_roughness_angle, stranding_probability;
+    double water_density;
+    /* particle set */
+    int32_t dim;
+    double particle_density;
+    int32_t drag_coefficient_model; double drag_coefficient;
+    int32_t added_mass_force; double added_mass_coef;
+    int32_t buoyancy_velocity_model; double buoyancy_velocity;
+    /* GPU-only */
+    int32_t precision;               /* CG_PRECISION_* */
+    uint64_t seed;                   /* PCG32 streams: pcg32_seed(seed, tag) */
+} cg_params;
+
+/* Particle state: device pointers in the reference layout
+ * (cylag/core/lagrangian_particle_set.pxd): rows of dim doubles.
+ * tri == -1 marks an inactive particle, tri == -2 one awaiting
+ * initialization (lagrangian_particle_set.pyx:620-710). */
+typedef struct {
+    int32_t n;
+    double *position, *velocity, *fluid_velocity_seen;   /* [n][dim] */
+    double *last_position, *last_velocity;               /* [n][dim] */
+    int32_t *tri, *last_tri, *lowerlayer, *tag;          /* [n] */
+    double *diameter;                                    /* [n] */
+    uint64_t *rng_state;                                 /* [n] PCG32 state */
+} cg_state_desc;
+
+/* ---- context ---------------------------------------------------------- */
+/* Creates a context on `device` with its own stream; hbm_budget_bytes bounds
+ * what cg_run_create may admit (0 = no bound).  No reference counterpart:
+ * the reference holds everything in Python objects. */
+int cg_ctx_create(int32_t device, uint64_t hbm_budget_bytes, cg_ctx **out);
+int cg_ctx_destroy(cg_ctx *ctx);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int cg_last_error(const cg_ctx *ctx, char *buf, uint64_t len);
+/* The context's cudaStream_t, as an integer handle. */
+uint64_t cg_ctx_stream(const cg_ctx *ctx);
+int cg_ctx_sync(cg_ctx *ctx);
+
+/* Replaces TriangularMesh.__init__ (triangular_mesh.pyx:75-179): packs and
+ * uploads the mesh once.  Synchronous. */
+int cg_mesh_upload(cg_ctx *ctx, const cg_mesh_desc *mesh);
+
+/* Replaces EulerianFieldSet.__init__ + _init_tmp
+ * (eulerian_field_set.pyx:125-256, 743-776): uploads every time record.
+ * Synchronous. */
+int cg_fields_upload(cg_ctx *ctx, const cg_fields_desc *fields);
+
+/* ---- runs ------------------------------------------------------------- */
+/* Replaces Solver.__init__ up to the particle loop (solver.pyx:74-197):
+ * checks, time state, model coefficients.  `state` points to caller-owned
+ * device buffers.  Fails with CG_ENOMEM_BUDGET when the run's bytes would
+ * exceed the context budget. */
+int cg_run_create(cg_ctx *ctx, const cg_params *params,
+                  const cg_state_desc *state, cg_run **out);
+int cg_run_destroy(cg_run *run);
+
+/* Seeds the per-particle PCG32 streams: rng_state[i] = pcg32_seed(seed, tag[i])
+ * (random_utils.pyx:30-37). */
+int cg_run_seed(cg_run *run);
+
+/* Replaces Solver.initialize_particle_state for every particle with
+ * tri == -2 (solver.pyx:238-379): point location, vertical clamp, velocity
+ * initialization.  Asynchronous. */
+int cg_run_init(cg_run *run);
+
+/* Replaces `nsteps` calls of Solver.forward (solver.pyx:413-585): time
+ * interpolation of the fields at each step-start time, the fused particle
+ * step, time += dt.  bnd_stats_host (optional) receives [nsteps][nopen]
+ * open-boundary exit counts (solver.pyx:567-572).  Synchronous: returns
+ * after the last step, CG_EDEVICE if the device raised an error flag. */
+int cg_run_step(cg_run *run, int32_t nsteps, int32_t *bnd_stats_host);
+
+/* Current simulated time and iteration (cylag/core/simutime.pyx:77-84). */
+int cg_run_time(const cg_run *run, double *time, int64_t *iteration);
+
+/* Device error word accumulated since the last call (then cleared). */
+int cg_run_errors(cg_run *run, uint32_t *flags);
+
+/* Number of active particles and deleted-this-call counts are derived by the
+ * caller from tri (tri == -1 inactive). */
+
+/* ---- measurement ------------------------------------------------------ */
+/* Mean device time (ms) of the step kernel over the last cg_run_step call,
+ * measured with CUDA events on the context stream. */
+int cg_run_last_kernel_ms(const cg_run *run, double *ms, int32_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,98 @@
+"""The oracle (C restatement) pinned against the reference's own outputs.
+
+Golden fixtures come from the compiled reference (tests/golden/make_golden.py).
+On x86-64 the oracle must reproduce them bit for bit; elsewhere integer
+state stays bit-exact and floating state agrees to 1e-10.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, X86, assert_state_close, golden_names, load_golden, run_oracle
+
+
+def test_rng_streams_match_reference(oracle_lib):
+    z = np.load(GOLDEN / "rng.npz")
+    pairs = z["pairs"]
+    for j, (seed, stream) in enumerate(pairs.tolist()):
+        np.testing.assert_array_equal(oracle_lib.rng_draws(seed, stream, 0, 512), z[f"uniform_{j}"])
+        np.testing.assert_array_equal(oracle_lib.rng_draws(seed, stream, 1, 512), z[f"zig_{j}"])
+        np.testing.assert_array_equal(oracle_lib.rng_draws(seed, stream, 2, 256), z[f"polar_{j}"])
+        np.testing.assert_array_equal(oracle_lib.rng_draws(seed, stream, 3, 128, method=3), z[f"pair3_{j}"])
+        np.testing.assert_array_equal(oracle_lib.rng_draws(seed, stream, 3, 128, method=1), z[f"pair1_{j}"])
+
+
+def test_pcg32_advance_matches_reference(oracle_lib):
+    import ctypes as C
+    z = np.load(GOLDEN / "rng.npz")
+    L = oracle_lib.lib()
+    for j, (seed, stream) in enumerate(z["pairs"].tolist()):
+        st, inc = oracle_lib.pcg32_seed(seed, stream)
+        s = np.array([st], np.uint64)
+        L.cgo_pcg32_advance(s.ctypes.data, inc, 1000)
+        # next 16 uniforms from the advanced state (PCG32 output function)
+        out = []
+        state = int(s[0])
+        for _ in range(16):
+            old = state
+            state = (old * 6364136223846793005 + inc) & (2**64 - 1)
+            xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+            rot = old >> 59
+            out.append((((xs >> rot) | (xs << ((32 - rot) & 31))) & 0xFFFFFFFF) / 4294967296.0)
+        np.testing.assert_array_equal(np.array(out), z[f"adv_{j}"])
+
+
+def test_seed_streams_vectorized(oracle_lib):
+    tags = np.arange(0, 5000, 37)
+    st, inc = oracle_lib.seed_streams(3, tags)
+    for t, s, i in zip(tags, st, inc):
+        assert (int(s), int(i)) == oracle_lib.pcg32_seed(3, int(t))
+
+
+def test_ziggurat_tables_pinned(oracle_lib):
+    z = np.load(GOLDEN / "rng.npz")
+    big = oracle_lib.rng_draws(0, 99, 1, 200_000)
+    digest = np.frombuffer(hashlib.sha256(big.tobytes()).digest(), dtype=np.uint8)
+    if X86:
+        np.testing.assert_array_equal(digest, z["zig_big_sha256"])
+
+
+def test_ziggurat_tables_equal_device_header(oracle_lib):
+    """The device kernels use generated hex-float tables; they must equal
+    the tables the reference recurrence gives with the host libm."""
+    import importlib.util
+    from conftest import ROOT
+    spec = importlib.util.spec_from_file_location(
+        "gz", ROOT / "cylag_gb300" / "csrc" / "gen_ziggurat_tables.py")
+    gz = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gz)
+    kn, wn, fn = gz.tables()
+    okn, own, ofn = oracle_lib.ziggurat_tables()
+    np.testing.assert_array_equal(okn, np.array(kn, dtype=np.uint32))
+    np.testing.assert_array_equal(own, np.array(wn))
+    np.testing.assert_array_equal(ofn, np.array(fn))
+    text = (ROOT / "cylag_gb300" / "csrc" / "ziggurat_tables.h").read_text()
+    for v in wn + fn:
+        assert v.hex() in text
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_trajectories_match_reference(oracle_lib, name):
+    case, meta, want = load_golden(name)
+    o = run_oracle(case, meta)
+    got = dict(position=o.pos, velocity=o.vel, fluid_velocity_seen=o.fvs, tri=o.tri,
+               inactive=o.inactive, lowerlayer=o.lowerlayer, last_position=o.last_pos)
+    assert_state_close(got, want, exact=X86, what=name)
+    if meta["params"].get("bnd_statistics"):
+        np.testing.assert_array_equal(np.stack(o.bnd_stats), want["bnd_stats"])
+
+
+@pytest.mark.parametrize("name", ["keps_ts1_rm2", "open"])
+def test_oracle_threads_do_not_change_results(oracle_lib, name):
+    case, meta, want = load_golden(name)
+    a = run_oracle(case, meta, nthreads=1)
+    b = run_oracle(case, meta, nthreads=4)
+    np.testing.assert_array_equal(a.pos, b.pos)
+    np.testing.assert_array_equal(a.tri, b.tri)
+    np.testing.assert_array_equal(a.tag, b.tag)
