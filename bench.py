@@ -42,13 +42,22 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both")
     ap.add_argument("--npart", type=int, default=10_000_000)
     ap.add_argument("--nx", type=int, default=1001)
     ap.add_argument("--ny", type=int, default=251)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
+
+
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Phase log on stderr (the JSON line alone goes to stdout)."""
+    if os.environ.get("CYLAG_BENCH_QUIET") != "1":
+        print(f"[bench {time.perf_counter() - _T0:8.2f}s] {msg}", file=sys.stderr, flush=True)
 
 
 def dist_info():
@@ -194,33 +203,26 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def run_gpu_arm(args):
+def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
+    """Warm-up, then K timed steps (CUDA events on the library's stream),
+    then optionally K end-to-end steps through the C ABI with host buffers."""
     import torch
     import cylag_gb300 as cg
     from cylag_gb300 import _lib
-    rank, world, local = dist_info()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-    torch.cuda.set_device(local)
-    c = make_workload(args, rank)
-    params = dict(c["parameters"])
-    total_steps = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
-    if total_steps * params["time_step"] > 1200.0:
-        raise SystemExit("warmup + 2*steps must stay within the 1,200 s field records")
     from cylag_gb300.mesh import TriangularMesh
     mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
     fs = cg.EulerianFieldSet(mesh, dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
                              velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
                              opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
     ps = cg.LagrangianParticleSet(c["position"], dim=2)
-    solver = cg.Solver(fs, ps, params, precision=args.precision, seed=rank, device=local)
+    log(f"creating solver ({precision})")
+    solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local)
     L = solver.L
-    stream = torch.cuda.ExternalStream(L.cg_ctx_stream(solver._ctx), device=local)
+    # all library work on a torch-owned stream (torch manages its lifetime)
+    stream = torch.cuda.Stream(device=local)
+    _lib.check(solver._ctx, L.cg_ctx_set_stream(solver._ctx, stream.cuda_stream))
     n = ps.npart
-
-    # warm-up
+    log("warm-up")
     solver.forward(nsteps=args.warmup)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -231,6 +233,7 @@ def run_gpu_arm(args):
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    log("timed region")
     ev0.record(stream)
     solver.forward(nsteps=args.steps)
     ev1.record(stream)
@@ -242,12 +245,14 @@ def run_gpu_arm(args):
         t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * n * args.steps / (ms / 1e3)
-
-    # end to end: host state (pinned) -> device, one step through the C ABI,
-    # device -> host, every step
-    e2e = None
-    if not args.no_e2e:
+    log(f"{precision}: timed {ms:.3f} ms, kernel {kern_ms:.4f} ms/launch")
+    res = {"precision": precision, "ms": ms, "kernel_ms": kern_ms, "launches": launches,
+           "value": world * n * args.steps / (ms / 1e3), "clocks": clk, "n": n,
+           "position": ps.position, "inactive": ps.inactive, "nt": int(mesh.nt)}
+    if do_e2e:
+        # end to end: host state (pinned) -> device, one step through the C
+        # ABI, device -> host, every step
+        log("end-to-end region")
         d = ps._dev
         keys_in = ("position", "tri", "tag", "rng_state")
         keys_out = ("position", "tri", "rng_state")
@@ -274,46 +279,87 @@ def run_gpu_arm(args):
         e1.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        del host
         ems = e0.elapsed_time(e1)
         if dist:
             t = torch.tensor([ems], dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ems = float(t.item())
-        e2e = {"value": world * n * args.steps / (ems / 1e3), "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "wall_s": wall}
+        res["e2e"] = {"value": world * n * args.steps / (ems / 1e3), "unit": UNIT,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "wall_s": wall}
+    torch.cuda.synchronize()
+    solver.close()
+    del ps, solver
+    torch.cuda.empty_cache()
+    return res
 
+
+def run_gpu_arm(args):
+    import torch
+    rank, world, local = dist_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    log("building workload")
+    c = make_workload(args, rank)
+    params = dict(c["parameters"])
+    total_steps = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
+    if total_steps * params["time_step"] > 1200.0:
+        raise SystemExit("warmup + 2*steps must stay within the 1,200 s field records")
+    forms = [args.precision] if args.precision != "both" else ["mixed", "fp64"]
+    res = {}
+    for prec in forms:
+        res[prec] = measure(args, c, params, prec, rank, world, local, dist,
+                            do_e2e=(not args.no_e2e and prec == forms[0]))
     if rank != 0:
         return
-    bpp = bytes_per_particle_step(args.precision)
+    main_form = forms[0]
+    r = res[main_form]
+    n = r["n"]
+    bpp = bytes_per_particle_step(main_form)
     peak, peak_kind = peaks()
-    achieved = bpp * n / (kern_ms / 1e3) / 1e9
+    achieved = bpp * n / (r["kernel_ms"] / 1e3) / 1e9
     traffic = os.environ.get("CYLAG_NCU_TRAFFIC_PER_LAUNCH")
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles_per_gpu": n, "triangles": int(mesh.nt),
-                   "precision": args.precision, "dt": params["time_step"],
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if main_form == "fp64" else "f32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles_per_gpu": n, "triangles": r["nt"],
+                   "precision": main_form, "dt": params["time_step"],
                    "l2": "state larger than L2 (no flush)", "model": "LSM1 Euler, k-eps drift"},
-        "gpu_launches": int(launches) + args.steps,  # step kernels + field blends
+        "gpu_launches": int(r["launches"]) + args.steps,  # step kernels + field blends
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": float(traffic) if traffic else None,
-                     "peak_kind": peak_kind, "kernel_ms": kern_ms,
+                     "peak_kind": peak_kind, "kernel_ms": r["kernel_ms"],
                      "bytes_per_particle_step": bpp},
-        "clocks": clk,
+        "clocks": r["clocks"],
     }
-    if e2e:
-        line["e2e"] = e2e
+    if "e2e" in r:
+        line["e2e"] = r["e2e"]
+    if "fp64" in res and main_form != "fp64":
+        from cylag_gb300.stats import displacement_report
+        q = res["fp64"]
+        act = (r["inactive"] == 0) & (q["inactive"] == 0)
+        rep = displacement_report(c["position"], r["position"], q["position"], act)
+        line["plain_fp64"] = {"value": q["value"], "kernel_ms": q["kernel_ms"],
+                              "ms_per_step": q["ms"] / args.steps, "clocks": q["clocks"]}
+        line["mixed_over_plain"] = r["value"] / q["value"]
+        line["mixed_error_vs_fp64"] = {
+            "steps": args.warmup + args.steps, "rms_displacement_diff_m": rep["rms_displacement_diff"],
+            "var_rel_err": max(rep["var_rel_err"]), "mean_rel_err": max(rep["mean_rel_err"])}
     if not args.no_cpu_baseline:
+        log("cpu baseline")
         threads = os.cpu_count() or 1
         nsample = int(os.environ.get("CYLAG_CPU_SAMPLE", "200000"))
         rate, dt = cpu_rate(c, params, nsample, 4, threads)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{nsample} particles x 4 steps of the workload"}
-    print(json.dumps(line))
-    solver.close()
+    print(json.dumps(line), flush=True)
+    log("done")
 
 
 def main():

@@ -80,6 +80,7 @@ SIGNATURES = [
     ("cg_ctx_destroy", C.c_int, [P]),
     ("cg_last_error", C.c_int, [P, C.c_char_p, C.c_uint64]),
     ("cg_ctx_stream", C.c_uint64, [P]),
+    ("cg_ctx_set_stream", C.c_int, [P, C.c_uint64]),
     ("cg_ctx_sync", C.c_int, [P]),
     ("cg_mesh_upload", C.c_int, [P, C.POINTER(MeshDesc)]),
     ("cg_fields_upload", C.c_int, [P, C.POINTER(FieldsDesc)]),

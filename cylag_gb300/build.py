@@ -28,6 +28,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "cg_api.cu": ["-fmad=false"],
     "cg_kernels_plain.cu": ["-fmad=false"],
+    "cg_kernels_mixed.cu": [],
 }
 
 

@@ -236,6 +236,8 @@ class LagrangianParticleSet:
         dev = torch.device("cuda", device)
         self._dev = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in self._host.items()}
         self._dev["rng_state"] = torch.zeros(self.npart, dtype=torch.int64, device=dev)
+        # the library works on its own (non-blocking) stream: make the copies land first
+        torch.cuda.synchronize(dev)
         self._host = None
         self._ctx = ctx
 

@@ -25,7 +25,8 @@ struct DevBuf {
 
 struct cg_ctx {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // stream all work is issued on
+    cudaStream_t own_stream = nullptr;  // the context's own stream
     uint64_t budget = 0;
     uint64_t used = 0;
     std::string err;
@@ -121,11 +122,12 @@ int cg_ctx_create(int32_t device, uint64_t hbm_budget_bytes, cg_ctx** out) {
     c->device = device;
     c->budget = hbm_budget_bytes;
     cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
         return CG_ECUDA;
     }
+    c->stream = c->own_stream;
     *out = c;
     return CG_OK;
 }
@@ -136,7 +138,8 @@ int cg_ctx_destroy(cg_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (auto& b : c->mesh_bufs) dfree(b);
     dfree(c->frames_buf);
-    cudaStreamDestroy(c->stream);
+    cudaStreamSynchronize(c->own_stream);
+    cudaStreamDestroy(c->own_stream);
     delete c;
     return CG_OK;
 }
@@ -148,6 +151,14 @@ int cg_last_error(const cg_ctx* c, char* buf, uint64_t len) {
 }
 
 uint64_t cg_ctx_stream(const cg_ctx* c) { return c ? (uint64_t)(uintptr_t)c->stream : 0; }
+
+int cg_ctx_set_stream(cg_ctx* c, uint64_t stream) {
+    if (!c) return CG_EINVAL;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)(uintptr_t)stream : c->own_stream;
+    return CG_OK;
+}
 
 int cg_ctx_sync(cg_ctx* c) {
     if (!c) return CG_EINVAL;
@@ -209,6 +220,24 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         basis[5 * k + 3] = make_double2(gy[0], gy[1]);
         basis[5 * k + 4] = make_double2(gy[2], 0.0);
     }
+    // exact-test geometry: vertices and edge vectors, FP64 subtractions as in
+    // utils.pyx:332-361; FP32 P1 gradients for the mixed form
+    std::vector<double2> geo(6 * (size_t)nt);
+    std::vector<float4> g32(2 * (size_t)nt);
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        double xa = d->x[t[0]], ya = d->y[t[0]], xb = d->x[t[1]], yb = d->y[t[1]];
+        double xc = d->x[t[2]], yc = d->y[t[2]];
+        geo[6 * k + 0] = make_double2(xa, ya);
+        geo[6 * k + 1] = make_double2(xb, yb);
+        geo[6 * k + 2] = make_double2(xc, yc);
+        geo[6 * k + 3] = make_double2(xb - xa, yb - ya);
+        geo[6 * k + 4] = make_double2(xc - xb, yc - yb);
+        geo[6 * k + 5] = make_double2(xa - xc, ya - yc);
+        const double *gx = d->gradx + 3 * k, *gy = d->grady + 3 * k;
+        g32[2 * k] = make_float4((float)gx[0], (float)gx[1], (float)gx[2], (float)gy[0]);
+        g32[2 * k + 1] = make_float4((float)gy[1], (float)gy[2], 0.f, 0.f);
+    }
     std::vector<int4> edge(ne);
     std::vector<int> lab(ne);
     for (int j = 0; j < ne; ++j) {
@@ -221,17 +250,21 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     DevMesh m{};
     m.nv = nv; m.nt = nt; m.ne = ne;
     int rc;
-    const double2 *p_xy, *p_basis;
+    const double2 *p_xy, *p_basis, *p_geo;
+    const float4* p_g32;
     const int4 *p_tv, *p_edge;
     const int *p_lab, *p_gs, *p_gt;
     if ((rc = upload(c, xy, p_xy))) return rc;
     if ((rc = upload(c, tv, p_tv))) return rc;
     if ((rc = upload(c, basis, p_basis))) return rc;
+    if ((rc = upload(c, geo, p_geo))) return rc;
+    if ((rc = upload(c, g32, p_g32))) return rc;
     if ((rc = upload(c, edge, p_edge))) return rc;
     if ((rc = upload(c, lab, p_lab))) return rc;
     if ((rc = upload(c, gstart, p_gs))) return rc;
     if ((rc = upload(c, gtris, p_gt))) return rc;
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
+    m.geo = p_geo; m.g32 = p_g32;
     m.gstart = p_gs; m.gtris = p_gt;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;
@@ -311,8 +344,8 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     *out = nullptr;
     if (!c->have_mesh || !c->have_fields)
         return set_err(c, CG_ESTATE, "cg_run_create before mesh/field upload");
-    if (p->precision != CG_PRECISION_FP64)
-        return set_err(c, CG_EINVAL, "precision %d is not built", p->precision);
+    if (p->precision != CG_PRECISION_FP64 && p->precision != CG_PRECISION_MIXED)
+        return set_err(c, CG_EINVAL, "unknown precision %d", p->precision);
     if (p->model != 1)
         return set_err(c, CG_EINVAL, "model %d is not built in this library", p->model);
     if (p->dim != c->fdim)
@@ -340,8 +373,7 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
         return set_err(c, CG_EINVAL, "final_time > EulerianFieldSet maximum time");
     CUDA_TRY(c, cudaSetDevice(c->device));
 
-    int rv = record_values(c->fdim);
-    size_t rec_bytes = (size_t)rv * sizeof(double) * c->frames.nnodes;
+    size_t rec_bytes = record_bytes(c->fdim, p->precision) * c->frames.nnodes;
     uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
     uint64_t need = state_bytes + 2 * rec_bytes + 64;
     if (c->budget && c->used + need > c->budget)
@@ -449,7 +481,7 @@ static int time_interpolation(cg_run* r, double time) {
     cg_ctx* c = r->ctx;
     if (r->frozen) {
         if (!r->fields_ready) {
-            launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, 0, c->stream);
+            launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
             CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes,
                                         cudaMemcpyDeviceToDevice, c->stream));
             r->fields_ready = true;
@@ -465,7 +497,7 @@ static int time_interpolation(cg_run* r, double time) {
     if (std::fabs(dt) < EPSILON)
         return set_err(c, CG_EINVAL, "Time interpolation failed: duplicate times at record %d", rec);
     double tf = (time - c->times[rec + 1]) / dt;
-    launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, 0, c->stream);
+    launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
     r->fields_ready = true;
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -477,7 +509,7 @@ static int ensure_fields(cg_run* r) {
     if (r->frozen) return time_interpolation(r, r->time);
     // EulerianFieldSet._init_tmp (743-776): both temps hold record 0, then
     // Solver.__init__ interpolates at initial_time (solver.pyx:190-191).
-    launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, 0, c->stream);
+    launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
     CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes, cudaMemcpyDeviceToDevice,
                                 c->stream));
     return time_interpolation(r, r->prm.initial_time);
@@ -489,8 +521,8 @@ int cg_run_init(cg_run* r) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = ensure_fields(r);
     if (rc) return rc;
-    launch_init_plain(c->fdim, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st,
-                      r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
+    launch_init(c->fdim, r->prm.precision, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp,
+                r->st, r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
 }
@@ -521,9 +553,14 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * nopen;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
-        launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                          r->prev_valid, r->dp, r->st, aux, (int)(r->iteration),
-                          stats, (uint32_t*)r->errw.p, c->stream);
+        if (r->prm.precision == CG_PRECISION_MIXED)
+            launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
+                              r->prev_valid, r->dp, r->st, aux, (int)(r->iteration), stats,
+                              (uint32_t*)r->errw.p, c->stream);
+        else
+            launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
+                              r->prev_valid, r->dp, r->st, aux, (int)(r->iteration), stats,
+                              (uint32_t*)r->errw.p, c->stream);
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
         // simutime.pyx:77-84

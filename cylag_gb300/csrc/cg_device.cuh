@@ -45,6 +45,12 @@ constexpr uint32_t ERR_UNSUPPORTED = 8;
 struct DevMesh {
     int nv, nt, ne;
     const double2* __restrict__ xy;     // [nv]
+    // [6*nt]: vertices a, b, c, then edge vectors b-a, c-b, a-c (FP64,
+    // computed on the host with the same subtractions the reference's
+    // point-in-triangle test performs, utils.pyx:332-385)
+    const double2* __restrict__ geo;
+    // [2*nt] FP32 P1 gradients {gx0,gx1,gx2,gy0}, {gy1,gy2,-,-} (mixed form)
+    const float4* __restrict__ g32;
     const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
     const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
     const int4* __restrict__ edge;      // [ne]: {n0, n1, t0, t1}
@@ -206,19 +212,43 @@ __device__ __forceinline__ double pintri(double x, double y, double xa, double y
            ((x - xa) * (yc - ya) - (xc - xa) * (y - ya));
 }
 
+// Decision of (t1 * t2 >= 0) taken on the sign bits (integer pipe) instead
+// of an FP64 multiply and compare.  Identical for every finite t1, t2 whose
+// product is not subnormal; a subnormal product needs cross products below
+// ~1e-154, i.e. coordinates below ~1e-77 m.
+__device__ __forceinline__ bool prod_nonneg(double t1, double t2) {
+    long long b1 = __double_as_longlong(t1), b2 = __double_as_longlong(t2);
+    const long long EXP = 0x7ff0000000000000LL, ABS = 0x7fffffffffffffffLL;
+    bool nan = ((b1 & ABS) > EXP) || ((b2 & ABS) > EXP);
+    bool zero = ((b1 << 1) == 0) || ((b2 << 1) == 0);
+    return !nan && (zero || (b1 ^ b2) >= 0);
+}
+
+// One rotation of point_in_triangle_dotp (utils.pyx:363-385): with w = p - v,
+// t1 = eo x w, t2 = ei x w for the edge leaving v (eo) and entering v (ei).
+// Exactly the reference's pintri(x, y, v, next, prev): (next - v) is eo and
+// (prev - v) == -ei bit for bit, and negated operands give negated products.
+// Written with _rn intrinsics so that no build flag can contract it to FMA.
+__device__ __forceinline__ bool rot_ok(double x, double y, double2 v, double2 eo, double2 ei) {
+    double wx = __dsub_rn(x, v.x), wy = __dsub_rn(y, v.y);
+    double t1 = __dsub_rn(__dmul_rn(eo.x, wy), __dmul_rn(wx, eo.y));
+    double t2 = __dsub_rn(__dmul_rn(ei.x, wy), __dmul_rn(wx, ei.y));
+    return prod_nonneg(t1, t2);
+}
+
 // utils.pyx:363-385 with xylocalizer.pyx:126-167
 __device__ __forceinline__ bool in_tri(const DevMesh& m, int k, double x, double y) {
-    int4 t = __ldg(&m.tv[2 * k]);
-    double2 a = __ldg(&m.xy[t.x]), b = __ldg(&m.xy[t.y]), c = __ldg(&m.xy[t.z]);
-    return pintri(x, y, a.x, a.y, b.x, b.y, c.x, c.y) >= 0 &&
-           pintri(x, y, b.x, b.y, c.x, c.y, a.x, a.y) >= 0 &&
-           pintri(x, y, c.x, c.y, a.x, a.y, b.x, b.y) >= 0;
+    const double2* g = m.geo + 6 * (size_t)k;
+    double2 a = __ldg(&g[0]), b = __ldg(&g[1]), c = __ldg(&g[2]);
+    double2 dab = __ldg(&g[3]), dbc = __ldg(&g[4]), dca = __ldg(&g[5]);
+    return rot_ok(x, y, a, dab, dca) && rot_ok(x, y, b, dbc, dab) && rot_ok(x, y, c, dca, dbc);
 }
 
 // utils.pyx:228-252
 __device__ __forceinline__ int orientation(double v0x, double v0y, double v1x, double v1y,
                                            double v2x, double v2y) {
-    double delta = (v0y - v1y) * (v2x - v0x) - (v0x - v1x) * (v2y - v0y);
+    double delta = __dsub_rn(__dmul_rn(__dsub_rn(v0y, v1y), __dsub_rn(v2x, v0x)),
+                             __dmul_rn(__dsub_rn(v0x, v1x), __dsub_rn(v2y, v0y)));
     if (delta == 0.) return 0;
     if (delta > 0.) return 1;
     return 2;
@@ -251,8 +281,8 @@ __device__ inline bool intersec2d(double p0x, double p0y, double p1x, double p1y
 // xylocalizer.pyx:200-286; same result unless the point lies exactly on an
 // edge shared by two triangles.
 __device__ inline int grid_locate(const DevMesh& m, double x, double y) {
-    double fx = floor((x - m.gx0) * m.ginv);
-    double fy = floor((y - m.gy0) * m.ginv);
+    double fx = floor(__dmul_rn(__dsub_rn(x, m.gx0), m.ginv));
+    double fy = floor(__dmul_rn(__dsub_rn(y, m.gy0), m.ginv));
     if (!(fx >= 0.)) fx = 0.;
     if (!(fy >= 0.)) fy = 0.;
     int cx = fx > (double)(m.gnx - 1) ? m.gnx - 1 : (int)fx;

@@ -31,15 +31,24 @@ void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* p
                        int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
                        int step_index, int* stats, uint32_t* err, cudaStream_t st);
 
-// Solver.initialize_particle_state for particles with tri == -2.
-void launch_init_plain(int dim, const DevMesh& m, const void* cur, int npoints, int nlayers,
-                       const DevParams& p, const DevState& s, int velocity_init, uint32_t* err,
-                       cudaStream_t st);
+// The same step, mixed-precision form (FP32 node records).
+void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
+                       int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
+                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+
+// Solver.initialize_particle_state for particles with tri == -2 (FP64
+// arithmetic; node records FP64 or FP32 by precision).
+void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int npoints,
+                 int nlayers, const DevParams& p, const DevState& s, int velocity_init,
+                 uint32_t* err, cudaStream_t st);
 
 // rng[i] = pcg32_seed(seed, tag[i])
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);
 
-// bytes of one packed node record
+// values in one packed node record, and its bytes by precision
 inline int record_values(int dim) { return dim == 2 ? Slots<2>::NF : Slots<3>::NF; }
+inline size_t record_bytes(int dim, int precision) {
+    return (size_t)record_values(dim) * (precision ? sizeof(float) : sizeof(double));
+}
 
 }  // namespace cg

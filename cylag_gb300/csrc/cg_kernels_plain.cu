@@ -51,11 +51,18 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
                   int precision, cudaStream_t st) {
     int bs = 256;
     int64_t nb = (fr.nnodes + bs - 1) / bs;
-    if (precision != 0) return;  // the mixed form has its own translation unit
-    if (fr.dim == 2)
-        blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
-    else
-        blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
+    if (precision == 0) {
+        if (fr.dim == 2)
+            blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
+        else
+            blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
+    } else {
+        // FP64 interpolation, rounded once to the FP32 record
+        if (fr.dim == 2)
+            blend_kernel<2, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (float*)cur);
+        else
+            blend_kernel<3, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (float*)cur);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -136,12 +143,22 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
     if (q.err) atomicOr(err, q.err);
 }
 
-void launch_init_plain(int dim, const DevMesh& m, const void* cur, int npoints, int nlayers,
-                       const DevParams& p, const DevState& s, int vinit, uint32_t* err,
-                       cudaStream_t st) {
+void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int npoints,
+                 int nlayers, const DevParams& p, const DevState& s, int vinit, uint32_t* err,
+                 cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
+    if (precision != 0) {
+        if (dim == 2) {
+            DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
+            init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+        } else {
+            DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 3, 0};
+            init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+        }
+        return;
+    }
     if (dim == 2) {
         DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
         init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);

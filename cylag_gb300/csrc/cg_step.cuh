@@ -39,8 +39,13 @@ struct Particle {
     // eulerian_field_set.pyx:1057-1115 (2D) and 1289-1394 (3D, zlocalize=0)
     __device__ void velocity(int k, int l, double px, double py, double pz, double& ux,
                              double& uy, double& uz) {
-        using S = Slots<DIM>;
         P1 q = p1_at(m, k, px, py);
+        velocity_q(q, l, pz, ux, uy, uz);
+    }
+
+    __device__ void velocity_q(const P1& q, int l, double pz, double& ux, double& uy,
+                               double& uz) {
+        using S = Slots<DIM>;
         if (DIM == 2) {
             ux = p1_eval<DIM>(f.cur, 0, q, S::UX);
             uy = p1_eval<DIM>(f.cur, 0, q, S::UY);
@@ -81,10 +86,9 @@ struct Particle {
     }
 
     // eulerian_field_set.pyx:1644-1763
-    __device__ void diffusivity(int k, int l, double px, double py, double pz, double& K,
-                                double& dKdx, double& dKdy, double& dKdz) {
+    __device__ void diffusivity_q(const P1& q, int l, double pz, double& K, double& dKdx,
+                                  double& dKdy, double& dKdz) {
         using S = Slots<DIM>;
-        P1 q = p1_at(m, k, px, py);
         if (DIM == 2) {
             double kn0 = nodev<DIM>(f.cur, q.i0, S::K), kn1 = nodev<DIM>(f.cur, q.i1, S::K),
                    kn2 = nodev<DIM>(f.cur, q.i2, S::K);
@@ -157,10 +161,10 @@ struct Particle {
         return false;
     }
 
-    // update_state_lsm1.pyx:135-656
-    __device__ int advect_lsm1() {
+    // update_state_lsm1.pyx:135-656; q0: P1 factors at the step-start point
+    __device__ int advect_lsm1(const P1& q0) {
         double dt = p.dt, ux, uy, uz;
-        velocity(tri, ll, x[0], x[1], DIM == 3 ? x[2] : 0., ux, uy, uz);
+        velocity_q(q0, ll, DIM == 3 ? x[2] : 0., ux, uy, uz);
         set_up_us(ux, uy, uz);
         if (p.time_scheme == 1) {  // 135-177
             x[0] += ux * dt;
@@ -225,15 +229,15 @@ struct Particle {
         return -1;
     }
 
-    // update_state_lsm1.pyx:658-726
-    __device__ void diffusion_lsm1() {
+    // update_state_lsm1.pyx:658-726 (K at the start point, same factors q0)
+    __device__ void diffusion_lsm1(const P1& q0) {
         double dt = p.dt;
         double xix = 0., xiy = 0., xiz = 0.;
         double diffx, diffy, diffz = 0.;
         double driftx = 0., drifty = 0., driftz = 0.;
         if (p.diffmod == 2 || p.diffmod == 3) {
             double Kp, dKdx, dKdy, dKdz;
-            diffusivity(tri0, ll0, x0[0], x0[1], DIM == 3 ? x0[2] : 0., Kp, dKdx, dKdy, dKdz);
+            diffusivity_q(q0, ll0, DIM == 3 ? x0[2] : 0., Kp, dKdx, dKdy, dKdz);
             diffx = sqrt(2. * Kp) * p.sqrtdt;
             diffy = diffx;
             driftx = dKdx * dt;
@@ -260,8 +264,9 @@ struct Particle {
 
     // update_state_lsm1.pyx:30-133
     __device__ int update_lsm1(double dp) {
-        int bnd_j = advect_lsm1();
-        if (p.diffmod != 0) diffusion_lsm1();
+        P1 q0 = p1_at(m, tri0, x0[0], x0[1]);
+        int bnd_j = advect_lsm1(q0);
+        if (p.diffmod != 0) diffusion_lsm1(q0);
         if (DIM == 3) {
             double wb = buoyancy_velocity(dp);
             x[2] += wb * p.dt;

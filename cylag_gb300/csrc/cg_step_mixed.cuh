@@ -1,0 +1,321 @@
+// cg_step_mixed.cuh -- the mixed-precision form of the fused step (LSM1 2D).
+//
+// FP64 is kept only where stability needs it: particle positions and their
+// accumulation, the in-element test and the edge-crossing tests that decide
+// localization, simulated time (host).  Node fields are stored in FP32 and
+// interpolated, differentiated and integrated in FP32; random normals are
+// FP32 ziggurat draws from the same per-particle PCG32 stream.
+//
+// In-element test: barycentric coordinates are evaluated in FP32 from the
+// FP64 offset to vertex a, with a rounding bound per coordinate.  Points
+// certainly inside (every coordinate above its bound) or certainly outside
+// (one below minus its bound) are decided there; the thin band in between
+// is decided by the exact FP64 predicate of the plain form.  So the mixed
+// form takes the same localization decision as the plain form for the same
+// position; only the positions themselves differ (FP32 increments).
+#pragma once
+
+#include "cg_step.cuh"
+
+namespace cg {
+
+struct Zig32 {
+    uint32_t kn[128];
+    float wn[128];
+    float fn[128];
+};
+
+// random_utils.pyx:55-67 in FP32
+__device__ __forceinline__ float uniform32(Rng& r) {
+    return (float)pcg_next(r) * 2.3283064365386963e-10f;
+}
+
+// random_utils.pyx:154-194 in FP32 (same stream consumption as the FP64
+// version except where an FP32 wedge/tail test rounds the other way)
+__device__ inline float zig32(Rng& r, const Zig32& z) {
+    for (int tries = 0; tries < RNG_MAX_TRIES; ++tries) {
+        int32_t hz = (int32_t)pcg_next(r);
+        uint32_t iz = (uint32_t)hz & 127u;
+        uint32_t ahz = hz < 0 ? 0u - (uint32_t)hz : (uint32_t)hz;
+        if (ahz < z.kn[iz]) return (float)hz * z.wn[iz];
+        if (iz == 0) {
+            for (int t2 = 0; t2 < RNG_MAX_TRIES; ++t2) {
+                float x = -__logf(uniform32(r)) * 0.2904764f;
+                float y = -__logf(uniform32(r));
+                if (y + y >= x * x) return hz > 0 ? 3.442619855899f + x : -3.442619855899f - x;
+            }
+            r.err |= ERR_RNG_LIMIT;
+            return 0.f;
+        }
+        float x = (float)hz * z.wn[iz];
+        if (z.fn[iz] + uniform32(r) * (z.fn[iz - 1] - z.fn[iz]) < __expf(-0.5f * x * x)) return x;
+    }
+    r.err |= ERR_RNG_LIMIT;
+    return 0.f;
+}
+
+__device__ inline void polar32(Rng& r, float& a, float& b) {
+    float x1 = 0.f, x2 = 0.f, w = 2.f;
+    int tries = 0;
+    while ((w >= 1.f || w == 0.f) && tries < RNG_MAX_TRIES) {
+        x1 = 2.f * uniform32(r) - 1.f;
+        x2 = 2.f * uniform32(r) - 1.f;
+        w = x1 * x1 + x2 * x2;
+        ++tries;
+    }
+    if (tries == RNG_MAX_TRIES) { r.err |= ERR_RNG_LIMIT; a = b = 0.f; return; }
+    w = sqrtf((-2.f * __logf(w)) / w);
+    a = x1 * w;
+    b = x2 * w;
+}
+
+__device__ inline void pair32(Rng& r, int method, const Zig32& z, float& a, float& b) {
+    if (method == 1) {
+        a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+        b = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+    } else if (method == 2) {
+        a = zig32(r, z);
+        b = zig32(r, z);
+    } else {
+        polar32(r, a, b);
+    }
+}
+
+// per-triangle data of the FP32 barycentric evaluation
+struct Tri32 {
+    int4 tv;      // v0, v1, v2, e0
+    double2 a;    // vertex a (FP64)
+    float4 g0;    // gx0 gx1 gx2 gy0
+    float4 g1;    // gy1 gy2 - -
+};
+
+__device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
+    Tri32 t;
+    t.tv = __ldg(&m.tv[2 * k]);
+    t.a = __ldg(&m.geo[6 * (size_t)k]);
+    t.g0 = __ldg(&m.g32[2 * k]);
+    t.g1 = __ldg(&m.g32[2 * k + 1]);
+    return t;
+}
+
+struct Bary {
+    float l0, l1, l2;
+    float e0, e1, e2;   // rounding bounds of l0, l1, l2
+};
+
+// barycentric coordinates of (x, y): l_j = gx_j (x - xa) + gy_j (y - ya)
+__device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
+    Bary b;
+    float rx = (float)(x - t.a.x), ry = (float)(y - t.a.y);
+    float p1 = t.g0.y * rx, q1 = t.g1.x * ry;
+    float p2 = t.g0.z * rx, q2 = t.g1.y * ry;
+    b.l1 = p1 + q1;
+    b.l2 = p2 + q2;
+    b.l0 = 1.f - b.l1 - b.l2;
+    // |error| <= ~4 ulp of the terms (offset, gradient and product roundings)
+    b.e1 = 6.0e-7f * (fabsf(p1) + fabsf(q1)) + 1.0e-6f;
+    b.e2 = 6.0e-7f * (fabsf(p2) + fabsf(q2)) + 1.0e-6f;
+    b.e0 = b.e1 + b.e2 + 1.0e-6f;
+    return b;
+}
+
+// same decision as in_tri (the FP64 predicate), FP32 outside the band
+__device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, int k, double x,
+                                             double y) {
+    Bary b = bary32(t, x, y);
+    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return true;
+    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return false;
+    return in_tri(m, k, x, y);
+}
+
+// xylocalizer.pyx:27-124 method 3, first test through the FP32 filter
+__device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32& t, int k,
+                                                  double p0x, double p0y, double x, double y,
+                                                  int& new_k, int& bnd) {
+    bnd = -1;
+    if (in_tri_mixed(m, t, k, x, y)) { new_k = k; return; }
+    path_walk(m, k, p0x, p0y, x, y, new_k, bnd);
+    if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
+}
+
+// FP32 P1 interpolation of the packed node record {ux, uy, K, zs}
+struct Node4 {
+    float4 n0, n1, n2;
+};
+
+__device__ __forceinline__ Node4 load_nodes(const float4* __restrict__ f, const Tri32& t) {
+    Node4 r;
+    r.n0 = __ldg(&f[t.tv.x]);
+    r.n1 = __ldg(&f[t.tv.y]);
+    r.n2 = __ldg(&f[t.tv.z]);
+    return r;
+}
+
+__device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, float& uy) {
+    ux = b.l0 * n.n0.x + b.l1 * n.n1.x + b.l2 * n.n2.x;
+    uy = b.l0 * n.n0.y + b.l1 * n.n1.y + b.l2 * n.n2.y;
+}
+
+// LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
+// diffusion 658-726) with the boundary conditions of compute_bc.pyx.
+__global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
+                                                           DevParams p, DevState s, int aux,
+                                                           int step_index, int* __restrict__ stats,
+                                                           uint32_t* __restrict__ err_word) {
+    __shared__ Zig32 z32;
+    __shared__ ZigTables z64;
+    for (int t = threadIdx.x; t < 128; t += blockDim.x) {
+        z32.kn[t] = c_zig.kn[t];
+        z32.wn[t] = (float)c_zig.wn[t];
+        z32.fn[t] = (float)c_zig.fn[t];
+        z64.kn[t] = c_zig.kn[t];
+        z64.wn[t] = c_zig.wn[t];
+        z64.fn[t] = c_zig.fn[t];
+    }
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    int tri0 = s.tri[i];
+    if (tri0 < 0) return;
+    const float4* __restrict__ cur = reinterpret_cast<const float4*>(f.cur);
+    double2 x0 = reinterpret_cast<const double2*>(s.pos)[i];
+    Rng rng;
+    rng.state = s.rng[i];
+    rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
+    rng.err = 0;
+    double2 lastv = make_double2(0., 0.);
+    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[i];
+
+    const float dt = (float)p.dt;
+    Tri32 t0 = load_tri32(m, tri0);
+    Node4 n0 = load_nodes(cur, t0);
+    Bary b0 = bary32(t0, x0.x, x0.y);
+    float ux, uy;
+    vel32(n0, b0, ux, uy);
+    float up0 = ux, up1 = uy;   // velocity = fluid velocity seen = U(x0)
+    double xn = x0.x, yn = x0.y;
+    int tri = tri0, ltri = tri0, bnd_j = -1;
+    bool stopped = false;
+
+    if (p.time_scheme == 1) {
+        xn += (double)(ux * dt);
+        yn += (double)(uy * dt);
+    } else {
+        // Runge-Kutta stages (update_state_lsm1.pyx:179-656): each stage point
+        // is localized from (tri0, x0); a stage leaving the domain stops the
+        // scheme with an Euler step.
+        const int ns = p.time_scheme == 2 ? 1 : (p.time_scheme == 3 ? 2 : 3);
+        float kx[4], ky[4];
+        kx[0] = ux * dt;
+        ky[0] = uy * dt;
+        for (int st = 0; st < ns && !stopped; ++st) {
+            float cst;
+            if (p.time_scheme == 2) cst = 0.5f;
+            else if (p.time_scheme == 3) cst = st == 0 ? (1.f / 3.f) : (2.f / 3.f);
+            else cst = st < 2 ? 0.5f : 1.f;
+            float fx = (p.time_scheme == 2) ? 0.5f * ux * dt : cst * kx[st];
+            float fy = (p.time_scheme == 2) ? 0.5f * uy * dt : cst * ky[st];
+            double xt = x0.x + (double)fx, yt = x0.y + (double)fy;
+            int tt, bnd;
+            ltri = tri0;
+            xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xt, yt, tt, bnd);
+            if (bnd != -1) {
+                tri = tt;
+                xn = x0.x + (double)(up0 * dt);
+                yn = x0.y + (double)(up1 * dt);
+                bnd_j = bnd;
+                stopped = true;
+                break;
+            }
+            Tri32 ts = load_tri32(m, tt);
+            Node4 ns4 = load_nodes(cur, ts);
+            float sx, sy;
+            vel32(ns4, bary32(ts, xt, yt), sx, sy);
+            kx[st + 1] = sx * dt;
+            ky[st + 1] = sy * dt;
+        }
+        if (!stopped) {
+            float dxs, dys;
+            if (p.time_scheme == 2) { dxs = kx[1]; dys = ky[1]; }
+            else if (p.time_scheme == 3) { dxs = 0.25f * kx[0] + 0.75f * kx[2]; dys = 0.25f * ky[0] + 0.75f * ky[2]; }
+            else { dxs = (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) / 6.f; dys = (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) / 6.f; }
+            xn += (double)dxs;
+            yn += (double)dys;
+        }
+    }
+
+    // diffusion (update_state_lsm1.pyx:658-726), K at the start point
+    if (p.diffmod != 0) {
+        float diffx, driftx = 0.f, drifty = 0.f;
+        if (p.diffmod == 2 || p.diffmod == 3) {
+            float K = b0.l0 * n0.n0.z + b0.l1 * n0.n1.z + b0.l2 * n0.n2.z;
+            float dKdx = n0.n0.z * t0.g0.x + n0.n1.z * t0.g0.y + n0.n2.z * t0.g0.z;
+            float dKdy = n0.n0.z * t0.g0.w + n0.n1.z * t0.g1.x + n0.n2.z * t0.g1.y;
+            K = fmaxf(0.f, K);
+            diffx = sqrtf(2.f * K) * (float)p.sqrtdt;
+            driftx = dKdx * dt;
+            drifty = dKdy * dt;
+        } else {
+            diffx = (float)p.diffx_const;
+        }
+        float xix = 0.f, xiy = 0.f;
+        if (diffx != 0.f) pair32(rng, p.rng_method, z32, xix, xiy);
+        xn += (double)(driftx + diffx * xix);
+        yn += (double)(drifty + diffx * xiy);
+    }
+
+    if (bnd_j == -1) {
+        ltri = tri0;
+        xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xn, yn, tri, bnd_j);
+    }
+
+    bool deleted = false;
+    if (bnd_j != -1 || tri == PART_LOC_O) {
+        // rare: boundary conditions with the FP64 mirror and exact walk
+        Particle<2, float> q(m, f, p, z64);
+        q.rng = rng;
+        q.x[0] = xn; q.x[1] = yn;
+        q.x0[0] = x0.x; q.x0[1] = x0.y;
+        q.up[0] = up0; q.up[1] = up1;
+        q.us[0] = up0; q.us[1] = up1;
+        q.tri = tri; q.tri0 = tri0; q.ltri = ltri; q.ll = 0; q.ll0 = 0;
+        if (p.bc_on) q.compute_bc(bnd_j, stats);
+        else if (q.tri == PART_LOC_O) q.deleted = true;
+        rng = q.rng;
+        xn = q.x[0];
+        yn = q.x[1];
+        tri = q.tri;
+        deleted = q.deleted;
+        rng.err |= q.err;
+    }
+    if (rng.err) atomicOr(err_word, rng.err);
+
+    if (deleted) {
+        reinterpret_cast<double2*>(s.pos)[i] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.vel)[i] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.fvs)[i] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_pos)[i] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_vel)[i] = make_double2(0., 0.);
+        s.diameter[i] = 0.;
+        s.tri[i] = -1;
+        s.last_tri[i] = -1;
+        s.lowerlayer[i] = 0;
+        s.tag[i] = -2 - step_index;
+        s.rng[i] = rng.state;
+        return;
+    }
+    reinterpret_cast<double2*>(s.pos)[i] = make_double2(xn, yn);
+    s.tri[i] = tri;
+    s.rng[i] = rng.state;
+    if (aux >= 1) {
+        reinterpret_cast<double2*>(s.vel)[i] = make_double2(up0, up1);
+        reinterpret_cast<double2*>(s.fvs)[i] = make_double2(up0, up1);
+    }
+    if (aux >= 2) {
+        reinterpret_cast<double2*>(s.last_pos)[i] = x0;
+        reinterpret_cast<double2*>(s.last_vel)[i] = lastv;
+        s.last_tri[i] = ltri;
+    }
+}
+
+}  // namespace cg

@@ -116,8 +116,13 @@ int cg_ctx_create(int32_t device, uint64_t hbm_budget_bytes, cg_ctx **out);
 int cg_ctx_destroy(cg_ctx *ctx);
 /* Copies the last error message (NUL-terminated, truncated to len). */
 int cg_last_error(const cg_ctx *ctx, char *buf, uint64_t len);
-/* The context's cudaStream_t, as an integer handle. */
+/* The stream the context issues work on (a cudaStream_t as an integer). */
 uint64_t cg_ctx_stream(const cg_ctx *ctx);
+/* Issue all further work on the caller's stream (e.g. a torch stream); the
+ * caller keeps it alive until the context is destroyed or the stream is
+ * reset with 0 (back to the context's own stream).  Synchronizes the
+ * previous stream first.  No reference counterpart. */
+int cg_ctx_set_stream(cg_ctx *ctx, uint64_t stream);
 int cg_ctx_sync(cg_ctx *ctx);
 
 /* Replaces TriangularMesh.__init__ (triangular_mesh.pyx:75-179): packs and

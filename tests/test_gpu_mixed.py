@@ -1,0 +1,80 @@
+"""Mixed-precision form: stated error against the FP64 oracle and the plain
+form, and the analytical 2Kt spread.
+
+Tolerance (the mixed form's contract): ensemble variance of the
+displacement within 1e-3 relative of the FP64 result; ensemble mean within
+1e-3 of the spread; element decisions identical to the FP64 predicate.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, run_oracle
+from test_gpu_parity import gpu_run
+
+pytestmark = pytest.mark.gpu
+
+VAR_TOL = 1e-3
+
+
+def keps_case(npart, nx=101, ny=26, seed=5):
+    from cylag_gb300 import synth
+    c = synth.keps_drift_channel(npart=npart, nx=nx, ny=ny, seed=seed)
+    case = {k: c[k] for k in ("x", "y", "triangles", "times", "elevation", "velocity_x",
+                              "velocity_y", "opt_fields", "position")}
+    case["opt_fields_names"] = c["opt_fields_names"]
+    p = dict(c["parameters"])
+    p.update(time_step=2.0, final_time=400.0)
+    return case, p
+
+
+def test_mixed_vs_fp64_oracle_keps():
+    from cylag_gb300.stats import displacement_report
+    case, p = keps_case(50_000)
+    meta = dict(params=p, nsteps=150, seed=11, pset={})
+    o = run_oracle(case, meta, nthreads=8)
+    s, ps = gpu_run(case, meta, precision="mixed")
+    act = (o.inactive == 0) & (ps.inactive == 0)
+    rep = displacement_report(case["position"], ps.position, o.pos, act)
+    print(rep)
+    assert max(rep["var_rel_err"]) <= VAR_TOL, rep
+    assert max(rep["mean_rel_err"]) <= VAR_TOL, rep
+    # same per-particle streams: trajectories stay close particle by particle
+    assert rep["rms_displacement_diff"] < 1e-2 * np.sqrt(max(rep["var_ref"])), rep
+    s.close()
+
+
+def test_mixed_vs_plain_same_decisions():
+    """From identical positions one mixed step and one plain step give the
+    same element indices when the displacement is identical (zero
+    diffusion, frozen uniform flow)."""
+    name = "couette"
+    case, meta, _ = load_golden(name)
+    meta = dict(meta)
+    meta["params"] = dict(meta["params"], diffusion_model=0, time_scheme=1)
+    sa, pa = gpu_run(case, meta, nsteps=50, precision="fp64")
+    sb, pb = gpu_run(case, meta, nsteps=50, precision="mixed")
+    np.testing.assert_array_equal(pa.tri, pb.tri)
+    assert np.max(np.abs(pa.position - pb.position)) < 1e-5
+    sa.close()
+    sb.close()
+
+
+def test_mixed_pure_diffusion_matches_2Kt():
+    """Zero velocity, constant K: the spread of 200,000 particles after t
+    seconds is 2Kt within 5 standard errors (walls far away)."""
+    from cylag_gb300 import synth
+    from cylag_gb300.stats import diffusion_report
+    x, y, tri = synth.channel_mesh(2000.0, 2000.0, 41, 41, seed=2)
+    n = 200_000
+    pos = np.tile([[1000.0, 1000.0]], (n, 1))
+    case = dict(x=x, y=y, triangles=tri, times=np.zeros(1), elevation=np.ones((1, len(x))),
+                velocity_x=np.zeros((1, len(x))), velocity_y=np.zeros((1, len(x))), position=pos)
+    K, dt, nsteps = 0.5, 1.0, 200
+    p = dict(model=1, diffusion_model=1, horizontal_diffusivity=K, time_scheme=1,
+             frozen_eulerian_fields=True, time_step=dt, final_time=dt * nsteps)
+    for prec in ("mixed", "fp64"):
+        s, ps = gpu_run(case, dict(params=p, nsteps=nsteps, seed=1, pset={}), precision=prec)
+        rep = diffusion_report(pos, ps.position, K, dt * nsteps)
+        print(prec, rep)
+        assert max(abs(z) for z in rep["z"]) < 5.0, (prec, rep)
+        s.close()
