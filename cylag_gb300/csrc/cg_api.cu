@@ -61,6 +61,8 @@ struct cg_run {
     DevBuf stats;
     int stats_rows = 0;
     DevBuf errw;
+    DevBuf queue;          // walk queue: count (first 256 B) + one entry per particle
+    bool use_queue = false;
     uint64_t bytes = 0;
     std::vector<cudaEvent_t> ev;
     int last_launches = 0;
@@ -375,7 +377,9 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
 
     size_t rec_bytes = record_bytes(c->fdim, p->precision) * c->frames.nnodes;
     uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
-    uint64_t need = state_bytes + 2 * rec_bytes + 64;
+    bool use_queue = c->fdim == 2 && s->n > 0;
+    size_t queue_bytes = use_queue ? 256 + (size_t)s->n * sizeof(WalkEntry) : 0;
+    uint64_t need = state_bytes + 2 * rec_bytes + 64 + queue_bytes;
     if (c->budget && c->used + need > c->budget)
         return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
                        (unsigned long long)need, (unsigned long long)c->used,
@@ -387,11 +391,12 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->prm = *p;
     int rc;
     if ((rc = dalloc(c, r->cur, rec_bytes)) || (rc = dalloc(c, r->prev, rec_bytes)) ||
-        (rc = dalloc(c, r->errw, 64))) {
-        dfree(r->cur); dfree(r->prev); dfree(r->errw);
+        (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->queue, queue_bytes))) {
+        dfree(r->cur); dfree(r->prev); dfree(r->errw); dfree(r->queue);
         delete r;
         return rc;
     }
+    r->use_queue = use_queue;
     cudaMemsetAsync(r->errw.p, 0, 64, c->stream);
     r->bytes = need;
     c->used += need;
@@ -458,6 +463,7 @@ int cg_run_destroy(cg_run* r) {
     dfree(r->prev);
     dfree(r->stats);
     dfree(r->errw);
+    dfree(r->queue);
     for (auto e : r->ev) cudaEventDestroy(e);
     c->used -= r->bytes;
     delete r;
@@ -553,14 +559,23 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * nopen;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
+        WalkQueue wq{nullptr, nullptr};
+        if (r->use_queue) {
+            wq.count = (int*)r->queue.p;
+            wq.e = (WalkEntry*)((char*)r->queue.p + 256);
+            CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
+        }
         if (r->prm.precision == CG_PRECISION_MIXED)
             launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, aux, (int)(r->iteration), stats,
+                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), stats,
                               (uint32_t*)r->errw.p, c->stream);
         else
             launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, aux, (int)(r->iteration), stats,
+                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), stats,
                               (uint32_t*)r->errw.p, c->stream);
+        if (r->use_queue)
+            launch_walk(r->prm.precision, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st,
+                        wq, aux, (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
         // simutime.pyx:77-84

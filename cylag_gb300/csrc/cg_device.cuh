@@ -101,6 +101,32 @@ struct DevState {
     uint64_t* __restrict__ rng;
 };
 
+// Particles that leave their start triangle are finished by a second kernel
+// (path walk + boundary conditions) from a compacted queue, so that the
+// walk's FP64 work runs with full warps instead of inside divergent ones.
+struct WalkEntry {
+    double xn, yn;       // end-of-step position (before localization)
+    uint64_t rng;        // PCG32 state after the step's draws
+    int i;               // particle index
+    int pad;
+};
+
+struct WalkQueue {
+    int* count;          // entries this step (reset before the step)
+    WalkEntry* e;        // capacity: one entry per particle
+};
+
+// warp-aggregated slot reservation
+__device__ __forceinline__ int queue_slot(const WalkQueue& q) {
+    unsigned mask = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(q.count, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
 // ---------------------------------------------------------------------------
 // PCG32 + normal variates (cylag/lsm/random_utils.pyx)
 // ---------------------------------------------------------------------------

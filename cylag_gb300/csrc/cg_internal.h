@@ -27,14 +27,22 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
                   void* cur, int precision, cudaStream_t st);
 
 // One fused step over every particle of a run (plain FP64 form).
+// wq.e == nullptr: walk inline; else queue leavers and run launch_walk after.
 void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
+                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
+                       cudaStream_t st);
+
+// second half of a 2D step: path walk + boundary conditions of queued particles
+void launch_walk(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
+                 const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
+                 int step_index, int* stats, uint32_t* err, cudaStream_t st);
 
 // The same step, mixed-precision form (FP32 node records).
 void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
+                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
+                       cudaStream_t st);
 
 // Solver.initialize_particle_state for particles with tri == -2 (FP64
 // arithmetic; node records FP64 or FP32 by precision).

@@ -69,17 +69,37 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
 // the fused step
 // ---------------------------------------------------------------------------
 void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st) {
+                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
+                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
+                       cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
     if (dim == 2) {
         DevFields<double> f{(const double*)cur, (const double*)prev, npoints, nlayers, 2, prev_valid};
-        step_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, aux, step_index, stats, err);
+        step_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
     } else {
         DevFields<double> f{(const double*)cur, (const double*)prev, npoints, nlayers, 3, prev_valid};
-        step_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, aux, step_index, stats, err);
+        WalkQueue none{nullptr, nullptr};
+        step_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, none, aux, step_index, stats, err);
+    }
+}
+
+void launch_walk(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
+                 const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
+                 int step_index, int* stats, uint32_t* err, cudaStream_t st) {
+    // grid-stride over the (device-side) entry count: a fixed grid of
+    // 8 blocks per SM covers any count without a host round trip
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int nb = nsm * 8;
+    if (precision == 0) {
+        DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
+        walk_kernel<double><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+    } else {
+        DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
+        walk_kernel<float><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
     }
 }
 

@@ -30,10 +30,12 @@ struct Particle {
     int tri, tri0, ltri, ll, ll0;
     uint32_t err;
     bool deleted;
+    bool defer;       // in: 2D final localization may be deferred to the walk queue
+    bool deferred;    // out: the particle left its start triangle, queue it
 
     __device__ Particle(const DevMesh& m_, const DevFields<FT>& f_, const DevParams& p_,
                         const ZigTables& z_)
-        : m(m_), f(f_), p(p_), z(z_), err(0), deleted(false) {}
+        : m(m_), f(f_), p(p_), z(z_), err(0), deleted(false), defer(false), deferred(false) {}
 
     // ---- field interpolation -------------------------------------------------
     // eulerian_field_set.pyx:1057-1115 (2D) and 1289-1394 (3D, zlocalize=0)
@@ -274,11 +276,62 @@ struct Particle {
         }
         if (bnd_j == -1) {
             ltri = tri;
+            if (DIM == 2 && defer) {
+                // xylocalizer.pyx:65-70 here, the path walk in walk_kernel
+                if (!in_tri(m, ltri, x[0], x[1])) deferred = true;
+                return -1;
+            }
             xy_localize(m, ltri, x0[0], x0[1], x[0], x[1], tri, bnd_j);
             if (DIM == 3) ll = z_localize(tri, x[0], x[1], x[2]);
         }
         return bnd_j;
     }
+
+    // end of the step (solver.pyx:505-524): state write-back; deletion per
+    // lagrangian_particle_set.pyx:766-788, the tag recording the iteration
+    // for the host-side retag (maxtag+1, ... in iteration then index order)
+    __device__ void store(DevState& s, int i, int aux, int step_index, const double* lastv) {
+        const int D = DIM;
+        if (deleted) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                s.pos[(size_t)i * D + d] = 0.;
+                s.vel[(size_t)i * D + d] = 0.;
+                s.fvs[(size_t)i * D + d] = 0.;
+                s.last_pos[(size_t)i * D + d] = 0.;
+                s.last_vel[(size_t)i * D + d] = 0.;
+            }
+            s.diameter[i] = 0.;
+            s.tri[i] = -1;
+            s.last_tri[i] = -1;
+            s.lowerlayer[i] = 0;
+            s.tag[i] = -2 - step_index;
+            s.rng[i] = rng.state;
+            return;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = x[d];
+        s.tri[i] = tri;
+        if (DIM == 3) s.lowerlayer[i] = ll;
+        s.rng[i] = rng.state;
+        if (p.model >= 2 || aux >= 1) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) s.vel[(size_t)i * D + d] = up[d];
+        }
+        if (p.model == 3 || aux >= 1) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) s.fvs[(size_t)i * D + d] = us[d];
+        }
+        if (aux >= 2) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                s.last_pos[(size_t)i * D + d] = x0[d];
+                s.last_vel[(size_t)i * D + d] = lastv[d];
+            }
+            s.last_tri[i] = ltri;
+        }
+    }
+
 
     // ---- boundary conditions (compute_bc.pyx:35-395) ----------------------------
     // compute_bc.pyx:190-240 (normal2u utils.pyx:99-119)
@@ -381,21 +434,28 @@ struct Particle {
     }
 };
 
-// aux: 0 = state only; 1 = also write velocity / fluid velocity seen;
-//      2 = also write last_position / last_velocity / last_tri (the last
-//      step of a batch, so that every public array is current afterwards).
-template <int DIM, typename FT>
-__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
-                                                   DevState s, int aux, int step_index,
-                                                   int* __restrict__ stats,
-                                                   uint32_t* __restrict__ err_word) {
-    __shared__ ZigTables zt;
+// ziggurat tables into shared memory
+__device__ __forceinline__ void load_zig(ZigTables& zt) {
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
         zt.kn[t] = c_zig.kn[t];
         zt.wn[t] = c_zig.wn[t];
         zt.fn[t] = c_zig.fn[t];
     }
     __syncthreads();
+}
+
+// aux: 0 = state only; 1 = also write velocity / fluid velocity seen;
+//      2 = also write last_position / last_velocity / last_tri (the last
+//      step of a batch, so that every public array is current afterwards).
+// q.e != nullptr (2D): particles leaving their start triangle are queued
+// for walk_kernel instead of walking here.
+template <int DIM, typename FT>
+__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+                                                   DevState s, WalkQueue wq, int aux,
+                                                   int step_index, int* __restrict__ stats,
+                                                   uint32_t* __restrict__ err_word) {
+    __shared__ ZigTables zt;
+    load_zig(zt);
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
     int tri = s.tri[i];
@@ -407,6 +467,7 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     q.ltri = tri;
     q.ll = DIM == 3 ? s.lowerlayer[i] : 0;
     q.ll0 = q.ll;
+    q.defer = (DIM == 2) && (wq.e != nullptr);
     const int D = DIM;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -432,54 +493,78 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     if (p.model == 1) bnd_j = q.update_lsm1(dp);
     else q.err |= ERR_UNSUPPORTED;
 
+    uint32_t e = q.err | q.rng.err;
+    if (e) atomicOr(err_word, e);
+    if (q.deferred) {
+        int slot = queue_slot(wq);
+        WalkEntry w;
+        w.xn = q.x[0];
+        w.yn = q.x[1];
+        w.rng = q.rng.state;
+        w.i = i;
+        w.pad = 0;
+        wq.e[slot] = w;
+        return;
+    }
     if (p.bc_on) {
         q.compute_bc(bnd_j, stats);
     } else if (q.tri == PART_LOC_O || q.ll == PART_LOC_B || q.ll == PART_LOC_A) {
         q.deleted = true;
     }
-
-    uint32_t e = q.err | q.rng.err;
+    e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
+    q.store(s, i, aux, step_index, lastv);
+}
 
-    if (q.deleted) {
-        // lagrangian_particle_set.pyx:766-788; the tag records the step for
-        // the host-side retag (maxtag+1, ... in step then index order)
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            s.pos[(size_t)i * D + d] = 0.;
-            s.vel[(size_t)i * D + d] = 0.;
-            s.fvs[(size_t)i * D + d] = 0.;
-            s.last_pos[(size_t)i * D + d] = 0.;
-            s.last_vel[(size_t)i * D + d] = 0.;
+// Second half of the step for queued (2D) particles: path walk from the
+// start triangle (xylocalizer.pyx:338-435, then the global fallback) and the
+// boundary conditions.  Grid-stride over the entries of this step.
+template <typename FT>
+__global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+                                                   DevState s, WalkQueue wq, int aux,
+                                                   int step_index, int* __restrict__ stats,
+                                                   uint32_t* __restrict__ err_word) {
+    __shared__ ZigTables zt;
+    load_zig(zt);
+    const int count = *wq.count;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+        WalkEntry w = wq.e[j];
+        int i = w.i;
+        Particle<2, FT> q(m, f, p, zt);
+        int tri0 = s.tri[i];
+        double2 x0 = reinterpret_cast<const double2*>(s.pos)[i];
+        q.tri0 = tri0;
+        q.ltri = tri0;
+        q.ll = q.ll0 = 0;
+        q.x[0] = w.xn;
+        q.x[1] = w.yn;
+        q.x0[0] = x0.x;
+        q.x0[1] = x0.y;
+        q.rng.state = w.rng;
+        q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
+        q.rng.err = 0;
+        double lastv[3] = {0., 0., 0.};
+        if (aux >= 2) {
+            double2 v = reinterpret_cast<const double2*>(s.vel)[i];
+            lastv[0] = v.x;
+            lastv[1] = v.y;
         }
-        s.diameter[i] = 0.;
-        s.tri[i] = -1;
-        s.last_tri[i] = -1;
-        s.lowerlayer[i] = 0;
-        s.tag[i] = -2 - step_index;
-        s.rng[i] = q.rng.state;
-        return;
-    }
-#pragma unroll
-    for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = q.x[d];
-    s.tri[i] = q.tri;
-    if (DIM == 3) s.lowerlayer[i] = q.ll;
-    s.rng[i] = q.rng.state;
-    if (p.model >= 2 || aux >= 1) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) s.vel[(size_t)i * D + d] = q.up[d];
-    }
-    if (p.model == 3 || aux >= 1) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) s.fvs[(size_t)i * D + d] = q.us[d];
-    }
-    if (aux >= 2) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            s.last_pos[(size_t)i * D + d] = q.x0[d];
-            s.last_vel[(size_t)i * D + d] = lastv[d];
+        if (aux >= 1 || p.model >= 2) {
+            // LSM1: up = us = U(x0) (update_state_lsm1.pyx:144-163)
+            double ux, uy, uz;
+            q.velocity(tri0, 0, x0.x, x0.y, 0., ux, uy, uz);
+            q.up[0] = q.us[0] = ux;
+            q.up[1] = q.us[1] = uy;
         }
-        s.last_tri[i] = q.ltri;
+        int nk, bnd;
+        path_walk(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
+        if (nk == -1 && bnd == -1) nk = grid_locate(m, w.xn, w.yn);
+        q.tri = nk;
+        if (p.bc_on) q.compute_bc(bnd, stats);
+        else if (q.tri == PART_LOC_O) q.deleted = true;
+        uint32_t e = q.err | q.rng.err;
+        if (e) atomicOr(err_word, e);
+        q.store(s, i, aux, step_index, lastv);
     }
 }
 

@@ -159,8 +159,9 @@ __device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, 
 // LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
 // diffusion 658-726) with the boundary conditions of compute_bc.pyx.
 __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
-                                                           DevParams p, DevState s, int aux,
-                                                           int step_index, int* __restrict__ stats,
+                                                           DevParams p, DevState s, WalkQueue wq,
+                                                           int aux, int step_index,
+                                                           int* __restrict__ stats,
                                                            uint32_t* __restrict__ err_word) {
     __shared__ Zig32 z32;
     __shared__ ZigTables z64;
@@ -266,7 +267,24 @@ __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<
 
     if (bnd_j == -1) {
         ltri = tri0;
-        xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xn, yn, tri, bnd_j);
+        if (wq.e != nullptr) {
+            // leaves the start triangle: walk + boundary conditions in walk_kernel
+            if (!in_tri_mixed(m, t0, tri0, xn, yn)) {
+                if (rng.err) atomicOr(err_word, rng.err);
+                int slot = queue_slot(wq);
+                WalkEntry w;
+                w.xn = xn;
+                w.yn = yn;
+                w.rng = rng.state;
+                w.i = i;
+                w.pad = 0;
+                wq.e[slot] = w;
+                return;
+            }
+            tri = tri0;
+        } else {
+            xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xn, yn, tri, bnd_j);
+        }
     }
 
     bool deleted = false;

@@ -1,0 +1,185 @@
+"""Host-side logic that needs no GPU: parameters, mesh preprocessing,
+point-location grid, the C ABI surface, the Python API's failure modes."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+# ---------------------------------------------------------------------------
+# parameters (cylag/core/parameters.pyx:116-351)
+# ---------------------------------------------------------------------------
+def test_parameters_defaults_and_time_scheme():
+    from cylag_gb300.parameters import Parameters
+    assert Parameters({}).time_scheme == 4                      # LSM1, no diffusion
+    assert Parameters({"diffusion_model": 1}).time_scheme == 1  # LSM1 + diffusion
+    assert Parameters({"model": 2}).time_scheme == 5
+    assert Parameters({"model": 3, "diffusion_model": 1}).time_scheme == 5
+    assert Parameters({"model": 1, "time_scheme": 2}).time_scheme == 2
+    p = Parameters({"frozen_eulerian_fields": True, "initial_time": 5.})
+    assert p.initial_time == 0.
+
+
+def test_parameters_errors():
+    from cylag_gb300.parameters import Parameters
+    with pytest.raises(TypeError):
+        Parameters({"not_a_key": 1})
+    with pytest.raises(TypeError):
+        Parameters({"time_step": 1})        # int where the default is float
+    for bad in ({"model": 4}, {"rng_method": 0}, {"model": 3, "diffusion_model": 0},
+                {"model": 2, "diffusion_model": 1, "time_scheme": 2},
+                {"rebound_damping_coef": 1.5}, {"stranding_probability": -0.1}):
+        with pytest.raises(ValueError):
+            Parameters(bad).check_values()
+
+
+def test_parameters_match_reference():
+    import refpath
+    if not refpath.available():
+        pytest.skip("reference build not present")
+    cy = refpath.use_reference()
+    from cylag_gb300.parameters import Parameters
+    for d in ({}, {"model": 2}, {"model": 1, "diffusion_model": 2},
+              {"frozen_eulerian_fields": True, "initial_time": 3.}):
+        a, b = Parameters(d), cy.Parameters(d)
+        for k in ("time_scheme", "initial_time", "rng_method", "max_wall_rebounds",
+                  "rebound_damping_coef", "schmidt_number", "lsm3_edge_opt"):
+            assert getattr(a, k) == getattr(b, k), (d, k)
+
+
+# ---------------------------------------------------------------------------
+# mesh (cylag/geom/triangular_mesh.pyx)
+# ---------------------------------------------------------------------------
+def test_mesh_arrays_match_reference_golden():
+    from cylag_gb300.mesh import TriangularMesh
+    z = np.load(GOLDEN / "mesh_open.npz")
+    m = TriangularMesh(z["x"], z["y"], z["triangles"], boundary_points=z["boundary_points"],
+                       nopen=int(z["nopen"]))
+    for a in ("edges", "triedge_map", "edgetri_map", "edges_labels", "vertex_labels",
+              "gradx", "grady", "det", "signed_area"):
+        np.testing.assert_array_equal(getattr(m, a), z[a], err_msg=a)
+
+
+def test_mesh_rejects_bad_input():
+    from cylag_gb300.mesh import TriangularMesh
+    x = np.array([0., 1., 0., 2.])
+    y = np.array([0., 0., 1., 0.])
+    with pytest.raises(ValueError):
+        TriangularMesh(x, y, np.array([[0, 1, 3]], dtype=np.int32))   # zero area
+    with pytest.raises(ValueError):
+        TriangularMesh(x, y, np.array([[0, 1, 7]], dtype=np.int32))   # index out of range
+    with pytest.raises(ValueError):
+        TriangularMesh(np.array([0., np.nan, 0.]), y[:3], np.array([[0, 1, 2]], dtype=np.int32))
+
+
+def test_locator_grid_finds_lowest_index_triangle(oracle_lib):
+    """The bucket grid returns what an exhaustive lowest-index search returns,
+    for centroids, vertices (ties) and points outside."""
+    import ctypes as C
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    x, y, tri = synth.channel_mesh(400.0, 100.0, 41, 11, seed=3, jitter=0.3)
+    m = TriangularMesh(x, y, tri)
+    g = m.locator_grid()
+    ptr = lambda a: a.ctypes.data
+    mesh = oracle_lib.Mesh(m.nv, m.nt, m.ne, ptr(m.x), ptr(m.y), ptr(m.triangles), ptr(m.gradx),
+                           ptr(m.grady), ptr(m.det), ptr(m.edges), ptr(m.triedge_map),
+                           ptr(m.edgetri_map), ptr(m.edges_labels), g[0], g[1], g[2], g[3], g[4],
+                           ptr(g[5]), ptr(g[6]))
+    L = oracle_lib.lib()
+    cen = np.stack([x[tri].mean(1), y[tri].mean(1)], 1)
+    rng = np.random.default_rng(0)
+    pts = np.concatenate([cen, np.stack([x, y], 1), rng.uniform(-50, 450, (2000, 2))])
+    for px, py in pts:
+        a = L.cgo_locate(C.byref(mesh), px, py)
+        b = L.cgo_locate_exhaustive(C.byref(mesh), px, py)
+        assert a == b, (px, py, a, b)
+
+
+# ---------------------------------------------------------------------------
+# the C ABI
+# ---------------------------------------------------------------------------
+def header_functions():
+    text = (ROOT / "include" / "cylag_gpu.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|uint64_t)\s+(cg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from cylag_gb300 import _lib
+    if not _lib.library_path().exists():
+        from cylag_gb300 import build
+        build.build()
+    L = C.CDLL(str(_lib.library_path()))
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+    declared = {n for n, _, _ in _lib.SIGNATURES}
+    assert set(names) <= declared, set(names) - declared
+
+
+def test_library_fails_cleanly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from cylag_gb300 import _lib
+    L = _lib.load()
+    ctx = C.c_void_p()
+    assert L.cg_ctx_create(0, 0, C.byref(ctx)) == _lib.CG_ECUDA
+    assert not ctx.value
+    # null arguments are rejected, not dereferenced
+    assert L.cg_run_step(None, 1, None) == _lib.CG_EINVAL
+    assert L.cg_ctx_destroy(None) == _lib.CG_EINVAL
+
+
+def test_solver_refuses_to_run_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import cylag_gb300 as cg
+    from conftest import fields_from_case, load_golden, mesh_from_case
+    case, meta, _ = load_golden("couette")
+    f = fields_from_case(case)
+    fs = cg.EulerianFieldSet(mesh_from_case(case), dim=2, times=f["times"],
+                             elevation=f["elevation"], velocity_x=f["velocity_x"],
+                             velocity_y=f["velocity_y"])
+    ps = cg.LagrangianParticleSet(case["position"], dim=2)
+    with pytest.raises((RuntimeError, cg._lib.CylagGpuError)):
+        cg.Solver(fs, ps, meta["params"])
+
+
+def test_particle_set_host_arrays_before_attach():
+    import cylag_gb300 as cg
+    pos = np.array([[1., 2.], [3., 4.]])
+    ps = cg.LagrangianParticleSet(pos, dim=2, initial_pool_size=5)
+    assert ps.npart == 5 and ps.npart_active == 2
+    np.testing.assert_array_equal(ps.position[:2], pos)
+    np.testing.assert_array_equal(ps.inactive, [0, 0, 1, 1, 1])
+    with pytest.raises(ValueError):
+        cg.LagrangianParticleSet(np.zeros((3, 3)), dim=2)
+    with pytest.raises(ValueError):
+        cg.LagrangianParticleSet(pos, dim=2, initial_pool_size=1)
+
+
+def test_field_set_validation():
+    import cylag_gb300 as cg
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    x, y, tri = synth.channel_mesh(10., 10., 3, 3)
+    m = TriangularMesh(x, y, tri)
+    nv = len(x)
+    with pytest.raises(ValueError):
+        cg.EulerianFieldSet(m, times=np.array([0., 0.]), elevation=np.ones((2, nv)),
+                            velocity_x=np.ones((2, nv)), velocity_y=np.ones((2, nv)))
+    with pytest.raises(ValueError):
+        cg.EulerianFieldSet(m, times=np.zeros(1), elevation=np.ones((1, nv + 1)),
+                            velocity_x=np.ones((1, nv)), velocity_y=np.ones((1, nv)))
+    fs = cg.EulerianFieldSet(m, times=np.zeros(1), elevation=np.ones((1, nv)),
+                             velocity_x=np.ones((1, nv)), velocity_y=np.ones((1, nv)),
+                             opt_fields=np.ones((2, 1, nv)),
+                             opt_fields_names=["DISSIPATION", "TURBULENT ENERG."])
+    assert fs.fid_dissip == 4 and fs.fid_turbeng == 5
