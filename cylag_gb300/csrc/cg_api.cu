@@ -573,9 +573,14 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
                               r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), stats,
                               (uint32_t*)r->errw.p, c->stream);
-        if (r->use_queue)
-            launch_walk(r->prm.precision, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st,
-                        wq, aux, (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
+        if (r->use_queue) {
+            if (r->prm.precision == CG_PRECISION_MIXED)
+                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq, aux,
+                                  (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
+            else
+                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq,
+                                  aux, (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
+        }
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
         // simutime.pyx:77-84

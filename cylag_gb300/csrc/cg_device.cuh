@@ -357,6 +357,39 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
     bnd = -1;
 }
 
+// ---- FP32-filtered walk (mixed form) --------------------------------------
+// Orientation of (a, b, c) from FP32 offsets to a common origin, with a
+// bound on its rounding error; `certain` is false inside the bound.  Offsets
+// are rounded FP64 differences (relative error <= 2^-24 each), so the
+// computed value differs from the exact one by at most ~48 eps32 M^2, M the
+// largest offset magnitude; the bound takes 4e-6 M^2 (~67 eps32 M^2).  Beyond
+// it the exact value is nonzero with the FP32 sign, which is also the sign
+// the FP64 evaluation gives.
+__device__ __forceinline__ int orient32(float2 a, float2 b, float2 c, bool& certain) {
+    float d = (a.y - b.y) * (c.x - a.x) - (a.x - b.x) * (c.y - a.y);
+    float M = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(b.x), fabsf(b.y))),
+                    fmaxf(fabsf(c.x), fabsf(c.y)));
+    float bound = 4.0e-6f * M * M + 1.0e-30f;
+    certain = fabsf(d) > bound;
+    return d > 0.f ? 1 : 2;
+}
+
+// intersections.pyx:106-148 with the orientations decided in FP32 when all
+// four are certain (then none is zero and the result is o1 != o2 && o3 != o4,
+// exactly what the FP64 test gives); otherwise the FP64 test.
+__device__ __forceinline__ bool intersec2d_filtered(float2 p1, float2 e0, float2 e1, double p0x,
+                                                    double p0y, double p1x, double p1y,
+                                                    double2 E0, double2 E1) {
+    const float2 p0 = make_float2(0.f, 0.f);
+    bool c1, c2, c3, c4;
+    int o1 = orient32(p0, p1, e0, c1);
+    int o2 = orient32(p0, p1, e1, c2);
+    int o3 = orient32(e0, e1, p0, c3);
+    int o4 = orient32(e0, e1, p1, c4);
+    if (c1 && c2 && c3 && c4) return o1 != o2 && o3 != o4;
+    return intersec2d(p0x, p0y, p1x, p1y, E0.x, E0.y, E1.x, E1.y);
+}
+
 // xylocalizer.pyx:27-124, method 3
 __device__ inline void xy_localize(const DevMesh& m, int k, double p0x, double p0y, double x,
                                    double y, int& new_k, int& bnd) {
@@ -429,6 +462,97 @@ template <int DIM, typename FT>
 __device__ __forceinline__ double p1_gy(const FT* __restrict__ f, int off, const P1& p, int slot) {
     return nodev<DIM>(f, off + p.i0, slot) * p.gy0 + nodev<DIM>(f, off + p.i1, slot) * p.gy1 +
            nodev<DIM>(f, off + p.i2, slot) * p.gy2;
+}
+
+// per-triangle data of the FP32 barycentric evaluation
+struct Tri32 {
+    int4 tv;      // v0, v1, v2, e0
+    double2 a;    // vertex a (FP64)
+    float4 g0;    // gx0 gx1 gx2 gy0
+    float4 g1;    // gy1 gy2 - -
+};
+
+__device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
+    Tri32 t;
+    t.tv = __ldg(&m.tv[2 * k]);
+    t.a = __ldg(&m.geo[6 * (size_t)k]);
+    t.g0 = __ldg(&m.g32[2 * k]);
+    t.g1 = __ldg(&m.g32[2 * k + 1]);
+    return t;
+}
+
+struct Bary {
+    float l0, l1, l2;
+    float e0, e1, e2;   // rounding bounds of l0, l1, l2
+};
+
+// barycentric coordinates of (x, y): l_j = gx_j (x - xa) + gy_j (y - ya)
+__device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
+    Bary b;
+    float rx = (float)(x - t.a.x), ry = (float)(y - t.a.y);
+    float p1 = t.g0.y * rx, q1 = t.g1.x * ry;
+    float p2 = t.g0.z * rx, q2 = t.g1.y * ry;
+    b.l1 = p1 + q1;
+    b.l2 = p2 + q2;
+    b.l0 = 1.f - b.l1 - b.l2;
+    // |error| <= ~4 ulp of the terms (offset, gradient and product roundings)
+    b.e1 = 6.0e-7f * (fabsf(p1) + fabsf(q1)) + 1.0e-6f;
+    b.e2 = 6.0e-7f * (fabsf(p2) + fabsf(q2)) + 1.0e-6f;
+    b.e0 = b.e1 + b.e2 + 1.0e-6f;
+    return b;
+}
+
+// same decision as in_tri (the FP64 predicate), FP32 outside the band
+__device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, int k, double x,
+                                             double y) {
+    Bary b = bary32(t, x, y);
+    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return true;
+    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return false;
+    return in_tri(m, k, x, y);
+}
+
+// xylocalizer.pyx:338-435 with FP32-filtered predicates: the in-element
+// tests through in_tri_mixed, the segment/edge tests through
+// intersec2d_filtered, both falling back to FP64 where the FP32 value is
+// within its rounding bound.  Same decisions, hence the same triangle or
+// boundary edge, as path_walk.
+__device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, double p0y, double x,
+                                       double y, int& new_k, int& bnd) {
+    int intersected_edge = -1;
+    const float2 p1 = make_float2((float)(x - p0x), (float)(y - p0y));
+    for (int niter = 0; niter <= NITER_MAX; ++niter) {
+        int4 ta = __ldg(&m.tv[2 * k]);
+        int4 tb = __ldg(&m.tv[2 * k + 1]);
+        int ed[3] = {ta.w, tb.x, tb.y};
+        bool intersects = false;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int j = ed[i];
+            if (j == intersected_edge) continue;
+            int4 e = __ldg(&m.edge[j]);
+            double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+            float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
+            float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
+            if (intersec2d_filtered(p1, fa, fb, p0x, p0y, x, y, a, b)) {
+                intersects = true;
+                int kn = (e.z == k) ? e.w : e.z;
+                if (kn == -1) { new_k = -1; bnd = j; return; }
+                Tri32 tn = load_tri32(m, kn);
+                if (in_tri_mixed(m, tn, kn, x, y)) { new_k = kn; bnd = -1; return; }
+                k = kn;
+                intersected_edge = j;
+                break;
+            }
+        }
+        if (!intersects) {
+            Tri32 tk = load_tri32(m, k);
+            new_k = in_tri_mixed(m, tk, k, x, y) ? k : -1;
+            bnd = -1;
+            return;
+        }
+    }
+    new_k = -1;
+    bnd = -1;
 }
 
 }  // namespace cg

@@ -33,10 +33,14 @@ void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* p
                        const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
                        cudaStream_t st);
 
-// second half of a 2D step: path walk + boundary conditions of queued particles
-void launch_walk(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
-                 const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
-                 int step_index, int* stats, uint32_t* err, cudaStream_t st);
+// second half of a 2D step: path walk + boundary conditions of queued
+// particles (exact FP64 predicates / FP32-filtered predicates)
+void launch_walk_plain(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
+                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
+                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+void launch_walk_mixed(const DevMesh& m, const void* cur, int npoints, int nlayers,
+                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
+                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
 
 // The same step, mixed-precision form (FP32 node records).
 void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,

@@ -2,6 +2,8 @@
 // increments, FP64 positions and localization decisions).  Compiled with
 // the default FMA contraction; the exact FP64 predicates it shares with the
 // plain form are written with _rn intrinsics and are not contracted.
+#include <cstdlib>
+
 #include "cg_internal.h"
 #include "cg_step_mixed.cuh"
 
@@ -16,13 +18,31 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
     if (nb == 0) return;
     if (dim == 2) {
         DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 2, prev_valid};
-        step_mixed2d_kernel<<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+        // occupancy variant: 4 blocks/SM (64 registers) by default, 3 (80) on request
+        static int minb = [] {
+            const char* e = getenv("CYLAG_MIXED_MINB");
+            return (e && atoi(e) == 3) ? 3 : 4;
+        }();
+        if (minb == 3)
+            step_mixed2d_kernel<3><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+        else
+            step_mixed2d_kernel<4><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
     } else {
         // 3D: FP32 node records, FP64 arithmetic
         DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 3, prev_valid};
         WalkQueue none{nullptr, nullptr};
         step_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, none, aux, step_index, stats, err);
     }
+}
+
+void launch_walk_mixed(const DevMesh& m, const void* cur, int npoints, int nlayers,
+                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
+                       int step_index, int* stats, uint32_t* err, cudaStream_t st) {
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
+    walk_kernel<float, true><<<nsm * 8, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
 }
 
 }  // namespace cg

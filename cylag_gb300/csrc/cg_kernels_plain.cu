@@ -85,7 +85,7 @@ void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* p
     }
 }
 
-void launch_walk(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
+void launch_walk_plain(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
                  const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
                  int step_index, int* stats, uint32_t* err, cudaStream_t st) {
     // grid-stride over the (device-side) entry count: a fixed grid of
@@ -94,13 +94,9 @@ void launch_walk(int precision, const DevMesh& m, const void* cur, int npoints, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int nb = nsm * 8;
-    if (precision == 0) {
-        DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
-        walk_kernel<double><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
-    } else {
-        DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
-        walk_kernel<float><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
-    }
+    (void)precision;
+    DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
+    walk_kernel<double, false><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
 }
 
 // ---------------------------------------------------------------------------

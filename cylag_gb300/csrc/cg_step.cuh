@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
 // Second half of the step for queued (2D) particles: path walk from the
 // start triangle (xylocalizer.pyx:338-435, then the global fallback) and the
 // boundary conditions.  Grid-stride over the entries of this step.
-template <typename FT>
+template <typename FT, bool MIXED>
 __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, DevParams p,
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
@@ -557,7 +557,8 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
             q.up[1] = q.us[1] = uy;
         }
         int nk, bnd;
-        path_walk(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
+        if (MIXED) path_walk_mixed(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
+        else path_walk(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
         if (nk == -1 && bnd == -1) nk = grid_locate(m, w.xn, w.yn);
         q.tri = nk;
         if (p.bc_on) q.compute_bc(bnd, stats);

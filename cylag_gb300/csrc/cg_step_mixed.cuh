@@ -81,60 +81,13 @@ __device__ inline void pair32(Rng& r, int method, const Zig32& z, float& a, floa
     }
 }
 
-// per-triangle data of the FP32 barycentric evaluation
-struct Tri32 {
-    int4 tv;      // v0, v1, v2, e0
-    double2 a;    // vertex a (FP64)
-    float4 g0;    // gx0 gx1 gx2 gy0
-    float4 g1;    // gy1 gy2 - -
-};
-
-__device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
-    Tri32 t;
-    t.tv = __ldg(&m.tv[2 * k]);
-    t.a = __ldg(&m.geo[6 * (size_t)k]);
-    t.g0 = __ldg(&m.g32[2 * k]);
-    t.g1 = __ldg(&m.g32[2 * k + 1]);
-    return t;
-}
-
-struct Bary {
-    float l0, l1, l2;
-    float e0, e1, e2;   // rounding bounds of l0, l1, l2
-};
-
-// barycentric coordinates of (x, y): l_j = gx_j (x - xa) + gy_j (y - ya)
-__device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
-    Bary b;
-    float rx = (float)(x - t.a.x), ry = (float)(y - t.a.y);
-    float p1 = t.g0.y * rx, q1 = t.g1.x * ry;
-    float p2 = t.g0.z * rx, q2 = t.g1.y * ry;
-    b.l1 = p1 + q1;
-    b.l2 = p2 + q2;
-    b.l0 = 1.f - b.l1 - b.l2;
-    // |error| <= ~4 ulp of the terms (offset, gradient and product roundings)
-    b.e1 = 6.0e-7f * (fabsf(p1) + fabsf(q1)) + 1.0e-6f;
-    b.e2 = 6.0e-7f * (fabsf(p2) + fabsf(q2)) + 1.0e-6f;
-    b.e0 = b.e1 + b.e2 + 1.0e-6f;
-    return b;
-}
-
-// same decision as in_tri (the FP64 predicate), FP32 outside the band
-__device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, int k, double x,
-                                             double y) {
-    Bary b = bary32(t, x, y);
-    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return true;
-    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return false;
-    return in_tri(m, k, x, y);
-}
-
 // xylocalizer.pyx:27-124 method 3, first test through the FP32 filter
 __device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32& t, int k,
                                                   double p0x, double p0y, double x, double y,
                                                   int& new_k, int& bnd) {
     bnd = -1;
     if (in_tri_mixed(m, t, k, x, y)) { new_k = k; return; }
-    path_walk(m, k, p0x, p0y, x, y, new_k, bnd);
+    path_walk_mixed(m, k, p0x, p0y, x, y, new_k, bnd);
     if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
 }
 
@@ -156,9 +109,79 @@ __device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, 
     uy = b.l0 * n.n0.y + b.l1 * n.n1.y + b.l2 * n.n2.y;
 }
 
+// Runge-Kutta stages of update_state_lsm1.pyx:179-656 in the mixed form:
+// each stage point is localized from (tri0, x0); a stage leaving the domain
+// stops the scheme with an Euler step.  Kept out of line (cold path).
+__device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __restrict__ cur,
+                                      const DevParams& p, const Tri32& t0, int tri0, double2 x0,
+                                      float ux, float uy, double& xn, double& yn, int& tri,
+                                      int& bnd_j) {
+    const float dt = (float)p.dt;
+    const float up0 = ux, up1 = uy;
+    const int ns = p.time_scheme == 2 ? 1 : (p.time_scheme == 3 ? 2 : 3);
+    float kx[4], ky[4];
+    kx[0] = ux * dt;
+    ky[0] = uy * dt;
+    for (int st = 0; st < ns; ++st) {
+        float cst;
+        if (p.time_scheme == 2) cst = 0.5f;
+        else if (p.time_scheme == 3) cst = st == 0 ? (1.f / 3.f) : (2.f / 3.f);
+        else cst = st < 2 ? 0.5f : 1.f;
+        float fx = (p.time_scheme == 2) ? 0.5f * ux * dt : cst * kx[st];
+        float fy = (p.time_scheme == 2) ? 0.5f * uy * dt : cst * ky[st];
+        double xt = x0.x + (double)fx, yt = x0.y + (double)fy;
+        int tt, bnd;
+        xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xt, yt, tt, bnd);
+        if (bnd != -1) {
+            tri = tt;
+            xn = x0.x + (double)(up0 * dt);
+            yn = x0.y + (double)(up1 * dt);
+            bnd_j = bnd;
+            return;
+        }
+        Tri32 ts = load_tri32(m, tt);
+        Node4 ns4 = load_nodes(cur, ts);
+        float sx, sy;
+        vel32(ns4, bary32(ts, xt, yt), sx, sy);
+        kx[st + 1] = sx * dt;
+        ky[st + 1] = sy * dt;
+    }
+    float dxs, dys;
+    if (p.time_scheme == 2) { dxs = kx[1]; dys = ky[1]; }
+    else if (p.time_scheme == 3) { dxs = 0.25f * kx[0] + 0.75f * kx[2]; dys = 0.25f * ky[0] + 0.75f * ky[2]; }
+    else { dxs = (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) / 6.f; dys = (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) / 6.f; }
+    xn += (double)dxs;
+    yn += (double)dys;
+}
+
+// Boundary conditions (compute_bc.pyx:35-395) with the FP64 mirror and the
+// exact walk of the plain form.  Out of line (cold path).
+__device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<float>& f,
+                                      const DevParams& p, const ZigTables& z64, Rng& rng,
+                                      double2 x0, float up0, float up1, int tri0, int ltri,
+                                      int bnd_j, int* stats, double& xn, double& yn, int& tri,
+                                      bool& deleted) {
+    Particle<2, float> q(m, f, p, z64);
+    q.rng = rng;
+    q.x[0] = xn; q.x[1] = yn;
+    q.x0[0] = x0.x; q.x0[1] = x0.y;
+    q.up[0] = up0; q.up[1] = up1;
+    q.us[0] = up0; q.us[1] = up1;
+    q.tri = tri; q.tri0 = tri0; q.ltri = ltri; q.ll = 0; q.ll0 = 0;
+    if (p.bc_on) q.compute_bc(bnd_j, stats);
+    else if (q.tri == PART_LOC_O) q.deleted = true;
+    rng = q.rng;
+    rng.err |= q.err;
+    xn = q.x[0];
+    yn = q.x[1];
+    tri = q.tri;
+    deleted = q.deleted;
+}
+
 // LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
 // diffusion 658-726) with the boundary conditions of compute_bc.pyx.
-__global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                            DevParams p, DevState s, WalkQueue wq,
                                                            int aux, int step_index,
                                                            int* __restrict__ stats,
@@ -176,13 +199,15 @@ __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
-    int tri0 = s.tri[i];
+    // particle state streams through L2 once per step: evict-first loads and
+    // stores keep the mesh and node records resident in L2
+    int tri0 = __ldcs(&s.tri[i]);
     if (tri0 < 0) return;
     const float4* __restrict__ cur = reinterpret_cast<const float4*>(f.cur);
-    double2 x0 = reinterpret_cast<const double2*>(s.pos)[i];
+    double2 x0 = __ldcs(reinterpret_cast<const double2*>(s.pos) + i);
     Rng rng;
-    rng.state = s.rng[i];
-    rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
+    rng.state = __ldcs(reinterpret_cast<const unsigned long long*>(s.rng) + i);
+    rng.inc = ((uint64_t)(uint32_t)__ldcs(&s.tag[i]) << 1) | 1ULL;
     rng.err = 0;
     double2 lastv = make_double2(0., 0.);
     if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[i];
@@ -196,53 +221,12 @@ __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<
     float up0 = ux, up1 = uy;   // velocity = fluid velocity seen = U(x0)
     double xn = x0.x, yn = x0.y;
     int tri = tri0, ltri = tri0, bnd_j = -1;
-    bool stopped = false;
 
     if (p.time_scheme == 1) {
         xn += (double)(ux * dt);
         yn += (double)(uy * dt);
     } else {
-        // Runge-Kutta stages (update_state_lsm1.pyx:179-656): each stage point
-        // is localized from (tri0, x0); a stage leaving the domain stops the
-        // scheme with an Euler step.
-        const int ns = p.time_scheme == 2 ? 1 : (p.time_scheme == 3 ? 2 : 3);
-        float kx[4], ky[4];
-        kx[0] = ux * dt;
-        ky[0] = uy * dt;
-        for (int st = 0; st < ns && !stopped; ++st) {
-            float cst;
-            if (p.time_scheme == 2) cst = 0.5f;
-            else if (p.time_scheme == 3) cst = st == 0 ? (1.f / 3.f) : (2.f / 3.f);
-            else cst = st < 2 ? 0.5f : 1.f;
-            float fx = (p.time_scheme == 2) ? 0.5f * ux * dt : cst * kx[st];
-            float fy = (p.time_scheme == 2) ? 0.5f * uy * dt : cst * ky[st];
-            double xt = x0.x + (double)fx, yt = x0.y + (double)fy;
-            int tt, bnd;
-            ltri = tri0;
-            xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xt, yt, tt, bnd);
-            if (bnd != -1) {
-                tri = tt;
-                xn = x0.x + (double)(up0 * dt);
-                yn = x0.y + (double)(up1 * dt);
-                bnd_j = bnd;
-                stopped = true;
-                break;
-            }
-            Tri32 ts = load_tri32(m, tt);
-            Node4 ns4 = load_nodes(cur, ts);
-            float sx, sy;
-            vel32(ns4, bary32(ts, xt, yt), sx, sy);
-            kx[st + 1] = sx * dt;
-            ky[st + 1] = sy * dt;
-        }
-        if (!stopped) {
-            float dxs, dys;
-            if (p.time_scheme == 2) { dxs = kx[1]; dys = ky[1]; }
-            else if (p.time_scheme == 3) { dxs = 0.25f * kx[0] + 0.75f * kx[2]; dys = 0.25f * ky[0] + 0.75f * ky[2]; }
-            else { dxs = (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) / 6.f; dys = (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) / 6.f; }
-            xn += (double)dxs;
-            yn += (double)dys;
-        }
+        rk_mixed(m, cur, p, t0, tri0, x0, ux, uy, xn, yn, tri, bnd_j);
     }
 
     // diffusion (update_state_lsm1.pyx:658-726), K at the start point
@@ -288,24 +272,8 @@ __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<
     }
 
     bool deleted = false;
-    if (bnd_j != -1 || tri == PART_LOC_O) {
-        // rare: boundary conditions with the FP64 mirror and exact walk
-        Particle<2, float> q(m, f, p, z64);
-        q.rng = rng;
-        q.x[0] = xn; q.x[1] = yn;
-        q.x0[0] = x0.x; q.x0[1] = x0.y;
-        q.up[0] = up0; q.up[1] = up1;
-        q.us[0] = up0; q.us[1] = up1;
-        q.tri = tri; q.tri0 = tri0; q.ltri = ltri; q.ll = 0; q.ll0 = 0;
-        if (p.bc_on) q.compute_bc(bnd_j, stats);
-        else if (q.tri == PART_LOC_O) q.deleted = true;
-        rng = q.rng;
-        xn = q.x[0];
-        yn = q.x[1];
-        tri = q.tri;
-        deleted = q.deleted;
-        rng.err |= q.err;
-    }
+    if (bnd_j != -1 || tri == PART_LOC_O)
+        bc_mixed(m, f, p, z64, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted);
     if (rng.err) atomicOr(err_word, rng.err);
 
     if (deleted) {
@@ -322,9 +290,9 @@ __global__ void __launch_bounds__(256) step_mixed2d_kernel(DevMesh m, DevFields<
         s.rng[i] = rng.state;
         return;
     }
-    reinterpret_cast<double2*>(s.pos)[i] = make_double2(xn, yn);
-    s.tri[i] = tri;
-    s.rng[i] = rng.state;
+    __stcs(reinterpret_cast<double2*>(s.pos) + i, make_double2(xn, yn));
+    __stcs(&s.tri[i], tri);
+    __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);
     if (aux >= 1) {
         reinterpret_cast<double2*>(s.vel)[i] = make_double2(up0, up1);
         reinterpret_cast<double2*>(s.fvs)[i] = make_double2(up0, up1);
