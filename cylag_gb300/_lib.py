@@ -65,7 +65,7 @@ class Params(C.Structure):
                 ("drag_coefficient_model", I32), ("drag_coefficient", F64),
                 ("added_mass_force", I32), ("added_mass_coef", F64),
                 ("buoyancy_velocity_model", I32), ("buoyancy_velocity", F64),
-                ("precision", I32), ("seed", C.c_uint64)]
+                ("precision", I32), ("seed", C.c_uint64), ("sort_period", I32)]
 
 
 class StateDesc(C.Structure):

@@ -29,6 +29,7 @@ UNITS = {
     "cg_api.cu": ["-fmad=false"],
     "cg_kernels_plain.cu": ["-fmad=false"],
     "cg_kernels_mixed.cu": [],
+    "cg_sort.cu": [],
 }
 
 

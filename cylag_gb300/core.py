@@ -377,11 +377,14 @@ class Solver:
 
     Extra keyword arguments (not in the reference): ``precision``
     ('fp64' plain form or 'mixed'), ``seed`` (PCG32 seed of every particle
-    stream), ``device`` (CUDA ordinal), ``hbm_budget`` (bytes, 0 = none).
+    stream), ``device`` (CUDA ordinal), ``hbm_budget`` (bytes, 0 = none),
+    ``sort_period`` (steps between re-sorts of the particles by element, 0 =
+    never; results do not depend on it).
     """
 
     def __init__(self, field_set, particle_set, parameters={}, sources=None,
-                 control_sections=None, precision="fp64", seed=0, device=0, hbm_budget=0):
+                 control_sections=None, precision="fp64", seed=0, device=0, hbm_budget=0,
+                 sort_period=25):
         self.parameters = Parameters(parameters)
         self.parameters.check_values()
         P = self.parameters
@@ -431,7 +434,7 @@ class Solver:
             P.rebound_damping_coef, P.wall_roughness_angle, P.stranding_probability,
             P.water_density, ps.dim, ps.density, ps.drag_coef_model, ps.drag_coef,
             int(bool(ps.added_mass_force)), ps.added_mass_coef, ps.buoyancy_velocity_model,
-            ps.buoyancy_velocity_value, prec, self.seed)
+            ps.buoyancy_velocity_value, prec, self.seed, int(sort_period))
         self._run = C.c_void_p()
         self._create_run()
         _lib.check(self._ctx, self.L.cg_run_seed(self._run))

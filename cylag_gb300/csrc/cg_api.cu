@@ -63,6 +63,9 @@ struct cg_run {
     DevBuf errw;
     DevBuf queue;          // walk queue: count (first 256 B) + one entry per particle
     bool use_queue = false;
+    DevBuf sortbuf;        // element-order working copies (cg_sort.cu)
+    SortBuffers sb{};
+    int sort_period = 0;
     uint64_t bytes = 0;
     std::vector<cudaEvent_t> ev;
     int last_launches = 0;
@@ -240,6 +243,27 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         g32[2 * k] = make_float4((float)gx[0], (float)gx[1], (float)gx[2], (float)gy[0]);
         g32[2 * k + 1] = make_float4((float)gy[1], (float)gy[2], 0.f, 0.f);
     }
+    // packed 64-byte mixed-form record (see DevMesh::t64)
+    std::vector<int4> t64(4 * (size_t)nt);
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        const int32_t* e = d->triedge_map + 3 * k;
+        double xa = d->x[t[0]], ya = d->y[t[0]];
+        long long bx, by;
+        memcpy(&bx, &xa, 8);
+        memcpy(&by, &ya, 8);
+        t64[4 * k + 0] = make_int4(t[0], t[1], t[2], e[0]);
+        t64[4 * k + 1] = make_int4((int)(bx & 0xffffffffLL), (int)(bx >> 32),
+                                   (int)(by & 0xffffffffLL), (int)(by >> 32));
+        float4 g0 = g32[2 * k], g1 = g32[2 * k + 1];
+        int4 gi0, gi1;
+        memcpy(&gi0, &g0, 16);
+        memcpy(&gi1, &g1, 8);
+        gi1.z = e[1];
+        gi1.w = e[2];
+        t64[4 * k + 2] = gi0;
+        t64[4 * k + 3] = gi1;
+    }
     std::vector<int4> edge(ne);
     std::vector<int> lab(ne);
     for (int j = 0; j < ne; ++j) {
@@ -254,19 +278,20 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     int rc;
     const double2 *p_xy, *p_basis, *p_geo;
     const float4* p_g32;
-    const int4 *p_tv, *p_edge;
+    const int4 *p_tv, *p_edge, *p_t64;
     const int *p_lab, *p_gs, *p_gt;
     if ((rc = upload(c, xy, p_xy))) return rc;
     if ((rc = upload(c, tv, p_tv))) return rc;
     if ((rc = upload(c, basis, p_basis))) return rc;
     if ((rc = upload(c, geo, p_geo))) return rc;
     if ((rc = upload(c, g32, p_g32))) return rc;
+    if ((rc = upload(c, t64, p_t64))) return rc;
     if ((rc = upload(c, edge, p_edge))) return rc;
     if ((rc = upload(c, lab, p_lab))) return rc;
     if ((rc = upload(c, gstart, p_gs))) return rc;
     if ((rc = upload(c, gtris, p_gt))) return rc;
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
-    m.geo = p_geo; m.g32 = p_g32;
+    m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64;
     m.gstart = p_gs; m.gtris = p_gt;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;
@@ -379,7 +404,26 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
     bool use_queue = c->fdim == 2 && s->n > 0;
     size_t queue_bytes = use_queue ? 256 + (size_t)s->n * sizeof(WalkEntry) : 0;
-    uint64_t need = state_bytes + 2 * rec_bytes + 64 + queue_bytes;
+    // element sort: 2D runs, keys nt + 1 <= 4096 scan tiles of 4096
+    int nkeys = c->mesh.nt + 1;
+    bool use_sort = p->sort_period > 0 && c->fdim == 2 && s->n > 0 &&
+                    scan_scratch_ints(nkeys) <= 4096;
+    size_t n = (size_t)s->n;
+    size_t sort_bytes = 0;
+    size_t off_count = 0, off_sums = 0, off_perm = 0, off_pos = 0, off_tri = 0, off_tag = 0,
+           off_rng = 0;
+    if (use_sort) {
+        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+        off_count = 0;
+        off_sums = al(off_count + (size_t)nkeys * 4);
+        off_perm = al(off_sums + (size_t)scan_scratch_ints(nkeys) * 4);
+        off_pos = al(off_perm + n * 4);
+        off_tri = al(off_pos + n * 16);
+        off_tag = al(off_tri + n * 4);
+        off_rng = al(off_tag + n * 4);
+        sort_bytes = al(off_rng + n * 8);
+    }
+    uint64_t need = state_bytes + 2 * rec_bytes + 64 + queue_bytes + sort_bytes;
     if (c->budget && c->used + need > c->budget)
         return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
                        (unsigned long long)need, (unsigned long long)c->used,
@@ -391,12 +435,24 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->prm = *p;
     int rc;
     if ((rc = dalloc(c, r->cur, rec_bytes)) || (rc = dalloc(c, r->prev, rec_bytes)) ||
-        (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->queue, queue_bytes))) {
-        dfree(r->cur); dfree(r->prev); dfree(r->errw); dfree(r->queue);
+        (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->queue, queue_bytes)) ||
+        (rc = dalloc(c, r->sortbuf, sort_bytes))) {
+        dfree(r->cur); dfree(r->prev); dfree(r->errw); dfree(r->queue); dfree(r->sortbuf);
         delete r;
         return rc;
     }
     r->use_queue = use_queue;
+    if (use_sort) {
+        char* b = (char*)r->sortbuf.p;
+        r->sb.count = (int*)(b + off_count);
+        r->sb.block_sums = (int*)(b + off_sums);
+        r->sb.perm = (int*)(b + off_perm);
+        r->sb.pos = (double2*)(b + off_pos);
+        r->sb.tri = (int*)(b + off_tri);
+        r->sb.tag = (int*)(b + off_tag);
+        r->sb.rng = (unsigned long long*)(b + off_rng);
+        r->sort_period = p->sort_period;
+    }
     cudaMemsetAsync(r->errw.p, 0, 64, c->stream);
     r->bytes = need;
     c->used += need;
@@ -464,6 +520,7 @@ int cg_run_destroy(cg_run* r) {
     dfree(r->stats);
     dfree(r->errw);
     dfree(r->queue);
+    dfree(r->sortbuf);
     for (auto e : r->ev) cudaEventDestroy(e);
     c->used -= r->bytes;
     delete r;
@@ -553,7 +610,19 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaEventCreate(&e));
         r->ev.push_back(e);
     }
+    // element-sorted working state for chunks of sort_period steps
+    DevState ws = r->st;
+    if (r->sort_period > 0) {
+        ws.pos = (double*)r->sb.pos;
+        ws.tri = r->sb.tri;
+        ws.tag = r->sb.tag;
+        ws.rng = (uint64_t*)r->sb.rng;
+        ws.slot = r->sb.perm;
+    }
     for (int s = 0; s < nsteps; ++s) {
+        if (r->sort_period > 0 && s % r->sort_period == 0)
+            launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
+        const DevState& run_state = r->sort_period > 0 ? ws : r->st;
         // solver.pyx:440: fields at the step-start time
         if ((rc = time_interpolation(r, r->time))) return rc;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
@@ -567,22 +636,24 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         }
         if (r->prm.precision == CG_PRECISION_MIXED)
             launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), stats,
+                              r->prev_valid, r->dp, run_state, wq, aux, (int)(r->iteration), stats,
                               (uint32_t*)r->errw.p, c->stream);
         else
             launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), stats,
+                              r->prev_valid, r->dp, run_state, wq, aux, (int)(r->iteration), stats,
                               (uint32_t*)r->errw.p, c->stream);
         if (r->use_queue) {
             if (r->prm.precision == CG_PRECISION_MIXED)
-                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq, aux,
+                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, run_state, wq, aux,
                                   (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
             else
-                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq,
+                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, run_state, wq,
                                   aux, (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
         }
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
+        if (r->sort_period > 0 && (s % r->sort_period == r->sort_period - 1 || s == nsteps - 1))
+            launch_sort_scatter(r->st, r->sb, c->stream);
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;

@@ -51,6 +51,9 @@ struct DevMesh {
     const double2* __restrict__ geo;
     // [2*nt] FP32 P1 gradients {gx0,gx1,gx2,gy0}, {gy1,gy2,-,-} (mixed form)
     const float4* __restrict__ g32;
+    // [4*nt] packed 64-byte record per triangle for the mixed form:
+    // {v0, v1, v2, e0} | {xa, ya} (FP64) | {gx0, gx1, gx2, gy0} | {gy1, gy2, e1, e2}
+    const int4* __restrict__ t64;
     const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
     const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
     const int4* __restrict__ edge;      // [ne]: {n0, n1, t0, t1}
@@ -99,7 +102,15 @@ struct DevState {
     int* __restrict__ tag;
     double* __restrict__ diameter;
     uint64_t* __restrict__ rng;
+    // sorted runs: pos/tri/tag/rng are working copies in sorted order and
+    // slot[i] is the caller's index of working particle i, where the
+    // remaining arrays (velocities, last_*, diameter, lowerlayer) live
+    const int* __restrict__ slot;
 };
+
+__device__ __forceinline__ int aux_index(const DevState& s, int i) {
+    return s.slot ? __ldg(&s.slot[i]) : i;
+}
 
 // Particles that leave their start triangle are finished by a second kernel
 // (path walk + boundary conditions) from a compacted queue, so that the
@@ -474,11 +485,21 @@ struct Tri32 {
 
 __device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
     Tri32 t;
-    t.tv = __ldg(&m.tv[2 * k]);
-    t.a = __ldg(&m.geo[6 * (size_t)k]);
-    t.g0 = __ldg(&m.g32[2 * k]);
-    t.g1 = __ldg(&m.g32[2 * k + 1]);
+    const int4* r = m.t64 + 4 * (size_t)k;
+    t.tv = __ldg(&r[0]);
+    int4 a = __ldg(&r[1]);
+    t.a = make_double2(__hiloint2double(a.y, a.x), __hiloint2double(a.w, a.z));
+    int4 g0 = __ldg(&r[2]);
+    t.g0 = make_float4(__int_as_float(g0.x), __int_as_float(g0.y), __int_as_float(g0.z),
+                       __int_as_float(g0.w));
+    int4 g1 = __ldg(&r[3]);
+    t.g1 = make_float4(__int_as_float(g1.x), __int_as_float(g1.y), __int_as_float(g1.z),
+                       __int_as_float(g1.w));   // z, w: edge ids e1, e2 as bits
     return t;
+}
+
+__device__ __forceinline__ int tri32_edge(const Tri32& t, int i) {
+    return i == 0 ? t.tv.w : (i == 1 ? __float_as_int(t.g1.z) : __float_as_int(t.g1.w));
 }
 
 struct Bary {
@@ -520,14 +541,12 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
                                        double y, int& new_k, int& bnd) {
     int intersected_edge = -1;
     const float2 p1 = make_float2((float)(x - p0x), (float)(y - p0y));
+    Tri32 tk = load_tri32(m, k);
     for (int niter = 0; niter <= NITER_MAX; ++niter) {
-        int4 ta = __ldg(&m.tv[2 * k]);
-        int4 tb = __ldg(&m.tv[2 * k + 1]);
-        int ed[3] = {ta.w, tb.x, tb.y};
         bool intersects = false;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            int j = ed[i];
+            int j = tri32_edge(tk, i);
             if (j == intersected_edge) continue;
             int4 e = __ldg(&m.edge[j]);
             double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
@@ -540,12 +559,12 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
                 Tri32 tn = load_tri32(m, kn);
                 if (in_tri_mixed(m, tn, kn, x, y)) { new_k = kn; bnd = -1; return; }
                 k = kn;
+                tk = tn;
                 intersected_edge = j;
                 break;
             }
         }
         if (!intersects) {
-            Tri32 tk = load_tri32(m, k);
             new_k = in_tri_mixed(m, tk, k, x, y) ? k : -1;
             bnd = -1;
             return;

@@ -54,6 +54,20 @@ void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int 
                  int nlayers, const DevParams& p, const DevState& s, int velocity_init,
                  uint32_t* err, cudaStream_t st);
 
+// Working copies of the per-step state in element order (cg_sort.cu).
+struct SortBuffers {
+    int* count;          // [nt + 1] histogram, then scan offsets
+    int* block_sums;     // [scan_scratch_ints(nt + 1)]
+    int* perm;           // [n] working index -> caller index
+    double2* pos;        // [n]
+    int* tri;            // [n]
+    int* tag;            // [n]
+    unsigned long long* rng;  // [n]
+};
+int scan_scratch_ints(int nkeys);
+void launch_sort_gather(const DevState& user, int nt, const SortBuffers& b, cudaStream_t st);
+void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st);
+
 // rng[i] = pcg32_seed(seed, tag[i])
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);
 

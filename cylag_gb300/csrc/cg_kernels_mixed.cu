@@ -18,10 +18,10 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
     if (nb == 0) return;
     if (dim == 2) {
         DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 2, prev_valid};
-        // occupancy variant: 4 blocks/SM (64 registers) by default, 3 (80) on request
+        // occupancy variant: 3 blocks/SM (80 registers) by default, 4 (64) on request
         static int minb = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
-            return (e && atoi(e) == 3) ? 3 : 4;
+            return (e && atoi(e) == 4) ? 4 : 3;
         }();
         if (minb == 3)
             step_mixed2d_kernel<3><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);

@@ -292,19 +292,20 @@ struct Particle {
     // for the host-side retag (maxtag+1, ... in iteration then index order)
     __device__ void store(DevState& s, int i, int aux, int step_index, const double* lastv) {
         const int D = DIM;
+        const int a = aux_index(s, i);   // slot of the per-particle arrays outside the sort
         if (deleted) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.pos[(size_t)i * D + d] = 0.;
-                s.vel[(size_t)i * D + d] = 0.;
-                s.fvs[(size_t)i * D + d] = 0.;
-                s.last_pos[(size_t)i * D + d] = 0.;
-                s.last_vel[(size_t)i * D + d] = 0.;
+                s.vel[(size_t)a * D + d] = 0.;
+                s.fvs[(size_t)a * D + d] = 0.;
+                s.last_pos[(size_t)a * D + d] = 0.;
+                s.last_vel[(size_t)a * D + d] = 0.;
             }
-            s.diameter[i] = 0.;
+            s.diameter[a] = 0.;
             s.tri[i] = -1;
-            s.last_tri[i] = -1;
-            s.lowerlayer[i] = 0;
+            s.last_tri[a] = -1;
+            s.lowerlayer[a] = 0;
             s.tag[i] = -2 - step_index;
             s.rng[i] = rng.state;
             return;
@@ -312,23 +313,23 @@ struct Particle {
 #pragma unroll
         for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = x[d];
         s.tri[i] = tri;
-        if (DIM == 3) s.lowerlayer[i] = ll;
+        if (DIM == 3) s.lowerlayer[a] = ll;
         s.rng[i] = rng.state;
         if (p.model >= 2 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.vel[(size_t)i * D + d] = up[d];
+            for (int d = 0; d < D; ++d) s.vel[(size_t)a * D + d] = up[d];
         }
         if (p.model == 3 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.fvs[(size_t)i * D + d] = us[d];
+            for (int d = 0; d < D; ++d) s.fvs[(size_t)a * D + d] = us[d];
         }
         if (aux >= 2) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                s.last_pos[(size_t)i * D + d] = x0[d];
-                s.last_vel[(size_t)i * D + d] = lastv[d];
+                s.last_pos[(size_t)a * D + d] = x0[d];
+                s.last_vel[(size_t)a * D + d] = lastv[d];
             }
-            s.last_tri[i] = ltri;
+            s.last_tri[a] = ltri;
         }
     }
 
@@ -465,7 +466,8 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     q.tri = tri;
     q.tri0 = tri;
     q.ltri = tri;
-    q.ll = DIM == 3 ? s.lowerlayer[i] : 0;
+    const int ai = aux_index(s, i);
+    q.ll = DIM == 3 ? s.lowerlayer[ai] : 0;
     q.ll0 = q.ll;
     q.defer = (DIM == 2) && (wq.e != nullptr);
     const int D = DIM;
@@ -477,17 +479,17 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     bool need_vel = (p.model >= 2) || aux >= 2;
     if (need_vel) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)i * D + d];
+        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)ai * D + d];
     }
     double lastv[3] = {q.up[0], q.up[1], DIM == 3 ? q.up[2] : 0.};
     if (p.model == 3) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)i * D + d];
+        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)ai * D + d];
     }
     q.rng.state = s.rng[i];
     q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
     q.rng.err = 0;
-    double dp = DIM == 3 ? s.diameter[i] : 0.;
+    double dp = DIM == 3 ? s.diameter[ai] : 0.;
 
     int bnd_j = -1;
     if (p.model == 1) bnd_j = q.update_lsm1(dp);
@@ -545,7 +547,7 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
         q.rng.err = 0;
         double lastv[3] = {0., 0., 0.};
         if (aux >= 2) {
-            double2 v = reinterpret_cast<const double2*>(s.vel)[i];
+            double2 v = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
             lastv[0] = v.x;
             lastv[1] = v.y;
         }

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     rng.inc = ((uint64_t)(uint32_t)__ldcs(&s.tag[i]) << 1) | 1ULL;
     rng.err = 0;
     double2 lastv = make_double2(0., 0.);
-    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[i];
+    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
 
     const float dt = (float)p.dt;
     Tri32 t0 = load_tri32(m, tri0);
@@ -277,15 +277,16 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     if (rng.err) atomicOr(err_word, rng.err);
 
     if (deleted) {
+        const int a = aux_index(s, i);
         reinterpret_cast<double2*>(s.pos)[i] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.vel)[i] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.fvs)[i] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.last_pos)[i] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.last_vel)[i] = make_double2(0., 0.);
-        s.diameter[i] = 0.;
+        reinterpret_cast<double2*>(s.vel)[a] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.fvs)[a] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_pos)[a] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_vel)[a] = make_double2(0., 0.);
+        s.diameter[a] = 0.;
         s.tri[i] = -1;
-        s.last_tri[i] = -1;
-        s.lowerlayer[i] = 0;
+        s.last_tri[a] = -1;
+        s.lowerlayer[a] = 0;
         s.tag[i] = -2 - step_index;
         s.rng[i] = rng.state;
         return;
@@ -294,13 +295,14 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     __stcs(&s.tri[i], tri);
     __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);
     if (aux >= 1) {
-        reinterpret_cast<double2*>(s.vel)[i] = make_double2(up0, up1);
-        reinterpret_cast<double2*>(s.fvs)[i] = make_double2(up0, up1);
-    }
-    if (aux >= 2) {
-        reinterpret_cast<double2*>(s.last_pos)[i] = x0;
-        reinterpret_cast<double2*>(s.last_vel)[i] = lastv;
-        s.last_tri[i] = ltri;
+        const int a = aux_index(s, i);
+        reinterpret_cast<double2*>(s.vel)[a] = make_double2(up0, up1);
+        reinterpret_cast<double2*>(s.fvs)[a] = make_double2(up0, up1);
+        if (aux >= 2) {
+            reinterpret_cast<double2*>(s.last_pos)[a] = x0;
+            reinterpret_cast<double2*>(s.last_vel)[a] = lastv;
+            s.last_tri[a] = ltri;
+        }
     }
 }
 

@@ -93,6 +93,8 @@ typedef struct {
     /* GPU-only */
     int32_t precision;               /* CG_PRECISION_* */
     uint64_t seed;                   /* PCG32 streams: pcg32_seed(seed, tag) */
+    int32_t sort_period;             /* re-sort particles by element every this many
+                                        steps (0: never); 2D runs; invisible to callers */
 } cg_params;
 
 /* Particle state: device pointers in the reference layout
