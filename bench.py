@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--npart", type=int, default=10_000_000)
     ap.add_argument("--nx", type=int, default=1001)
     ap.add_argument("--ny", type=int, default=251)
+    ap.add_argument("--sort-period", type=int, default=25,
+                    help="steps between re-sorts of the particles by element (0: never)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -216,7 +218,8 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
                              opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
     ps = cg.LagrangianParticleSet(c["position"], dim=2)
     log(f"creating solver ({precision})")
-    solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local)
+    solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local,
+                       sort_period=args.sort_period)
     L = solver.L
     # all library work on a torch-owned stream (torch manages its lifetime)
     stream = torch.cuda.Stream(device=local)
@@ -330,7 +333,8 @@ def run_gpu_arm(args):
         "dtype": "f64" if main_form == "fp64" else "f32+f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "particles_per_gpu": n, "triangles": r["nt"],
                    "precision": main_form, "dt": params["time_step"],
-                   "l2": "state larger than L2 (no flush)", "model": "LSM1 Euler, k-eps drift"},
+                   "l2": "state larger than L2 (no flush)", "model": "LSM1 Euler, k-eps drift",
+                   "sort_period": args.sort_period},
         "gpu_launches": int(r["launches"]) + args.steps,  # step kernels + field blends
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": float(traffic) if traffic else None,
