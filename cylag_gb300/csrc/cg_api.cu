@@ -410,18 +410,15 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
                     scan_scratch_ints(nkeys) <= 4096;
     size_t n = (size_t)s->n;
     size_t sort_bytes = 0;
-    size_t off_count = 0, off_sums = 0, off_perm = 0, off_pos = 0, off_tri = 0, off_tag = 0,
-           off_rng = 0;
+    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0};
+    const size_t work_bytes = ((n * 16 + 255) & ~(size_t)255) + 4 * ((n * 8 + 255) & ~(size_t)255);
     if (use_sort) {
         auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-        off_count = 0;
-        off_sums = al(off_count + (size_t)nkeys * 4);
+        off_sums = al((size_t)nkeys * 4);
         off_perm = al(off_sums + (size_t)scan_scratch_ints(nkeys) * 4);
-        off_pos = al(off_perm + n * 4);
-        off_tri = al(off_pos + n * 16);
-        off_tag = al(off_tri + n * 4);
-        off_rng = al(off_tag + n * 4);
-        sort_bytes = al(off_rng + n * 8);
+        off_w[0] = al(off_perm + n * 4);
+        off_w[1] = off_w[0] + work_bytes;
+        sort_bytes = off_w[1] + work_bytes;
     }
     uint64_t need = state_bytes + 2 * rec_bytes + 64 + queue_bytes + sort_bytes;
     if (c->budget && c->used + need > c->budget)
@@ -444,13 +441,23 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->use_queue = use_queue;
     if (use_sort) {
         char* b = (char*)r->sortbuf.p;
-        r->sb.count = (int*)(b + off_count);
+        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+        r->sb.count = (int*)b;
         r->sb.block_sums = (int*)(b + off_sums);
         r->sb.perm = (int*)(b + off_perm);
-        r->sb.pos = (double2*)(b + off_pos);
-        r->sb.tri = (int*)(b + off_tri);
-        r->sb.tag = (int*)(b + off_tag);
-        r->sb.rng = (unsigned long long*)(b + off_rng);
+        WorkState* ws[2] = {&r->sb.a, &r->sb.b};
+        for (int k = 0; k < 2; ++k) {
+            char* w = b + off_w[k];
+            ws[k]->pos = (double2*)w;
+            w += al(n * 16);
+            ws[k]->rng = (unsigned long long*)w;
+            w += al(n * 8);
+            ws[k]->tri = (int*)w;
+            w += al(n * 8);
+            ws[k]->tag = (int*)w;
+            w += al(n * 8);
+            ws[k]->slot = (int*)w;
+        }
         r->sort_period = p->sort_period;
     }
     cudaMemsetAsync(r->errw.p, 0, 64, c->stream);
@@ -610,19 +617,21 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaEventCreate(&e));
         r->ev.push_back(e);
     }
-    // element-sorted working state for chunks of sort_period steps
+    // element-sorted working state: only for calls long enough to pay for the
+    // gather/scatter (a few steps per sort period)
+    const bool sorted = r->sort_period > 0 && nsteps >= r->sort_period;
     DevState ws = r->st;
-    if (r->sort_period > 0) {
-        ws.pos = (double*)r->sb.pos;
-        ws.tri = r->sb.tri;
-        ws.tag = r->sb.tag;
-        ws.rng = (uint64_t*)r->sb.rng;
-        ws.slot = r->sb.perm;
-    }
     for (int s = 0; s < nsteps; ++s) {
-        if (r->sort_period > 0 && s % r->sort_period == 0)
-            launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
-        const DevState& run_state = r->sort_period > 0 ? ws : r->st;
+        if (sorted && s % r->sort_period == 0) {
+            if (s == 0) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
+            else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
+            ws.pos = (double*)r->sb.a.pos;
+            ws.tri = r->sb.a.tri;
+            ws.tag = r->sb.a.tag;
+            ws.rng = (uint64_t*)r->sb.a.rng;
+            ws.slot = r->sb.a.slot;
+        }
+        const DevState& run_state = sorted ? ws : r->st;
         // solver.pyx:440: fields at the step-start time
         if ((rc = time_interpolation(r, r->time))) return rc;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
@@ -652,8 +661,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         }
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
-        if (r->sort_period > 0 && (s % r->sort_period == r->sort_period - 1 || s == nsteps - 1))
-            launch_sort_scatter(r->st, r->sb, c->stream);
+        if (sorted && s == nsteps - 1) launch_sort_scatter(r->st, r->sb, c->stream);
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;

@@ -55,17 +55,25 @@ void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int 
                  uint32_t* err, cudaStream_t st);
 
 // Working copies of the per-step state in element order (cg_sort.cu).
+struct WorkState {
+    double2* pos;             // [n]
+    int* tri;                 // [n]
+    int* tag;                 // [n]
+    unsigned long long* rng;  // [n]
+    int* slot;                // [n] caller index of each working particle
+};
 struct SortBuffers {
     int* count;          // [nt + 1] histogram, then scan offsets
     int* block_sums;     // [scan_scratch_ints(nt + 1)]
-    int* perm;           // [n] working index -> caller index
-    double2* pos;        // [n]
-    int* tri;            // [n]
-    int* tag;            // [n]
-    unsigned long long* rng;  // [n]
+    int* perm;           // [n] new order -> old order
+    WorkState a, b;      // current and spare working copies
 };
 int scan_scratch_ints(int nkeys);
-void launch_sort_gather(const DevState& user, int nt, const SortBuffers& b, cudaStream_t st);
+// caller arrays -> b.a in element order
+void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream_t st);
+// b.a -> re-sorted by element (through b.b; swaps a and b)
+void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st);
+// b.a -> caller arrays
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st);
 
 // rng[i] = pcg32_seed(seed, tag[i])

@@ -4,9 +4,11 @@
 // element's mesh record and node values are fetched once per warp instead
 // of once per particle, and the neighbour walks touch few distinct lines.
 // The reference never reorders particles; the sort is invisible to callers:
-// the step runs on working copies in sorted order and the results are
-// scattered back to the caller's slots at the end of each chunk of steps
-// (every per-particle computation is independent of the order).
+// a call of several steps gathers the state into working copies in element
+// order, re-sorts them every few steps (a nearly coherent gather, since
+// particles move little between sorts) and scatters the results back to the
+// caller's slots when it returns.  Every per-particle computation is
+// independent of the order, so results do not depend on the sort.
 //
 // Counting sort on the key tri (inactive and uninitialized particles, tri <
 // 0, get the key nt and go last):
@@ -14,7 +16,7 @@
 //   2. exclusive scan of the nt+1 counts (warp-shuffle block scans, then a
 //      scan of the block sums, then the carry-in),
 //   3. scatter of the particle indices (one atomic per particle),
-//   4. gather of the working state in sorted order.
+//   4. gather of the working state in the new order.
 #include "cg_internal.h"
 
 namespace cg {
@@ -112,48 +114,74 @@ __global__ void scatter_index_kernel(const int* __restrict__ tri, int n, int nt,
     if (i < n) perm[atomicAdd(&offset[sort_key(__ldg(&tri[i]), nt)], 1)] = i;
 }
 
-__global__ void gather_state_kernel(SortBuffers b, DevState user, int n) {
+// dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays
+__global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src, WorkState dst,
+                                    int n) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    int i = __ldg(&b.perm[j]);
-    b.pos[j] = __ldcs(reinterpret_cast<const double2*>(user.pos) + i);
-    b.tri[j] = __ldcs(&user.tri[i]);
-    b.tag[j] = __ldcs(&user.tag[i]);
-    b.rng[j] = __ldcs(reinterpret_cast<const unsigned long long*>(user.rng) + i);
+    int i = __ldg(&perm[j]);
+    dst.pos[j] = __ldcs(src.pos + i);
+    dst.tri[j] = __ldcs(src.tri + i);
+    dst.tag[j] = __ldcs(src.tag + i);
+    dst.rng[j] = __ldcs(src.rng + i);
+    dst.slot[j] = src.slot ? __ldcs(src.slot + i) : i;
 }
 
-__global__ void scatter_state_kernel(SortBuffers b, DevState user, int n) {
+// caller[slot[j]] = work[j]
+__global__ void scatter_state_kernel(WorkState w, WorkState user, int n) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    int i = __ldg(&b.perm[j]);
-    __stcs(reinterpret_cast<double2*>(user.pos) + i, b.pos[j]);
-    __stcs(&user.tri[i], b.tri[j]);
-    __stcs(&user.tag[i], b.tag[j]);
-    __stcs(reinterpret_cast<unsigned long long*>(user.rng) + i, b.rng[j]);
+    int i = __ldg(&w.slot[j]);
+    __stcs(user.pos + i, w.pos[j]);
+    __stcs(user.tri + i, w.tri[j]);
+    __stcs(user.tag + i, w.tag[j]);
+    __stcs(user.rng + i, w.rng[j]);
 }
 
 int scan_scratch_ints(int nkeys) { return (nkeys + SCAN_TILE - 1) / SCAN_TILE; }
 
-void launch_sort_gather(const DevState& user, int nt, const SortBuffers& b, cudaStream_t st) {
-    int n = user.n;
-    if (n == 0) return;
+static void sort_perm(const int* tri, int n, int nt, SortBuffers& b, cudaStream_t st) {
     int nkeys = nt + 1;
     int bs = 256;
     cudaMemsetAsync(b.count, 0, (size_t)nkeys * sizeof(int), st);
-    hist_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(user.tri, n, nt, b.count);
+    hist_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, n, nt, b.count);
     int ntiles = scan_scratch_ints(nkeys);
     scan_tiles_kernel<<<ntiles, SCAN_BLOCK, 0, st>>>(b.count, nkeys, b.block_sums);
     scan_sums_kernel<<<1, SCAN_BLOCK, 0, st>>>(b.block_sums, ntiles);
     add_carry_kernel<<<(nkeys + bs - 1) / bs, bs, 0, st>>>(b.count, nkeys, b.block_sums);
-    scatter_index_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(user.tri, n, nt, b.count, b.perm);
-    gather_state_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(b, user, n);
+    scatter_index_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, n, nt, b.count, b.perm);
+}
+
+static WorkState user_view(const DevState& u) {
+    WorkState w;
+    w.pos = reinterpret_cast<double2*>(u.pos);
+    w.tri = u.tri;
+    w.tag = u.tag;
+    w.rng = reinterpret_cast<unsigned long long*>(u.rng);
+    w.slot = nullptr;
+    return w;
+}
+
+void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream_t st) {
+    int n = user.n;
+    if (n == 0) return;
+    sort_perm(user.tri, n, nt, b, st);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user), b.a, n);
+}
+
+void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
+    if (n == 0) return;
+    sort_perm(b.a.tri, n, nt, b, st);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n);
+    WorkState t = b.a;
+    b.a = b.b;
+    b.b = t;
 }
 
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st) {
     int n = user.n;
     if (n == 0) return;
-    int bs = 256;
-    scatter_state_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(b, user, n);
+    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user), n);
 }
 
 }  // namespace cg
