@@ -16,6 +16,13 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
+    auto wave = [](auto kernel, int bs_) {
+        int dev = 0, nsm = 152, per = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs_, 0);
+        return nsm * (per < 1 ? 1 : per);
+    };
     if (dim == 2) {
         DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 2, prev_valid};
         // occupancy variant: 3 blocks/SM (80 registers) by default, 4 (64) on request
@@ -23,10 +30,14 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
             const char* e = getenv("CYLAG_MIXED_MINB");
             return (e && atoi(e) == 4) ? 4 : 3;
         }();
+        // persistent grid: one wave of resident blocks
+        static int w3 = wave(step_mixed2d_kernel<3>, bs), w4 = wave(step_mixed2d_kernel<4>, bs);
         if (minb == 3)
-            step_mixed2d_kernel<3><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+            step_mixed2d_kernel<3><<<nb < w3 ? nb : w3, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                   step_index, stats, err);
         else
-            step_mixed2d_kernel<4><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+            step_mixed2d_kernel<4><<<nb < w4 ? nb : w4, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                   step_index, stats, err);
     } else {
         // 3D: FP32 node records, FP64 arithmetic
         DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 3, prev_valid};

@@ -68,13 +68,31 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
 // ---------------------------------------------------------------------------
 // the fused step
 // ---------------------------------------------------------------------------
+// one wave of resident blocks (persistent grid), capped by the work
+template <typename K>
+static int resident_grid(K kernel, int n, int bs) {
+    int dev = 0, nsm = 152, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs, 0);
+    if (per < 1) per = 1;
+    int need = (n + bs - 1) / bs;
+    int wave = nsm * per;
+    return need < wave ? need : wave;
+}
+
 void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
                        int nlayers, int prev_valid, const DevParams& p, const DevState& s,
                        const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
                        cudaStream_t st) {
     int bs = 256;
-    int nb = (s.n + bs - 1) / bs;
-    if (nb == 0) return;
+    if (s.n == 0) return;
+    static int nb2 = 0, nb3 = 0;
+    if (!nb2) nb2 = resident_grid(step_kernel<2, double>, 1 << 30, bs);
+    if (!nb3) nb3 = resident_grid(step_kernel<3, double>, 1 << 30, bs);
+    int need = (s.n + bs - 1) / bs;
+    int nb = dim == 2 ? nb2 : nb3;
+    nb = need < nb ? need : nb;
     if (dim == 2) {
         DevFields<double> f{(const double*)cur, (const double*)prev, npoints, nlayers, 2, prev_valid};
         step_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
@@ -107,9 +125,9 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
                             uint32_t* err) {
     __shared__ ZigTables zt;
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
-        zt.kn[t] = c_zig.kn[t];
-        zt.wn[t] = c_zig.wn[t];
-        zt.fn[t] = c_zig.fn[t];
+        zt.kn[t] = g_zig.kn[t];
+        zt.wn[t] = g_zig.wn[t];
+        zt.fn[t] = g_zig.fn[t];
     }
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -14,7 +14,9 @@
 
 namespace cg {
 
-__constant__ ZigTables c_zig = {CG_ZIG_KN_INIT, CG_ZIG_WN_INIT, CG_ZIG_FN_INIT};
+// ziggurat tables in global memory: blocks copy them to shared memory with
+// coalesced loads (constant memory would serialize the 128 distinct indices)
+__device__ const ZigTables g_zig = {CG_ZIG_KN_INIT, CG_ZIG_WN_INIT, CG_ZIG_FN_INIT};
 
 template <int DIM, typename FT>
 struct Particle {
@@ -438,9 +440,9 @@ struct Particle {
 // ziggurat tables into shared memory
 __device__ __forceinline__ void load_zig(ZigTables& zt) {
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
-        zt.kn[t] = c_zig.kn[t];
-        zt.wn[t] = c_zig.wn[t];
-        zt.fn[t] = c_zig.fn[t];
+        zt.kn[t] = g_zig.kn[t];
+        zt.wn[t] = g_zig.wn[t];
+        zt.fn[t] = g_zig.fn[t];
     }
     __syncthreads();
 }
@@ -450,15 +452,14 @@ __device__ __forceinline__ void load_zig(ZigTables& zt) {
 //      step of a batch, so that every public array is current afterwards).
 // q.e != nullptr (2D): particles leaving their start triangle are queued
 // for walk_kernel instead of walking here.
+// One particle of the step (the body of the particle loop).
 template <int DIM, typename FT>
-__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
-                                                   DevState s, WalkQueue wq, int aux,
-                                                   int step_index, int* __restrict__ stats,
-                                                   uint32_t* __restrict__ err_word) {
-    __shared__ ZigTables zt;
-    load_zig(zt);
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
+__device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<FT>& f,
+                                              const DevParams& p, DevState& s,
+                                              const WalkQueue& wq, int aux, int step_index,
+                                              int* __restrict__ stats,
+                                              uint32_t* __restrict__ err_word,
+                                              const ZigTables& zt, int i) {
     int tri = s.tri[i];
     if (tri < 0) return;  // inactive (-1) or awaiting initialization (-2)
 
@@ -516,6 +517,23 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
     q.store(s, i, aux, step_index, lastv);
+}
+
+// aux: 0 = state only; 1 = also write velocity / fluid velocity seen;
+//      2 = also write last_position / last_velocity / last_tri (the last
+//      step of a batch, so that every public array is current afterwards).
+// wq.e != nullptr (2D): particles leaving their start triangle are queued
+// for walk_kernel instead of walking here.  Persistent grid (one wave of
+// resident blocks) striding over the particles.
+template <int DIM, typename FT>
+__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+                                                   DevState s, WalkQueue wq, int aux,
+                                                   int step_index, int* __restrict__ stats,
+                                                   uint32_t* __restrict__ err_word) {
+    __shared__ ZigTables zt;
+    load_zig(zt);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
+        step_particle<DIM, FT>(m, f, p, s, wq, aux, step_index, stats, err_word, zt, i);
 }
 
 // Second half of the step for queued (2D) particles: path walk from the

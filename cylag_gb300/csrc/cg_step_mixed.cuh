@@ -180,25 +180,12 @@ __device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<float>& 
 
 // LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
 // diffusion 658-726) with the boundary conditions of compute_bc.pyx.
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
-                                                           DevParams p, DevState s, WalkQueue wq,
-                                                           int aux, int step_index,
-                                                           int* __restrict__ stats,
-                                                           uint32_t* __restrict__ err_word) {
-    __shared__ Zig32 z32;
-    __shared__ ZigTables z64;
-    for (int t = threadIdx.x; t < 128; t += blockDim.x) {
-        z32.kn[t] = c_zig.kn[t];
-        z32.wn[t] = (float)c_zig.wn[t];
-        z32.fn[t] = (float)c_zig.fn[t];
-        z64.kn[t] = c_zig.kn[t];
-        z64.wn[t] = c_zig.wn[t];
-        z64.fn[t] = c_zig.fn[t];
-    }
-    __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.n) return;
+__device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
+                                                    const DevParams& p, DevState& s,
+                                                    const WalkQueue& wq, int aux, int step_index,
+                                                    int* __restrict__ stats,
+                                                    uint32_t* __restrict__ err_word,
+                                                    const Zig32& z32, int i) {
     // particle state streams through L2 once per step: evict-first loads and
     // stores keep the mesh and node records resident in L2
     int tri0 = __ldcs(&s.tri[i]);
@@ -273,7 +260,7 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
 
     bool deleted = false;
     if (bnd_j != -1 || tri == PART_LOC_O)
-        bc_mixed(m, f, p, z64, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted);
+        bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted);
     if (rng.err) atomicOr(err_word, rng.err);
 
     if (deleted) {
@@ -304,6 +291,25 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
             s.last_tri[a] = ltri;
         }
     }
+}
+
+// Persistent grid (one wave of resident blocks) striding over the particles.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
+                                                                DevParams p, DevState s,
+                                                                WalkQueue wq, int aux,
+                                                                int step_index,
+                                                                int* __restrict__ stats,
+                                                                uint32_t* __restrict__ err_word) {
+    __shared__ Zig32 z32;
+    for (int t = threadIdx.x; t < 128; t += blockDim.x) {
+        z32.kn[t] = g_zig.kn[t];
+        z32.wn[t] = (float)g_zig.wn[t];
+        z32.fn[t] = (float)g_zig.fn[t];
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
+        step_mixed_particle(m, f, p, s, wq, aux, step_index, stats, err_word, z32, i);
 }
 
 }  // namespace cg
