@@ -507,29 +507,56 @@ struct Bary {
     float e0, e1, e2;   // rounding bounds of l0, l1, l2
 };
 
-// barycentric coordinates of (x, y): l_j = gx_j (x - xa) + gy_j (y - ya)
-__device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
+// barycentric coordinates from the FP32 offset (rx, ry) to vertex a:
+// l_j = gx_j rx + gy_j ry.  The bounds cover the offset rounding (relative
+// 2^-24), the FP32 gradients and products: <= ~4 ulp of the terms.
+__device__ __forceinline__ Bary bary32_off(const Tri32& t, float rx, float ry) {
     Bary b;
-    float rx = (float)(x - t.a.x), ry = (float)(y - t.a.y);
     float p1 = t.g0.y * rx, q1 = t.g1.x * ry;
     float p2 = t.g0.z * rx, q2 = t.g1.y * ry;
     b.l1 = p1 + q1;
     b.l2 = p2 + q2;
     b.l0 = 1.f - b.l1 - b.l2;
-    // |error| <= ~4 ulp of the terms (offset, gradient and product roundings)
     b.e1 = 6.0e-7f * (fabsf(p1) + fabsf(q1)) + 1.0e-6f;
     b.e2 = 6.0e-7f * (fabsf(p2) + fabsf(q2)) + 1.0e-6f;
     b.e0 = b.e1 + b.e2 + 1.0e-6f;
     return b;
 }
 
-// same decision as in_tri (the FP64 predicate), FP32 outside the band
-__device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, int k, double x,
-                                             double y) {
-    Bary b = bary32(t, x, y);
+// barycentric coordinates of (x, y): l_j = gx_j (x - xa) + gy_j (y - ya)
+__device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
+    return bary32_off(t, (float)(x - t.a.x), (float)(y - t.a.y));
+}
+
+// Offset of an FP64 position advanced by an FP32 increment, (x0 + d) - a,
+// formed in FP32 as (x0 - a) + d: one more rounding of the start offset
+// (relative 2^-24 of |x0 - a|), so the bounds get that term added.
+__device__ __forceinline__ Bary bary32_moved(const Tri32& t, float rx0, float ry0, float dx,
+                                             float dy) {
+    Bary b = bary32_off(t, rx0 + dx, ry0 + dy);
+    float s1 = 1.2e-7f * (fabsf(t.g0.y * rx0) + fabsf(t.g1.x * ry0));
+    float s2 = 1.2e-7f * (fabsf(t.g0.z * rx0) + fabsf(t.g1.y * ry0));
+    b.e1 += s1;
+    b.e2 += s2;
+    b.e0 += s1 + s2;
+    return b;
+}
+
+// the in-element decision from FP32 barycentrics, exact FP64 test in the band
+__device__ __forceinline__ bool in_tri_decide(const DevMesh& m, const Bary& b, int k, double x,
+                                              double y);
+
+__device__ __forceinline__ bool in_tri_decide(const DevMesh& m, const Bary& b, int k, double x,
+                                              double y) {
     if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return true;
     if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return false;
     return in_tri(m, k, x, y);
+}
+
+// same decision as in_tri (the FP64 predicate), FP32 outside the band
+__device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, int k, double x,
+                                             double y) {
+    return in_tri_decide(m, bary32(t, x, y), k, x, y);
 }
 
 // xylocalizer.pyx:338-435 with FP32-filtered predicates: the in-element

@@ -202,16 +202,20 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     const float dt = (float)p.dt;
     Tri32 t0 = load_tri32(m, tri0);
     Node4 n0 = load_nodes(cur, t0);
-    Bary b0 = bary32(t0, x0.x, x0.y);
+    const float rx0 = (float)(x0.x - t0.a.x), ry0 = (float)(x0.y - t0.a.y);
+    Bary b0 = bary32_off(t0, rx0, ry0);
     float ux, uy;
     vel32(n0, b0, ux, uy);
     float up0 = ux, up1 = uy;   // velocity = fluid velocity seen = U(x0)
     double xn = x0.x, yn = x0.y;
     int tri = tri0, ltri = tri0, bnd_j = -1;
-
-    if (p.time_scheme == 1) {
-        xn += (double)(ux * dt);
-        yn += (double)(uy * dt);
+    // Euler: the whole step's increment is accumulated in FP32 and added to
+    // the FP64 position once
+    float dx = 0.f, dy = 0.f;
+    const bool euler = p.time_scheme == 1;
+    if (euler) {
+        dx = ux * dt;
+        dy = uy * dt;
     } else {
         rk_mixed(m, cur, p, t0, tri0, x0, ux, uy, xn, yn, tri, bnd_j);
     }
@@ -232,15 +236,26 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         }
         float xix = 0.f, xiy = 0.f;
         if (diffx != 0.f) pair32(rng, p.rng_method, z32, xix, xiy);
-        xn += (double)(driftx + diffx * xix);
-        yn += (double)(drifty + diffx * xiy);
+        if (euler) {
+            dx += driftx + diffx * xix;
+            dy += drifty + diffx * xiy;
+        } else {
+            xn += (double)(driftx + diffx * xix);
+            yn += (double)(drifty + diffx * xiy);
+        }
+    }
+    if (euler) {
+        xn = x0.x + (double)dx;
+        yn = x0.y + (double)dy;
     }
 
     if (bnd_j == -1) {
         ltri = tri0;
         if (wq.e != nullptr) {
             // leaves the start triangle: walk + boundary conditions in walk_kernel
-            if (!in_tri_mixed(m, t0, tri0, xn, yn)) {
+            bool inside = euler ? in_tri_decide(m, bary32_moved(t0, rx0, ry0, dx, dy), tri0, xn, yn)
+                                : in_tri_mixed(m, t0, tri0, xn, yn);
+            if (!inside) {
                 if (rng.err) atomicOr(err_word, rng.err);
                 int slot = queue_slot(wq);
                 WalkEntry w;
