@@ -28,6 +28,8 @@ CG_ERR_UNSUPPORTED = 8
 CG_PRECISION_FP64 = 0
 CG_PRECISION_MIXED = 1
 
+CG_NOALLOC_MAX_PARTICLES = 262144
+
 P = C.c_void_p
 I32 = C.c_int32
 F64 = C.c_double
@@ -89,6 +91,7 @@ SIGNATURES = [
     ("cg_run_seed", C.c_int, [P]),
     ("cg_run_init", C.c_int, [P]),
     ("cg_run_step", C.c_int, [P, I32, P]),
+    ("cg_run_step_noalloc", C.c_int, [P, I32]),
     ("cg_run_time", C.c_int, [P, C.POINTER(F64), C.POINTER(C.c_int64)]),
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),

@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -116,6 +117,41 @@ static int upload(cg_ctx* c, const std::vector<T>& h, const T*& out) {
     return CG_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Scratch of cg_run_step_noalloc: the walk queue of one step, in a
+// file-scope device array instead of memory from cudaMalloc.  Every GPU that
+// loads the library holds it (8 MiB + 256 B) until the process exits.
+// ---------------------------------------------------------------------------
+#define CG_NOALLOC_QUEUE_COUNT_INTS 64
+struct NoallocScratch {
+    int count[CG_NOALLOC_QUEUE_COUNT_INTS];        // entry counter (256 B)
+    WalkEntry entries[CG_NOALLOC_MAX_PARTICLES];   // one entry per particle at most
+};
+static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch per device ordinal, looked up once per
+// device with that device current (in host code the symbol's name is only a
+// stand-in for the device array, never an address a kernel may use).
+static std::mutex g_noalloc_mutex;
+static NoallocScratch* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(cg_ctx* c, NoallocScratch** out) {
+    if (c->device < 0 || c->device >= 64)
+        return set_err(c, CG_EINVAL, "cg_run_step_noalloc: device ordinal %d out of range",
+                       c->device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[c->device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return set_err(c, CG_ECUDA, "cudaGetSymbolAddress(g_noalloc_scratch) failed: %s",
+                           cudaGetErrorString(e));
+        g_noalloc_ptr[c->device] = (NoallocScratch*)ptr;
+    }
+    *out = g_noalloc_ptr[c->device];
+    return CG_OK;
+}
 
 extern "C" {
 
@@ -688,6 +724,60 @@ int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
     if (!r) return CG_EINVAL;
     if (time) *time = r->time;
     if (iteration) *iteration = r->iteration;
+    return CG_OK;
+}
+
+// Allocation-free variant of cg_run_step: see include/cylag_gpu.h.
+int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
+    if (!r || nsteps < 0) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (r->st.n > CG_NOALLOC_MAX_PARTICLES)
+        return set_err(c, CG_EINVAL,
+                       "cg_run_step_noalloc: run has %d particles, the allocation-free "
+                       "scratch holds at most %d (use cg_run_step)",
+                       r->st.n, CG_NOALLOC_MAX_PARTICLES);
+    if (nsteps == 0) return CG_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    NoallocScratch* scratch = nullptr;
+    int rc = noalloc_scratch(c, &scratch);
+    if (rc) return rc;
+    if ((rc = ensure_fields(r))) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if ((rc = time_interpolation(r, r->time))) return rc;
+        int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
+        WalkQueue wq{nullptr, nullptr};
+        if (c->fdim == 2) {
+            // the array keeps the previous call's contents: the counter must
+            // start at zero every step
+            wq.count = scratch->count;
+            wq.e = scratch->entries;
+            CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
+        }
+        if (r->prm.precision == CG_PRECISION_MIXED)
+            launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
+                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), nullptr,
+                              (uint32_t*)r->errw.p, c->stream);
+        else
+            launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
+                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), nullptr,
+                              (uint32_t*)r->errw.p, c->stream);
+        if (wq.e) {
+            if (r->prm.precision == CG_PRECISION_MIXED)
+                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq, aux,
+                                  (int)(r->iteration), nullptr, (uint32_t*)r->errw.p, c->stream);
+            else
+                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq,
+                                  aux, (int)(r->iteration), nullptr, (uint32_t*)r->errw.p,
+                                  c->stream);
+        }
+        CUDA_TRY(c, cudaGetLastError());
+        r->time += r->prm.time_step;
+        r->iteration += 1;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    uint32_t flags = 0;
+    CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
     return CG_OK;
 }
 

@@ -161,6 +161,27 @@ int cg_run_init(cg_run *run);
  * after the last step, CG_EDEVICE if the device raised an error flag. */
 int cg_run_step(cg_run *run, int32_t nsteps, int32_t *bnd_stats_host);
 
+/* Allocation-free variant of cg_run_step, for callers that cannot call
+ * cudaMalloc while they step: code running under a memory pool or arena that
+ * owns all device memory (frameworks that forbid allocations outside their
+ * allocator), real-time loops that must not block in the driver's allocator,
+ * and hosts that cap device memory once at start-up.  No counterpart in the
+ * reference.
+ *
+ * Same step as cg_run_step (same kernels, same results for the same run
+ * state) except: no open-boundary statistics, no element re-sort, no kernel
+ * timing.  Its scratch (the queue of particles leaving their triangle) is a
+ * file-scope device array of CG_NOALLOC_MAX_PARTICLES entries (8 MiB) that
+ * every GPU loading the library holds until exit; runs with more particles
+ * are rejected with CG_EINVAL.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the
+ * GPU (two runs stepped concurrently on different streams) race on it.
+ * Synchronous, like cg_run_step. */
+#define CG_NOALLOC_MAX_PARTICLES 262144
+int cg_run_step_noalloc(cg_run *run, int32_t nsteps);
+
 /* Current simulated time and iteration (cylag/core/simutime.pyx:77-84). */
 int cg_run_time(const cg_run *run, double *time, int64_t *iteration);
 
