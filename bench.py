@@ -142,6 +142,12 @@ def bytes_per_particle_step(precision):
     return 32 + 8 + 16 + 4
 
 
+# DRAM bytes per particle-step of one step's kernels (step + walk), from the
+# ncu captures summarised in profiles/step_{mixed,fp64}_lsm1_2d_keps_4M.md
+# (4e6 particles, element-sorted; traffic grows with the particles processed)
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {"mixed": 122.2, "fp64": 147.0}
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -325,7 +331,7 @@ def run_gpu_arm(args):
     bpp = bytes_per_particle_step(main_form)
     peak, peak_kind = peaks()
     achieved = bpp * n / (r["kernel_ms"] / 1e3) / 1e9
-    traffic = os.environ.get("CYLAG_NCU_TRAFFIC_PER_LAUNCH")
+    traffic = NCU_TRAFFIC_B_PER_PARTICLE_STEP.get(main_form)
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps,
@@ -337,7 +343,10 @@ def run_gpu_arm(args):
                    "sort_period": args.sort_period},
         "gpu_launches": int(r["launches"]) + args.steps,  # step kernels + field blends
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": float(traffic) if traffic else None,
+                     "frac": achieved / peak,
+                     "traffic": float(traffic * n) if traffic else None,
+                     "traffic_source": "ncu dram bytes (read+write) of the step and walk "
+                                       "kernels at 4e6 particles, scaled to the launch",
                      "peak_kind": peak_kind, "kernel_ms": r["kernel_ms"],
                      "bytes_per_particle_step": bpp},
         "clocks": r["clocks"],
