@@ -8,6 +8,7 @@
  */
 #include "cylag_oracle.h"
 
+#include <complex.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -33,6 +34,7 @@
 #define C0KOLM 1.2
 #define CMU 0.09
 #define KAPPA 0.41
+#define DBL_EPS 2.220446049250313e-16
 
 /* ======================================================================
  * PCG32 + normal variates (cylag/lsm/random_utils.pyx)
@@ -283,14 +285,17 @@ int cgo_locate(const cgo_mesh *m, double x, double y) {
     return -1;
 }
 
-/* xylocalizer.pyx:338-435 */
+/* xylocalizer.pyx:338-435.  k == -1 (a particle whose element was set to
+ * "outside" by an aborted Runge-Kutta stage) reads the last triangle's row
+ * (numpy wraparound) but compares as -1, as the reference does. */
 static void path_walk(const cgo_mesh *m, int k, double p0x, double p0y,
                       double x, double y, int *new_k_out, int *bnd_out) {
     int new_k = -1, niter = 0, niter_max = 50, intersected_edge = -1;
     while (new_k == -1 && niter <= niter_max) {
         int intersects = 0;
+        int row = k < 0 ? k + m->nt : k;
         for (int i = 0; i < 3; i++) {
-            int j = m->triedge[3 * k + i];
+            int j = m->triedge[3 * row + i];
             if (j == intersected_edge) continue;
             int i0 = m->edges[2 * j], i1 = m->edges[2 * j + 1];
             if (intersec2d(p0x, p0y, x, y, m->x[i0], m->y[i0], m->x[i1], m->y[i1])) {
@@ -323,8 +328,7 @@ void cgo_xy_localize(const cgo_mesh *m, int k, double p0x, double p0y,
     int nk = cgo_point_in_tri(m, k, x, y);
     *bnd_j = -1;
     if (nk != -1) { *new_k = nk; return; }
-    int kk = k < 0 ? k + m->nt : k;
-    path_walk(m, kk, p0x, p0y, x, y, &nk, bnd_j);
+    path_walk(m, k, p0x, p0y, x, y, &nk, bnd_j);
     if (nk == -1 && *bnd_j == -1) nk = cgo_locate(m, x, y);
     *new_k = nk;
 }
@@ -591,6 +595,9 @@ static int rk_stage_locate(ctx_t *c, double xt, double yt, double zt,
         if (c->pd == 3) POS(c, 2) += VEL(c, 2) * dt;
         return 1;
     }
+    /* stage point outside the mesh without a boundary crossing: the
+     * reference's next interpolation raises ValueError */
+    if (*tmp_tri < 0) { c->err = 1; return 1; }
     return 0;
 }
 
@@ -755,6 +762,965 @@ static int update_state_lsm1(ctx_t *c) {
 }
 
 /* ======================================================================
+ * Fields needed by LSM2 / LSM3
+ * ====================================================================== */
+
+/* eulerian_field_set.pyx:1184-1287 with zlocalize == 0 (layer given) */
+static int interp_field_3d(const cgo_mesh *m, const cgo_fields *f, const double *fld,
+                           int k, int ll, double x, double y, double z, double *out) {
+    p1_t p = p1_factors(m, k, x, y);
+    if (ll == PART_LOC_B || ll == PART_LOC_A) return -1;
+    int jl = ll * f->npoints, ju = (ll + 1) * f->npoints;
+    double zlp = p1_eval(f->zs, jl, &p);
+    double zup = p1_eval(f->zs, ju, &p);
+    double dz = zlp - zup;
+    if (fabs(dz) < EPSILON) return -2;
+    double zf0 = (z - zup) / dz;
+    double zf1 = (zlp - z) / dz;
+    double resl = p1_eval(fld, jl, &p);
+    double resu = p1_eval(fld, ju, &p);
+    *out = zf0 * resl + zf1 * resu;
+    return 0;
+}
+
+/* turbulent energy and dissipation at the particle, 2D P1 or 3D prism */
+static int turb_fields(ctx_t *c, int k, int ll, double x, double y, double z,
+                       double *kt, double *ep) {
+    if (c->f->dim == 2) {
+        *kt = interp_field_2d(c->m, c->f, c->f->kt, k, -1, x, y);
+        *ep = interp_field_2d(c->m, c->f, c->f->ep, k, -1, x, y);
+        return 0;
+    }
+    if (interp_field_3d(c->m, c->f, c->f->kt, k, ll, x, y, z, kt)) return -1;
+    if (interp_field_3d(c->m, c->f, c->f->ep, k, ll, x, y, z, ep)) return -1;
+    return 0;
+}
+
+/* eulerian_field_set.pyx:1396-1454 */
+static void interp_acceleration_2d(ctx_t *c, int k, double x, double y, double dt,
+                                   double ua, double va, double *ax, double *ay) {
+    const cgo_mesh *m = c->m;
+    const cgo_fields *f = c->f;
+    const double *u = f->ux, *v = f->uy, *u0 = f->u0, *v0 = f->v0;
+    const double *gx = m->gradx + 3 * k, *gy = m->grady + 3 * k;
+    int i0 = m->tri[3 * k], i1 = m->tri[3 * k + 1], i2 = m->tri[3 * k + 2];
+    double dudx = u[i0] * gx[0] + u[i1] * gx[1] + u[i2] * gx[2];
+    double dudy = u[i0] * gy[0] + u[i1] * gy[1] + u[i2] * gy[2];
+    double dvdx = v[i0] * gx[0] + v[i1] * gx[1] + v[i2] * gx[2];
+    double dvdy = v[i0] * gy[0] + v[i1] * gy[1] + v[i2] * gy[2];
+    double dudt = 0., dvdt = 0.;
+    if (f->frozen == 0 && f->prev_valid) {
+        p1_t p = p1_factors(m, k, x, y);
+        dudt = ((u[i0] - u0[i0]) * p.f0 + (u[i1] - u0[i1]) * p.f1 + (u[i2] - u0[i2]) * p.f2) / dt;
+        dvdt = ((v[i0] - v0[i0]) * p.f0 + (v[i1] - v0[i1]) * p.f1 + (v[i2] - v0[i2]) * p.f2) / dt;
+    }
+    *ax = dudt + ua * dudx + va * dudy;
+    *ay = dvdt + ua * dvdx + va * dvdy;
+}
+
+/* eulerian_field_set.pyx:1999-2023 */
+static void prism_value_gradient(const double *fld, int jl, int ju, const p1_t *p,
+                                 const double *gx, const double *gy, double s, double dz,
+                                 double zlx, double zly, double zux, double zuy,
+                                 double *val, double *ddx, double *ddy, double *ddz) {
+    double fl = fld[jl + p->i0] * p->f0 + fld[jl + p->i1] * p->f1 + fld[jl + p->i2] * p->f2;
+    double fu = fld[ju + p->i0] * p->f0 + fld[ju + p->i1] * p->f1 + fld[ju + p->i2] * p->f2;
+    double gxl = fld[jl + p->i0] * gx[0] + fld[jl + p->i1] * gx[1] + fld[jl + p->i2] * gx[2];
+    double gyl = fld[jl + p->i0] * gy[0] + fld[jl + p->i1] * gy[1] + fld[jl + p->i2] * gy[2];
+    double gxu = fld[ju + p->i0] * gx[0] + fld[ju + p->i1] * gx[1] + fld[ju + p->i2] * gx[2];
+    double gyu = fld[ju + p->i0] * gy[0] + fld[ju + p->i1] * gy[1] + fld[ju + p->i2] * gy[2];
+    double dfdz = (fu - fl) / dz;
+    *val = (1. - s) * fl + s * fu;
+    *ddx = (1. - s) * gxl + s * gxu - dfdz * ((1. - s) * zlx + s * zux);
+    *ddy = (1. - s) * gyl + s * gyu - dfdz * ((1. - s) * zly + s * zuy);
+    *ddz = dfdz;
+}
+
+/* eulerian_field_set.pyx:1456-1579 */
+static int interp_acceleration_3d(ctx_t *c, int k, int ll, double x, double y, double z,
+                                  double dt, double ua, double va, double wa,
+                                  double *ax, double *ay, double *az) {
+    const cgo_mesh *m = c->m;
+    const cgo_fields *f = c->f;
+    p1_t p = p1_factors(m, k, x, y);
+    const double *gx = m->gradx + 3 * k, *gy = m->grady + 3 * k;
+    if (ll == PART_LOC_B || ll == PART_LOC_A) return -1;
+    int jl = ll * f->npoints, ju = (ll + 1) * f->npoints;
+    const double *el = f->zs;
+    double zlp = p1_eval(el, jl, &p);
+    double zup = p1_eval(el, ju, &p);
+    double dz = zup - zlp;
+    if (fabs(dz) < EPSILON) return -2;
+    double s = (z - zlp) / dz;
+    double zlx = el[jl + p.i0] * gx[0] + el[jl + p.i1] * gx[1] + el[jl + p.i2] * gx[2];
+    double zly = el[jl + p.i0] * gy[0] + el[jl + p.i1] * gy[1] + el[jl + p.i2] * gy[2];
+    double zux = el[ju + p.i0] * gx[0] + el[ju + p.i1] * gx[1] + el[ju + p.i2] * gx[2];
+    double zuy = el[ju + p.i0] * gy[0] + el[ju + p.i1] * gy[1] + el[ju + p.i2] * gy[2];
+    double un, dudx, dudy, dudz, vn, dvdx, dvdy, dvdz, wn, dwdx, dwdy, dwdz, t0, t1, t2, t3;
+    prism_value_gradient(f->ux, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &un, &dudx, &dudy, &dudz);
+    prism_value_gradient(f->uy, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &vn, &dvdx, &dvdy, &dvdz);
+    prism_value_gradient(f->uz, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &wn, &dwdx, &dwdy, &dwdz);
+    double dudt = 0., dvdt = 0., dwdt = 0.;
+    if (f->frozen == 0 && f->prev_valid) {
+        prism_value_gradient(f->u0, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &t0, &t1, &t2, &t3);
+        dudt = (un - t0) / dt;
+        prism_value_gradient(f->v0, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &t0, &t1, &t2, &t3);
+        dvdt = (vn - t0) / dt;
+        prism_value_gradient(f->w0, jl, ju, &p, gx, gy, s, dz, zlx, zly, zux, zuy, &t0, &t1, &t2, &t3);
+        dwdt = (wn - t0) / dt;
+    }
+    *ax = dudt + ua * dudx + va * dudy + wa * dudz;
+    *ay = dvdt + ua * dvdx + va * dvdy + wa * dvdz;
+    *az = dwdt + ua * dwdx + va * dwdy + wa * dwdz;
+    return 0;
+}
+
+/* x**y for x >= 0 as the compiled reference evaluates it: Cython (cpow
+ * directive off) gives double ** double a complex result, computed by the C
+ * library's cpow, i.e. exp(y * log|x|) through the complex logarithm (whose
+ * real part uses log1p((x-1)(x+1))/2 for 0.5 <= x < 2).  This differs from
+ * pow(x, y) in the last bits, so the restatement calls cpow too. */
+static double cpow_re(double x, double y) {
+    return creal(cpow(CMPLX(x, 0.), CMPLX(y, 0.)));
+}
+
+/* lagrangian_particle_set.pyx:790-832 (the powers with a non-integer or a
+ * fractional-looking exponent go through cpow_re, as in the compiled
+ * reference; (24/Re)**10, 0.4**10, 0.5**-10, 0.2**-10 and the last three
+ * powers are real pow) */
+static double drag_coefficient(const cgo_params *p, double U, double dp) {
+    double Re = fmax(EPSILON, U * dp / NU0);
+    if (p->drag_model == 0) return p->drag_coef;
+    if (p->drag_model == 1) {
+        if (Re <= 1000.) return (24. / Re) * (1. + 0.15 * cpow_re(Re, 0.687));
+        return 0.44;
+    }
+    if (p->drag_model == 2) {
+        double phi1 = pow(24. / Re, 10.) + cpow_re(21. * cpow_re(Re, -0.67), 10.) +
+                      cpow_re(4. * cpow_re(Re, -0.33), 10.) + pow(0.4, 10.);
+        double phi2 = 1. / (cpow_re(0.148 * cpow_re(Re, 0.11), -10.) + pow(0.5, -10.));
+        double phi3 = cpow_re(1.57 * cpow_re(Re, -1.625) * 1.e8, 10.);
+        double phi4 = 1. / (cpow_re(6e-17 * cpow_re(Re, 2.63), -10.) + pow(0.2, -10.));
+        return pow(1. / (pow(phi1 + phi2, -1.) + pow(phi3, -1.)) + phi4, 1. / 10.);
+    }
+    return 0.44;
+}
+
+/* the mean velocity of the LSM2/3 schemes at (k, ll, x, y, z) */
+static void mean_velocity(ctx_t *c, int k, int ll, double x, double y, double z,
+                          double *ux, double *uy, double *uz) {
+    lsm1_velocity(c, k, ll, x, y, z, ux, uy, uz);
+}
+
+static void mean_acceleration(ctx_t *c, int k, int ll, double x, double y, double z,
+                              double ux, double uy, double uz,
+                              double *ax, double *ay, double *az) {
+    if (c->f->dim == 2) {
+        interp_acceleration_2d(c, k, x, y, c->p->dt, ux, uy, ax, ay);
+        *az = 0.;
+    } else {
+        if (interp_acceleration_3d(c, k, ll, x, y, z, c->p->dt, ux, uy, uz, ax, ay, az)) c->err = 1;
+    }
+}
+
+/* ======================================================================
+ * LSM2 (cylag/lsm/update_state_lsm2.pyx)
+ * ====================================================================== */
+
+/* drag rate a1 = A1c (1.5/dp) Cd |U - Up| for a slip (dx, dy, dz),
+ * update_state_lsm2.pyx:192-198: ((a1c*(1.5/dp))*Cd)*unorm */
+static double lsm2_a1(ctx_t *c, double rx, double ry, double rz) {
+    double unorm = c->pd == 2 ? sqrt(rx * rx + ry * ry) : sqrt(rx * rx + ry * ry + rz * rz);
+    unorm = fmax(EPSILON_LSM2, unorm);
+    double dp = c->s->diameter[c->i];
+    double Cd = drag_coefficient(c->p, unorm, dp);
+    return c->p->a1c * (1.5 / dp) * Cd * unorm;
+}
+
+/* update_state_lsm2.pyx:141-217 */
+static void euler_lsm2(ctx_t *c) {
+    const cgo_params *p = c->p;
+    double dt = p->dt, ux, uy, uz, ax = 0., ay = 0., az = 0.;
+    double z = c->pd == 3 ? POS(c, 2) : 0.;
+    int k = c->s->tri[c->i], ll = c->s->lowerlayer[c->i];
+    mean_velocity(c, k, ll, POS(c, 0), POS(c, 1), z, &ux, &uy, &uz);
+    if (p->added_mass) mean_acceleration(c, k, ll, POS(c, 0), POS(c, 1), z, ux, uy, uz, &ax, &ay, &az);
+    double a1 = lsm2_a1(c, ux - VEL(c, 0), uy - VEL(c, 1), c->pd == 3 ? uz - VEL(c, 2) : 0.);
+    FVS(c, 0) = ux;
+    FVS(c, 1) = uy;
+    VEL(c, 0) += (ux - VEL(c, 0)) * dt * a1 + ax * p->a2c * dt;
+    VEL(c, 1) += (uy - VEL(c, 1)) * dt * a1 + ay * p->a2c * dt;
+    POS(c, 0) += VEL(c, 0) * dt;
+    POS(c, 1) += VEL(c, 1) * dt;
+    if (c->pd == 3) {
+        FVS(c, 2) = uz;
+        VEL(c, 2) += (uz - VEL(c, 2)) * dt * a1 + az * p->a2c * dt - GRAV * p->a0c * dt;
+        POS(c, 2) += VEL(c, 2) * dt;
+    }
+}
+
+/* Runge-Kutta schemes of LSM2 (update_state_lsm2.pyx:219-1021).  Stage s
+ * evaluates U (and the added-mass acceleration) at the stage point, the
+ * slip against up + cs f(s-1), and k = (up + cs f(s-1)) dt,
+ * f = (U - (up + cs f(s-1))) dt a1 + a a2c dt [- g a0c dt]. */
+static int rk_lsm2(ctx_t *c, int scheme) {
+    const cgo_params *p = c->p;
+    double dt = p->dt, ux, uy, uz, ax = 0., ay = 0., az = 0.;
+    int pd = c->pd, i = c->i;
+    double kx[4] = {0}, ky[4] = {0}, kz[4] = {0}, fx[4] = {0}, fy[4] = {0}, fz[4] = {0};
+    int nst = scheme == 2 ? 2 : (scheme == 3 ? 3 : 4);
+    /* stage point offsets (applied to k) and slip offsets (applied to f) */
+    double cpos[4], cvel[4];
+    if (scheme == 2) { cpos[1] = 0.5; cvel[1] = 0.5; }
+    else if (scheme == 3) { cpos[1] = 1. / 3.; cvel[1] = 1. / 3.; cpos[2] = 2. / 3.; cvel[2] = 2. / 3.; }
+    else { cpos[1] = 0.5; cvel[1] = 0.5; cpos[2] = 0.5; cvel[2] = 0.5; cpos[3] = 1.; cvel[3] = 1.; }
+    int k = c->s->tri[i], ll = c->s->lowerlayer[i];
+    double xs = POS(c, 0), ys = POS(c, 1), zs = pd == 3 ? POS(c, 2) : 0.;
+    for (int st = 0; st < nst; st++) {
+        mean_velocity(c, k, ll, xs, ys, zs, &ux, &uy, &uz);
+        if (p->added_mass) mean_acceleration(c, k, ll, xs, ys, zs, ux, uy, uz, &ax, &ay, &az);
+        double a1;
+        double vx, vy, vz;
+        if (st == 0) {
+            a1 = lsm2_a1(c, ux - VEL(c, 0), uy - VEL(c, 1), pd == 3 ? uz - VEL(c, 2) : 0.);
+            vx = VEL(c, 0); vy = VEL(c, 1); vz = pd == 3 ? VEL(c, 2) : 0.;
+            kx[0] = vx * dt; ky[0] = vy * dt;
+            fx[0] = (ux - vx) * dt * a1 + ax * p->a2c * dt;
+            fy[0] = (uy - vy) * dt * a1 + ay * p->a2c * dt;
+            if (pd == 3) {
+                kz[0] = vz * dt;
+                fz[0] = (uz - vz) * dt * a1 + az * p->a2c * dt - GRAV * p->a0c * dt;
+            }
+        } else {
+            double cv = cvel[st];
+            /* slip: (ux-up[0]-cv*f)**2 ... evaluated left to right */
+            double sx = ux - VEL(c, 0) - cv * fx[st - 1];
+            double sy = uy - VEL(c, 1) - cv * fy[st - 1];
+            double sz = pd == 3 ? uz - VEL(c, 2) - cv * fz[st - 1] : 0.;
+            a1 = lsm2_a1(c, sx, sy, sz);
+            vx = VEL(c, 0) + cv * fx[st - 1];
+            vy = VEL(c, 1) + cv * fy[st - 1];
+            kx[st] = vx * dt; ky[st] = vy * dt;
+            fx[st] = (ux - vx) * dt * a1 + ax * p->a2c * dt;
+            fy[st] = (uy - vy) * dt * a1 + ay * p->a2c * dt;
+            if (pd == 3) {
+                vz = VEL(c, 2) + cv * fz[st - 1];
+                kz[st] = vz * dt;
+                fz[st] = (uz - vz) * dt * a1 + az * p->a2c * dt - GRAV * p->a0c * dt;
+            }
+        }
+        if (st == nst - 1) {
+            /* final update */
+            FVS(c, 0) = ux; FVS(c, 1) = uy;
+            if (scheme == 2) {
+                VEL(c, 0) += fx[1]; VEL(c, 1) += fy[1];
+                POS(c, 0) += kx[1]; POS(c, 1) += ky[1];
+                if (pd == 3) { FVS(c, 2) = uz; VEL(c, 2) += fz[1]; POS(c, 2) += kz[1]; }
+            } else if (scheme == 3) {
+                VEL(c, 0) += (0.25 * fx[0] + 0.75 * fx[2]);
+                VEL(c, 1) += (0.25 * fy[0] + 0.75 * fy[2]);
+                POS(c, 0) += (0.25 * kx[0] + 0.75 * kx[2]);
+                POS(c, 1) += (0.25 * ky[0] + 0.75 * ky[2]);
+                if (pd == 3) {
+                    FVS(c, 2) = uz;
+                    VEL(c, 2) += (0.25 * fz[0] + 0.75 * fz[2]);
+                    POS(c, 2) += (0.25 * kz[0] + 0.75 * kz[2]);
+                }
+            } else {
+                VEL(c, 0) += (1. / 6.) * (fx[0] + 2. * fx[1] + 2. * fx[2] + fx[3]);
+                VEL(c, 1) += (1. / 6.) * (fy[0] + 2. * fy[1] + 2. * fy[2] + fy[3]);
+                POS(c, 0) += (1. / 6.) * (kx[0] + 2. * kx[1] + 2. * kx[2] + kx[3]);
+                POS(c, 1) += (1. / 6.) * (ky[0] + 2. * ky[1] + 2. * ky[2] + ky[3]);
+                if (pd == 3) {
+                    FVS(c, 2) = uz;
+                    VEL(c, 2) += (1. / 6.) * (fz[0] + 2. * fz[1] + 2. * fz[2] + fz[3]);
+                    POS(c, 2) += (1. / 6.) * (kz[0] + 2. * kz[1] + 2. * kz[2] + kz[3]);
+                }
+            }
+            return -1;
+        }
+        /* next stage point and its localization (e.g. 2*, 3*, 4* stages) */
+        double cp = cpos[st + 1];
+        double xt = POS(c, 0) + cp * kx[st], yt = POS(c, 1) + cp * ky[st];
+        double zt = pd == 3 ? POS(c, 2) + cp * kz[st] : 0.;
+        int tt, tl = 0, bnd;
+        c->s->last_tri[i] = c->s->tri[i];
+        cgo_xy_localize(c->m, c->s->last_tri[i], LPOS(c, 0), LPOS(c, 1), xt, yt, &tt, &bnd);
+        if (pd == 3) tl = z_localize(c->m, c->f, tt, xt, yt, zt);
+        if (bnd != -1 || (pd == 3 && (tl == -2 || tl == -3))) {
+            /* Euler step with the first-stage quantities of this stage's
+             * evaluation point (update_state_lsm2.pyx:315-333) */
+            c->s->tri[i] = tt;
+            if (pd == 3) c->s->lowerlayer[i] = tl;
+            /* note: U, a, a1 here are those of the stage just evaluated */
+            FVS(c, 0) = ux; FVS(c, 1) = uy;
+            VEL(c, 0) += (ux - VEL(c, 0)) * dt * a1 + ax * p->a2c * dt;
+            VEL(c, 1) += (uy - VEL(c, 1)) * dt * a1 + ay * p->a2c * dt;
+            if (pd == 3) {
+                FVS(c, 2) = uz;
+                VEL(c, 2) += (uz - VEL(c, 2)) * dt * a1 + az * p->a2c * dt - GRAV * p->a0c * dt;
+            }
+            POS(c, 0) += VEL(c, 0) * dt;
+            POS(c, 1) += VEL(c, 1) * dt;
+            if (pd == 3) POS(c, 2) += VEL(c, 2) * dt;
+            return bnd;
+        }
+        /* outside without a boundary crossing: the reference raises
+         * ValueError at the next interpolation */
+        if (tt < 0) { c->err = 1; return -1; }
+        k = tt; ll = tl; xs = xt; ys = yt; zs = zt;
+    }
+    return -1;
+}
+
+/* update_state_lsm2.pyx:1023-1086 (same law as diffusion_lsm1) */
+static void diffusion_lsm2(ctx_t *c, int tri0, int ll0) { diffusion_lsm1(c, tri0, ll0); }
+
+/* update_state_lsm2.pyx:1088-1230 */
+static void euler_maruyama_lsm2_u(ctx_t *c) {
+    const cgo_params *p = c->p;
+    double dt = p->dt, sqrtdt = sqrt(dt), ux, uy, uz, ax = 0., ay = 0., az = 0.;
+    int pd = c->pd, diffmod = p->diffusion_model, nuopt = p->diffusion_lsm2_option;
+    double z = pd == 3 ? POS(c, 2) : 0.;
+    int k = c->s->tri[c->i], ll = c->s->lowerlayer[c->i];
+    mean_velocity(c, k, ll, POS(c, 0), POS(c, 1), z, &ux, &uy, &uz);
+    if (p->added_mass) mean_acceleration(c, k, ll, POS(c, 0), POS(c, 1), z, ux, uy, uz, &ax, &ay, &az);
+    double a1 = lsm2_a1(c, ux - VEL(c, 0), uy - VEL(c, 1), pd == 3 ? uz - VEL(c, 2) : 0.);
+    double xix = 0., xiy = 0., xiz = 0., diffx = 0., diffy = 0., diffz = 0.;
+    if (diffmod != 0) {
+        rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+        if (pd == 3) xiz = rng_single(&c->rng, p->rng_method);
+    }
+    if (diffmod == 2 || diffmod == 3) {
+        double kt, ep;
+        if (turb_fields(c, k, ll, POS(c, 0), POS(c, 1), z, &kt, &ep)) c->err = 1;
+        ep = fmax(ep, EPSILON);
+        double tml = (kt / ep) / (0.5 + (3. / 4.) * C0KOLM);
+        diffx = a1 * tml * sqrt(C0KOLM * ep) * sqrtdt;
+        diffy = diffx;
+        if (pd == 3) {
+            if (diffmod == 2) diffz = nuopt == 2 ? p->nuz * sqrtdt : a1 * sqrt(2. * p->nuz) * sqrtdt;
+            else diffz = diffx;
+        }
+    } else {
+        if (nuopt == 2) {
+            diffx = p->nux * sqrtdt; diffy = diffx;
+            if (pd == 3) diffz = p->nuz * sqrtdt;
+        } else if (nuopt == 3) {
+            diffx = a1 * sqrt(2. * p->nux) * sqrtdt; diffy = diffx;
+            if (pd == 3) diffz = a1 * sqrt(2. * p->nuz) * sqrtdt;
+        }
+    }
+    FVS(c, 0) = ux;
+    FVS(c, 1) = uy;
+    VEL(c, 0) += (ux - VEL(c, 0)) * dt * a1 + ax * p->a2c * dt + diffx * xix;
+    VEL(c, 1) += (uy - VEL(c, 1)) * dt * a1 + ay * p->a2c * dt + diffy * xiy;
+    POS(c, 0) += VEL(c, 0) * dt;
+    POS(c, 1) += VEL(c, 1) * dt;
+    if (pd == 3) {
+        FVS(c, 2) = uz;
+        VEL(c, 2) += (uz - VEL(c, 2)) * dt * a1 + az * p->a2c * dt - GRAV * p->a0c * dt + diffz * xiz;
+        POS(c, 2) += VEL(c, 2) * dt;
+    }
+}
+
+/* update_state_lsm2.pyx:1240-1327 */
+static int lsm2_direct_coefficients(double a1, double dt, double *beta, double *D1,
+                                    double *D2, double *force_x, double *q_uu,
+                                    double *q_xu, double *q_xx) {
+    double r = a1 * dt;
+    if (!isfinite(a1) || !isfinite(dt) || a1 < 0. || dt < 0. || !isfinite(r)) return -1;
+    *beta = exp(-r);
+    if (r < 0.1) {
+        double phi1 = 1., phi2 = 0.5, term = 1.;
+        for (int n = 1; n < 13; n++) {
+            term *= -r / (n + 1.);
+            phi1 += term;
+            phi2 += term / (n + 2.);
+        }
+        *D1 = dt * phi1;
+        *D2 = dt * r * phi2;
+        *force_x = dt * dt * phi2;
+    } else {
+        *D1 = -expm1(-r) / a1;
+        *D2 = dt - *D1;
+        *force_x = *D2 / a1;
+    }
+    if (r == 0.) *q_uu = dt;
+    else *q_uu = dt * (-expm1(-2. * r) / (2. * r));
+    *q_xu = 0.5 * *D1 * *D1;
+    if (r < 1.) {
+        double term = 1. / 6., power2 = 4., qxx = 1. / 3.;
+        for (int n = 1; n < 24; n++) {
+            term *= -r / (n + 3.);
+            power2 *= 2.;
+            qxx += (power2 - 2.) * term;
+        }
+        *q_xx = qxx * dt * dt * dt;
+    } else {
+        *q_xx = ((dt - 2. * *D1 + *q_uu) / a1) / a1;
+    }
+    return 0;
+}
+
+/* update_state_lsm2.pyx:1329-1542 (diffmod 0: di_ode_lsm2, 1232-1238) */
+static void di_lsm2(ctx_t *c, int diffmod, double nux, double nuz, int nuopt) {
+    const cgo_params *p = c->p;
+    double dt = p->dt, ux, uy, uz, ax = 0., ay = 0., az = 0.;
+    int pd = c->pd;
+    double xp0[3], up0[3];
+    for (int d = 0; d < pd; d++) { xp0[d] = POS(c, d); up0[d] = VEL(c, d); }
+    int k = c->s->tri[c->i], ll = c->s->lowerlayer[c->i];
+    double z0 = pd == 3 ? xp0[2] : 0.;
+    mean_velocity(c, k, ll, xp0[0], xp0[1], z0, &ux, &uy, &uz);
+    if (p->added_mass) mean_acceleration(c, k, ll, xp0[0], xp0[1], z0, ux, uy, uz, &ax, &ay, &az);
+    double unorm;
+    if (pd == 2) unorm = sqrt((ux - up0[0]) * (ux - up0[0]) + (uy - up0[1]) * (uy - up0[1]));
+    else unorm = sqrt((ux - up0[0]) * (ux - up0[0]) + (uy - up0[1]) * (uy - up0[1]) +
+                      (uz - up0[2]) * (uz - up0[2]));
+    unorm = fmax(EPSILON_LSM2, unorm);
+    double dp = c->s->diameter[c->i];
+    double Cd = drag_coefficient(p, unorm, dp);
+    double a1 = p->a1c * (1.5 / dp) * Cd * unorm;
+    double beta, D1, D2, force_x, q_uu, q_xu, q_xx;
+    if (lsm2_direct_coefficients(a1, dt, &beta, &D1, &D2, &force_x, &q_uu, &q_xu, &q_xx)) {
+        c->err = 1;
+        return;
+    }
+    double um_beta = -expm1(-a1 * dt);
+    double b2[3] = {0., 0., 0.};
+    if (diffmod == 2 || diffmod == 3) {
+        double kt, ep;
+        if (turb_fields(c, k, ll, xp0[0], xp0[1], z0, &kt, &ep)) c->err = 1;
+        ep = fmax(ep, EPSILON);
+        double tml = (kt / ep) / (0.5 + (3. / 4.) * C0KOLM);
+        b2[0] = a1 * a1 * C0KOLM * ep * (tml * tml);
+        b2[1] = b2[0];
+        if (diffmod == 2) b2[2] = nuopt == 2 ? nuz * nuz : 2. * nuz * a1 * a1;
+        else b2[2] = b2[0];
+    } else if (diffmod != 0) {
+        if (nuopt == 2) { b2[0] = nux * nux; b2[1] = b2[0]; b2[2] = nuz * nuz; }
+        else if (nuopt == 3) { b2[0] = 2. * nux * a1 * a1; b2[1] = b2[0]; b2[2] = 2. * nuz * a1 * a1; }
+    }
+    for (int d = 0; d < pd; d++) {
+        double u_k = d == 0 ? ux : (d == 1 ? uy : uz);
+        double Fp = d == 0 ? p->a2c * ax : (d == 1 ? p->a2c * ay : p->a2c * az - GRAV * p->a0c);
+        double up_mean = up0[d] * beta + u_k * um_beta + Fp * D1;
+        double xp_mean = xp0[d] + up0[d] * D1 + u_k * D2 + Fp * force_x;
+        if (b2[d] == 0. || dt == 0.) {
+            FVS(c, d) = u_k;
+            VEL(c, d) = up_mean;
+            POS(c, d) = xp_mean;
+            continue;
+        }
+        double var_gp = b2[d] * q_uu, cov = b2[d] * q_xu, var_gx = b2[d] * q_xx;
+        double L_pp = sqrt(fmax(0., var_gp));
+        double L_xp = L_pp > 0. ? cov / L_pp : 0.;
+        double L_xx = sqrt(fmax(0., var_gx - L_xp * L_xp));
+        double xix, xiy;
+        rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+        double Gp = L_pp * xix;
+        double Gx = L_xp * xix + L_xx * xiy;
+        FVS(c, d) = u_k;
+        VEL(c, d) = up_mean + Gp;
+        POS(c, d) = xp_mean + Gx;
+    }
+}
+
+/* update_state_lsm2.pyx:30-139 */
+static int update_state_lsm2(ctx_t *c) {
+    const cgo_params *p = c->p;
+    int bnd_j = -1, i = c->i, diffmod = p->diffusion_model, nuopt = p->diffusion_lsm2_option;
+    int tri0 = c->s->tri[i], ll0 = 0;
+    for (int d = 0; d < c->pd; d++) { LPOS(c, d) = POS(c, d); LVEL(c, d) = VEL(c, d); }
+    if (c->pd == 3) ll0 = c->s->lowerlayer[i];
+    if (nuopt == 1 || (nuopt >= 2 && diffmod == 0)) {
+        switch (p->time_scheme) {
+        case 1: euler_lsm2(c); break;
+        case 2: case 3: case 4: bnd_j = rk_lsm2(c, p->time_scheme); break;
+        case 5: di_lsm2(c, 0, 0., 0., 2); break;
+        default: c->err = 1; return -1;
+        }
+        if (diffmod != 0) diffusion_lsm2(c, tri0, ll0);
+    } else {
+        if (p->time_scheme == 1) euler_maruyama_lsm2_u(c);
+        else if (p->time_scheme == 5) di_lsm2(c, diffmod, p->nux, p->nuz, nuopt);
+        else { c->err = 1; return -1; }
+    }
+    (void)bnd_j;
+    /* localization is unconditional (update_state_lsm2.pyx:122-137) */
+    c->s->last_tri[i] = c->s->tri[i];
+    cgo_xy_localize(c->m, c->s->last_tri[i], LPOS(c, 0), LPOS(c, 1), POS(c, 0), POS(c, 1),
+                    &c->s->tri[i], &bnd_j);
+    if (c->pd == 3)
+        c->s->lowerlayer[i] = z_localize(c->m, c->f, c->s->tri[i], POS(c, 0), POS(c, 1), POS(c, 2));
+    return bnd_j;
+}
+
+/* init_lsm2_fluctuations.pyx:28-129 */
+static int lsm2_fluctuations(ctx_t *c, double *f1, double *f2, double *f3) {
+    const cgo_params *p = c->p;
+    *f1 = *f2 = *f3 = 0.;
+    if (p->diffusion_model == 0) return 0;
+    double unorm = EPSILON_LSM2, dp = c->s->diameter[c->i];
+    double Cd = drag_coefficient(p, unorm, dp);
+    double a1 = p->a1c * (1.5 / dp) * Cd * unorm;
+    if (a1 == 0.) {
+        if (p->diffusion_lsm2_option == 2 &&
+            ((p->diffusion_model != 2 && p->diffusion_model != 3 && p->nux != 0.) ||
+             (c->pd == 3 && p->diffusion_model != 3 && p->nuz != 0.)))
+            return -1;
+        return 0;
+    }
+    double b0, b1, b2;
+    if (p->diffusion_model == 2 || p->diffusion_model == 3) {
+        double kt, ep, z = c->pd == 3 ? POS(c, 2) : 0.;
+        if (turb_fields(c, c->s->tri[c->i], c->s->lowerlayer[c->i], POS(c, 0), POS(c, 1), z, &kt, &ep))
+            c->err = 1;
+        ep = fmax(ep, EPSILON);
+        double tml = (kt / ep) / (0.5 + (3. / 4.) * C0KOLM);
+        b0 = a1 * C0KOLM * ep * (tml * tml);
+        b1 = b0;
+        if (p->diffusion_model == 2)
+            b2 = p->diffusion_lsm2_option == 2 ? (p->nuz * p->nuz) / a1 : 2. * p->nuz * a1;
+        else b2 = b0;
+    } else {
+        if (p->diffusion_lsm2_option == 2) {
+            b0 = (p->nux * p->nux) / a1; b1 = b0; b2 = (p->nuz * p->nuz) / a1;
+        } else {
+            b0 = 2. * p->nux * a1; b1 = b0; b2 = 2. * p->nuz * a1;
+        }
+    }
+    if (b0 > 0.) {
+        double xix, xiy;
+        rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+        *f1 = sqrt(0.5 * b0) * xix;
+        *f2 = sqrt(0.5 * b1) * xiy;
+    }
+    if (c->pd == 3 && b2 > 0.) *f3 = sqrt(0.5 * b2) * rng_single(&c->rng, p->rng_method);
+    return 0;
+}
+
+/* ======================================================================
+ * LSM3 (cylag/lsm/update_state_lsm3.pyx)
+ * ====================================================================== */
+
+/* update_state_lsm3.pyx:32-216 (lsm3_edge_opt = 1) */
+static int lsm3_direct_coefficients(double a, double a2, double tl, double dt, double *phi,
+                                    double *q, double *force, double *flow) {
+    if (!isfinite(a) || !isfinite(a2) || !isfinite(tl) || !isfinite(dt) || a < 0. || tl <= 0. || dt < 0.)
+        return -1;
+    double b = 1. / tl;
+    if (!isfinite(b) || !isfinite(a * dt) || !isfinite(b * dt) || !isfinite(a * (1. - a2) * dt)) return -1;
+    for (int k = 0; k < 9; k++) { phi[k] = 0.; q[k] = 0.; }
+    phi[0] = phi[4] = phi[8] = 1.;
+    for (int k = 0; k < 3; k++) { force[k] = 0.; flow[k] = 0.; }
+    if (dt == 0.) return 0;
+    double h = dt;
+    int doublings = 0;
+    while (h > 0. && fmax(a * h, b * h) > 0.5) { h *= 0.5; doublings += 1; }
+    double ah = a * h, bh = b * h, kh = a * (1. - a2) * h;
+    double qbar[10];
+    qbar[0] = 1.;
+    for (int k = 1; k < 10; k++) qbar[k] = 0.;
+    double tss = 1., tsp = 0., tsx = 0., tpp = 0., tpx = 0., txx = 0.;
+    double tsi = 0., tpi = 0., txi = 0., tii = 0.;
+    double s = 1., pp = 0., x = 0., si = 0.;
+    double sum_p = 0., sum_x = 0., sum_si = 0., int_p = 0., int_x = 0., int_si = 0.;
+    double beta_term = 1., phi1 = 1., phi2 = 0.5;
+    for (int n = 1; n < 25; n++) {
+        double divisor = n + 1.;
+        double nss = -2. * bh * tss / divisor;
+        double nsp = (tss - (ah + bh) * tsp) / divisor;
+        double nsx = (tsp - bh * tsx) / divisor;
+        double npp = (2. * tsp - 2. * ah * tpp) / divisor;
+        double npx = (tsx + tpp - ah * tpx) / divisor;
+        double nxx = 2. * tpx / divisor;
+        double nsi = (tss - bh * tsi) / divisor;
+        double npi = (tsi + tsp - ah * tpi) / divisor;
+        double nxi = (tpi + tsx) / divisor;
+        double nii = 2. * tsi / divisor;
+        tss = nss; tsp = nsp; tsx = nsx;
+        tpp = npp; tpx = npx; txx = nxx;
+        tsi = nsi; tpi = npi; txi = nxi; tii = nii;
+        qbar[0] += tss; qbar[1] += tsp; qbar[2] += tsx; qbar[3] += tpp; qbar[4] += tpx;
+        qbar[5] += txx; qbar[6] += tsi; qbar[7] += tpi; qbar[8] += txi; qbar[9] += tii;
+        double sn = -bh * s / n, pn = (s - ah * pp) / n, xn = pp / n, sin_ = s / n;
+        s = sn; pp = pn; x = xn; si = sin_;
+        sum_p += pp; sum_x += x; sum_si += si;
+        int_p += pp / (n + 1.); int_x += x / (n + 1.); int_si += si / (n + 1.);
+        beta_term *= -ah / n;
+        phi1 += beta_term / (n + 1.);
+        phi2 += beta_term / ((n + 1.) * (n + 2.));
+    }
+    q[0] = h * qbar[0];
+    q[1] = q[3] = h * kh * qbar[1];
+    q[2] = q[6] = h * h * (kh * qbar[2] + a2 * qbar[6]);
+    q[4] = h * kh * kh * qbar[3];
+    q[5] = q[7] = h * h * kh * (kh * qbar[4] + a2 * qbar[7]);
+    q[8] = h * h * h * (kh * kh * qbar[5] + 2. * kh * a2 * qbar[8] + a2 * a2 * qbar[9]);
+    phi[0] = exp(-bh);
+    phi[3] = kh * sum_p;
+    phi[4] = exp(-ah);
+    phi[6] = h * (kh * sum_x + a2 * sum_si);
+    phi[7] = h * phi1;
+    force[1] = phi[7];
+    force[2] = h * h * phi2;
+    flow[0] = -expm1(-bh);
+    flow[1] = kh * bh * int_p;
+    flow[2] = h * bh * (kh * int_x + a2 * int_si);
+    for (int n = 0; n < doublings; n++) {
+        double work[9], qnew[9];
+        for (int r = 0; r < 3; r++)
+            for (int cc = 0; cc < 3; cc++) {
+                double value = 0.;
+                for (int k = 0; k < r + 1; k++) value += phi[3 * r + k] * q[3 * k + cc];
+                work[3 * r + cc] = value;
+            }
+        for (int r = 0; r < 3; r++)
+            for (int cc = 0; cc < r + 1; cc++) {
+                double value = q[3 * r + cc];
+                for (int k = 0; k < cc + 1; k++) value += work[3 * r + k] * phi[3 * cc + k];
+                qnew[3 * r + cc] = qnew[3 * cc + r] = value;
+            }
+        for (int k = 0; k < 9; k++) q[k] = qnew[k];
+        flow[2] = 2. * flow[2] + phi[6] * flow[0] + phi[7] * flow[1];
+        flow[1] = (1. + phi[4]) * flow[1] + phi[3] * flow[0];
+        flow[0] = -expm1(-2. * b * h);
+        phi[6] = phi[6] * (1. + phi[0]) + phi[7] * phi[3];
+        phi[3] *= phi[0] + phi[4];
+        force[2] = 2. * force[2] + phi[7] * phi[7];
+        phi[7] *= 1. + phi[4];
+        force[1] = phi[7];
+        h *= 2.;
+        phi[0] = exp(-b * h);
+        phi[4] = exp(-a * h);
+    }
+    for (int k = 0; k < 9; k++) if (!isfinite(phi[k]) || !isfinite(q[k])) return -1;
+    if (!isfinite(force[1]) || !isfinite(force[2])) return -1;
+    for (int k = 0; k < 3; k++) if (!isfinite(flow[k])) return -1;
+    return 0;
+}
+
+/* update_state_lsm3.pyx:218-233 */
+static double phi1_(double z) { return z == 0. ? 1. : expm1(z) / z; }
+static double exp_divdiff(double x, double y) { return exp(-fmin(x, y)) * phi1_(-fabs(x - y)); }
+static double phi2_(double z) {
+    if (fabs(z) < 0.05)
+        return 0.5 + z * (1. / 6. + z * (1. / 24. + z * (1. / 120. + z * (1. / 720. +
+               z * (1. / 5040. + z * (1. / 40320. + z / 362880.))))));
+    return (expm1(z) - z) / (z * z);
+}
+
+/* update_state_lsm3.pyx:235-264 */
+static void lsm3_closed_covariance(double a, double b, double a2, double h, double *q) {
+    double d = a - b;
+    double cc = a * (1. - a2) / d;
+    double bb = (1. - a2) / d;
+    double aa = (a2 + cc) / b;
+    double sb = h * phi1_(-b * h), sa = h * phi1_(-a * h);
+    double s2b = h * phi1_(-2. * b * h), s2a = h * phi1_(-2. * a * h);
+    double sab = h * phi1_(-(a + b) * h);
+    q[0] = s2b;
+    q[1] = q[3] = cc * (s2b - sab);
+    q[2] = q[6] = aa * (sb - s2b) - bb * (sb - sab);
+    q[4] = cc * cc * (s2b - 2. * sab + s2a);
+    q[5] = q[7] = cc * (aa * (sb - s2b - sa + sab) - bb * (sb - sab - sa + s2a));
+    q[8] = (aa * aa * (h - 2. * sb + s2b) - 2. * aa * bb * (h - sb - sa + sab) +
+            bb * bb * (h - 2. * sa + s2a));
+}
+
+/* update_state_lsm3.pyx:266-307 */
+static void lsm3_clipped_covariance(double a, double b, double a2, double h, double *q) {
+    double d = a - b, m = 0.5 * (a + b), x = m * h, delta;
+    if (x > 1.) delta = fmin(0.5, LSM3_CLIP_STEP * sqrt(x)) / h;
+    else delta = fmin(0.5, LSM3_CLIP_STEP / sqrt(x)) * m;
+    if (fabs(d) >= delta) {
+        lsm3_closed_covariance(a, b, a2, h, q);
+    } else {
+        double qp[9], qm[9];
+        lsm3_closed_covariance(m + 0.5 * delta, m - 0.5 * delta, a2, h, qp);
+        lsm3_closed_covariance(m - 0.5 * delta, m + 0.5 * delta, a2, h, qm);
+        double w = 0.5 * (1. + d / delta);
+        for (int k = 0; k < 9; k++) q[k] = qm[k] + w * (qp[k] - qm[k]);
+    }
+    for (int k = 0; k < 3; k++) q[4 * k] = fmax(q[4 * k], 0.);
+    for (int r = 0; r < 3; r++)
+        for (int cc = 0; cc < r; cc++) {
+            double bound = sqrt(q[4 * r] * q[4 * cc]);
+            q[3 * r + cc] = q[3 * cc + r] = fmax(-bound, fmin(bound, q[3 * r + cc]));
+        }
+}
+
+/* update_state_lsm3.pyx:309-374 (lsm3_edge_opt = 2, the default) */
+static int lsm3_clipped_coefficients(double a, double a2, double tl, double dt, double *phi,
+                                     double *q, double *force, double *flow) {
+    if (!isfinite(a) || !isfinite(a2) || !isfinite(tl) || !isfinite(dt) || a < 0. || tl <= 0. || dt < 0.)
+        return -1;
+    double b = 1. / tl;
+    if (!isfinite(b) || !isfinite(a * dt) || !isfinite(b * dt) || !isfinite(a * (1. - a2) * dt)) return -1;
+    for (int j = 0; j < 9; j++) { phi[j] = 0.; q[j] = 0.; }
+    phi[0] = phi[4] = phi[8] = 1.;
+    for (int j = 0; j < 3; j++) { force[j] = 0.; flow[j] = 0.; }
+    if (dt == 0.) return 0;
+    double ah = a * dt, bh = b * dt, k = a * (1. - a2);
+    double alpha = exp(-bh), beta = exp(-ah);
+    double divdiff = exp_divdiff(ah, bh);
+    double ib = dt * phi1_(-bh), ia = dt * phi1_(-ah);
+    phi[0] = alpha;
+    phi[3] = k * dt * divdiff;
+    phi[4] = beta;
+    phi[6] = ib - (1. - a2) * dt * divdiff;
+    phi[7] = ia;
+    force[1] = ia;
+    force[2] = dt * dt * phi2_(-ah);
+    flow[0] = -expm1(-bh);
+    flow[1] = k * dt * (phi1_(-ah) - divdiff);
+    flow[2] = (a2 * (dt - ib) + (1. - a2) * (dt - ia - ib + dt * divdiff));
+    lsm3_clipped_covariance(a, b, a2, dt, q);
+    for (int j = 0; j < 9; j++) if (!isfinite(phi[j]) || !isfinite(q[j])) return -1;
+    if (!isfinite(force[1]) || !isfinite(force[2])) return -1;
+    for (int j = 0; j < 3; j++) if (!isfinite(flow[j])) return -1;
+    return 0;
+}
+
+static int lsm3_coefficients(double a, double a2, double tl, double dt, int edge_opt,
+                             double *phi, double *q, double *force, double *flow) {
+    if (edge_opt == 2) return lsm3_clipped_coefficients(a, a2, tl, dt, phi, q, force, flow);
+    return lsm3_direct_coefficients(a, a2, tl, dt, phi, q, force, flow);
+}
+
+/* update_state_lsm3.pyx:523-557 */
+static int lsm3_cholesky(const double *q, double *lower) {
+    for (int k = 0; k < 9; k++) lower[k] = 0.;
+    for (int r = 0; r < 3; r++) {
+        double pivot = q[3 * r + r];
+        for (int cc = 0; cc < r; cc++) {
+            double residual = q[3 * r + cc];
+            for (int k = 0; k < cc; k++) residual -= lower[3 * r + k] * lower[3 * cc + k];
+            if (lower[3 * cc + cc] > 0.) {
+                lower[3 * r + cc] = residual / lower[3 * cc + cc];
+            } else {
+                double tol = (128. * DBL_EPS * sqrt(fabs(q[3 * r + r])) * sqrt(fabs(q[3 * cc + cc])));
+                if (fabs(residual) > tol) return -1;
+            }
+            pivot -= lower[3 * r + cc] * lower[3 * r + cc];
+        }
+        if (pivot < 0.) {
+            if (-pivot > 128. * DBL_EPS * fabs(q[3 * r + r])) return -1;
+            pivot = 0.;
+        }
+        lower[3 * r + r] = sqrt(pivot);
+    }
+    return 0;
+}
+
+/* update_state_lsm3.pyx:559-585 */
+static void lsm3_cholesky_clipped(const double *q, double *lower) {
+    for (int k = 0; k < 9; k++) lower[k] = 0.;
+    for (int r = 0; r < 3; r++) {
+        double remaining = fmax(q[3 * r + r], 0.);
+        for (int cc = 0; cc < r; cc++) {
+            if (lower[3 * cc + cc] > 0.) {
+                double value = q[3 * r + cc];
+                for (int k = 0; k < cc; k++) value -= lower[3 * r + k] * lower[3 * cc + k];
+                value /= lower[3 * cc + cc];
+                if (value * value > remaining) value = copysign(sqrt(remaining), value);
+                lower[3 * r + cc] = value;
+                remaining -= value * value;
+            }
+        }
+        lower[3 * r + r] = sqrt(fmax(remaining, 0.));
+    }
+}
+
+/* slip drag rate of LSM3: ((a1c*(1.5/dp))*unorm)*Cd (update_state_lsm3.pyx:728) */
+static double lsm3_a1(ctx_t *c, double unorm) {
+    double dp = c->s->diameter[c->i];
+    double Cd = drag_coefficient(c->p, unorm, dp);
+    return c->p->a1c * (1.5 / dp) * unorm * Cd;
+}
+
+/* update_state_lsm3.pyx:664-820 */
+static void euler_maruyama_lsm3(ctx_t *c) {
+    const cgo_params *p = c->p;
+    double dt = p->dt, sqrtdt = sqrt(dt), ux, uy, uz, ax = 0., ay = 0., az = 0.;
+    int pd = c->pd, diffmod = p->diffusion_model;
+    double z = pd == 3 ? POS(c, 2) : 0.;
+    int k = c->s->tri[c->i], ll = c->s->lowerlayer[c->i];
+    mean_velocity(c, k, ll, POS(c, 0), POS(c, 1), z, &ux, &uy, &uz);
+    mean_acceleration(c, k, ll, POS(c, 0), POS(c, 1), z, ux, uy, uz, &ax, &ay, &az);
+    double unorm;
+    if (pd == 2) unorm = sqrt((FVS(c, 0) - VEL(c, 0)) * (FVS(c, 0) - VEL(c, 0)) +
+                              (FVS(c, 1) - VEL(c, 1)) * (FVS(c, 1) - VEL(c, 1)));
+    else unorm = sqrt((FVS(c, 0) - VEL(c, 0)) * (FVS(c, 0) - VEL(c, 0)) +
+                      (FVS(c, 1) - VEL(c, 1)) * (FVS(c, 1) - VEL(c, 1)) +
+                      (FVS(c, 2) - VEL(c, 2)) * (FVS(c, 2) - VEL(c, 2)));
+    unorm = fmax(EPSILON_LSM2, unorm);
+    double a1 = lsm3_a1(c, unorm);
+    double xix, xiy, xiz = 0.;
+    rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+    if (pd == 3) xiz = rng_single(&c->rng, p->rng_method);
+    double kt = 0., ep = 0., tml, unstml, diffx, diffz = 0.;
+    if (diffmod == 2 || diffmod == 3) {
+        if (turb_fields(c, k, ll, POS(c, 0), POS(c, 1), z, &kt, &ep)) c->err = 1;
+        ep = fmax(ep, EPSILON);
+    }
+    if (diffmod == 2 || diffmod == 3) {
+        tml = (kt / ep) / (0.5 + (3. / 4.) * C0KOLM);
+        unstml = 1. / fmax(EPSILON_LSM3, tml);
+        diffx = sqrt(C0KOLM * ep) * sqrtdt;
+    } else {
+        unstml = 1. / p->tl_h;
+        diffx = sqrt(2. * p->nux) * sqrtdt / p->tl_h;
+    }
+    double diffy = diffx;
+    double dusx = (ax + (ux - FVS(c, 0)) * unstml) * dt + diffx * xix;
+    double dusy = (ay + (uy - FVS(c, 1)) * unstml) * dt + diffy * xiy;
+    VEL(c, 0) += (FVS(c, 0) - VEL(c, 0)) * dt * a1;
+    VEL(c, 1) += (FVS(c, 1) - VEL(c, 1)) * dt * a1;
+    FVS(c, 0) += dusx;
+    FVS(c, 1) += dusy;
+    if (p->added_mass) { VEL(c, 0) += p->a2c * dusx; VEL(c, 1) += p->a2c * dusy; }
+    POS(c, 0) += VEL(c, 0) * dt;
+    POS(c, 1) += VEL(c, 1) * dt;
+    if (pd == 3) {
+        if (diffmod == 1 || diffmod == 2) {
+            unstml = 1. / p->tl_v;
+            diffz = sqrt(2. * p->nuz) * sqrtdt / p->tl_v;
+        } else {
+            tml = (kt / ep) / (0.5 + (3. / 4.) * C0KOLM);
+            unstml = 1. / fmax(EPSILON_LSM3, tml);
+            diffz = sqrt(C0KOLM * ep) * sqrtdt;
+        }
+        double dusz = (az + (uz - FVS(c, 2)) * unstml) * dt + diffz * xiz;
+        VEL(c, 2) += (FVS(c, 2) - VEL(c, 2)) * dt * a1 - GRAV * p->a0c * dt;
+        FVS(c, 2) += dusz;
+        if (p->added_mass) VEL(c, 2) += p->a2c * dusz;
+        POS(c, 2) += VEL(c, 2) * dt;
+    }
+}
+
+/* update_state_lsm3.pyx:822-996 */
+static void di_lsm3(ctx_t *c) {
+    const cgo_params *p = c->p;
+    double dt = p->dt;
+    if (dt == 0.) return;
+    int pd = c->pd, diffmod = p->diffusion_model, edge_opt = p->lsm3_edge_opt;
+    double xp0[3], up0[3], us0[3];
+    for (int d = 0; d < pd; d++) { xp0[d] = POS(c, d); up0[d] = VEL(c, d); us0[d] = FVS(c, d); }
+    int k = c->s->tri[c->i], ll = c->s->lowerlayer[c->i];
+    double z0 = pd == 3 ? xp0[2] : 0.;
+    double ux, uy, uz, ax, ay, az, kt = 0., ep = 0.;
+    mean_velocity(c, k, ll, xp0[0], xp0[1], z0, &ux, &uy, &uz);
+    mean_acceleration(c, k, ll, xp0[0], xp0[1], z0, ux, uy, uz, &ax, &ay, &az);
+    if (diffmod == 2 || diffmod == 3)
+        if (turb_fields(c, k, ll, xp0[0], xp0[1], z0, &kt, &ep)) c->err = 1;
+    double unorm = (us0[0] - up0[0]) * (us0[0] - up0[0]) + (us0[1] - up0[1]) * (us0[1] - up0[1]);
+    if (pd == 3) unorm += (us0[2] - up0[2]) * (us0[2] - up0[2]);
+    unorm = fmax(EPSILON_LSM2, sqrt(unorm));
+    double a1 = lsm3_a1(c, unorm);
+    double a2 = p->added_mass ? p->a2c : 0.;
+    double tl_h = p->tl_h, tl_v = p->tl_v, sigma_h, sigma_v = 0.;
+    if (diffmod == 2 || diffmod == 3) {
+        ep = fmax(ep, EPSILON);
+        tl_h = fmax(EPSILON_LSM3, (kt / ep) / (0.5 + (3. / 4.) * C0KOLM));
+        sigma_h = sqrt(C0KOLM * ep);
+    } else {
+        sigma_h = sqrt(2. * p->nux) / tl_h;
+    }
+    if (pd == 3) {
+        if (diffmod == 3) { tl_v = tl_h; sigma_v = sigma_h; }
+        else sigma_v = sqrt(2. * p->nuz) / tl_v;
+    }
+    double mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
+    double phi[9], q[9], force[3], flow[3], lower[9];
+    if (lsm3_coefficients(a1, a2, tl_h, dt, edge_opt, phi, q, force, flow)) { c->err = 1; return; }
+    int factored = 0;
+    double sigma_s = sigma_h;
+    for (int d = 0; d < pd; d++) {
+        double tl_k = tl_h;
+        if (d == 2) {
+            tl_k = tl_v;
+            sigma_s = sigma_v;
+            if (tl_v != tl_h) {
+                if (lsm3_coefficients(a1, a2, tl_v, dt, edge_opt, phi, q, force, flow)) { c->err = 1; return; }
+                factored = 0;
+            }
+        }
+        double u_k = mean_flow[d];
+        double Fp = d == 2 ? -GRAV * p->a0c : 0.;
+        double ur0 = up0[d] - a2 * us0[d];
+        double us_mean = (us0[d] * phi[0] + u_k * flow[0] + mean_acc[d] * tl_k * flow[0]);
+        double ur_mean = (ur0 * phi[4] + us0[d] * phi[3] + u_k * flow[1] +
+                          mean_acc[d] * tl_k * flow[1] + Fp * force[1]);
+        double xp_mean = (xp0[d] + ur0 * force[1] + us0[d] * phi[6] + u_k * flow[2] +
+                          mean_acc[d] * tl_k * flow[2] + Fp * force[2]);
+        if (sigma_s > 0. && q[0] > 0.) {
+            if (!factored) {
+                if (edge_opt == 2) lsm3_cholesky_clipped(q, lower);
+                else if (lsm3_cholesky(q, lower)) { c->err = 1; return; }
+                factored = 1;
+            }
+            double xix, xiy, xiz;
+            if (lower[4] > 0.) rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+            else { xix = rng_single(&c->rng, p->rng_method); xiy = 0.; }
+            xiz = lower[8] > 0. ? rng_single(&c->rng, p->rng_method) : 0.;
+            us_mean += sigma_s * lower[0] * xix;
+            ur_mean += sigma_s * (lower[3] * xix + lower[4] * xiy);
+            xp_mean += sigma_s * (lower[6] * xix + lower[7] * xiy + lower[8] * xiz);
+        }
+        FVS(c, d) = us_mean;
+        VEL(c, d) = ur_mean + a2 * us_mean;
+        POS(c, d) = xp_mean;
+    }
+}
+
+/* update_state_lsm3.pyx:587-662 */
+static int update_state_lsm3(ctx_t *c) {
+    const cgo_params *p = c->p;
+    int bnd_j = -1, i = c->i;
+    for (int d = 0; d < c->pd; d++) { LPOS(c, d) = POS(c, d); LVEL(c, d) = VEL(c, d); }
+    if (p->time_scheme == 1) euler_maruyama_lsm3(c);
+    else if (p->time_scheme == 5) di_lsm3(c);
+    else { c->err = 1; return -1; }
+    c->s->last_tri[i] = c->s->tri[i];
+    cgo_xy_localize(c->m, c->s->last_tri[i], LPOS(c, 0), LPOS(c, 1), POS(c, 0), POS(c, 1),
+                    &c->s->tri[i], &bnd_j);
+    if (c->pd == 3)
+        c->s->lowerlayer[i] = z_localize(c->m, c->f, c->s->tri[i], POS(c, 0), POS(c, 1), POS(c, 2));
+    return bnd_j;
+}
+
+/* init_lsm3_fluctuations.pyx:28-90 */
+static void lsm3_fluctuations(ctx_t *c, double *f1, double *f2, double *f3) {
+    const cgo_params *p = c->p;
+    int diffmod = p->diffusion_model;
+    double sigma_h, sigma_v, kt, ep;
+    *f1 = *f2 = *f3 = 0.;
+    if (diffmod == 2 || diffmod == 3) {
+        double z = c->pd == 3 ? POS(c, 2) : 0.;
+        if (turb_fields(c, c->s->tri[c->i], c->s->lowerlayer[c->i], POS(c, 0), POS(c, 1), z, &kt, &ep))
+            c->err = 1;
+        ep = fmax(ep, EPSILON);
+        double tml = fmax(EPSILON_LSM3, (kt / ep) / (0.5 + (3. / 4.) * C0KOLM));
+        sigma_h = sqrt(0.5 * C0KOLM * ep * tml);
+    } else {
+        sigma_h = sqrt(p->nux / p->tl_h);
+    }
+    if (sigma_h > 0.) {
+        double xix, xiy;
+        rng_pair(&c->rng, p->rng_method, &xix, &xiy);
+        *f1 = sigma_h * xix;
+        *f2 = sigma_h * xiy;
+    }
+    if (c->pd == 3) {
+        sigma_v = diffmod == 3 ? sigma_h : sqrt(p->nuz / p->tl_v);
+        if (sigma_v > 0.) *f3 = sigma_v * rng_single(&c->rng, p->rng_method);
+    }
+}
+
+/* ======================================================================
  * Boundary conditions (cylag/boundary_conditions/compute_bc.pyx:35-395)
  * ====================================================================== */
 
@@ -898,7 +1864,7 @@ static void compute_bc(ctx_t *c, int bnd_j, int32_t *bnd_stats) {
  * Solver (cylag/core/solver.pyx)
  * ====================================================================== */
 
-/* solver.pyx:238-379 (LSM1 subset: no LSM2/LSM3 fluctuation draws) */
+/* solver.pyx:238-379 */
 static void init_particle(ctx_t *c) {
     const cgo_params *p = c->p;
     cgo_particles *s = c->s;
@@ -927,7 +1893,21 @@ static void init_particle(ctx_t *c) {
             VEL(c, 0) = ux; VEL(c, 1) = uy; VEL(c, 2) = uz;
             FVS(c, 0) = ux; FVS(c, 1) = uy; FVS(c, 2) = uz;
         }
+        if (p->model == 2 && p->diffusion_lsm2_option >= 2 && p->diffusion_model != 0) {
+            double f1, f2, f3;
+            if (lsm2_fluctuations(c, &f1, &f2, &f3)) c->err = 1;
+            VEL(c, 0) += f1;
+            VEL(c, 1) += f2;
+            if (c->pd == 3) VEL(c, 2) += f3;
+        }
         for (int d = 0; d < c->pd; d++) FVS(c, d) = VEL(c, d);
+        if (p->model == 3) {
+            double f1, f2, f3;
+            lsm3_fluctuations(c, &f1, &f2, &f3);
+            FVS(c, 0) += f1;
+            FVS(c, 1) += f2;
+            if (c->pd == 3) FVS(c, 2) += f3;
+        }
     }
 }
 
@@ -939,8 +1919,21 @@ static int ctx_begin(ctx_t *c, const cgo_mesh *m, const cgo_fields *f, const cgo
     return 0;
 }
 
+static int g_errors = 0;
+
+int cgo_take_errors(void) {
+    int e;
+#pragma omp atomic capture
+    { e = g_errors; g_errors = 0; }
+    return e;
+}
+
 static void ctx_end(ctx_t *c) {
     c->s->rng_state[c->i] = c->rng.state;
+    if (c->err) {
+#pragma omp atomic
+        g_errors += 1;
+    }
 }
 
 int cgo_init_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
@@ -971,6 +1964,8 @@ int cgo_step_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
         if (s->inactive[i] == 0) {
             int bnd_j = -1;
             if (p->model == 1) bnd_j = update_state_lsm1(&c);
+            else if (p->model == 2) bnd_j = update_state_lsm2(&c);
+            else if (p->model == 3) bnd_j = update_state_lsm3(&c);
             else c.err = 1;
             if (p->boundary_conditions == 1) {
                 compute_bc(&c, bnd_j, bnd_stats);

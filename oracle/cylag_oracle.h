@@ -121,6 +121,12 @@ int cgo_retag(cgo_particles *s, int maxtag);
 int cgo_init_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
                    cgo_particles *s, int i0, int i1);
 
+/* Number of particles, since the previous call, whose step or
+ * initialization met a condition on which the reference raises ValueError
+ * (interpolation outside the mesh or the column, non-finite LSM2/LSM3
+ * coefficients, ...); their state is then unspecified.  Resets the count. */
+int cgo_take_errors(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,6 +109,8 @@ def lib():
             L.cgo_step.restype = C.c_int
             L.cgo_init_range.argtypes = [P, P, P, P, C.c_int, C.c_int]
             L.cgo_init_range.restype = C.c_int
+            L.cgo_take_errors.argtypes = []
+            L.cgo_take_errors.restype = C.c_int
             L.cgo_retag.argtypes = [P, C.c_int]
             L.cgo_retag.restype = C.c_int
             L.cgo_xy_localize.argtypes = [P, C.c_int, C.c_double, C.c_double,
@@ -270,9 +272,17 @@ class OracleSolver:
         self.bnd_stats = []
         if not self.frozen:
             self._time_interpolation(P.initial_time)
+        self.L.cgo_take_errors()
         self.L.cgo_init_range(C.byref(self._m), C.byref(self._fields()), C.byref(self._p),
                               C.byref(self._s), 0, n)
+        self._raise_errors("initialization")
         self.maxtag = self.L.cgo_retag(C.byref(self._s), self.maxtag)
+
+    def _raise_errors(self, where):
+        e = self.L.cgo_take_errors()
+        if e:
+            raise ValueError(f"{e} particle(s) failed during {where} (point outside the "
+                             "mesh or the water column, or non-finite LSM2/LSM3 coefficients)")
 
     # simutime/zlocalizer helpers ------------------------------------------------
     def _lower_index(self, value, last):
@@ -317,6 +327,7 @@ class OracleSolver:
         stats = np.zeros(max(1, self.nopen), np.int32)
         self.L.cgo_step(C.byref(self._m), C.byref(self._fields()), C.byref(self._p),
                         C.byref(self._s), _p(stats), self.nthreads)
+        self._raise_errors(f"the step at t={self.time}")
         self.maxtag = self.L.cgo_retag(C.byref(self._s), self.maxtag)
         self.bnd_stats.append(stats[: self.nopen].copy())
         self.time += self.dt

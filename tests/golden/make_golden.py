@@ -18,7 +18,8 @@ this is the reference's own code path under the per-particle stream
 convention, with no source change.
 
 Usage (needs the reference build; run in the development container):
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py && python tests/golden/make_golden.py [group ...]
+with groups rng, mesh, lsm1, lsm23 (default: all).
 """
 from __future__ import annotations
 
@@ -208,7 +209,144 @@ def traj_fixtures():
                            buoyancy_velocity_model=1))
 
 
+def _keps2d(npart=40):
+    c = synth.keps_drift_channel(npart=npart, nx=41, ny=11)
+    case = {k: c[k] for k in ("x", "y", "triangles", "times", "elevation", "velocity_x",
+                              "velocity_y", "opt_fields", "position")}
+    case["opt_fields_names"] = c["opt_fields_names"]
+    return case
+
+
+def _loglaw3d(npart=40, unsteady=False):
+    c = synth.loglaw_case(nx=21, ny=11, lx=400.0, ly=200.0, nplanes=6, npart=npart)
+    case = {k: c[k] for k in ("x", "y", "triangles", "times", "elevation", "velocity_x",
+                              "velocity_y", "velocity_z", "opt_fields", "position")}
+    case.update(dim=3, nlayers=6, opt_fields_names=c["opt_fields_names"])
+    if unsteady:
+        # two records 300 s apart, the second current 25% stronger with a
+        # small vertical component: exercises the Eulerian time derivative of
+        # the added-mass acceleration
+        case["times"] = np.array([0.0, 300.0])
+        case["elevation"] = np.concatenate([case["elevation"]] * 2)
+        w = 1e-3 * np.sin(2 * np.pi * c["x"] / 400.0)
+        w = np.tile(w, 6)
+        case["velocity_x"] = np.concatenate([case["velocity_x"], 1.25 * case["velocity_x"]])
+        case["velocity_y"] = np.concatenate([case["velocity_y"], 1.25 * case["velocity_y"]])
+        case["velocity_z"] = np.concatenate([case["velocity_z"], w[None, :]])
+        case["opt_fields"] = np.concatenate([case["opt_fields"]] * 2, axis=1)
+    return case
+
+
+def lsm23_fixtures():
+    """LSM2 (particle velocity) and LSM3 (velocity seen) cases, 2D and 3D.
+    The reference accepts the Runge-Kutta schemes (2-4) for LSM2 only
+    without diffusion, and only Euler-Maruyama (1) or the direct
+    integrator (5) otherwise (cylag/core/parameters.pyx:219-238)."""
+    c2 = _keps2d()
+    base2 = dict(frozen_eulerian_fields=False, time_step=2.0, final_time=500.0,
+                 schmidt_number=0.72)
+    lsm2_2d = [
+        # name, parameters, particle-set keywords
+        ("lsm2_ts1_am", dict(model=2, time_scheme=1, diffusion_model=1,
+                             horizontal_diffusivity=0.5),
+         dict(added_mass_force=True)),
+        ("lsm2_ts2_cd0", dict(model=2, time_scheme=2, diffusion_model=0),
+         dict(drag_coefficient_model=0, drag_coefficient=0.8)),
+        ("lsm2_ts3_am_cd2", dict(model=2, time_scheme=3, diffusion_model=0),
+         dict(added_mass_force=True, drag_coefficient_model=2)),
+        ("lsm2_ts4", dict(model=2, time_scheme=4, diffusion_model=0), {}),
+        ("lsm2_ts5_ode_keps_rm2", dict(model=2, time_scheme=5, diffusion_model=2, rng_method=2),
+         {}),
+        # explicit velocity updates are stable for a1*dt < 2: smaller steps
+        ("lsm2_em_opt2", dict(model=2, time_scheme=1, diffusion_model=1, diffusion_lsm2_option=2,
+                              horizontal_diffusivity=0.01, time_step=0.25), {}),
+        # the k-epsilon velocity noise grows with the drag rate, which grows
+        # with the slip for Cd*|slip| drag: a small constant Cd keeps it bounded
+        ("lsm2_em_opt3_keps", dict(model=2, time_scheme=1, diffusion_model=2,
+                                   diffusion_lsm2_option=3, time_step=1.0),
+         dict(added_mass_force=True, drag_coefficient_model=0, drag_coefficient=0.01)),
+        ("lsm2_di_opt2_am", dict(model=2, time_scheme=5, diffusion_model=1,
+                                 diffusion_lsm2_option=2, horizontal_diffusivity=0.01),
+         dict(added_mass_force=True)),
+        ("lsm2_di_opt3_keps3_small", dict(model=2, time_scheme=5, diffusion_model=3,
+                                          diffusion_lsm2_option=3),
+         dict(particle_diameter=1e-3, particle_density=1050.)),
+        ("lsm3_em_const", dict(model=3, time_scheme=1, diffusion_model=1, time_step=0.25,
+                               horizontal_diffusivity=0.5, diffusion_lsm3_tl_horizontal=20.),
+         dict(particle_diameter=0.05)),
+        ("lsm3_em_keps_am", dict(model=3, time_scheme=1, diffusion_model=2, time_step=0.25),
+         dict(added_mass_force=True, particle_diameter=0.05)),
+        ("lsm3_di_keps3_am", dict(model=3, time_scheme=5, diffusion_model=3),
+         dict(added_mass_force=True)),
+        ("lsm3_di_edge1_const", dict(model=3, time_scheme=5, diffusion_model=1, lsm3_edge_opt=1,
+                                     horizontal_diffusivity=0.5,
+                                     diffusion_lsm3_tl_horizontal=5.), {}),
+        ("lsm3_di_edge1_keps_small", dict(model=3, time_scheme=5, diffusion_model=2,
+                                          lsm3_edge_opt=1),
+         dict(particle_diameter=1e-3, particle_density=1050.)),
+    ]
+    for name, prm, pkw in lsm2_2d:
+        p = dict(base2)
+        p.update(prm)
+        save_traj(name, c2, p, 60 if p["time_step"] >= 1.0 else 100, seed=5, pset_kw=pkw)
+
+    # particles released within 2 m of the walls: Runge-Kutta stages that
+    # leave the domain stop the step early and leave the element index at -1
+    # for the final localization (cylag/lsm/update_state_lsm2.pyx:291-333)
+    cw = dict(c2)
+    rng = np.random.default_rng(21)
+    side = rng.integers(0, 4, 40)
+    t = rng.uniform(0.0, 1.0, 40)
+    d = rng.uniform(0.05, 2.0, 40)
+    px = np.where(side == 0, d, np.where(side == 1, 4000.0 - d, 5.0 + t * 3990.0))
+    py = np.where(side == 2, d, np.where(side == 3, 1000.0 - d, 5.0 + t * 990.0))
+    cw["position"] = np.stack([px, py], 1)
+    for ts in (2, 3, 4):
+        p = dict(base2)
+        p.update(model=2, time_scheme=ts, diffusion_model=0, time_step=2.0)
+        save_traj(f"lsm2_ts{ts}_walls", cw, p, 60, seed=6)
+
+    c3 = _loglaw3d()
+    c3u = _loglaw3d(unsteady=True)
+    base3 = dict(time_step=1.0, final_time=100.0, vertical_diffusivity=1e-3,
+                 horizontal_diffusivity=0.05)
+    lsm23_3d = [
+        ("lsm2_3d_rk4_settling", c3, dict(model=2, time_scheme=4, diffusion_model=0,
+                                          frozen_eulerian_fields=True, time_step=0.1),
+         dict(particle_density=1200.)),
+        ("lsm2_3d_di_opt3_keps_am", c3u, dict(model=2, time_scheme=5, diffusion_model=2,
+                                              diffusion_lsm2_option=3,
+                                              frozen_eulerian_fields=False),
+         dict(added_mass_force=True)),
+        ("lsm2_3d_em_opt2_keps3", c3, dict(model=2, time_scheme=1, diffusion_model=3,
+                                           diffusion_lsm2_option=2, time_step=0.5,
+                                           frozen_eulerian_fields=True),
+         dict(drag_coefficient_model=0, drag_coefficient=0.01)),
+        # explicit seen-velocity updates need dt < T_L: constant T_L here (the
+        # k-epsilon T_L of the log-law case vanishes at the bed)
+        ("lsm3_3d_em_const", c3, dict(model=3, time_scheme=1, diffusion_model=1,
+                                      diffusion_lsm3_tl_horizontal=10.,
+                                      diffusion_lsm3_tl_vertical=5.,
+                                      frozen_eulerian_fields=True, time_step=0.5),
+         dict(particle_diameter=0.05)),
+        ("lsm3_3d_di_keps_am", c3u, dict(model=3, time_scheme=5, diffusion_model=2,
+                                         diffusion_lsm3_tl_vertical=10.,
+                                         frozen_eulerian_fields=False),
+         dict(added_mass_force=True, particle_density=1100.)),
+        ("lsm3_3d_di_edge1_const", c3, dict(model=3, time_scheme=5, diffusion_model=1,
+                                            lsm3_edge_opt=1, diffusion_lsm3_tl_horizontal=10.,
+                                            diffusion_lsm3_tl_vertical=5.,
+                                            frozen_eulerian_fields=True), {}),
+    ]
+    for name, case, prm, pkw in lsm23_3d:
+        p = dict(base3)
+        p.update(prm)
+        save_traj(name, case, p, 50 if p["time_step"] >= 0.5 else 100, seed=8, pset_kw=pkw)
+
+
+GROUPS = {"rng": rng_fixture, "mesh": mesh_fixture, "lsm1": traj_fixtures,
+          "lsm23": lsm23_fixtures}
+
 if __name__ == "__main__":
-    rng_fixture()
-    mesh_fixture()
-    traj_fixtures()
+    for g in (sys.argv[1:] or list(GROUPS)):
+        GROUPS[g]()
