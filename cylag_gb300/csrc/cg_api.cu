@@ -59,6 +59,7 @@ struct cg_run {
     bool prev_valid = false;
     bool fields_ready = false;
     DevBuf cur, prev;
+    DevBuf turb;          // {k, eps} per node (LSM2/LSM3 k-epsilon runs)
     DevBuf stats;
     int stats_rows = 0;
     DevBuf errw;
@@ -409,13 +410,28 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
         return set_err(c, CG_ESTATE, "cg_run_create before mesh/field upload");
     if (p->precision != CG_PRECISION_FP64 && p->precision != CG_PRECISION_MIXED)
         return set_err(c, CG_EINVAL, "unknown precision %d", p->precision);
-    if (p->model != 1)
-        return set_err(c, CG_EINVAL, "model %d is not built in this library", p->model);
+    if (p->model < 1 || p->model > 3)
+        return set_err(c, CG_EINVAL, "model %d is not built in this library (1, 2, 3)", p->model);
     if (p->dim != c->fdim)
         return set_err(c, CG_EINVAL, "particle dim %d != field dim %d (pseudo-3D not built)",
                        p->dim, c->fdim);
-    if (p->time_scheme < 1 || p->time_scheme > 4)
+    // parameters.pyx:208-279
+    if (p->model == 1 && (p->time_scheme < 1 || p->time_scheme > 4))
         return set_err(c, CG_EINVAL, "LSM1 time_scheme must be 1..4");
+    if (p->model == 2 && p->diffusion_model == 0 && (p->time_scheme < 1 || p->time_scheme > 5))
+        return set_err(c, CG_EINVAL, "LSM2 time_scheme must be 1..5");
+    if (p->model >= 2 && p->diffusion_model != 0 && p->time_scheme != 1 && p->time_scheme != 5)
+        return set_err(c, CG_EINVAL, "LSM%d with diffusion needs time_scheme 1 or 5", p->model);
+    if (p->model == 3 && p->diffusion_model == 0)
+        return set_err(c, CG_EINVAL, "LSM3 needs a diffusion model");
+    if (p->diffusion_lsm2_option < 1 || p->diffusion_lsm2_option > 3)
+        return set_err(c, CG_EINVAL, "diffusion_lsm2_option must be 1..3");
+    if (p->lsm3_edge_opt < 1 || p->lsm3_edge_opt > 2)
+        return set_err(c, CG_EINVAL, "lsm3_edge_opt must be 1 or 2");
+    if (!(p->tl_horizontal > 0.) || !(p->tl_vertical > 0.))
+        return set_err(c, CG_EINVAL, "diffusion_lsm3_tl_* must be > 0");
+    if (p->diffusion_model < 0 || p->diffusion_model > 3)
+        return set_err(c, CG_EINVAL, "diffusion_model must be 0..3");
     if (p->rng_method < 1 || p->rng_method > 3) return set_err(c, CG_EINVAL, "bad rng_method");
     if ((p->diffusion_model == 2 || p->diffusion_model == 3) && !c->has_keps)
         return set_err(c, CG_EINVAL,
@@ -437,8 +453,12 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     CUDA_TRY(c, cudaSetDevice(c->device));
 
     size_t rec_bytes = record_bytes(c->fdim, p->precision) * c->frames.nnodes;
+    // LSM2/LSM3 with k-epsilon diffusion read k and eps themselves
+    bool need_turb = p->model >= 2 && (p->diffusion_model == 2 || p->diffusion_model == 3);
+    size_t turb_bytes = need_turb ? 2 * c->frames.nnodes * (p->precision ? 4 : 8) : 0;
     uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
-    bool use_queue = c->fdim == 2 && s->n > 0;
+    // deferred 2D walk: LSM1 (its queue entry carries no velocities)
+    bool use_queue = c->fdim == 2 && s->n > 0 && p->model == 1;
     size_t queue_bytes = use_queue ? 256 + (size_t)s->n * sizeof(WalkEntry) : 0;
     // element sort: 2D runs, keys nt + 1 <= 4096 scan tiles of 4096
     int nkeys = c->mesh.nt + 1;
@@ -456,7 +476,7 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
         off_w[1] = off_w[0] + work_bytes;
         sort_bytes = off_w[1] + work_bytes;
     }
-    uint64_t need = state_bytes + 2 * rec_bytes + 64 + queue_bytes + sort_bytes;
+    uint64_t need = state_bytes + 2 * rec_bytes + turb_bytes + 64 + queue_bytes + sort_bytes;
     if (c->budget && c->used + need > c->budget)
         return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
                        (unsigned long long)need, (unsigned long long)c->used,
@@ -469,8 +489,9 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     int rc;
     if ((rc = dalloc(c, r->cur, rec_bytes)) || (rc = dalloc(c, r->prev, rec_bytes)) ||
         (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->queue, queue_bytes)) ||
-        (rc = dalloc(c, r->sortbuf, sort_bytes))) {
+        (rc = dalloc(c, r->sortbuf, sort_bytes)) || (rc = dalloc(c, r->turb, turb_bytes))) {
         dfree(r->cur); dfree(r->prev); dfree(r->errw); dfree(r->queue); dfree(r->sortbuf);
+        dfree(r->turb);
         delete r;
         return rc;
     }
@@ -526,6 +547,28 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     d.density = p->particle_density;
     d.rho0 = p->water_density;
     d.drag_coef = p->drag_coefficient;
+    d.added_mass = p->added_mass_force != 0;
+    d.drag_model = p->drag_coefficient_model;
+    d.nuopt = p->diffusion_lsm2_option;
+    d.edge_opt = p->lsm3_edge_opt;
+    d.tl_h = p->tl_horizontal;
+    d.tl_v = p->tl_vertical;
+    // lagrangian_particle_set.pyx:361-375
+    {
+        double rhop = p->particle_density, rho0 = p->water_density;
+        if (!d.added_mass) {
+            d.a0c = (rhop - rho0) / rhop;
+            d.a1c = 0.5 * (rho0 / rhop);
+            d.a2c = 0.;
+            d.a3c = 1. / rhop;
+        } else {
+            double aux = 1. / (rhop + p->added_mass_coef * rho0);
+            d.a0c = (rhop - rho0) * aux;
+            d.a1c = 0.5 * rho0 * aux;
+            d.a2c = rho0 * (1. + p->added_mass_coef) * aux;
+            d.a3c = aux;
+        }
+    }
 
     DevState& st = r->st;
     st.n = s->n;
@@ -560,6 +603,7 @@ int cg_run_destroy(cg_run* r) {
     cudaStreamSynchronize(c->stream);
     dfree(r->cur);
     dfree(r->prev);
+    dfree(r->turb);
     dfree(r->stats);
     dfree(r->errw);
     dfree(r->queue);
@@ -581,13 +625,20 @@ int cg_run_seed(cg_run* r) {
 
 static double keps_fac(const cg_run* r) { return CMU / r->prm.schmidt_number; }
 
+static FieldView field_view(const cg_run* r) {
+    const cg_ctx* c = r->ctx;
+    return FieldView{r->cur.p, r->prev.p, r->turb.p, c->npoints, c->nlayers, c->fdim,
+                     r->prev_valid ? 1 : 0};
+}
+
 // eulerian_field_set.pyx:866-938: saves the previous temps (pointer swap)
 // and interpolates at `time` into the current ones.
 static int time_interpolation(cg_run* r, double time) {
     cg_ctx* c = r->ctx;
     if (r->frozen) {
         if (!r->fields_ready) {
-            launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
+            launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
+                     c->stream);
             CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes,
                                         cudaMemcpyDeviceToDevice, c->stream));
             r->fields_ready = true;
@@ -603,7 +654,8 @@ static int time_interpolation(cg_run* r, double time) {
     if (std::fabs(dt) < EPSILON)
         return set_err(c, CG_EINVAL, "Time interpolation failed: duplicate times at record %d", rec);
     double tf = (time - c->times[rec + 1]) / dt;
-    launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
+    launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
+                 c->stream);
     r->fields_ready = true;
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -615,7 +667,8 @@ static int ensure_fields(cg_run* r) {
     if (r->frozen) return time_interpolation(r, r->time);
     // EulerianFieldSet._init_tmp (743-776): both temps hold record 0, then
     // Solver.__init__ interpolates at initial_time (solver.pyx:190-191).
-    launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->prm.precision, c->stream);
+    launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
+                     c->stream);
     CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes, cudaMemcpyDeviceToDevice,
                                 c->stream));
     return time_interpolation(r, r->prm.initial_time);
@@ -627,8 +680,8 @@ int cg_run_init(cg_run* r) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = ensure_fields(r);
     if (rc) return rc;
-    launch_init(c->fdim, r->prm.precision, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp,
-                r->st, r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
+    launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, r->st,
+                r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
 }
@@ -679,21 +732,18 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             wq.e = (WalkEntry*)((char*)r->queue.p + 256);
             CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
         }
+        const FieldView fv = field_view(r);
+        uint32_t* errw = (uint32_t*)r->errw.p;
+        const int it = (int)r->iteration;
         if (r->prm.precision == CG_PRECISION_MIXED)
-            launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, run_state, wq, aux, (int)(r->iteration), stats,
-                              (uint32_t*)r->errw.p, c->stream);
+            launch_step_mixed(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         else
-            launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, run_state, wq, aux, (int)(r->iteration), stats,
-                              (uint32_t*)r->errw.p, c->stream);
+            launch_step_plain(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         if (r->use_queue) {
             if (r->prm.precision == CG_PRECISION_MIXED)
-                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, run_state, wq, aux,
-                                  (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
+                launch_walk_mixed(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
             else
-                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, run_state, wq,
-                                  aux, (int)(r->iteration), stats, (uint32_t*)r->errw.p, c->stream);
+                launch_walk_plain(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         }
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
@@ -746,29 +796,25 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
         if ((rc = time_interpolation(r, r->time))) return rc;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         WalkQueue wq{nullptr, nullptr};
-        if (c->fdim == 2) {
+        if (r->use_queue) {
             // the array keeps the previous call's contents: the counter must
             // start at zero every step
             wq.count = scratch->count;
             wq.e = scratch->entries;
             CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
         }
+        const FieldView fv = field_view(r);
+        uint32_t* errw = (uint32_t*)r->errw.p;
+        const int it = (int)r->iteration;
         if (r->prm.precision == CG_PRECISION_MIXED)
-            launch_step_mixed(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), nullptr,
-                              (uint32_t*)r->errw.p, c->stream);
+            launch_step_mixed(c->mesh, fv, r->dp, r->st, wq, aux, it, nullptr, errw, c->stream);
         else
-            launch_step_plain(c->fdim, c->mesh, r->cur.p, r->prev.p, c->npoints, c->nlayers,
-                              r->prev_valid, r->dp, r->st, wq, aux, (int)(r->iteration), nullptr,
-                              (uint32_t*)r->errw.p, c->stream);
+            launch_step_plain(c->mesh, fv, r->dp, r->st, wq, aux, it, nullptr, errw, c->stream);
         if (wq.e) {
             if (r->prm.precision == CG_PRECISION_MIXED)
-                launch_walk_mixed(c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq, aux,
-                                  (int)(r->iteration), nullptr, (uint32_t*)r->errw.p, c->stream);
+                launch_walk_mixed(c->mesh, fv, r->dp, r->st, wq, aux, it, nullptr, errw, c->stream);
             else
-                launch_walk_plain(0, c->mesh, r->cur.p, c->npoints, c->nlayers, r->dp, r->st, wq,
-                                  aux, (int)(r->iteration), nullptr, (uint32_t*)r->errw.p,
-                                  c->stream);
+                launch_walk_plain(c->mesh, fv, r->dp, r->st, wq, aux, it, nullptr, errw, c->stream);
         }
         CUDA_TRY(c, cudaGetLastError());
         r->time += r->prm.time_step;

@@ -18,6 +18,8 @@ constexpr double EPSILON = 1.e-16;
 constexpr double EPSILON_LSM2 = 1.e-8;
 constexpr double EPSILON_LSM3 = 1.e-8;
 constexpr double EPSILON_REBOUND = 1.e-8;
+constexpr double LSM3_CLIP_STEP = 1.e-4;
+constexpr double DBL_EPS = 2.220446049250313e-16;   // DBL_EPSILON
 constexpr double DEG_TO_RAD = 0.017453292519943295;
 constexpr double TWO_SQRT3 = 3.4641016151377544;
 constexpr double GRAV = 9.80665;
@@ -38,6 +40,7 @@ constexpr uint32_t ERR_INTERP_OUTSIDE = 1;
 constexpr uint32_t ERR_DEGENERATE_LAYER = 2;
 constexpr uint32_t ERR_RNG_LIMIT = 4;
 constexpr uint32_t ERR_UNSUPPORTED = 8;
+constexpr uint32_t ERR_NONFINITE = 16;   // LSM2/LSM3 coefficients the reference rejects
 
 // ---------------------------------------------------------------------------
 // device views
@@ -69,12 +72,17 @@ struct DevMesh {
 // where K = (Cmu/sigc) k^2 / max(eps, EPSILON) is the nodal k-epsilon
 // diffusivity (eulerian_field_set.pyx:1995-1997), exactly what the
 // reference evaluates per node inside _interpolate_diffusivity_gradient_c.
+// prev: the record of the previous time interpolation (the Eulerian time
+// derivative of the LSM2/LSM3 acceleration, valid when prev_valid).
+// turb: {k, eps} per node, time-interpolated, for the LSM2/LSM3 k-epsilon
+// diffusion (nullptr when the run does not need them).
 template <typename FT>
 struct DevFields {
     const FT* __restrict__ cur;
     const FT* __restrict__ prev;
     int npoints, nlayers, dim;
     int prev_valid;
+    const FT* __restrict__ turb;   // [nnodes][2]
 };
 
 struct DevParams {
@@ -87,6 +95,11 @@ struct DevParams {
     double buoy_wb;                      // constant buoyancy velocity (model 0)
     int buoy_model;
     double density, rho0, drag_coef;
+    // LSM2 / LSM3: particle coefficients (lagrangian_particle_set.pyx:355-375)
+    // and model options (parameters.pyx)
+    int added_mass, drag_model, nuopt, edge_opt;
+    double a0c, a1c, a2c, a3c;
+    double tl_h, tl_v;               // diffusion_lsm3_tl_horizontal / _vertical
 };
 
 struct DevState {
@@ -338,8 +351,13 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
                                  double y, int& new_k, int& bnd) {
     int intersected_edge = -1;
     for (int niter = 0; niter <= NITER_MAX; ++niter) {
-        int4 ta = __ldg(&m.tv[2 * k]);
-        int4 tb = __ldg(&m.tv[2 * k + 1]);
+        // k == -1 (an element index set to "outside" by a Runge-Kutta stage
+        // that left the mesh): the reference reads the last triangle's row
+        // (numpy wraparound) but compares with -1
+        int row = k < 0 ? k + m.nt : k;
+        if (row < 0) break;
+        int4 ta = __ldg(&m.tv[2 * row]);
+        int4 tb = __ldg(&m.tv[2 * row + 1]);
         int ed[3] = {ta.w, tb.x, tb.y};
         bool intersects = false;
 #pragma unroll
@@ -359,7 +377,7 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
             }
         }
         if (!intersects) {
-            new_k = in_tri(m, k, x, y) ? k : -1;
+            new_k = (k >= 0 && in_tri(m, k, x, y)) ? k : -1;
             bnd = -1;
             return;
         }
@@ -405,7 +423,9 @@ __device__ __forceinline__ bool intersec2d_filtered(float2 p1, float2 e0, float2
 __device__ inline void xy_localize(const DevMesh& m, int k, double p0x, double p0y, double x,
                                    double y, int& new_k, int& bnd) {
     bnd = -1;
-    if (in_tri(m, k, x, y)) { new_k = k; return; }
+    // point_in_tri with k == -1 returns -1 whether or not the point is in the
+    // last triangle (xylocalizer.pyx:126-167): "not found"
+    if (k >= 0 && in_tri(m, k, x, y)) { new_k = k; return; }
     path_walk(m, k, p0x, p0y, x, y, new_k, bnd);
     if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
 }

@@ -21,38 +21,50 @@ struct DevFrames {
     int dim;
 };
 
+// The node records a step reads, type-erased for the launchers: cur/prev
+// are FP64 (plain form) or FP32 (mixed form) records.
+struct FieldView {
+    const void* cur;
+    const void* prev;
+    const void* turb;   // {k, eps} per node or nullptr
+    int npoints, nlayers, dim, prev_valid;
+    template <typename FT>
+    DevFields<FT> as() const {
+        return DevFields<FT>{(const FT*)cur, (const FT*)prev, npoints, nlayers, dim, prev_valid,
+                             (const FT*)turb};
+    }
+};
+
 // Time interpolation + nodal diffusivity into the packed per-node record
-// (eulerian_field_set.pyx:866-938 and 1995-1997).  frozen: copy record 0.
+// (eulerian_field_set.pyx:866-938 and 1995-1997); turb != nullptr also
+// receives {k, eps} per node.  frozen: copy record 0.
 void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac_keps,
-                  void* cur, int precision, cudaStream_t st);
+                  void* cur, void* turb, int precision, cudaStream_t st);
 
 // One fused step over every particle of a run (plain FP64 form).
 // wq.e == nullptr: walk inline; else queue leavers and run launch_walk after.
-void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
-                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
-                       cudaStream_t st);
+void launch_step_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st);
 
-// second half of a 2D step: path walk + boundary conditions of queued
+// second half of a 2D LSM1 step: path walk + boundary conditions of queued
 // particles (exact FP64 predicates / FP32-filtered predicates)
-void launch_walk_plain(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
-                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
-void launch_walk_mixed(const DevMesh& m, const void* cur, int npoints, int nlayers,
-                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st);
+void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st);
+void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st);
 
 // The same step, mixed-precision form (FP32 node records).
-void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
-                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
-                       cudaStream_t st);
+void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st);
 
 // Solver.initialize_particle_state for particles with tri == -2 (FP64
 // arithmetic; node records FP64 or FP32 by precision).
-void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int npoints,
-                 int nlayers, const DevParams& p, const DevState& s, int velocity_init,
-                 uint32_t* err, cudaStream_t st);
+void launch_init(int precision, const DevMesh& m, const FieldView& fv, const DevParams& p,
+                 const DevState& s, int velocity_init, uint32_t* err, cudaStream_t st);
 
 // Working copies of the per-step state in element order (cg_sort.cu).
 struct WorkState {

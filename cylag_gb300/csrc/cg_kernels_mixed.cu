@@ -9,10 +9,9 @@
 
 namespace cg {
 
-void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
-                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
-                       cudaStream_t st) {
+void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
@@ -23,8 +22,12 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs_, 0);
         return nsm * (per < 1 ? 1 : per);
     };
-    if (dim == 2) {
-        DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 2, prev_valid};
+    DevFields<float> f = fv.as<float>();
+    WalkQueue none{nullptr, nullptr};
+    if (fv.dim == 2 && p.model >= 2) {
+        // LSM2 / LSM3: FP32 node records, FP64 arithmetic, inline walk
+        launch_step_kernel<2, float>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
+    } else if (fv.dim == 2) {
         // occupancy variant: 3 blocks/SM (80 registers) by default, 4 (64) on request
         static int minb = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
@@ -40,19 +43,17 @@ void launch_step_mixed(int dim, const DevMesh& m, const void* cur, const void* p
                                                                    step_index, stats, err);
     } else {
         // 3D: FP32 node records, FP64 arithmetic
-        DevFields<float> f{(const float*)cur, (const float*)prev, npoints, nlayers, 3, prev_valid};
-        WalkQueue none{nullptr, nullptr};
-        step_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, none, aux, step_index, stats, err);
+        launch_step_kernel<3, float>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
     }
 }
 
-void launch_walk_mixed(const DevMesh& m, const void* cur, int npoints, int nlayers,
-                       const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
-                       int step_index, int* stats, uint32_t* err, cudaStream_t st) {
+void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st) {
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
+    DevFields<float> f = fv.as<float>();
     walk_kernel<float, true><<<nsm * 8, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
 }
 

@@ -15,7 +15,7 @@ namespace cg {
 // ---------------------------------------------------------------------------
 template <int DIM, typename FT>
 __global__ void blend_kernel(DevFrames fr, int rec, double tf, int frozen, double fac,
-                             FT* __restrict__ cur) {
+                             FT* __restrict__ cur, FT* __restrict__ turb) {
     using S = Slots<DIM>;
     int64_t n = fr.nnodes;
     int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -45,75 +45,53 @@ __global__ void blend_kernel(DevFrames fr, int rec, double tf, int frozen, doubl
         r[6] = (FT)0;
         r[7] = (FT)0;
     }
+    if (turb) {
+        turb[2 * node] = (FT)kt;
+        turb[2 * node + 1] = (FT)ep;
+    }
 }
 
 void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac, void* cur,
-                  int precision, cudaStream_t st) {
+                  void* turb, int precision, cudaStream_t st) {
     int bs = 256;
     int64_t nb = (fr.nnodes + bs - 1) / bs;
     if (precision == 0) {
-        if (fr.dim == 2)
-            blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
-        else
-            blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (double*)cur);
+        double *c = (double*)cur, *t = (double*)turb;
+        if (fr.dim == 2) blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
+        else blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
     } else {
         // FP64 interpolation, rounded once to the FP32 record
-        if (fr.dim == 2)
-            blend_kernel<2, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (float*)cur);
-        else
-            blend_kernel<3, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, (float*)cur);
+        float *c = (float*)cur, *t = (float*)turb;
+        if (fr.dim == 2) blend_kernel<2, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
+        else blend_kernel<3, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
     }
 }
 
 // ---------------------------------------------------------------------------
 // the fused step
 // ---------------------------------------------------------------------------
-// one wave of resident blocks (persistent grid), capped by the work
-template <typename K>
-static int resident_grid(K kernel, int n, int bs) {
-    int dev = 0, nsm = 152, per = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs, 0);
-    if (per < 1) per = 1;
-    int need = (n + bs - 1) / bs;
-    int wave = nsm * per;
-    return need < wave ? need : wave;
-}
-
-void launch_step_plain(int dim, const DevMesh& m, const void* cur, const void* prev, int npoints,
-                       int nlayers, int prev_valid, const DevParams& p, const DevState& s,
-                       const WalkQueue& wq, int aux, int step_index, int* stats, uint32_t* err,
-                       cudaStream_t st) {
-    int bs = 256;
-    if (s.n == 0) return;
-    static int nb2 = 0, nb3 = 0;
-    if (!nb2) nb2 = resident_grid(step_kernel<2, double>, 1 << 30, bs);
-    if (!nb3) nb3 = resident_grid(step_kernel<3, double>, 1 << 30, bs);
-    int need = (s.n + bs - 1) / bs;
-    int nb = dim == 2 ? nb2 : nb3;
-    nb = need < nb ? need : nb;
-    if (dim == 2) {
-        DevFields<double> f{(const double*)cur, (const double*)prev, npoints, nlayers, 2, prev_valid};
-        step_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+void launch_step_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st) {
+    DevFields<double> f = fv.as<double>();
+    if (fv.dim == 2) {
+        launch_step_kernel<2, double>(p.model, m, f, p, s, wq, aux, step_index, stats, err, st);
     } else {
-        DevFields<double> f{(const double*)cur, (const double*)prev, npoints, nlayers, 3, prev_valid};
         WalkQueue none{nullptr, nullptr};
-        step_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, none, aux, step_index, stats, err);
+        launch_step_kernel<3, double>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
     }
 }
 
-void launch_walk_plain(int precision, const DevMesh& m, const void* cur, int npoints, int nlayers,
-                 const DevParams& p, const DevState& s, const WalkQueue& wq, int aux,
-                 int step_index, int* stats, uint32_t* err, cudaStream_t st) {
+void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                       const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                       int* stats, uint32_t* err, cudaStream_t st) {
     // grid-stride over the (device-side) entry count: a fixed grid of
     // 8 blocks per SM covers any count without a host round trip
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int nb = nsm * 8;
-    (void)precision;
-    DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
+    DevFields<double> f = fv.as<double>();
     walk_kernel<double, false><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
 }
 
@@ -167,39 +145,54 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
     if (vinit == 1) {
         double ux, uy, uz;
         q.velocity(k, ll, q.x[0], q.x[1], DIM == 3 ? q.x[2] : 0., ux, uy, uz);
-        double u[3] = {ux, uy, uz};
+        double u[3] = {ux, uy, uz}, w[3] = {ux, uy, uz};
+        if (p.model >= 2) {
+            // stationary fluctuations from the particle's own stream
+            // (solver.pyx:342-379)
+            q.tri = k;
+            q.ll = ll;
+            q.rng.state = s.rng[i];
+            q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
+            q.rng.err = 0;
+            double fl[3];
+            if (p.model == 2 && p.nuopt >= 2 && p.diffmod != 0) {
+                lsm2_fluctuations(q, s.diameter[i], fl);
+#pragma unroll
+                for (int d = 0; d < D; ++d) u[d] += fl[d];
+            }
+#pragma unroll
+            for (int d = 0; d < D; ++d) w[d] = u[d];
+            if (p.model == 3) {
+                lsm3_fluctuations(q, fl);
+#pragma unroll
+                for (int d = 0; d < D; ++d) w[d] += fl[d];
+            }
+            s.rng[i] = q.rng.state;
+            q.err |= q.rng.err;
+        }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             s.vel[(size_t)i * D + d] = u[d];
-            s.fvs[(size_t)i * D + d] = u[d];
+            s.fvs[(size_t)i * D + d] = w[d];
         }
     }
     if (q.err) atomicOr(err, q.err);
 }
 
-void launch_init(int dim, int precision, const DevMesh& m, const void* cur, int npoints,
-                 int nlayers, const DevParams& p, const DevState& s, int vinit, uint32_t* err,
-                 cudaStream_t st) {
+void launch_init(int precision, const DevMesh& m, const FieldView& fv, const DevParams& p,
+                 const DevState& s, int vinit, uint32_t* err, cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
     if (precision != 0) {
-        if (dim == 2) {
-            DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 2, 0};
-            init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-        } else {
-            DevFields<float> f{(const float*)cur, (const float*)cur, npoints, nlayers, 3, 0};
-            init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-        }
+        DevFields<float> f = fv.as<float>();
+        if (fv.dim == 2) init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+        else init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
         return;
     }
-    if (dim == 2) {
-        DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 2, 0};
-        init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-    } else {
-        DevFields<double> f{(const double*)cur, (const double*)cur, npoints, nlayers, 3, 0};
-        init_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-    }
+    DevFields<double> f = fv.as<double>();
+    if (fv.dim == 2) init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+    else init_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
 }
 
 // ---------------------------------------------------------------------------

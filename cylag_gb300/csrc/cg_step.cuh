@@ -142,6 +142,123 @@ struct Particle {
         return wb;
     }
 
+    // ---- fields of the LSM2/LSM3 updates -----------------------------------------
+    // turbulent energy and dissipation: 2D P1 (eulerian_field_set.pyx:994-1055),
+    // 3D prism with the layer given (1184-1287)
+    __device__ void turb_q(const P1& q, int l, double pz, double& kt, double& ep) {
+        const FT* t = f.turb;
+        if (DIM == 2) {
+            kt = (double)t[2 * q.i0] * q.f0 + (double)t[2 * q.i1] * q.f1 + (double)t[2 * q.i2] * q.f2;
+            ep = (double)t[2 * q.i0 + 1] * q.f0 + (double)t[2 * q.i1 + 1] * q.f1 +
+                 (double)t[2 * q.i2 + 1] * q.f2;
+            return;
+        }
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; kt = ep = 0.; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        double zlp = p1_eval<DIM>(f.cur, jl, q, Slots<DIM>::ZS);
+        double zup = p1_eval<DIM>(f.cur, ju, q, Slots<DIM>::ZS);
+        double dz = zlp - zup;
+        if (fabs(dz) < EPSILON) { err |= ERR_DEGENERATE_LAYER; kt = ep = 0.; return; }
+        double zf0 = (pz - zup) / dz;
+        double zf1 = (zlp - pz) / dz;
+        const FT* tl = t + 2 * (size_t)jl;
+        const FT* tu = t + 2 * (size_t)ju;
+        double ktl = (double)tl[2 * q.i0] * q.f0 + (double)tl[2 * q.i1] * q.f1 + (double)tl[2 * q.i2] * q.f2;
+        double ktu = (double)tu[2 * q.i0] * q.f0 + (double)tu[2 * q.i1] * q.f1 + (double)tu[2 * q.i2] * q.f2;
+        double epl = (double)tl[2 * q.i0 + 1] * q.f0 + (double)tl[2 * q.i1 + 1] * q.f1 +
+                     (double)tl[2 * q.i2 + 1] * q.f2;
+        double epu = (double)tu[2 * q.i0 + 1] * q.f0 + (double)tu[2 * q.i1 + 1] * q.f1 +
+                     (double)tu[2 * q.i2 + 1] * q.f2;
+        kt = zf0 * ktl + zf1 * ktu;
+        ep = zf0 * epl + zf1 * epu;
+    }
+
+    // value and gradient of a nodal prism field (eulerian_field_set.pyx:1999-2023)
+    __device__ void prism_vg(const FT* fld, int jl, int ju, int slot, const P1& q, double s_,
+                             double dz, double zlx, double zly, double zux, double zuy,
+                             double& val, double& ddx, double& ddy, double& ddz) {
+        double a0 = nodev<DIM>(fld, jl + q.i0, slot), a1 = nodev<DIM>(fld, jl + q.i1, slot),
+               a2 = nodev<DIM>(fld, jl + q.i2, slot);
+        double b0 = nodev<DIM>(fld, ju + q.i0, slot), b1 = nodev<DIM>(fld, ju + q.i1, slot),
+               b2 = nodev<DIM>(fld, ju + q.i2, slot);
+        double fl = a0 * q.f0 + a1 * q.f1 + a2 * q.f2;
+        double fu = b0 * q.f0 + b1 * q.f1 + b2 * q.f2;
+        double gxl = a0 * q.gx0 + a1 * q.gx1 + a2 * q.gx2;
+        double gyl = a0 * q.gy0 + a1 * q.gy1 + a2 * q.gy2;
+        double gxu = b0 * q.gx0 + b1 * q.gx1 + b2 * q.gx2;
+        double gyu = b0 * q.gy0 + b1 * q.gy1 + b2 * q.gy2;
+        double dfdz = (fu - fl) / dz;
+        val = (1. - s_) * fl + s_ * fu;
+        ddx = (1. - s_) * gxl + s_ * gxu - dfdz * ((1. - s_) * zlx + s_ * zux);
+        ddy = (1. - s_) * gyl + s_ * gyu - dfdz * ((1. - s_) * zly + s_ * zuy);
+        ddz = dfdz;
+    }
+
+    // dU/dt along a path, Ua = (ua, va, wa): eulerian_field_set.pyx:1396-1454
+    // (2D) and 1456-1579 (3D); the Eulerian time derivative from the previous
+    // interpolation when it is valid (never for frozen fields)
+    __device__ void accel(int k, int l, double px, double py, double pz, double ua, double va,
+                          double wa, double& ax, double& ay, double& az) {
+        P1 q = p1_at(m, k, px, py);
+        double dt = p.dt;
+        if (DIM == 2) {
+            using S = Slots<2>;
+            double u0 = nodev<DIM>(f.cur, q.i0, S::UX), u1 = nodev<DIM>(f.cur, q.i1, S::UX),
+                   u2 = nodev<DIM>(f.cur, q.i2, S::UX);
+            double v0 = nodev<DIM>(f.cur, q.i0, S::UY), v1 = nodev<DIM>(f.cur, q.i1, S::UY),
+                   v2 = nodev<DIM>(f.cur, q.i2, S::UY);
+            double dudx = u0 * q.gx0 + u1 * q.gx1 + u2 * q.gx2;
+            double dudy = u0 * q.gy0 + u1 * q.gy1 + u2 * q.gy2;
+            double dvdx = v0 * q.gx0 + v1 * q.gx1 + v2 * q.gx2;
+            double dvdy = v0 * q.gy0 + v1 * q.gy1 + v2 * q.gy2;
+            double dudt = 0., dvdt = 0.;
+            if (f.prev_valid) {
+                double pu0 = nodev<DIM>(f.prev, q.i0, S::UX), pu1 = nodev<DIM>(f.prev, q.i1, S::UX),
+                       pu2 = nodev<DIM>(f.prev, q.i2, S::UX);
+                double pv0 = nodev<DIM>(f.prev, q.i0, S::UY), pv1 = nodev<DIM>(f.prev, q.i1, S::UY),
+                       pv2 = nodev<DIM>(f.prev, q.i2, S::UY);
+                dudt = ((u0 - pu0) * q.f0 + (u1 - pu1) * q.f1 + (u2 - pu2) * q.f2) / dt;
+                dvdt = ((v0 - pv0) * q.f0 + (v1 - pv1) * q.f1 + (v2 - pv2) * q.f2) / dt;
+            }
+            ax = dudt + ua * dudx + va * dudy;
+            ay = dvdt + ua * dvdx + va * dvdy;
+            az = 0.;
+            return;
+        }
+        using S = Slots<3>;
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ax = ay = az = 0.; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        double e0 = nodev<DIM>(f.cur, jl + q.i0, S::ZS), e1 = nodev<DIM>(f.cur, jl + q.i1, S::ZS),
+               e2 = nodev<DIM>(f.cur, jl + q.i2, S::ZS);
+        double h0 = nodev<DIM>(f.cur, ju + q.i0, S::ZS), h1 = nodev<DIM>(f.cur, ju + q.i1, S::ZS),
+               h2 = nodev<DIM>(f.cur, ju + q.i2, S::ZS);
+        double zlp = e0 * q.f0 + e1 * q.f1 + e2 * q.f2;
+        double zup = h0 * q.f0 + h1 * q.f1 + h2 * q.f2;
+        double dz = zup - zlp;
+        if (fabs(dz) < EPSILON) { err |= ERR_DEGENERATE_LAYER; ax = ay = az = 0.; return; }
+        double s_ = (pz - zlp) / dz;
+        double zlx = e0 * q.gx0 + e1 * q.gx1 + e2 * q.gx2;
+        double zly = e0 * q.gy0 + e1 * q.gy1 + e2 * q.gy2;
+        double zux = h0 * q.gx0 + h1 * q.gx1 + h2 * q.gx2;
+        double zuy = h0 * q.gy0 + h1 * q.gy1 + h2 * q.gy2;
+        double un, dudx, dudy, dudz, vn, dvdx, dvdy, dvdz, wn, dwdx, dwdy, dwdz, t0, t1, t2, t3;
+        prism_vg(f.cur, jl, ju, S::UX, q, s_, dz, zlx, zly, zux, zuy, un, dudx, dudy, dudz);
+        prism_vg(f.cur, jl, ju, S::UY, q, s_, dz, zlx, zly, zux, zuy, vn, dvdx, dvdy, dvdz);
+        prism_vg(f.cur, jl, ju, S::UZ, q, s_, dz, zlx, zly, zux, zuy, wn, dwdx, dwdy, dwdz);
+        double dudt = 0., dvdt = 0., dwdt = 0.;
+        if (f.prev_valid) {
+            prism_vg(f.prev, jl, ju, S::UX, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dudt = (un - t0) / dt;
+            prism_vg(f.prev, jl, ju, S::UY, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dvdt = (vn - t0) / dt;
+            prism_vg(f.prev, jl, ju, S::UZ, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dwdt = (wn - t0) / dt;
+        }
+        ax = dudt + ua * dudx + va * dudy + wa * dudz;
+        ay = dvdt + ua * dvdx + va * dvdy + wa * dvdz;
+        az = dwdt + ua * dwdx + va * dwdy + wa * dwdz;
+    }
+
     // ---- LSM1 (cylag/lsm/update_state_lsm1.pyx) ----------------------------------
     __device__ void set_up_us(double ux, double uy, double uz) {
         up[0] = ux; up[1] = uy; us[0] = ux; us[1] = uy;
@@ -162,6 +279,9 @@ struct Particle {
             if (DIM == 3) x[2] += up[2] * p.dt;
             return true;
         }
+        // outside the mesh with no boundary crossing found: the reference
+        // raises at the next interpolation; flag it and stop the step
+        if (tt < 0) { err |= ERR_INTERP_OUTSIDE; tri = tt; return true; }
         return false;
     }
 
@@ -437,6 +557,12 @@ struct Particle {
     }
 };
 
+}  // namespace cg
+
+#include "cg_lsm23.cuh"
+
+namespace cg {
+
 // ziggurat tables into shared memory
 __device__ __forceinline__ void load_zig(ZigTables& zt) {
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
@@ -453,7 +579,7 @@ __device__ __forceinline__ void load_zig(ZigTables& zt) {
 // q.e != nullptr (2D): particles leaving their start triangle are queued
 // for walk_kernel instead of walking here.
 // One particle of the step (the body of the particle loop).
-template <int DIM, typename FT>
+template <int DIM, typename FT, int MODEL>
 __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<FT>& f,
                                               const DevParams& p, DevState& s,
                                               const WalkQueue& wq, int aux, int step_index,
@@ -470,31 +596,32 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
     const int ai = aux_index(s, i);
     q.ll = DIM == 3 ? s.lowerlayer[ai] : 0;
     q.ll0 = q.ll;
-    q.defer = (DIM == 2) && (wq.e != nullptr);
+    q.defer = (DIM == 2) && (wq.e != nullptr) && MODEL == 1;
     const int D = DIM;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         q.x[d] = s.pos[(size_t)i * D + d];
         q.x0[d] = q.x[d];
     }
-    bool need_vel = (p.model >= 2) || aux >= 2;
+    bool need_vel = (MODEL >= 2) || aux >= 2;
     if (need_vel) {
 #pragma unroll
         for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)ai * D + d];
     }
     double lastv[3] = {q.up[0], q.up[1], DIM == 3 ? q.up[2] : 0.};
-    if (p.model == 3) {
+    if (MODEL == 3) {
 #pragma unroll
         for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)ai * D + d];
     }
     q.rng.state = s.rng[i];
     q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
     q.rng.err = 0;
-    double dp = DIM == 3 ? s.diameter[ai] : 0.;
+    double dp = (DIM == 3 || MODEL >= 2) ? s.diameter[ai] : 0.;
 
     int bnd_j = -1;
-    if (p.model == 1) bnd_j = q.update_lsm1(dp);
-    else q.err |= ERR_UNSUPPORTED;
+    if constexpr (MODEL == 1) bnd_j = q.update_lsm1(dp);
+    else if constexpr (MODEL == 2) bnd_j = update_lsm2(q, dp);
+    else bnd_j = update_lsm3(q, dp);
 
     uint32_t e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
@@ -525,7 +652,9 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
 // wq.e != nullptr (2D): particles leaving their start triangle are queued
 // for walk_kernel instead of walking here.  Persistent grid (one wave of
 // resident blocks) striding over the particles.
-template <int DIM, typename FT>
+// MODEL: 1, 2 or 3 (LSM1/2/3), one instantiation each so that the LSM1
+// kernels keep their register budget.
+template <int DIM, typename FT, int MODEL = 1>
 __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
@@ -533,7 +662,36 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     __shared__ ZigTables zt;
     load_zig(zt);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_particle<DIM, FT>(m, f, p, s, wq, aux, step_index, stats, err_word, zt, i);
+        step_particle<DIM, FT, MODEL>(m, f, p, s, wq, aux, step_index, stats, err_word, zt, i);
+}
+
+// blocks of one wave of resident blocks of `kernel` (persistent grid)
+template <typename K>
+inline int resident_blocks(K kernel, int bs) {
+    int dev = 0, nsm = 152, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs, 0);
+    return nsm * (per < 1 ? 1 : per);
+}
+
+// step_kernel<DIM, FT, model> over every particle on a persistent grid
+template <int DIM, typename FT>
+void launch_step_kernel(int model, const DevMesh& m, const DevFields<FT>& f, const DevParams& p,
+                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                        int* stats, uint32_t* err, cudaStream_t st) {
+    const int bs = 256;
+    const int need = (s.n + bs - 1) / bs;
+    if (need == 0) return;
+    static int wave[3] = {0, 0, 0};
+    auto go = [&](auto kernel, int idx) {
+        if (!wave[idx]) wave[idx] = resident_blocks(kernel, bs);
+        int nb = need < wave[idx] ? need : wave[idx];
+        kernel<<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+    };
+    if (model == 1) go(step_kernel<DIM, FT, 1>, 0);
+    else if (model == 2) go(step_kernel<DIM, FT, 2>, 1);
+    else go(step_kernel<DIM, FT, 3>, 2);
 }
 
 // Second half of the step for queued (2D) particles: path walk from the

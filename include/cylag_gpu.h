@@ -34,6 +34,11 @@ extern "C" {
 #define CG_ERR_DEGENERATE_LAYER 2 /* |dz| < EPSILON between layers (1356-1363) */
 #define CG_ERR_RNG_LIMIT 4        /* a rejection loop hit its iteration cap */
 #define CG_ERR_UNSUPPORTED 8      /* option combination not built */
+#define CG_ERR_NONFINITE 16       /* LSM2/LSM3 coefficients or stationary
+                                     fluctuations the reference rejects with
+                                     ValueError (update_state_lsm2.pyx:1283,
+                                     update_state_lsm3.pyx:98-104,
+                                     init_lsm2_fluctuations.pyx:68-77) */
 
 #define CG_PRECISION_FP64 0       /* plain form: FP64 end to end */
 #define CG_PRECISION_MIXED 1      /* FP32 fields/updates, FP64 position + localization */
