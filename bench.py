@@ -1,14 +1,20 @@
 """Throughput benchmark of the GPU particle step (particle-steps/s).
 
-Workload (default): LSM1 2D with k-epsilon diffusivity-gradient drift at
-scale -- 4 km x 1 km jittered mesh (1001x251 vertices, 500,000 triangles),
-node fields interpolated in time between records 600 s apart, 1e7 particles
-uniform in the domain, dt = 0.5 s.  One step = one Solver.forward over all
-particles (time interpolation of the fields + the fused particle kernel).
-Inputs are synthetic (cylag_gb300.synth, seeded); the particle state
-(~360 MB) is larger than L2, so no flush is needed between steps.
+Workload (default, --workload lsm1_2d): LSM1 2D with k-epsilon
+diffusivity-gradient drift at scale -- 4 km x 1 km jittered mesh (1001x251
+vertices, 500,000 triangles), node fields interpolated in time between
+records 600 s apart, 1e7 particles uniform in the domain, dt = 0.5 s.
+Other workloads: lsm2_3d (LSM2 Langevin, direct integrator, k-epsilon
+velocity diffusion in the 3D log-law channel: 2e5 triangles x 21 sigma
+planes, 4e6 particles, dt = 0.1 s) and lsm3_3d (LSM3 polydisperse settling
+in a Taylor-Green vortex on the same mesh, 1e7 particles, dt = 0.2 s).
+One step = one Solver.forward over all particles (time interpolation of
+the fields + the fused particle kernel).  Inputs are synthetic
+(cylag_gb300.synth, seeded); the particle state is larger than L2, so no
+flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+                  [--workload lsm1_2d|lsm2_3d|lsm3_3d]
   python bench.py --impl reference ...   # the CPU implementation, host cores
 
 Prints one JSON line (rank 0).  Under torchrun each rank advances its own
@@ -33,7 +39,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-steps/s on 1 GB300 (mixed vs plain FP64); p50/p99 request latency"
 UNIT = "particle-steps/s"
-WORKLOAD = "lsm1_2d_keps_drift_500k_tri_1e7_particles"
+WORKLOADS = {
+    "lsm1_2d": "lsm1_2d_keps_drift_500k_tri_1e7_particles",
+    "lsm2_3d": "lsm2_3d_loglaw_di_keps_200k_tri_21_planes_4e6_particles",
+    "lsm3_3d": "lsm3_3d_taylor_green_settling_200k_tri_21_planes_1e7_particles",
+}
 
 
 def parse():
@@ -43,9 +53,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both")
-    ap.add_argument("--npart", type=int, default=10_000_000)
-    ap.add_argument("--nx", type=int, default=1001)
-    ap.add_argument("--ny", type=int, default=251)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lsm1_2d")
+    ap.add_argument("--npart", type=int, default=None,
+                    help="particles per GPU (default: the workload's own count)")
+    ap.add_argument("--nx", type=int, default=None)
+    ap.add_argument("--ny", type=int, default=None)
     ap.add_argument("--sort-period", type=int, default=25,
                     help="steps between re-sorts of the particles by element (0: never)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -127,25 +139,66 @@ class ClockSampler:
 # workload
 # ---------------------------------------------------------------------------
 def make_workload(args, rank=0):
+    """The workload's case dict (mesh, fields, particles, parameters); rank r
+    > 0 gets its own particles (same count) from its own seed."""
     from cylag_gb300 import synth
-    c = synth.keps_drift_channel(npart=args.npart, nx=args.nx, ny=args.ny, seed=0)
+    kw = {k: v for k, v in (("npart", args.npart), ("nx", args.nx), ("ny", args.ny)) if v}
+    if args.workload == "lsm1_2d":
+        c = synth.keps_drift_channel(seed=0, **kw)
+        c.update(dim=2, nlayers=1, pset={})
+    elif args.workload == "lsm2_3d":
+        c = synth.lsm2_loglaw_workload(seed=0, **kw)
+    else:
+        c = synth.lsm3_taylor_green_workload(seed=0, **kw)
     if rank:
         rng = np.random.default_rng(1000 + rank)
-        c["position"] = np.stack([rng.uniform(0, 4000.0, args.npart),
-                                  rng.uniform(0, 1000.0, args.npart)], 1)
+        c["position"] = c["position"][rng.permutation(len(c["position"]))]
+        c["position"][:, :2] += rng.uniform(-1.0, 1.0, (len(c["position"]), 2))
+        lo, hi = c["x"].min() + 1.0, c["x"].max() - 1.0
+        c["position"][:, 0] = np.clip(c["position"][:, 0], lo, hi)
+        lo, hi = c["y"].min() + 1.0, c["y"].max() - 1.0
+        c["position"][:, 1] = np.clip(c["position"][:, 1], lo, hi)
+    c["parameters"]["final_time"] = 1e9 if c["parameters"].get("frozen_eulerian_fields") \
+        else c["parameters"]["final_time"]
     return c
 
 
-def bytes_per_particle_step(precision):
+def bytes_per_particle_step(workload, precision):
     """Algorithmic (compulsory) DRAM bytes per particle-step of the fused
-    step: position r+w 32, tri r+w 8, PCG32 state r+w 16, tag r 4."""
-    return 32 + 8 + 16 + 4
+    step, per particle: the state it must read and write.
+    LSM1 2D: position r+w 32, tri r+w 8, PCG32 state r+w 16, tag r 4.
+    LSM2 3D: position r+w 48, velocity r+w 48, tri r+w 8, layer r+w 8,
+             PCG32 r+w 16, tag r 4, diameter r 8.
+    LSM3 3D: the LSM2 set + fluid velocity seen r+w 48."""
+    if workload == "lsm1_2d":
+        return 32 + 8 + 16 + 4
+    b = 48 + 48 + 8 + 8 + 16 + 4 + 8
+    return b + 48 if workload == "lsm3_3d" else b
 
 
 # DRAM bytes per particle-step of one step's kernels (step + walk), from the
 # ncu captures summarised in profiles/step_{mixed,fp64}_lsm1_2d_keps_4M.md
 # (4e6 particles, element-sorted; traffic grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {"mixed": 122.2, "fp64": 147.0}
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 122.2, ("lsm1_2d", "fp64"): 147.0}
+
+
+def field_set_of(c):
+    import cylag_gb300 as cg
+    from cylag_gb300.mesh import TriangularMesh
+    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+    fs = cg.EulerianFieldSet(mesh, dim=c["dim"], nlayers=c["nlayers"], times=c["times"],
+                             elevation=c["elevation"], velocity_x=c["velocity_x"],
+                             velocity_y=c["velocity_y"], velocity_z=c.get("velocity_z"),
+                             opt_fields=c.get("opt_fields"),
+                             opt_fields_names=c.get("opt_fields_names"))
+    return mesh, fs
+
+
+def fields_dict(c):
+    return dict(dim=c["dim"], nlayers=c["nlayers"], times=c["times"], elevation=c["elevation"],
+                velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
+                velocity_z=c.get("velocity_z"), opt_fields=c.get("opt_fields"),
+                opt_fields_names=c.get("opt_fields_names"))
 
 
 def peaks():
@@ -164,10 +217,9 @@ def cpu_rate(c, params, nsample, nsteps, threads):
     import oracle
     from cylag_gb300.mesh import TriangularMesh
     mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
-    fields = dict(dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
-                  velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
-                  opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
-    o = oracle.OracleSolver(mesh, fields, params, c["position"][:nsample], nthreads=threads)
+    diam = c["diameter"][:nsample] if "diameter" in c else None
+    o = oracle.OracleSolver(mesh, fields_dict(c), params, c["position"][:nsample],
+                            pset=c.get("pset"), nthreads=threads, diameter=diam)
     o.forward()  # warm
     t0 = time.perf_counter()
     for _ in range(nsteps):
@@ -199,7 +251,7 @@ def run_reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_particles": nsample,
+        "config": {"workload": WORKLOADS[args.workload], "sample_particles": nsample,
                    "note": "each step advances a bounded sample of the particles on all host cores"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{nsample} particles of the workload, 1 step per timed step"},
@@ -217,12 +269,10 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
     import torch
     import cylag_gb300 as cg
     from cylag_gb300 import _lib
-    from cylag_gb300.mesh import TriangularMesh
-    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
-    fs = cg.EulerianFieldSet(mesh, dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
-                             velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
-                             opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
-    ps = cg.LagrangianParticleSet(c["position"], dim=2)
+    mesh, fs = field_set_of(c)
+    ps = cg.LagrangianParticleSet(c["position"], dim=c["dim"], **c.get("pset", {}))
+    if "diameter" in c:
+        ps.diameter = c["diameter"]
     log(f"creating solver ({precision})")
     solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local,
                        sort_period=args.sort_period)
@@ -257,14 +307,24 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
     log(f"{precision}: timed {ms:.3f} ms, kernel {kern_ms:.4f} ms/launch")
     res = {"precision": precision, "ms": ms, "kernel_ms": kern_ms, "launches": launches,
            "value": world * n * args.steps / (ms / 1e3), "clocks": clk, "n": n,
-           "position": ps.position, "inactive": ps.inactive, "nt": int(mesh.nt)}
+           "position": ps.position, "velocity": ps.velocity, "inactive": ps.inactive,
+           "nt": int(mesh.nt)}
     if do_e2e:
         # end to end: host state (pinned) -> device, one step through the C
         # ABI, device -> host, every step
         log("end-to-end region")
         d = ps._dev
-        keys_in = ("position", "tri", "tag", "rng_state")
-        keys_out = ("position", "tri", "rng_state")
+        keys_in = ["position", "tri", "tag", "rng_state"]
+        keys_out = ["position", "tri", "rng_state"]
+        if c["dim"] == 3:
+            keys_in.append("lowerlayer")
+            keys_out.append("lowerlayer")
+        if params["model"] >= 2:
+            keys_in.append("velocity")
+            keys_out.append("velocity")
+        if params["model"] == 3:
+            keys_in.append("fluid_velocity_seen")
+            keys_out.append("fluid_velocity_seen")
         host = {k: torch.empty_like(d[k], device="cpu").pin_memory() for k in keys_in}
         for k in keys_in:
             host[k].copy_(d[k])
@@ -316,8 +376,9 @@ def run_gpu_arm(args):
     c = make_workload(args, rank)
     params = dict(c["parameters"])
     total_steps = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
-    if total_steps * params["time_step"] > 1200.0:
-        raise SystemExit("warmup + 2*steps must stay within the 1,200 s field records")
+    if not params.get("frozen_eulerian_fields") and \
+            total_steps * params["time_step"] > float(c["times"][-1]):
+        raise SystemExit("warmup + 2*steps must stay within the field records")
     forms = [args.precision] if args.precision != "both" else ["mixed", "fp64"]
     res = {}
     for prec in forms:
@@ -328,20 +389,24 @@ def run_gpu_arm(args):
     main_form = forms[0]
     r = res[main_form]
     n = r["n"]
-    bpp = bytes_per_particle_step(main_form)
+    bpp = bytes_per_particle_step(args.workload, main_form)
     peak, peak_kind = peaks()
     achieved = bpp * n / (r["kernel_ms"] / 1e3) / 1e9
-    traffic = NCU_TRAFFIC_B_PER_PARTICLE_STEP.get(main_form)
+    traffic = NCU_TRAFFIC_B_PER_PARTICLE_STEP.get((args.workload, main_form))
+    model_desc = {"lsm1_2d": "LSM1 Euler, k-eps drift",
+                  "lsm2_3d": "LSM2 direct integrator, k-eps velocity diffusion",
+                  "lsm3_3d": "LSM3 direct integrator, constant K, polydisperse settling"}
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if main_form == "fp64" else "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles_per_gpu": n, "triangles": r["nt"],
-                   "precision": main_form, "dt": params["time_step"],
-                   "l2": "state larger than L2 (no flush)", "model": "LSM1 Euler, k-eps drift",
-                   "sort_period": args.sort_period},
-        "gpu_launches": int(r["launches"]) + args.steps,  # step kernels + field blends
+        "config": {"workload": WORKLOADS[args.workload], "particles_per_gpu": n,
+                   "triangles": r["nt"], "layers": c["nlayers"], "precision": main_form,
+                   "dt": params["time_step"], "l2": "state larger than L2 (no flush)",
+                   "model": model_desc[args.workload],
+                   "sort_period": args.sort_period if c["dim"] == 2 else 0},
+        "gpu_launches": int(r["launches"]),   # every kernel of the timed cg_run_step call
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": float(traffic * n) if traffic else None,
@@ -364,6 +429,10 @@ def run_gpu_arm(args):
         line["mixed_error_vs_fp64"] = {
             "steps": args.warmup + args.steps, "rms_displacement_diff_m": rep["rms_displacement_diff"],
             "var_rel_err": max(rep["var_rel_err"]), "mean_rel_err": max(rep["mean_rel_err"])}
+        if params["model"] >= 2:
+            va, vb = r["velocity"][act], q["velocity"][act]
+            line["mixed_error_vs_fp64"]["velocity_var_rel_err"] = float(
+                np.max(np.abs(va.var(0) - vb.var(0)) / np.maximum(vb.var(0), 1e-300)))
     if not args.no_cpu_baseline:
         log("cpu baseline")
         threads = os.cpu_count() or 1

@@ -710,10 +710,12 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     // gather/scatter (a few steps per sort period)
     const bool sorted = r->sort_period > 0 && nsteps >= r->sort_period;
     DevState ws = r->st;
+    int launches = 0;   // kernels launched by this call
     for (int s = 0; s < nsteps; ++s) {
         if (sorted && s % r->sort_period == 0) {
             if (s == 0) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
             else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
+            launches += 6;   // histogram, 3 scan passes, index scatter, gather
             ws.pos = (double*)r->sb.a.pos;
             ws.tri = r->sb.a.tri;
             ws.tag = r->sb.a.tag;
@@ -723,6 +725,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         const DevState& run_state = sorted ? ws : r->st;
         // solver.pyx:440: fields at the step-start time
         if ((rc = time_interpolation(r, r->time))) return rc;
+        if (!r->frozen) launches += 1;   // field blend
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * nopen;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
@@ -747,7 +750,11 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         }
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
-        if (sorted && s == nsteps - 1) launch_sort_scatter(r->st, r->sb, c->stream);
+        launches += r->st.n > 0 ? (r->use_queue ? 2 : 1) : 0;   // step (+ walk)
+        if (sorted && s == nsteps - 1) {
+            launch_sort_scatter(r->st, r->sb, c->stream);
+            launches += 1;
+        }
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;
@@ -760,7 +767,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         tot += ms;
     }
     r->last_ms = tot / nsteps;
-    r->last_launches = nsteps;
+    r->last_launches = launches;
     if (bnd_stats_host && c->nopen > 0)
         CUDA_TRY(c, cudaMemcpy(bnd_stats_host, r->stats.p, (size_t)nsteps * c->nopen * sizeof(int),
                                cudaMemcpyDeviceToHost));

@@ -212,3 +212,66 @@ def loglaw_case(nx: int = 501, ny: int = 201, lx: float = 2000.0, ly: float = 10
                 velocity_z=w[None, :], opt_fields=np.stack([k[None, :], eps[None, :]]),
                 opt_fields_names=["TURBULENT ENERG.", "DISSIPATION"],
                 position=np.stack([px, py, pz], axis=1), bathymetry=h)
+
+
+def lsm2_loglaw_workload(npart: int = 4_000_000, nx: int = 501, ny: int = 201,
+                         nplanes: int = 21, seed: int = 0, nsteps: int = 5000, dt: float = 0.1):
+    """LSM2 Langevin in the 3D log-law channel (2 km x 1 km, 2e5 triangles at
+    the default grid, 21 sigma planes): k-epsilon velocity diffusion on all
+    three components (diffusion_model 3, diffusion_lsm2_option 2), direct
+    integrator (time_scheme 5), frozen fields; particles rho_p = 1000 kg/m3,
+    d_p = 1e-4 m, uniform in the volume; dt = 0.1 s, 5,000 steps."""
+    c = loglaw_case(nx=nx, ny=ny, nplanes=nplanes, npart=npart, seed=seed)
+    c["dim"] = 3
+    c["parameters"] = {"model": 2, "time_scheme": 5, "diffusion_model": 3,
+                       "diffusion_lsm2_option": 2, "frozen_eulerian_fields": True,
+                       "time_step": dt, "final_time": nsteps * dt}
+    c["pset"] = {"particle_density": 1000., "particle_diameter": 1e-4}
+    c["nsteps"] = nsteps
+    return c
+
+
+def stokes_diameter(ws, rhop: float = 2650., rho0: float = 1000., nu: float = 1.3e-6,
+                    g: float = 9.80665):
+    """Diameter whose Stokes settling velocity is ws: ws = (s-1) g d^2 / (18 nu)."""
+    return np.sqrt(18.0 * nu * np.asarray(ws) / ((rhop / rho0 - 1.0) * g))
+
+
+def lsm3_taylor_green_workload(npart: int = 10_000_000, nx: int = 501, ny: int = 201,
+                               nplanes: int = 21, seed: int = 0, nsteps: int = 2000,
+                               dt: float = 0.2, U0: float = 0.2, L: float = 200.0):
+    """LSM3 polydisperse settling on the log-law channel's mesh and bathymetry:
+    horizontal Taylor-Green vortex in every layer, u = -U0 sin(pi x/L)
+    cos(pi y/L), v = U0 cos(pi x/L) sin(pi y/L), w = 0 (U0 = 0.2 m/s,
+    L = 200 m); constant diffusivities K_h = 0.01, K_v = 1e-3 m2/s with
+    T_L = 1 s (diffusion_model 1); direct integrator; quartz particles
+    (2650 kg/m3) whose Stokes settling velocity is log-normal (median 1 mm/s,
+    sigma_ln 0.8), i.e. diameters log-normal with median 3.80e-5 m and
+    sigma_ln 0.4; released uniformly in the top 20% of the column;
+    dt = 0.2 s, 2,000 steps.  The bed reflects, as in the reference."""
+    lx, ly = 2000.0, 1000.0
+    x, y, tri = channel_mesh(lx, ly, nx, ny, seed=seed, jitter=0.3)
+    h = bathymetry(x, y, seed + 7, lx=lx, ly=ly)
+    zb = -h
+    zs = np.zeros_like(zb)
+    elev = sigma_elevation(zb, zs, nplanes)
+    u1 = -U0 * np.sin(np.pi * x / L) * np.cos(np.pi * y / L)
+    v1 = U0 * np.cos(np.pi * x / L) * np.sin(np.pi * y / L)
+    u, v = np.tile(u1, nplanes), np.tile(v1, nplanes)
+    w = np.zeros_like(u)
+    rng = np.random.default_rng(seed + 3)
+    px = rng.uniform(0.0, lx, npart)
+    py = rng.uniform(0.0, ly, npart)
+    hp = bathymetry(px, py, seed + 7, lx=lx, ly=ly)
+    pz = -hp * rng.uniform(0.0, 0.2, npart)
+    ws = 1e-3 * np.exp(0.8 * rng.standard_normal(npart))
+    diam = stokes_diameter(ws)
+    params = {"model": 3, "time_scheme": 5, "diffusion_model": 1,
+              "horizontal_diffusivity": 0.01, "vertical_diffusivity": 1e-3,
+              "diffusion_lsm3_tl_horizontal": 1.0, "diffusion_lsm3_tl_vertical": 1.0,
+              "frozen_eulerian_fields": True, "time_step": dt, "final_time": nsteps * dt}
+    return dict(x=x, y=y, triangles=tri, nlayers=nplanes, dim=3, times=np.zeros(1),
+                elevation=elev[None, :], velocity_x=u[None, :], velocity_y=v[None, :],
+                velocity_z=w[None, :], position=np.stack([px, py, pz], axis=1),
+                diameter=diam, parameters=params, pset={"particle_density": 2650.},
+                nsteps=nsteps, bathymetry=h)

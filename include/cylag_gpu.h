@@ -197,8 +197,10 @@ int cg_run_errors(cg_run *run, uint32_t *flags);
  * caller from tri (tri == -1 inactive). */
 
 /* ---- measurement ------------------------------------------------------ */
-/* Mean device time (ms) of the step kernel over the last cg_run_step call,
- * measured with CUDA events on the context stream. */
+/* Mean device time (ms) per step of the step kernel (and, for 2D LSM1
+ * runs, the walk kernel) over the last cg_run_step call, measured with CUDA
+ * events on the context stream; launches = every kernel that call launched
+ * (step, walk, field time interpolation, element sort). */
 int cg_run_last_kernel_ms(const cg_run *run, double *ms, int32_t *launches);
 
 #ifdef __cplusplus
