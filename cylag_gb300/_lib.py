@@ -95,6 +95,15 @@ SIGNATURES = [
     ("cg_run_time", C.c_int, [P, C.POINTER(F64), C.POINTER(C.c_int64)]),
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),
+    ("cg_server_create", C.c_int, [P, I32, C.c_int64, I32, F64, C.POINTER(P)]),
+    ("cg_server_destroy", C.c_int, [P]),
+    ("cg_server_admit", C.c_int, [P, C.POINTER(Params), I32, P, F64, P, I32, C.POINTER(I32)]),
+    ("cg_server_step", C.c_int, [P, I32]),
+    ("cg_server_run_status", C.c_int, [P, I32, C.POINTER(I32)]),
+    ("cg_server_read", C.c_int, [P, I32, P, P, P, P, P, P, C.POINTER(C.c_uint32)]),
+    ("cg_server_release", C.c_int, [P, I32]),
+    ("cg_server_stats", C.c_int, [P, C.POINTER(I32), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64), C.POINTER(F64)]),
 ]
 
 

@@ -25,8 +25,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 
 # translation unit -> extra flags
+# host code: no contraction either, so host-computed coefficients round as
+# the reference's (e.g. 1/(rho_p + Ca rho_0), lagrangian_particle_set.pyx:371)
+HOST_EXACT = ["-Xcompiler", "-ffp-contract=off"]
 UNITS = {
-    "cg_api.cu": ["-fmad=false"],
+    "cg_api.cu": ["-fmad=false", *HOST_EXACT],
+    "cg_server.cu": HOST_EXACT,
     "cg_kernels_plain.cu": ["-fmad=false"],
     "cg_kernels_mixed.cu": [],
     "cg_sort.cu": [],

@@ -270,10 +270,7 @@ class LagrangianParticleSet:
             _torch().cuda.synchronize()
 
     def _retag(self):
-        """Deleted particles carry a negative marker (-1: deleted while being
-        initialized, -2-it: deleted during iteration it); give them
-        maxtag+1, maxtag+2, ... in deletion order then index order, as
-        delete_single does (lagrangian_particle_set.pyx:786-788)."""
+        """Gives the deleted particles their new tags (see retag)."""
         if self._dev is None:
             return
         self._sync()
@@ -281,14 +278,9 @@ class LagrangianParticleSet:
         neg = (tag < 0).nonzero().flatten()
         if neg.numel() == 0:
             return
-        idx = neg.cpu().numpy()
-        mark = tag[neg].cpu().numpy()
-        order = np.lexsort((idx, -mark))
-        new = np.empty(len(idx), dtype=np.int32)
-        new[order] = self.maxtag + 1 + np.arange(len(idx), dtype=np.int32)
-        self.maxtag += len(idx)
+        new, self.maxtag = retag(tag.cpu().numpy(), self.maxtag)
         torch = _torch()
-        tag[neg] = torch.from_numpy(new).to(tag.device)
+        tag.copy_(torch.from_numpy(new).to(tag.device))
         torch.cuda.synchronize()
 
     # ---- public arrays --------------------------------------------------------
@@ -372,6 +364,62 @@ class LagrangianParticleSet:
         self._set("tag", t)
 
 
+def c_params(P, dim, density=1000., drag_model=1, drag_coef=0.44, added_mass=False,
+             added_mass_coef=0.5, buoyancy_model=0, buoyancy_value=0.0,
+             precision=_lib.CG_PRECISION_FP64, seed=0, sort_period=0):
+    """The C-ABI parameter block (cg_params) of checked Parameters P and the
+    particle-set scalars (lagrangian_particle_set.pyx:158-261)."""
+    return _lib.Params(
+        P.model, P.time_scheme, P.rng_method, P.diffusion_model, P.diffusion_lsm2_option,
+        P.lsm3_edge_opt, int(bool(P.boundary_conditions)), P.boundary_conditions_type,
+        P.max_wall_rebounds, int(bool(P.bnd_statistics)), P.particle_velocity_init,
+        int(bool(P.frozen_eulerian_fields)), P.initial_time, P.final_time, P.time_step,
+        P.horizontal_diffusivity, P.vertical_diffusivity, P.schmidt_number,
+        P.diffusion_lsm3_tl_horizontal, P.diffusion_lsm3_tl_vertical,
+        P.rebound_damping_coef, P.wall_roughness_angle, P.stranding_probability,
+        P.water_density, dim, density, drag_model, drag_coef, int(bool(added_mass)),
+        added_mass_coef, buoyancy_model, buoyancy_value, precision, int(seed), int(sort_period))
+
+
+def retag(tag, maxtag):
+    """Deleted particles carry a negative marker (-1: deleted while being
+    initialized, -2-it: deleted during iteration it); give them maxtag+1,
+    maxtag+2, ... in deletion order then index order, as delete_single does
+    (lagrangian_particle_set.pyx:786-788).  Returns (tags, new maxtag)."""
+    tag = np.array(tag, dtype=np.int32, copy=True)
+    idx = np.nonzero(tag < 0)[0]
+    if len(idx) == 0:
+        return tag, maxtag
+    order = np.lexsort((idx, -tag[idx]))
+    new = np.empty(len(idx), dtype=np.int32)
+    new[order] = maxtag + 1 + np.arange(len(idx), dtype=np.int32)
+    tag[idx] = new
+    return tag, maxtag + len(idx)
+
+
+def upload_mesh_fields(L, ctx, field_set):
+    """cg_mesh_upload + cg_fields_upload of an EulerianFieldSet; returns the
+    host arrays that must stay alive until the uploads return."""
+    m = field_set.triangular_mesh
+    g = m.locator_grid()
+    keep = [m.x, m.y, m.triangles, m.gradx, m.grady, m.det, m.edges, m.triedge_map,
+            m.edgetri_map, m.edges_labels, g[5], g[6]]
+    md = _lib.MeshDesc(m.nv, m.nt, m.ne, m.nopen, m.x.ctypes.data, m.y.ctypes.data,
+                       m.triangles.ctypes.data, m.gradx.ctypes.data, m.grady.ctypes.data,
+                       m.det.ctypes.data, m.edges.ctypes.data, m.triedge_map.ctypes.data,
+                       m.edgetri_map.ctypes.data, m.edges_labels.ctypes.data,
+                       g[0], g[1], g[2], g[3], g[4], g[5].ctypes.data, g[6].ctypes.data)
+    _lib.check(ctx, L.cg_mesh_upload(ctx, C.byref(md)))
+    fs = field_set
+    ptr = lambda a: None if a is None else a.ctypes.data
+    fd = _lib.FieldsDesc(fs.dim, fs.nlayers, fs.npoints, fs.ntimes, ptr(fs.times),
+                         ptr(fs.elevation), ptr(fs.velocity_x), ptr(fs.velocity_y),
+                         ptr(fs.velocity_z), ptr(fs._opt.get("turbulent_energy")),
+                         ptr(fs._opt.get("dissipation")), ptr(fs._opt.get("bottom")))
+    _lib.check(ctx, L.cg_fields_upload(ctx, C.byref(fd)))
+    return keep
+
+
 class Solver:
     """Mirror of cylag.Solver (solver.pyx:42-236) running the GPU step.
 
@@ -424,17 +472,9 @@ class Solver:
         self._upload_mesh_fields()
         ps._attach(self._ctx, device)
         ps._solver = self
-        self._prm = _lib.Params(
-            P.model, P.time_scheme, P.rng_method, P.diffusion_model, P.diffusion_lsm2_option,
-            P.lsm3_edge_opt, int(bool(P.boundary_conditions)), P.boundary_conditions_type,
-            P.max_wall_rebounds, int(bool(P.bnd_statistics)), P.particle_velocity_init,
-            int(bool(P.frozen_eulerian_fields)), P.initial_time, P.final_time, P.time_step,
-            P.horizontal_diffusivity, P.vertical_diffusivity, P.schmidt_number,
-            P.diffusion_lsm3_tl_horizontal, P.diffusion_lsm3_tl_vertical,
-            P.rebound_damping_coef, P.wall_roughness_angle, P.stranding_probability,
-            P.water_density, ps.dim, ps.density, ps.drag_coef_model, ps.drag_coef,
-            int(bool(ps.added_mass_force)), ps.added_mass_coef, ps.buoyancy_velocity_model,
-            ps.buoyancy_velocity_value, prec, self.seed, int(sort_period))
+        self._prm = c_params(P, ps.dim, ps.density, ps.drag_coef_model, ps.drag_coef,
+                             ps.added_mass_force, ps.added_mass_coef, ps.buoyancy_velocity_model,
+                             ps.buoyancy_velocity_value, prec, self.seed, sort_period)
         self._run = C.c_void_p()
         self._create_run()
         _lib.check(self._ctx, self.L.cg_run_seed(self._run))
@@ -445,23 +485,7 @@ class Solver:
         self.nopen = nopen
 
     def _upload_mesh_fields(self):
-        m = self.field_set.triangular_mesh
-        g = m.locator_grid()
-        self._keep = [m.x, m.y, m.triangles, m.gradx, m.grady, m.det, m.edges, m.triedge_map,
-                      m.edgetri_map, m.edges_labels, g[5], g[6]]
-        md = _lib.MeshDesc(m.nv, m.nt, m.ne, m.nopen, m.x.ctypes.data, m.y.ctypes.data,
-                           m.triangles.ctypes.data, m.gradx.ctypes.data, m.grady.ctypes.data,
-                           m.det.ctypes.data, m.edges.ctypes.data, m.triedge_map.ctypes.data,
-                           m.edgetri_map.ctypes.data, m.edges_labels.ctypes.data,
-                           g[0], g[1], g[2], g[3], g[4], g[5].ctypes.data, g[6].ctypes.data)
-        _lib.check(self._ctx, self.L.cg_mesh_upload(self._ctx, C.byref(md)))
-        fs = self.field_set
-        ptr = lambda a: None if a is None else a.ctypes.data
-        fd = _lib.FieldsDesc(fs.dim, fs.nlayers, fs.npoints, fs.ntimes, ptr(fs.times),
-                             ptr(fs.elevation), ptr(fs.velocity_x), ptr(fs.velocity_y),
-                             ptr(fs.velocity_z), ptr(fs._opt.get("turbulent_energy")),
-                             ptr(fs._opt.get("dissipation")), ptr(fs._opt.get("bottom")))
-        _lib.check(self._ctx, self.L.cg_fields_upload(self._ctx, C.byref(fd)))
+        self._keep = upload_mesh_fields(self.L, self._ctx, self.field_set)
 
     def _create_run(self):
         sd = self.particle_set._state_desc()

@@ -15,35 +15,9 @@
 #include <vector>
 
 #include "../../include/cylag_gpu.h"
-#include "cg_internal.h"
+#include "cg_host.h"
 
 using namespace cg;
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-struct cg_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;      // stream all work is issued on
-    cudaStream_t own_stream = nullptr;  // the context's own stream
-    uint64_t budget = 0;
-    uint64_t used = 0;
-    std::string err;
-    // mesh
-    bool have_mesh = false;
-    DevMesh mesh{};
-    int nopen = 0;
-    std::vector<DevBuf> mesh_bufs;
-    // fields
-    bool have_fields = false;
-    DevFrames frames{};
-    DevBuf frames_buf;
-    std::vector<double> times;
-    int fdim = 2, nlayers = 1, npoints = 0;
-    bool has_keps = false;
-};
 
 struct cg_run {
     cg_ctx* ctx = nullptr;
@@ -73,38 +47,6 @@ struct cg_run {
     int last_launches = 0;
     double last_ms = 0.;
 };
-
-static int set_err(cg_ctx* c, int code, const char* fmt, ...) {
-    if (c) {
-        char buf[512];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof buf, fmt, ap);
-        va_end(ap);
-        c->err = buf;
-    }
-    return code;
-}
-
-#define CUDA_TRY(c, call)                                                                    \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
-            return set_err((c), CG_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
-    } while (0)
-
-static int dalloc(cg_ctx* c, DevBuf& b, size_t bytes) {
-    b.bytes = bytes;
-    if (bytes == 0) { b.p = nullptr; return CG_OK; }
-    CUDA_TRY(c, cudaMalloc(&b.p, bytes));
-    return CG_OK;
-}
-
-static void dfree(DevBuf& b) {
-    if (b.p) cudaFree(b.p);
-    b.p = nullptr;
-    b.bytes = 0;
-}
 
 template <typename T>
 static int upload(cg_ctx* c, const std::vector<T>& h, const T*& out) {
@@ -152,6 +94,94 @@ static int noalloc_scratch(cg_ctx* c, NoallocScratch** out) {
     }
     *out = g_noalloc_ptr[c->device];
     return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// run parameters
+// ---------------------------------------------------------------------------
+int check_params(cg_ctx* c, const cg_params* p) {
+    if (p->precision != CG_PRECISION_FP64 && p->precision != CG_PRECISION_MIXED)
+        return set_err(c, CG_EINVAL, "unknown precision %d", p->precision);
+    if (p->model < 1 || p->model > 3)
+        return set_err(c, CG_EINVAL, "model %d is not built in this library (1, 2, 3)", p->model);
+    if (p->dim != c->fdim)
+        return set_err(c, CG_EINVAL, "particle dim %d != field dim %d (pseudo-3D not built)",
+                       p->dim, c->fdim);
+    // parameters.pyx:208-279
+    if (p->model == 1 && (p->time_scheme < 1 || p->time_scheme > 4))
+        return set_err(c, CG_EINVAL, "LSM1 time_scheme must be 1..4");
+    if (p->model == 2 && p->diffusion_model == 0 && (p->time_scheme < 1 || p->time_scheme > 5))
+        return set_err(c, CG_EINVAL, "LSM2 time_scheme must be 1..5");
+    if (p->model >= 2 && p->diffusion_model != 0 && p->time_scheme != 1 && p->time_scheme != 5)
+        return set_err(c, CG_EINVAL, "LSM%d with diffusion needs time_scheme 1 or 5", p->model);
+    if (p->model == 3 && p->diffusion_model == 0)
+        return set_err(c, CG_EINVAL, "LSM3 needs a diffusion model");
+    if (p->diffusion_lsm2_option < 1 || p->diffusion_lsm2_option > 3)
+        return set_err(c, CG_EINVAL, "diffusion_lsm2_option must be 1..3");
+    if (p->lsm3_edge_opt < 1 || p->lsm3_edge_opt > 2)
+        return set_err(c, CG_EINVAL, "lsm3_edge_opt must be 1 or 2");
+    if (!(p->tl_horizontal > 0.) || !(p->tl_vertical > 0.))
+        return set_err(c, CG_EINVAL, "diffusion_lsm3_tl_* must be > 0");
+    if (p->diffusion_model < 0 || p->diffusion_model > 3)
+        return set_err(c, CG_EINVAL, "diffusion_model must be 0..3");
+    if (p->rng_method < 1 || p->rng_method > 3) return set_err(c, CG_EINVAL, "bad rng_method");
+    if ((p->diffusion_model == 2 || p->diffusion_model == 3) && !c->has_keps)
+        return set_err(c, CG_EINVAL,
+                       "diffusion_model=%d requires 'TURBULENT ENERG.' and 'DISSIPATION' fields",
+                       p->diffusion_model);
+    return CG_OK;
+}
+
+void make_dev_params(const cg_ctx* c, const cg_params* p, DevParams& d) {
+    d = DevParams{};
+    d.model = p->model;
+    d.time_scheme = p->time_scheme;
+    d.rng_method = p->rng_method;
+    d.diffmod = p->diffusion_model;
+    d.bc_on = p->boundary_conditions != 0;
+    d.bc_type = p->boundary_conditions_type;
+    d.max_rebounds = p->max_wall_rebounds;
+    d.bnd_statistics = p->bnd_statistics != 0;
+    d.nopen = c->nopen;
+    d.pdim = p->dim;
+    d.dt = p->time_step;
+    d.sqrtdt = std::sqrt(p->time_step);
+    d.nux = p->horizontal_diffusivity;
+    d.nuz = p->vertical_diffusivity;
+    // update_state_lsm1.pyx:708-713
+    d.diffx_const = std::sqrt(2. * d.nux) * d.sqrtdt;
+    d.diffz_const = std::sqrt(2. * d.nuz) * d.sqrtdt;
+    d.damp = std::fmin(p->rebound_damping_coef, 1.0 - EPSILON_REBOUND);  // compute_bc.pyx:76
+    d.strand = p->stranding_probability;
+    d.roughness = p->wall_roughness_angle * DEG_TO_RAD;
+    d.buoy_model = p->buoyancy_velocity_model;
+    d.buoy_wb = p->buoyancy_velocity;
+    d.density = p->particle_density;
+    d.rho0 = p->water_density;
+    d.drag_coef = p->drag_coefficient;
+    d.added_mass = p->added_mass_force != 0;
+    d.drag_model = p->drag_coefficient_model;
+    d.nuopt = p->diffusion_lsm2_option;
+    d.edge_opt = p->lsm3_edge_opt;
+    d.tl_h = p->tl_horizontal;
+    d.tl_v = p->tl_vertical;
+    // lagrangian_particle_set.pyx:361-375
+    {
+        double rhop = p->particle_density, rho0 = p->water_density;
+        if (!d.added_mass) {
+            d.a0c = (rhop - rho0) / rhop;
+            d.a1c = 0.5 * (rho0 / rhop);
+            d.a2c = 0.;
+            d.a3c = 1. / rhop;
+        } else {
+            double aux = 1. / (rhop + p->added_mass_coef * rho0);
+            d.a0c = (rhop - rho0) * aux;
+            d.a1c = 0.5 * rho0 * aux;
+            d.a2c = rho0 * (1. + p->added_mass_coef) * aux;
+            d.a3c = aux;
+        }
+    }
+
 }
 
 extern "C" {
@@ -408,35 +438,8 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     *out = nullptr;
     if (!c->have_mesh || !c->have_fields)
         return set_err(c, CG_ESTATE, "cg_run_create before mesh/field upload");
-    if (p->precision != CG_PRECISION_FP64 && p->precision != CG_PRECISION_MIXED)
-        return set_err(c, CG_EINVAL, "unknown precision %d", p->precision);
-    if (p->model < 1 || p->model > 3)
-        return set_err(c, CG_EINVAL, "model %d is not built in this library (1, 2, 3)", p->model);
-    if (p->dim != c->fdim)
-        return set_err(c, CG_EINVAL, "particle dim %d != field dim %d (pseudo-3D not built)",
-                       p->dim, c->fdim);
-    // parameters.pyx:208-279
-    if (p->model == 1 && (p->time_scheme < 1 || p->time_scheme > 4))
-        return set_err(c, CG_EINVAL, "LSM1 time_scheme must be 1..4");
-    if (p->model == 2 && p->diffusion_model == 0 && (p->time_scheme < 1 || p->time_scheme > 5))
-        return set_err(c, CG_EINVAL, "LSM2 time_scheme must be 1..5");
-    if (p->model >= 2 && p->diffusion_model != 0 && p->time_scheme != 1 && p->time_scheme != 5)
-        return set_err(c, CG_EINVAL, "LSM%d with diffusion needs time_scheme 1 or 5", p->model);
-    if (p->model == 3 && p->diffusion_model == 0)
-        return set_err(c, CG_EINVAL, "LSM3 needs a diffusion model");
-    if (p->diffusion_lsm2_option < 1 || p->diffusion_lsm2_option > 3)
-        return set_err(c, CG_EINVAL, "diffusion_lsm2_option must be 1..3");
-    if (p->lsm3_edge_opt < 1 || p->lsm3_edge_opt > 2)
-        return set_err(c, CG_EINVAL, "lsm3_edge_opt must be 1 or 2");
-    if (!(p->tl_horizontal > 0.) || !(p->tl_vertical > 0.))
-        return set_err(c, CG_EINVAL, "diffusion_lsm3_tl_* must be > 0");
-    if (p->diffusion_model < 0 || p->diffusion_model > 3)
-        return set_err(c, CG_EINVAL, "diffusion_model must be 0..3");
-    if (p->rng_method < 1 || p->rng_method > 3) return set_err(c, CG_EINVAL, "bad rng_method");
-    if ((p->diffusion_model == 2 || p->diffusion_model == 3) && !c->has_keps)
-        return set_err(c, CG_EINVAL,
-                       "diffusion_model=%d requires 'TURBULENT ENERG.' and 'DISSIPATION' fields",
-                       p->diffusion_model);
+    int rc0 = check_params(c, p);
+    if (rc0) return rc0;
     if (!(p->time_step > 0.) || !(p->final_time > p->initial_time))
         return set_err(c, CG_EINVAL, "bad time interval");
     if (s->n < 0 || (s->n > 0 && (!s->position || !s->velocity || !s->fluid_velocity_seen ||
@@ -521,54 +524,7 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->bytes = need;
     c->used += need;
 
-    DevParams& d = r->dp;
-    d.model = p->model;
-    d.time_scheme = p->time_scheme;
-    d.rng_method = p->rng_method;
-    d.diffmod = p->diffusion_model;
-    d.bc_on = p->boundary_conditions != 0;
-    d.bc_type = p->boundary_conditions_type;
-    d.max_rebounds = p->max_wall_rebounds;
-    d.bnd_statistics = p->bnd_statistics != 0;
-    d.nopen = c->nopen;
-    d.pdim = p->dim;
-    d.dt = p->time_step;
-    d.sqrtdt = std::sqrt(p->time_step);
-    d.nux = p->horizontal_diffusivity;
-    d.nuz = p->vertical_diffusivity;
-    // update_state_lsm1.pyx:708-713
-    d.diffx_const = std::sqrt(2. * d.nux) * d.sqrtdt;
-    d.diffz_const = std::sqrt(2. * d.nuz) * d.sqrtdt;
-    d.damp = std::fmin(p->rebound_damping_coef, 1.0 - EPSILON_REBOUND);  // compute_bc.pyx:76
-    d.strand = p->stranding_probability;
-    d.roughness = p->wall_roughness_angle * DEG_TO_RAD;
-    d.buoy_model = p->buoyancy_velocity_model;
-    d.buoy_wb = p->buoyancy_velocity;
-    d.density = p->particle_density;
-    d.rho0 = p->water_density;
-    d.drag_coef = p->drag_coefficient;
-    d.added_mass = p->added_mass_force != 0;
-    d.drag_model = p->drag_coefficient_model;
-    d.nuopt = p->diffusion_lsm2_option;
-    d.edge_opt = p->lsm3_edge_opt;
-    d.tl_h = p->tl_horizontal;
-    d.tl_v = p->tl_vertical;
-    // lagrangian_particle_set.pyx:361-375
-    {
-        double rhop = p->particle_density, rho0 = p->water_density;
-        if (!d.added_mass) {
-            d.a0c = (rhop - rho0) / rhop;
-            d.a1c = 0.5 * (rho0 / rhop);
-            d.a2c = 0.;
-            d.a3c = 1. / rhop;
-        } else {
-            double aux = 1. / (rhop + p->added_mass_coef * rho0);
-            d.a0c = (rhop - rho0) * aux;
-            d.a1c = 0.5 * rho0 * aux;
-            d.a2c = rho0 * (1. + p->added_mass_coef) * aux;
-            d.a3c = aux;
-        }
-    }
+    make_dev_params(c, p, r->dp);
 
     DevState& st = r->st;
     st.n = s->n;

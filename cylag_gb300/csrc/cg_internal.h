@@ -66,6 +66,31 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
 void launch_init(int precision, const DevMesh& m, const FieldView& fv, const DevParams& p,
                  const DevState& s, int velocity_init, uint32_t* err, cudaStream_t st);
 
+// Serving pool (cg_serve.cuh): one launch steps every admitted run.
+// Device run table entry:
+struct ServeRun {
+    DevParams p;
+    int first;        // first particle of the run's range in the pool
+    int count;        // particles
+    int horizon;      // steps
+    int pad;
+    long long start;  // global step at which the run's step 0 executes
+};
+struct ServeClock {
+    unsigned long long gstep;  // steps executed so far
+    unsigned int done;         // blocks finished in the current launch
+    unsigned int pad;
+};
+// blocks of one wave of resident serve_step_kernel blocks
+int serve_grid_plain();
+int serve_grid_mixed();
+void launch_serve_plain(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
+                        const ServeRun* runs, const int2* active, const int* nactive,
+                        ServeClock* clk, uint32_t* run_err, cudaStream_t st);
+void launch_serve_mixed(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
+                        const ServeRun* runs, const int2* active, const int* nactive,
+                        ServeClock* clk, uint32_t* run_err, cudaStream_t st);
+
 // Working copies of the per-step state in element order (cg_sort.cu).
 struct WorkState {
     double2* pos;             // [n]

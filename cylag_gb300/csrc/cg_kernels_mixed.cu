@@ -5,7 +5,7 @@
 #include <cstdlib>
 
 #include "cg_internal.h"
-#include "cg_step_mixed.cuh"
+#include "cg_serve.cuh"
 
 namespace cg {
 
@@ -45,6 +45,15 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         // 3D: FP32 node records, FP64 arithmetic
         launch_step_kernel<3, float>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
     }
+}
+
+int serve_grid_mixed() { return resident_blocks(serve_step_kernel<float, true>, 256); }
+
+void launch_serve_mixed(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
+                        const ServeRun* runs, const int2* active, const int* nactive,
+                        ServeClock* clk, uint32_t* run_err, cudaStream_t st) {
+    serve_step_kernel<float, true><<<grid, 256, 0, st>>>(m, fv.as<float>(), pool, runs, active,
+                                                         nactive, clk, run_err);
 }
 
 void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,

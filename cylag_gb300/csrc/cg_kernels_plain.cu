@@ -6,7 +6,7 @@
 #include <cstdio>
 
 #include "cg_internal.h"
-#include "cg_step.cuh"
+#include "cg_serve.cuh"
 
 namespace cg {
 
@@ -93,6 +93,18 @@ void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p
     int nb = nsm * 8;
     DevFields<double> f = fv.as<double>();
     walk_kernel<double, false><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+}
+
+// ---------------------------------------------------------------------------
+// serving pool: every admitted run in one launch (FP64 records)
+// ---------------------------------------------------------------------------
+int serve_grid_plain() { return resident_blocks(serve_step_kernel<double, false>, 256); }
+
+void launch_serve_plain(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
+                        const ServeRun* runs, const int2* active, const int* nactive,
+                        ServeClock* clk, uint32_t* run_err, cudaStream_t st) {
+    serve_step_kernel<double, false><<<grid, 256, 0, st>>>(m, fv.as<double>(), pool, runs, active,
+                                                           nactive, clk, run_err);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,83 @@
+// cg_serve.cuh -- one step of every admitted dispersion run in one launch.
+//
+// The serving pool holds the particles of many runs in one set of device
+// arrays; each run owns a range of whole warps (32 particles), so a warp
+// never mixes runs and every lane of a warp follows the same run's model
+// and parameters.  The kernel strides over the list of active warps
+// {warp, run}; a run's step index is the global step minus the step at which
+// it was admitted, so finished runs (and runs admitted later) are skipped
+// without host involvement, and the kernel itself advances the global step
+// (the last block to finish).  The launch arguments never change, which is
+// what lets the step be captured once in a CUDA graph and replayed.
+//
+// Per particle the work is exactly that of a standalone run's step kernel
+// (step_particle / step_mixed_particle with the walk inline), so a run's
+// result does not depend on which other runs share the launch.
+#pragma once
+
+#include "cg_internal.h"
+#include "cg_step_mixed.cuh"
+
+namespace cg {
+
+// ServeRun and ServeClock: cg_internal.h
+
+template <typename FT, bool MIXED>
+__global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT> f, DevState pool,
+                                                         const ServeRun* __restrict__ runs,
+                                                         const int2* __restrict__ active,
+                                                         const int* __restrict__ nactive,
+                                                         ServeClock* clk,
+                                                         uint32_t* __restrict__ run_err) {
+    __shared__ ZigTables zt;
+    __shared__ Zig32 z32;
+    if constexpr (MIXED) {
+        for (int t = threadIdx.x; t < 128; t += blockDim.x) {
+            z32.kn[t] = g_zig.kn[t];
+            z32.wn[t] = (float)g_zig.wn[t];
+            z32.fn[t] = (float)g_zig.fn[t];
+        }
+    }
+    load_zig(zt);   // ends with __syncthreads
+    const unsigned long long g = *(volatile unsigned long long*)&clk->gstep;
+    const int na = *nactive;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const WalkQueue none{nullptr, nullptr};
+    for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < na; a += nw) {
+        const int2 e = active[a];   // {warp, run}
+        const ServeRun& R = runs[e.y];
+        const long long k = (long long)g - R.start;
+        const int i = e.x * 32 + lane;
+        if (k < 0 || k >= R.horizon || i >= R.first + R.count) continue;
+        const int aux = (k == R.horizon - 1) ? 2 : (k == R.horizon - 2 ? 1 : 0);
+        uint32_t* err = run_err + e.y;
+        const int model = R.p.model;
+        if constexpr (MIXED) {
+            if (model == 1) {
+                step_mixed_particle(m, f, R.p, pool, none, aux, (int)k, nullptr, err, z32, i);
+                continue;
+            }
+        }
+        if (model == 1)
+            step_particle<2, FT, 1>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
+        else if (model == 2)
+            step_particle<2, FT, 2>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
+        else
+            step_particle<2, FT, 3>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
+    }
+    // the last block to finish advances the global step
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int t = atomicAdd(&clk->done, 1u);
+        if (t == gridDim.x - 1) {
+            clk->done = 0;
+            clk->gstep = g + 1;
+            __threadfence();
+        }
+    }
+}
+
+
+}  // namespace cg

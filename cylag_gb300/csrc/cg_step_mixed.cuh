@@ -112,7 +112,7 @@ __device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, 
 // Runge-Kutta stages of update_state_lsm1.pyx:179-656 in the mixed form:
 // each stage point is localized from (tri0, x0); a stage leaving the domain
 // stops the scheme with an Euler step.  Kept out of line (cold path).
-__device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __restrict__ cur,
+static __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __restrict__ cur,
                                       const DevParams& p, const Tri32& t0, int tri0, double2 x0,
                                       float ux, float uy, double& xn, double& yn, int& tri,
                                       int& bnd_j) {
@@ -156,7 +156,7 @@ __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __restrict
 
 // Boundary conditions (compute_bc.pyx:35-395) with the FP64 mirror and the
 // exact walk of the plain form.  Out of line (cold path).
-__device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<float>& f,
+static __device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<float>& f,
                                       const DevParams& p, const ZigTables& z64, Rng& rng,
                                       double2 x0, float up0, float up1, int tri0, int ltri,
                                       int bnd_j, int* stats, double& xn, double& yn, int& tri,

@@ -196,6 +196,55 @@ int cg_run_errors(cg_run *run, uint32_t *flags);
 /* Number of active particles and deleted-this-call counts are derived by the
  * caller from tri (tri == -1 inactive). */
 
+/* ---- serving pool ----------------------------------------------------- */
+/* Many dispersion runs on one context's mesh and frozen fields, stepped
+ * together: one launch per step advances every admitted run (continuous
+ * batching; the step is captured once in a CUDA graph).  No reference
+ * counterpart: the reference runs one Solver per process
+ * (cylag/core/solver.pyx:42-80, solver_parallel.pyx:113-179); each run here
+ * is that Solver's 2D step sequence, with the same results.
+ *
+ * Creates a pool of `capacity` particles (rounded up to 32) and `max_runs`
+ * run slots on fields of 2D (frozen: the first time record is used);
+ * schmidt_number is the one the nodal k-epsilon diffusivity is computed with.
+ * Fails with CG_ENOMEM_BUDGET beyond the context budget.  Destroy every
+ * server of a context before the context. */
+typedef struct cg_server cg_server;
+int cg_server_create(cg_ctx *ctx, int32_t precision, int64_t capacity, int32_t max_runs,
+                     double schmidt_number, cg_server **out);
+int cg_server_destroy(cg_server *srv);
+/* Admits a run: n particles at host positions [n][2] (the Solver's
+ * particle set), parameters as for cg_run_create (params->seed seeds its
+ * PCG32 streams pcg32_seed(seed, i), i = 0..n-1; precision must be the
+ * pool's; frozen fields), per-particle diameters from `diameter` [n] or all
+ * `particle_diameter`, `horizon` steps.  Initializes the particles
+ * (Solver.initialize_particle_state, solver.pyx:238-379); the run's step 0
+ * is the next cg_server_step step.  CG_ENOMEM_BUDGET when no contiguous
+ * range of the pool (or no run slot) is free: retry after a release. */
+int cg_server_admit(cg_server *srv, const cg_params *params, int32_t n, const double *position,
+                    double particle_diameter, const double *diameter, int32_t horizon,
+                    int32_t *run_id);
+/* Advances every admitted, unfinished run by nsteps steps (Solver.forward,
+ * solver.pyx:413-585, for each), one graph launch per step.  Asynchronous. */
+int cg_server_step(cg_server *srv, int32_t nsteps);
+/* Steps the run still needs (0: finished once the queued steps complete). */
+int cg_server_run_status(const cg_server *srv, int32_t run_id, int32_t *steps_left);
+/* Copies a finished run's state to host arrays (NULL to skip): position,
+ * velocity, fluid_velocity_seen [n][2]; tri, tag [n] (tag -1: deleted at
+ * initialization, -2-k: deleted at step k; retag as
+ * lagrangian_particle_set.pyx:754-788 does); rng_state [n].  Waits for the
+ * run's last step only.  CG_EDEVICE (with the flags) if the run raised a
+ * device error flag. */
+int cg_server_read(cg_server *srv, int32_t run_id, double *position, double *velocity,
+                   double *fluid_velocity_seen, int32_t *tri, int32_t *tag,
+                   uint64_t *rng_state, uint32_t *err_flags);
+/* Frees the run's slot and range (an unfinished run is cancelled). */
+int cg_server_release(cg_server *srv, int32_t run_id);
+/* Pool occupancy and the mean device time per step of the last
+ * cg_server_step call (waits for it). */
+int cg_server_stats(cg_server *srv, int32_t *active_runs, int64_t *active_particles,
+                    int64_t *largest_free_range, int64_t *steps_issued, double *last_step_ms);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Mean device time (ms) per step of the step kernel (and, for 2D LSM1
  * runs, the walk kernel) over the last cg_run_step call, measured with CUDA
