@@ -40,6 +40,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle-steps/s on 1 GB300 (mixed vs plain FP64); p50/p99 request latency"
 UNIT = "particle-steps/s"
 WORKLOADS = {
+    "serve": "serving_mix_couette_channel_poisson_10_per_s_60_s_lsm1_lsm2",
     "lsm1_2d": "lsm1_2d_keps_drift_500k_tri_1e7_particles",
     "lsm2_3d": "lsm2_3d_loglaw_di_keps_200k_tri_21_planes_4e6_particles",
     "lsm3_3d": "lsm3_3d_taylor_green_settling_200k_tri_21_planes_1e7_particles",
@@ -60,6 +61,9 @@ def parse():
     ap.add_argument("--ny", type=int, default=None)
     ap.add_argument("--sort-period", type=int, default=25,
                     help="steps between re-sorts of the particles by element (0: never)")
+    ap.add_argument("--serve-rate", type=float, default=10.0, help="requests per s (serve)")
+    ap.add_argument("--serve-duration", type=float, default=60.0, help="arrival window, s (serve)")
+    ap.add_argument("--serve-chunk", type=int, default=32, help="steps queued per loop (serve)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -233,9 +237,22 @@ def run_reference_arm(args):
     if rank != 0:
         print(json.dumps({"impl": "reference", "rank": rank, "skipped": True}), file=sys.stderr)
         return
+    threads = os.cpu_count() or 1
+    if args.workload == "serve":
+        from cylag_gb300 import synth
+        c = synth.couette_channel(npart=10)
+        value = serve_cpu_rate(c, threads)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": 4, "warmup": 1, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOADS["serve"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "100,000 LSM1 + 100,000 LSM2 particles x 4 steps"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     c = make_workload(args)
     params = dict(c["parameters"])
-    threads = os.cpu_count() or 1
     nsample = int(os.environ.get("CYLAG_REF_SAMPLE", "200000"))
     rates = []
     for _ in range(args.warmup):
@@ -444,10 +461,112 @@ def run_gpu_arm(args):
     log("done")
 
 
+# ---------------------------------------------------------------------------
+# serving mix: requests arriving in real time, continuous batching
+# ---------------------------------------------------------------------------
+def serve_cpu_rate(fs_case, threads, nsample=100_000, nsteps=4):
+    """The CPU implementation on half LSM1, half LSM2 particles of the mix's
+    parameters on the same channel."""
+    from cylag_gb300.serve import LSM1_PARAMS, LSM2_PARAMS
+    rates = []
+    for prm in (LSM1_PARAMS, LSM2_PARAMS):
+        c = dict(fs_case, dim=2, nlayers=1, pset={})
+        rng = np.random.default_rng(9)
+        c["position"] = np.stack([rng.uniform(0, 1000.0, nsample), rng.uniform(0, 100.0, nsample)], 1)
+        r, _ = cpu_rate(c, dict(prm, final_time=1e6), nsample, nsteps, threads)
+        rates.append(r)
+    return 2.0 / (1.0 / rates[0] + 1.0 / rates[1])
+
+
+def run_serve(args):
+    import torch
+    from cylag_gb300 import synth
+    from cylag_gb300.serve import DispersionServer, poisson_mix
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    c = synth.couette_channel(npart=10)
+    c.update(dim=2, nlayers=1)
+    mesh, fs = field_set_of(c)
+    reqs = poisson_mix(rate=args.serve_rate, duration=args.serve_duration, seed=5 + rank)
+    work = sum(len(r.position) * r.horizon for r in reqs)
+    npart = sum(len(r.position) for r in reqs)
+    log(f"serving mix: {len(reqs)} requests, {npart:.3e} particles, {work:.3e} particle-steps")
+    forms = [args.precision] if args.precision != "both" else ["mixed", "fp64"]
+    out = {}
+    for prec in forms:
+        # pool: every particle of the mix fits (120 GB admission budget)
+        srv = DispersionServer(fs, precision=prec, capacity=max(npart, 1 << 20) + 32 * len(reqs),
+                               max_runs=len(reqs) + 8, device=local, hbm_budget=120 * 10**9)
+        warm = poisson_mix(rate=100.0, duration=0.05, seed=99, nmax=1e4, hmax=200)
+        srv.serve(warm, realtime=False)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        log(f"{prec}: serving")
+        t0 = time.perf_counter()
+        res = srv.serve(reqs, realtime=True, chunk=args.serve_chunk)
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        st = srv.stats()
+        srv.close()
+        lat = np.array([r.latency for r in res])
+        queue = np.array([r.admitted - r.arrival for r in res])
+        out[prec] = {"value": work / wall, "wall_s": wall, "p50_s": float(np.percentile(lat, 50)),
+                     "p99_s": float(np.percentile(lat, 99)), "max_s": float(lat.max()),
+                     "admission_wait_p99_s": float(np.percentile(queue, 99)),
+                     "steps": int(st["steps_issued"]), "clocks": clk, "completed": len(res)}
+        log(f"{prec}: {wall:.1f} s, p50 {out[prec]['p50_s']:.2f} s, p99 {out[prec]['p99_s']:.2f} s")
+    if rank != 0:
+        return
+    m = out[forms[0]]
+    peak, peak_kind = peaks()
+    # LSM1: position, tri, PCG32 r+w, tag r (60 B); LSM2 adds velocity r+w
+    # and diameter r (100 B); half of the requests each
+    bpp = 80.0
+    achieved = bpp * work / m["wall_s"] / 1e9
+    line = {
+        "metric": METRIC, "value": m["value"], "unit": UNIT, "n_gpus": world,
+        "steps": m["steps"], "warmup": 1, "ms_per_step": 1e3 * m["wall_s"] / max(m["steps"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if forms[0] == "fp64" else "f32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS["serve"], "requests": len(reqs), "particles": npart,
+                   "particle_steps": work, "precision": forms[0], "arrival_rate_per_s": args.serve_rate,
+                   "arrival_window_s": args.serve_duration, "chunk_steps": args.serve_chunk,
+                   "hbm_budget_bytes": 120 * 10**9,
+                   "l2": "per-step state of the mix larger than L2 at load (no flush)"},
+        "latency_s": {"p50": m["p50_s"], "p99": m["p99_s"], "max": m["max_s"],
+                      "admission_wait_p99": m["admission_wait_p99_s"]},
+        "gpu_launches": m["steps"] + 3 * len(reqs),   # graph steps + prepare/seed/init per request
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "note": "serving-window average (wall clock incl. idle between arrivals)",
+                     "bytes_per_particle_step": bpp},
+        "clocks": m["clocks"],
+        "e2e": {"value": m["value"], "unit": UNIT,
+                "h2d_bytes_per_step": int(16 * npart / max(m["steps"], 1)),
+                "d2h_bytes_per_step": int(48 * npart / max(m["steps"], 1)),
+                "note": "requests enter as host arrays and results return to host arrays"},
+    }
+    if "fp64" in out and forms[0] != "fp64":
+        q = out["fp64"]
+        line["plain_fp64"] = {"value": q["value"], "latency_s": {"p50": q["p50_s"], "p99": q["p99_s"],
+                                                                 "max": q["max_s"]},
+                              "wall_s": q["wall_s"], "clocks": q["clocks"]}
+        line["mixed_over_plain"] = m["value"] / q["value"]
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        line["cpu_baseline"] = {"value": serve_cpu_rate(c, threads), "unit": UNIT, "cores": threads,
+                                "kind": "port",
+                                "sample": "100,000 LSM1 + 100,000 LSM2 particles x 4 steps on the channel"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu_arm(args)
 
