@@ -318,9 +318,8 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
     ms = ev0.elapsed_time(ev1)
     kern_ms, launches = solver.last_kernel_ms()
     if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        from cylag_gb300.shard import allreduce_max
+        ms = allreduce_max(ms, dist)
     log(f"{precision}: timed {ms:.3f} ms, kernel {kern_ms:.4f} ms/launch")
     res = {"precision": precision, "ms": ms, "kernel_ms": kern_ms, "launches": launches,
            "value": world * n * args.steps / (ms / 1e3), "clocks": clk, "n": n,
@@ -368,9 +367,8 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
         del host
         ems = e0.elapsed_time(e1)
         if dist:
-            t = torch.tensor([ems], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+            from cylag_gb300.shard import allreduce_max
+            ems = allreduce_max(ems, dist)
         res["e2e"] = {"value": world * n * args.steps / (ems / 1e3), "unit": UNIT,
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "wall_s": wall}
