@@ -9,47 +9,63 @@
 // after the Particle definition.
 #pragma once
 
+#include <type_traits>
+
 namespace cg {
+
+// Arithmetic of the Langevin coefficients (drag law, direct-integrator
+// transitions and covariances, Cholesky factors): FP64 in the plain form,
+// FP32 in the mixed form (FP32 node records).  Written with R(...) literals
+// so that the FP64 instantiation keeps the reference's expressions exactly.
+template <typename FT> struct ArithOf { using type = double; };
+template <> struct ArithOf<float> { using type = float; };
 
 // x**y (x > 0) as the compiled reference evaluates it: Cython gives
 // double ** double a complex result, computed by the C library's complex
 // power exp(y * log x) through the complex logarithm, whose real part is
 // log1p((x-1)(x+1))/2 for 0.5 <= x < 2 and log(x) elsewhere.
-__device__ __forceinline__ double cpow_re(double x, double y) {
-    double L = (x >= 0.5 && x < 2.) ? log1p((x - 1.) * (x + 1.)) / 2. : log(x);
+template <typename R>
+__device__ __forceinline__ R cpow_re(R x, R y) {
+    R L = (x >= R(0.5) && x < R(2.)) ? log1p((x - R(1.)) * (x + R(1.))) / R(2.) : log(x);
     return exp(y * L);
 }
 
-// lagrangian_particle_set.pyx:790-832
-__device__ inline double drag_coefficient(const DevParams& p, double U, double dp) {
-    double Re = fmax(EPSILON, U * dp / NU0);
-    if (p.drag_model == 0) return p.drag_coef;
+// lagrangian_particle_set.pyx:790-832.  The Almedeij powers overflow FP32
+// at small Re: that law is evaluated in FP64 in both forms.
+__device__ inline double drag_almedeij(double Re) {
+    double phi1 = pow(24. / Re, 10.) + cpow_re(21. * cpow_re(Re, -0.67), 10.) +
+                  cpow_re(4. * cpow_re(Re, -0.33), 10.) + pow(0.4, 10.);
+    double phi2 = 1. / (cpow_re(0.148 * cpow_re(Re, 0.11), -10.) + pow(0.5, -10.));
+    double phi3 = cpow_re(1.57 * cpow_re(Re, -1.625) * 1.e8, 10.);
+    double phi4 = 1. / (cpow_re(6e-17 * cpow_re(Re, 2.63), -10.) + pow(0.2, -10.));
+    return pow(1. / (1. / (phi1 + phi2) + 1. / phi3) + phi4, 1. / 10.);
+}
+
+template <typename R>
+__device__ inline R drag_coefficient(const DevParams& p, R U, R dp) {
+    R Re = fmax(R(EPSILON), U * dp / R(NU0));
+    if (p.drag_model == 0) return R(p.drag_coef);
     if (p.drag_model == 1) {
-        if (Re <= 1000.) return (24. / Re) * (1. + 0.15 * cpow_re(Re, 0.687));
-        return 0.44;
+        if (Re <= R(1000.)) return (R(24.) / Re) * (R(1.) + R(0.15) * cpow_re(Re, R(0.687)));
+        return R(0.44);
     }
-    if (p.drag_model == 2) {
-        double phi1 = pow(24. / Re, 10.) + cpow_re(21. * cpow_re(Re, -0.67), 10.) +
-                      cpow_re(4. * cpow_re(Re, -0.33), 10.) + pow(0.4, 10.);
-        double phi2 = 1. / (cpow_re(0.148 * cpow_re(Re, 0.11), -10.) + pow(0.5, -10.));
-        double phi3 = cpow_re(1.57 * cpow_re(Re, -1.625) * 1.e8, 10.);
-        double phi4 = 1. / (cpow_re(6e-17 * cpow_re(Re, 2.63), -10.) + pow(0.2, -10.));
-        return pow(1. / (1. / (phi1 + phi2) + 1. / phi3) + phi4, 1. / 10.);
-    }
-    return 0.44;
+    if (p.drag_model == 2) return R(drag_almedeij((double)Re));
+    return R(0.44);
 }
 
 // ---------------------------------------------------------------------------
 // LSM2 (cylag/lsm/update_state_lsm2.pyx)
 // ---------------------------------------------------------------------------
 
-// drag rate ((a1c*(1.5/dp))*Cd)*|slip| (update_state_lsm2.pyx:192-198)
+// drag rate ((a1c*(1.5/dp))*Cd)*|slip| (update_state_lsm2.pyx:192-198), in R
+template <typename R>
 __device__ __forceinline__ double lsm2_a1(const DevParams& p, int dim, double dp, double rx,
                                           double ry, double rz) {
-    double unorm = dim == 2 ? sqrt(rx * rx + ry * ry) : sqrt(rx * rx + ry * ry + rz * rz);
-    unorm = fmax(EPSILON_LSM2, unorm);
-    double Cd = drag_coefficient(p, unorm, dp);
-    return p.a1c * (1.5 / dp) * Cd * unorm;
+    R x = R(rx), y = R(ry), z = R(rz), d = R(dp);
+    R unorm = dim == 2 ? sqrt(x * x + y * y) : sqrt(x * x + y * y + z * z);
+    unorm = fmax(R(EPSILON_LSM2), unorm);
+    R Cd = drag_coefficient<R>(p, unorm, d);
+    return double(R(p.a1c) * (R(1.5) / d) * Cd * unorm);
 }
 
 template <int DIM, typename FT>
@@ -69,7 +85,7 @@ __device__ void euler_lsm2(Particle<DIM, FT>& q, double dp) {
     double dt = p.dt, ux, uy, uz, ax, ay, az;
     double z = DIM == 3 ? q.x[2] : 0.;
     mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
-    double a1 = lsm2_a1(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
+    double a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
     q.us[0] = ux;
     q.us[1] = uy;
     q.up[0] += (ux - q.up[0]) * dt * a1 + ax * p.a2c * dt;
@@ -106,7 +122,7 @@ __device__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
         const double cv = st == 0 ? 0. : (st == 1 ? c1 : (st == 2 ? c2 : 1.));
         double vx, vy, vz = 0.;
         if (st == 0) {
-            a1 = lsm2_a1(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
+            a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
             vx = q.up[0];
             vy = q.up[1];
             if (DIM == 3) vz = q.up[2];
@@ -115,7 +131,7 @@ __device__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
             double sx = ux - q.up[0] - cv * fx[st - 1];
             double sy = uy - q.up[1] - cv * fy[st - 1];
             double sz = DIM == 3 ? uz - q.up[2] - cv * fz[st - 1] : 0.;
-            a1 = lsm2_a1(p, DIM, dp, sx, sy, sz);
+            a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, sx, sy, sz);
             vx = q.up[0] + cv * fx[st - 1];
             vy = q.up[1] + cv * fy[st - 1];
             if (DIM == 3) vz = q.up[2] + cv * fz[st - 1];
@@ -217,7 +233,7 @@ __device__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, double dp) {
     const int diffmod = p.diffmod, nuopt = p.nuopt;
     double z = DIM == 3 ? q.x[2] : 0.;
     mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
-    double a1 = lsm2_a1(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
+    double a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
     double xix = 0., xiy = 0., xiz = 0., diffx = 0., diffy = 0., diffz = 0.;
     if (diffmod != 0) {
         rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
@@ -255,20 +271,22 @@ __device__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, double dp) {
 }
 
 // frozen-step coefficients of one LSM2 component (update_state_lsm2.pyx:1240-1327)
+template <typename R>
 struct Lsm2Coef {
-    double beta, D1, D2, force_x, q_uu, q_xu, q_xx;
+    R beta, D1, D2, force_x, q_uu, q_xu, q_xx;
 };
 
-__device__ inline bool lsm2_direct_coefficients(double a1, double dt, Lsm2Coef& c) {
-    double r = a1 * dt;
-    if (!isfinite(a1) || !isfinite(dt) || a1 < 0. || dt < 0. || !isfinite(r)) return false;
+template <typename R>
+__device__ inline bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>& c) {
+    R r = a1 * dt;
+    if (!isfinite(a1) || !isfinite(dt) || a1 < R(0.) || dt < R(0.) || !isfinite(r)) return false;
     c.beta = exp(-r);
-    if (r < 0.1) {
-        double phi1 = 1., phi2 = 0.5, term = 1.;
+    if (r < R(0.1)) {
+        R phi1 = R(1.), phi2 = R(0.5), term = R(1.);
         for (int n = 1; n < 13; ++n) {
-            term *= -r / (n + 1.);
+            term *= -r / (R(n) + R(1.));
             phi1 += term;
-            phi2 += term / (n + 2.);
+            phi2 += term / (R(n) + R(2.));
         }
         c.D1 = dt * phi1;
         c.D2 = dt * r * phi2;
@@ -278,27 +296,29 @@ __device__ inline bool lsm2_direct_coefficients(double a1, double dt, Lsm2Coef& 
         c.D2 = dt - c.D1;
         c.force_x = c.D2 / a1;
     }
-    c.q_uu = r == 0. ? dt : dt * (-expm1(-2. * r) / (2. * r));
-    c.q_xu = 0.5 * c.D1 * c.D1;
-    if (r < 1.) {
-        double term = 1. / 6., power2 = 4., qxx = 1. / 3.;
+    c.q_uu = r == R(0.) ? dt : dt * (-expm1(R(-2.) * r) / (R(2.) * r));
+    c.q_xu = R(0.5) * c.D1 * c.D1;
+    if (r < R(1.)) {
+        R term = R(1.) / R(6.), power2 = R(4.), qxx = R(1.) / R(3.);
         for (int n = 1; n < 24; ++n) {
-            term *= -r / (n + 3.);
-            power2 *= 2.;
-            qxx += (power2 - 2.) * term;
+            term *= -r / (R(n) + R(3.));
+            power2 *= R(2.);
+            qxx += (power2 - R(2.)) * term;
         }
         c.q_xx = qxx * dt * dt * dt;
     } else {
-        c.q_xx = ((dt - 2. * c.D1 + c.q_uu) / a1) / a1;
+        c.q_xx = ((dt - R(2.) * c.D1 + c.q_uu) / a1) / a1;
     }
     return true;
 }
 
 // update_state_lsm2.pyx:1329-1542 (diffmod 0, nux = nuz = 0, nuopt 2:
-// di_ode_lsm2, 1232-1238)
+// di_ode_lsm2, 1232-1238).  Mixed form: coefficients, means and increments
+// in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
 __device__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux, double nuz,
                         int nuopt) {
+    using R = typename ArithOf<FT>::type;
     const DevParams& p = q.p;
     const double dt = p.dt;
     double xp0[3], up0[3];
@@ -310,51 +330,61 @@ __device__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux
     double z0 = DIM == 3 ? xp0[2] : 0.;
     double ux, uy, uz, ax, ay, az;
     mean_fields(q, q.tri, q.ll, xp0[0], xp0[1], z0, p.added_mass, ux, uy, uz, ax, ay, az);
-    double a1 = lsm2_a1(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.);
-    Lsm2Coef c;
-    if (!lsm2_direct_coefficients(a1, dt, c)) { q.err |= ERR_NONFINITE; return; }
-    double um_beta = -expm1(-a1 * dt);
-    double b2[3] = {0., 0., 0.};
+    const R a1 = R(lsm2_a1<R>(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.));
+    const R rdt = R(dt);
+    Lsm2Coef<R> c;
+    if (!lsm2_direct_coefficients<R>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return; }
+    R um_beta = -expm1(-a1 * rdt);
+    R b2[3] = {R(0.), R(0.), R(0.)};
     if (diffmod == 2 || diffmod == 3) {
-        double ep;
-        double tml = keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
-        b2[0] = a1 * a1 * C0KOLM * ep * (tml * tml);
+        double epd;
+        const R tml = R(keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, epd));
+        const R ep = R(epd), rnuz = R(nuz);
+        b2[0] = a1 * a1 * R(C0KOLM) * ep * (tml * tml);
         b2[1] = b2[0];
-        if (diffmod == 2) b2[2] = nuopt == 2 ? nuz * nuz : 2. * nuz * a1 * a1;
+        if (diffmod == 2) b2[2] = nuopt == 2 ? rnuz * rnuz : R(2.) * rnuz * a1 * a1;
         else b2[2] = b2[0];
     } else if (diffmod != 0) {
+        const R rnux = R(nux), rnuz = R(nuz);
         if (nuopt == 2) {
-            b2[0] = nux * nux;
+            b2[0] = rnux * rnux;
             b2[1] = b2[0];
-            b2[2] = nuz * nuz;
+            b2[2] = rnuz * rnuz;
         } else if (nuopt == 3) {
-            b2[0] = 2. * nux * a1 * a1;
+            b2[0] = R(2.) * rnux * a1 * a1;
             b2[1] = b2[0];
-            b2[2] = 2. * nuz * a1 * a1;
+            b2[2] = R(2.) * rnuz * a1 * a1;
         }
     }
     const double mu[3] = {ux, uy, uz};
-    const double Fp3[3] = {p.a2c * ax, p.a2c * ay, p.a2c * az - GRAV * p.a0c};
+    const double acc[3] = {ax, ay, az};
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        double u_k = mu[d];
-        double Fp = Fp3[d];
-        double up_mean = up0[d] * c.beta + u_k * um_beta + Fp * c.D1;
-        double xp_mean = xp0[d] + up0[d] * c.D1 + u_k * c.D2 + Fp * c.force_x;
-        q.us[d] = u_k;
-        if (b2[d] == 0. || dt == 0.) {
-            q.up[d] = up_mean;
-            q.x[d] = xp_mean;
-            continue;
+        const R u_k = R(mu[d]);
+        const R Fp = d == 2 ? R(p.a2c) * R(acc[2]) - R(GRAV) * R(p.a0c) : R(p.a2c) * R(acc[d]);
+        const R v0 = R(up0[d]);
+        q.us[d] = mu[d];
+        R Gp = R(0.), Gx = R(0.);
+        const bool noise = !(b2[d] == R(0.) || dt == 0.);
+        if (noise) {
+            R var_gp = b2[d] * c.q_uu, cov = b2[d] * c.q_xu, var_gx = b2[d] * c.q_xx;
+            R L_pp = sqrt(fmax(R(0.), var_gp));
+            R L_xp = L_pp > R(0.) ? cov / L_pp : R(0.);
+            R L_xx = sqrt(fmax(R(0.), var_gx - L_xp * L_xp));
+            double xix, xiy;
+            rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
+            Gp = L_pp * R(xix);
+            Gx = L_xp * R(xix) + L_xx * R(xiy);
         }
-        double var_gp = b2[d] * c.q_uu, cov = b2[d] * c.q_xu, var_gx = b2[d] * c.q_xx;
-        double L_pp = sqrt(fmax(0., var_gp));
-        double L_xp = L_pp > 0. ? cov / L_pp : 0.;
-        double L_xx = sqrt(fmax(0., var_gx - L_xp * L_xp));
-        double xix, xiy;
-        rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
-        q.up[d] = up_mean + L_pp * xix;
-        q.x[d] = xp_mean + (L_xp * xix + L_xx * xiy);
+        if constexpr (std::is_same<R, double>::value) {
+            double up_mean = up0[d] * c.beta + u_k * um_beta + Fp * c.D1;
+            double xp_mean = xp0[d] + up0[d] * c.D1 + u_k * c.D2 + Fp * c.force_x;
+            q.up[d] = noise ? up_mean + Gp : up_mean;
+            q.x[d] = noise ? xp_mean + Gx : xp_mean;
+        } else {
+            q.up[d] = double(v0 * c.beta + u_k * um_beta + Fp * c.D1 + Gp);
+            q.x[d] = xp0[d] + double(v0 * c.D1 + u_k * c.D2 + Fp * c.force_x + Gx);
+        }
     }
 }
 
@@ -437,43 +467,53 @@ __device__ void lsm2_fluctuations(Particle<DIM, FT>& q, double dp, double* fl) {
 
 // frozen-step coefficients of one LSM3 component in state order (s, ur, x):
 // phi (transition), q (unit-noise covariance), force, flow
+// machine epsilon of the arithmetic type (DBL_EPSILON, FLT_EPSILON)
+template <typename R> struct EpsOf { static constexpr double value = 2.220446049250313e-16; };
+template <> struct EpsOf<float> { static constexpr float value = 1.1920928955078125e-7f; };
+
+template <typename R>
 struct Lsm3Coef {
-    double phi[9], q[9], force[3], flow[3];
+    R phi[9], q[9], force[3], flow[3];
 };
 
-__device__ __forceinline__ double phi1_(double z) { return z == 0. ? 1. : expm1(z) / z; }
-__device__ __forceinline__ double exp_divdiff(double x, double y) {
+template <typename R>
+__device__ __forceinline__ R phi1_(R z) { return z == R(0.) ? R(1.) : expm1(z) / z; }
+template <typename R>
+__device__ __forceinline__ R exp_divdiff(R x, R y) {
     return exp(-fmin(x, y)) * phi1_(-fabs(x - y));
 }
-__device__ __forceinline__ double phi2_(double z) {
-    if (fabs(z) < 0.05)
-        return 0.5 + z * (1. / 6. + z * (1. / 24. + z * (1. / 120. + z * (1. / 720. +
-               z * (1. / 5040. + z * (1. / 40320. + z / 362880.))))));
+template <typename R>
+__device__ __forceinline__ R phi2_(R z) {
+    if (fabs(z) < R(0.05))
+        return R(0.5) + z * (R(1.) / R(6.) + z * (R(1.) / R(24.) + z * (R(1.) / R(120.) + z * (R(1.) / R(720.) +
+               z * (R(1.) / R(5040.) + z * (R(1.) / R(40320.) + z / R(362880.)))))));
     return (expm1(z) - z) / (z * z);
 }
 
-__device__ inline bool lsm3_check(double a, double a2, double tl, double dt, Lsm3Coef& c) {
-    if (!isfinite(a) || !isfinite(a2) || !isfinite(tl) || !isfinite(dt) || a < 0. || tl <= 0. ||
-        dt < 0.)
+template <typename R>
+__device__ inline bool lsm3_check(R a, R a2, R tl, R dt, Lsm3Coef<R>& c) {
+    if (!isfinite(a) || !isfinite(a2) || !isfinite(tl) || !isfinite(dt) || a < R(0.) || tl <= R(0.) ||
+        dt < R(0.))
         return false;
-    double b = 1. / tl;
-    if (!isfinite(b) || !isfinite(a * dt) || !isfinite(b * dt) || !isfinite(a * (1. - a2) * dt))
+    R b = R(1.) / tl;
+    if (!isfinite(b) || !isfinite(a * dt) || !isfinite(b * dt) || !isfinite(a * (R(1.) - a2) * dt))
         return false;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        c.phi[k] = 0.;
-        c.q[k] = 0.;
+        c.phi[k] = R(0.);
+        c.q[k] = R(0.);
     }
-    c.phi[0] = c.phi[4] = c.phi[8] = 1.;
+    c.phi[0] = c.phi[4] = c.phi[8] = R(1.);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        c.force[k] = 0.;
-        c.flow[k] = 0.;
+        c.force[k] = R(0.);
+        c.flow[k] = R(0.);
     }
     return true;
 }
 
-__device__ inline bool lsm3_finite(const Lsm3Coef& c) {
+template <typename R>
+__device__ inline bool lsm3_finite(const Lsm3Coef<R>& c) {
 #pragma unroll
     for (int k = 0; k < 9; ++k)
         if (!isfinite(c.phi[k]) || !isfinite(c.q[k])) return false;
@@ -486,58 +526,59 @@ __device__ inline bool lsm3_finite(const Lsm3Coef& c) {
 
 // update_state_lsm3.pyx:32-216 (lsm3_edge_opt = 1: normalized Taylor series
 // at max(a h, b h) <= 1/2, then step doublings)
-__device__ inline bool lsm3_direct_coefficients(double a, double a2, double tl, double dt,
-                                                Lsm3Coef& c) {
+template <typename R>
+__device__ inline bool lsm3_direct_coefficients(R a, R a2, R tl, R dt,
+                                                Lsm3Coef<R>& c) {
     if (!lsm3_check(a, a2, tl, dt, c)) return false;
-    if (dt == 0.) return true;
-    double b = 1. / tl;
-    double h = dt;
+    if (dt == R(0.)) return true;
+    R b = R(1.) / tl;
+    R h = dt;
     int doublings = 0;
-    while (h > 0. && fmax(a * h, b * h) > 0.5 && doublings < 2100) {
-        h *= 0.5;
+    while (h > R(0.) && fmax(a * h, b * h) > R(0.5) && doublings < 2100) {
+        h *= R(0.5);
         doublings += 1;
     }
-    double ah = a * h, bh = b * h, kh = a * (1. - a2) * h;
-    double qb0 = 1., qb1 = 0., qb2 = 0., qb3 = 0., qb4 = 0., qb5 = 0., qb6 = 0., qb7 = 0.,
-           qb8 = 0., qb9 = 0.;
-    double tss = 1., tsp = 0., tsx = 0., tpp = 0., tpx = 0., txx = 0.;
-    double tsi = 0., tpi = 0., txi = 0., tii = 0.;
-    double s = 1., pp = 0., x = 0., si = 0.;
-    double sum_p = 0., sum_x = 0., sum_si = 0., int_p = 0., int_x = 0., int_si = 0.;
-    double beta_term = 1., phi1 = 1., phi2 = 0.5;
+    R ah = a * h, bh = b * h, kh = a * (R(1.) - a2) * h;
+    R qb0 = R(1.), qb1 = R(0.), qb2 = R(0.), qb3 = R(0.), qb4 = R(0.), qb5 = R(0.), qb6 = R(0.), qb7 = R(0.),
+           qb8 = R(0.), qb9 = R(0.);
+    R tss = R(1.), tsp = R(0.), tsx = R(0.), tpp = R(0.), tpx = R(0.), txx = R(0.);
+    R tsi = R(0.), tpi = R(0.), txi = R(0.), tii = R(0.);
+    R s = R(1.), pp = R(0.), x = R(0.), si = R(0.);
+    R sum_p = R(0.), sum_x = R(0.), sum_si = R(0.), int_p = R(0.), int_x = R(0.), int_si = R(0.);
+    R beta_term = R(1.), phi1 = R(1.), phi2 = R(0.5);
     for (int n = 1; n < 25; ++n) {
-        double divisor = n + 1.;
-        double nss = -2. * bh * tss / divisor;
-        double nsp = (tss - (ah + bh) * tsp) / divisor;
-        double nsx = (tsp - bh * tsx) / divisor;
-        double npp = (2. * tsp - 2. * ah * tpp) / divisor;
-        double npx = (tsx + tpp - ah * tpx) / divisor;
-        double nxx = 2. * tpx / divisor;
-        double nsi = (tss - bh * tsi) / divisor;
-        double npi = (tsi + tsp - ah * tpi) / divisor;
-        double nxi = (tpi + tsx) / divisor;
-        double nii = 2. * tsi / divisor;
+        R divisor = n + R(1.);
+        R nss = -R(2.) * bh * tss / divisor;
+        R nsp = (tss - (ah + bh) * tsp) / divisor;
+        R nsx = (tsp - bh * tsx) / divisor;
+        R npp = (R(2.) * tsp - R(2.) * ah * tpp) / divisor;
+        R npx = (tsx + tpp - ah * tpx) / divisor;
+        R nxx = R(2.) * tpx / divisor;
+        R nsi = (tss - bh * tsi) / divisor;
+        R npi = (tsi + tsp - ah * tpi) / divisor;
+        R nxi = (tpi + tsx) / divisor;
+        R nii = R(2.) * tsi / divisor;
         tss = nss; tsp = nsp; tsx = nsx;
         tpp = npp; tpx = npx; txx = nxx;
         tsi = nsi; tpi = npi; txi = nxi; tii = nii;
         qb0 += tss; qb1 += tsp; qb2 += tsx; qb3 += tpp; qb4 += tpx;
         qb5 += txx; qb6 += tsi; qb7 += tpi; qb8 += txi; qb9 += tii;
-        double sn = -bh * s / n, pn = (s - ah * pp) / n, xn = pp / n, sin_ = s / n;
+        R sn = -bh * s / n, pn = (s - ah * pp) / n, xn = pp / n, sin_ = s / n;
         s = sn; pp = pn; x = xn; si = sin_;
         sum_p += pp; sum_x += x; sum_si += si;
-        int_p += pp / (n + 1.); int_x += x / (n + 1.); int_si += si / (n + 1.);
+        int_p += pp / (n + R(1.)); int_x += x / (n + R(1.)); int_si += si / (n + R(1.));
         beta_term *= -ah / n;
-        phi1 += beta_term / (n + 1.);
-        phi2 += beta_term / ((n + 1.) * (n + 2.));
+        phi1 += beta_term / (n + R(1.));
+        phi2 += beta_term / ((n + R(1.)) * (n + R(2.)));
     }
-    double* q = c.q;
-    double* phi = c.phi;
+    R* q = c.q;
+    R* phi = c.phi;
     q[0] = h * qb0;
     q[1] = q[3] = h * kh * qb1;
     q[2] = q[6] = h * h * (kh * qb2 + a2 * qb6);
     q[4] = h * kh * kh * qb3;
     q[5] = q[7] = h * h * kh * (kh * qb4 + a2 * qb7);
-    q[8] = h * h * h * (kh * kh * qb5 + 2. * kh * a2 * qb8 + a2 * a2 * qb9);
+    q[8] = h * h * h * (kh * kh * qb5 + R(2.) * kh * a2 * qb8 + a2 * a2 * qb9);
     phi[0] = exp(-bh);
     phi[3] = kh * sum_p;
     phi[4] = exp(-ah);
@@ -550,12 +591,12 @@ __device__ inline bool lsm3_direct_coefficients(double a, double a2, double tl, 
     c.flow[2] = h * bh * (kh * int_x + a2 * int_si);
     for (int n = 0; n < doublings; ++n) {
         // Q(2h) = Q(h) + Phi(h) Q(h) Phi(h)^T, symmetric by construction
-        double work[9], qnew[9];
+        R work[9], qnew[9];
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) {
-                double value = 0.;
+                R value = R(0.);
 #pragma unroll
                 for (int k = 0; k < r + 1; ++k) value += phi[3 * r + k] * q[3 * k + cc];
                 work[3 * r + cc] = value;
@@ -564,22 +605,22 @@ __device__ inline bool lsm3_direct_coefficients(double a, double a2, double tl, 
         for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int cc = 0; cc < r + 1; ++cc) {
-                double value = q[3 * r + cc];
+                R value = q[3 * r + cc];
 #pragma unroll
                 for (int k = 0; k < cc + 1; ++k) value += work[3 * r + k] * phi[3 * cc + k];
                 qnew[3 * r + cc] = qnew[3 * cc + r] = value;
             }
 #pragma unroll
         for (int k = 0; k < 9; ++k) q[k] = qnew[k];
-        c.flow[2] = 2. * c.flow[2] + phi[6] * c.flow[0] + phi[7] * c.flow[1];
-        c.flow[1] = (1. + phi[4]) * c.flow[1] + phi[3] * c.flow[0];
-        c.flow[0] = -expm1(-2. * b * h);
-        phi[6] = phi[6] * (1. + phi[0]) + phi[7] * phi[3];
+        c.flow[2] = R(2.) * c.flow[2] + phi[6] * c.flow[0] + phi[7] * c.flow[1];
+        c.flow[1] = (R(1.) + phi[4]) * c.flow[1] + phi[3] * c.flow[0];
+        c.flow[0] = -expm1(-R(2.) * b * h);
+        phi[6] = phi[6] * (R(1.) + phi[0]) + phi[7] * phi[3];
         phi[3] *= phi[0] + phi[4];
-        c.force[2] = 2. * c.force[2] + phi[7] * phi[7];
-        phi[7] *= 1. + phi[4];
+        c.force[2] = R(2.) * c.force[2] + phi[7] * phi[7];
+        phi[7] *= R(1.) + phi[4];
         c.force[1] = phi[7];
-        h *= 2.;
+        h *= R(2.);
         phi[0] = exp(-b * h);
         phi[4] = exp(-a * h);
     }
@@ -587,102 +628,107 @@ __device__ inline bool lsm3_direct_coefficients(double a, double a2, double tl, 
 }
 
 // update_state_lsm3.pyx:235-264
-__device__ inline void lsm3_closed_covariance(double a, double b, double a2, double h, double* q) {
-    double d = a - b;
-    double cc = a * (1. - a2) / d;
-    double bb = (1. - a2) / d;
-    double aa = (a2 + cc) / b;
-    double sb = h * phi1_(-b * h), sa = h * phi1_(-a * h);
-    double s2b = h * phi1_(-2. * b * h), s2a = h * phi1_(-2. * a * h);
-    double sab = h * phi1_(-(a + b) * h);
+template <typename R>
+__device__ inline void lsm3_closed_covariance(R a, R b, R a2, R h, R* q) {
+    R d = a - b;
+    R cc = a * (R(1.) - a2) / d;
+    R bb = (R(1.) - a2) / d;
+    R aa = (a2 + cc) / b;
+    R sb = h * phi1_(-b * h), sa = h * phi1_(-a * h);
+    R s2b = h * phi1_(-R(2.) * b * h), s2a = h * phi1_(-R(2.) * a * h);
+    R sab = h * phi1_(-(a + b) * h);
     q[0] = s2b;
     q[1] = q[3] = cc * (s2b - sab);
     q[2] = q[6] = aa * (sb - s2b) - bb * (sb - sab);
-    q[4] = cc * cc * (s2b - 2. * sab + s2a);
+    q[4] = cc * cc * (s2b - R(2.) * sab + s2a);
     q[5] = q[7] = cc * (aa * (sb - s2b - sa + sab) - bb * (sb - sab - sa + s2a));
-    q[8] = (aa * aa * (h - 2. * sb + s2b) - 2. * aa * bb * (h - sb - sa + sab) +
-            bb * bb * (h - 2. * sa + s2a));
+    q[8] = (aa * aa * (h - R(2.) * sb + s2b) - R(2.) * aa * bb * (h - sb - sa + sab) +
+            bb * bb * (h - R(2.) * sa + s2a));
 }
 
 // update_state_lsm3.pyx:266-307
-__device__ inline void lsm3_clipped_covariance(double a, double b, double a2, double h, double* q) {
-    double d = a - b, m = 0.5 * (a + b), x = m * h, delta;
-    if (x > 1.) delta = fmin(0.5, LSM3_CLIP_STEP * sqrt(x)) / h;
-    else delta = fmin(0.5, LSM3_CLIP_STEP / sqrt(x)) * m;
+template <typename R>
+__device__ inline void lsm3_clipped_covariance(R a, R b, R a2, R h, R* q) {
+    R d = a - b, m = R(0.5) * (a + b), x = m * h, delta;
+    if (x > R(1.)) delta = fmin(R(0.5), R(LSM3_CLIP_STEP) * sqrt(x)) / h;
+    else delta = fmin(R(0.5), R(LSM3_CLIP_STEP) / sqrt(x)) * m;
     if (fabs(d) >= delta) {
         lsm3_closed_covariance(a, b, a2, h, q);
     } else {
-        double qp[9], qm[9];
-        lsm3_closed_covariance(m + 0.5 * delta, m - 0.5 * delta, a2, h, qp);
-        lsm3_closed_covariance(m - 0.5 * delta, m + 0.5 * delta, a2, h, qm);
-        double w = 0.5 * (1. + d / delta);
+        R qp[9], qm[9];
+        lsm3_closed_covariance(m + R(0.5) * delta, m - R(0.5) * delta, a2, h, qp);
+        lsm3_closed_covariance(m - R(0.5) * delta, m + R(0.5) * delta, a2, h, qm);
+        R w = R(0.5) * (R(1.) + d / delta);
 #pragma unroll
         for (int k = 0; k < 9; ++k) q[k] = qm[k] + w * (qp[k] - qm[k]);
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) q[4 * k] = fmax(q[4 * k], 0.);
+    for (int k = 0; k < 3; ++k) q[4 * k] = fmax(q[4 * k], R(0.));
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int cc = 0; cc < r; ++cc) {
-            double bound = sqrt(q[4 * r] * q[4 * cc]);
+            R bound = sqrt(q[4 * r] * q[4 * cc]);
             q[3 * r + cc] = q[3 * cc + r] = fmax(-bound, fmin(bound, q[3 * r + cc]));
         }
 }
 
 // update_state_lsm3.pyx:309-374 (lsm3_edge_opt = 2, the default)
-__device__ inline bool lsm3_clipped_coefficients(double a, double a2, double tl, double dt,
-                                                 Lsm3Coef& c) {
+template <typename R>
+__device__ inline bool lsm3_clipped_coefficients(R a, R a2, R tl, R dt,
+                                                 Lsm3Coef<R>& c) {
     if (!lsm3_check(a, a2, tl, dt, c)) return false;
-    if (dt == 0.) return true;
-    double b = 1. / tl;
-    double ah = a * dt, bh = b * dt, k = a * (1. - a2);
-    double alpha = exp(-bh), beta = exp(-ah);
-    double divdiff = exp_divdiff(ah, bh);
-    double ib = dt * phi1_(-bh), ia = dt * phi1_(-ah);
+    if (dt == R(0.)) return true;
+    R b = R(1.) / tl;
+    R ah = a * dt, bh = b * dt, k = a * (R(1.) - a2);
+    R alpha = exp(-bh), beta = exp(-ah);
+    R divdiff = exp_divdiff(ah, bh);
+    R ib = dt * phi1_(-bh), ia = dt * phi1_(-ah);
     c.phi[0] = alpha;
     c.phi[3] = k * dt * divdiff;
     c.phi[4] = beta;
-    c.phi[6] = ib - (1. - a2) * dt * divdiff;
+    c.phi[6] = ib - (R(1.) - a2) * dt * divdiff;
     c.phi[7] = ia;
     c.force[1] = ia;
     c.force[2] = dt * dt * phi2_(-ah);
     c.flow[0] = -expm1(-bh);
     c.flow[1] = k * dt * (phi1_(-ah) - divdiff);
-    c.flow[2] = (a2 * (dt - ib) + (1. - a2) * (dt - ia - ib + dt * divdiff));
+    c.flow[2] = (a2 * (dt - ib) + (R(1.) - a2) * (dt - ia - ib + dt * divdiff));
     lsm3_clipped_covariance(a, b, a2, dt, c.q);
     return lsm3_finite(c);
 }
 
-__device__ __forceinline__ bool lsm3_coefficients(double a, double a2, double tl, double dt,
-                                                  int edge_opt, Lsm3Coef& c) {
+template <typename R>
+__device__ __forceinline__ bool lsm3_coefficients(R a, R a2, R tl, R dt,
+                                                  int edge_opt, Lsm3Coef<R>& c) {
     return edge_opt == 2 ? lsm3_clipped_coefficients(a, a2, tl, dt, c)
                          : lsm3_direct_coefficients(a, a2, tl, dt, c);
 }
 
 // update_state_lsm3.pyx:523-557 (strict: only roundoff-sized negative pivots clip)
-__device__ inline bool lsm3_cholesky(const double* q, double* lower) {
+template <typename R>
+__device__ inline bool lsm3_cholesky(const R* q, R* lower) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) lower[k] = 0.;
+    for (int k = 0; k < 9; ++k) lower[k] = R(0.);
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-        double pivot = q[3 * r + r];
+        R pivot = q[3 * r + r];
 #pragma unroll
         for (int cc = 0; cc < r; ++cc) {
-            double residual = q[3 * r + cc];
+            R residual = q[3 * r + cc];
 #pragma unroll
             for (int k = 0; k < cc; ++k) residual -= lower[3 * r + k] * lower[3 * cc + k];
-            if (lower[3 * cc + cc] > 0.) {
+            if (lower[3 * cc + cc] > R(0.)) {
                 lower[3 * r + cc] = residual / lower[3 * cc + cc];
             } else {
-                double tol = (128. * DBL_EPS * sqrt(fabs(q[3 * r + r])) * sqrt(fabs(q[3 * cc + cc])));
+                R tol = (R(128.) * EpsOf<R>::value * sqrt(fabs(q[3 * r + r])) * sqrt(fabs(q[3 * cc + cc])));
                 if (fabs(residual) > tol) return false;
             }
             pivot -= lower[3 * r + cc] * lower[3 * r + cc];
         }
-        if (pivot < 0.) {
-            if (-pivot > 128. * DBL_EPS * fabs(q[3 * r + r])) return false;
-            pivot = 0.;
+        if (pivot < R(0.)) {
+            if (-pivot > R(128.) * EpsOf<R>::value * fabs(q[3 * r + r])) return false;
+            pivot = R(0.);
         }
         lower[3 * r + r] = sqrt(pivot);
     }
@@ -690,16 +736,17 @@ __device__ inline bool lsm3_cholesky(const double* q, double* lower) {
 }
 
 // update_state_lsm3.pyx:559-585
-__device__ inline void lsm3_cholesky_clipped(const double* q, double* lower) {
+template <typename R>
+__device__ inline void lsm3_cholesky_clipped(const R* q, R* lower) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) lower[k] = 0.;
+    for (int k = 0; k < 9; ++k) lower[k] = R(0.);
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-        double remaining = fmax(q[3 * r + r], 0.);
+        R remaining = fmax(q[3 * r + r], R(0.));
 #pragma unroll
         for (int cc = 0; cc < r; ++cc) {
-            if (lower[3 * cc + cc] > 0.) {
-                double value = q[3 * r + cc];
+            if (lower[3 * cc + cc] > R(0.)) {
+                R value = q[3 * r + cc];
 #pragma unroll
                 for (int k = 0; k < cc; ++k) value -= lower[3 * r + k] * lower[3 * cc + k];
                 value /= lower[3 * cc + cc];
@@ -708,14 +755,15 @@ __device__ inline void lsm3_cholesky_clipped(const double* q, double* lower) {
                 remaining -= value * value;
             }
         }
-        lower[3 * r + r] = sqrt(fmax(remaining, 0.));
+        lower[3 * r + r] = sqrt(fmax(remaining, R(0.)));
     }
 }
 
 // drag rate ((a1c*(1.5/dp))*unorm)*Cd (update_state_lsm3.pyx:728)
-__device__ __forceinline__ double lsm3_a1(const DevParams& p, double dp, double unorm) {
-    double Cd = drag_coefficient(p, unorm, dp);
-    return p.a1c * (1.5 / dp) * unorm * Cd;
+template <typename R>
+__device__ __forceinline__ R lsm3_a1(const DevParams& p, R dp, R unorm) {
+    R Cd = drag_coefficient(p, unorm, dp);
+    return R(p.a1c) * (R(1.5) / dp) * unorm * Cd;
 }
 
 template <int DIM>
@@ -733,8 +781,9 @@ __device__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double dp) {
     const int diffmod = p.diffmod;
     double z = DIM == 3 ? q.x[2] : 0.;
     mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, true, ux, uy, uz, ax, ay, az);
-    double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(q.us, q.up)));
-    double a1 = lsm3_a1(p, dp, unorm);
+    using R = typename ArithOf<FT>::type;
+    const double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(q.us, q.up)));
+    const double a1 = double(lsm3_a1<R>(p, R(dp), R(unorm)));
     double xix, xiy, xiz = 0.;
     rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
     if (DIM == 3) xiz = rng_single(q.rng, p.rng_method, q.z);
@@ -777,9 +826,12 @@ __device__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double dp) {
     }
 }
 
-// update_state_lsm3.pyx:822-996
+// update_state_lsm3.pyx:822-996.  Mixed form: coefficients, Cholesky factor,
+// means and increments in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
 __device__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
+    using R = typename ArithOf<FT>::type;
+    constexpr bool exact = std::is_same<R, double>::value;
     const DevParams& p = q.p;
     const double dt = p.dt;
     if (dt == 0.) return;
@@ -796,76 +848,84 @@ __device__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
     mean_fields(q, q.tri, q.ll, xp0[0], xp0[1], z0, true, ux, uy, uz, ax, ay, az);
     if (diffmod == 2 || diffmod == 3) tml_ke = keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
     double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(us0, up0)));
-    double a1 = lsm3_a1(p, dp, unorm);
-    double a2 = p.added_mass ? p.a2c : 0.;
-    double tl_h = p.tl_h, tl_v = p.tl_v, sigma_h, sigma_v = 0.;
+    const R a1 = lsm3_a1<R>(p, R(dp), R(unorm));
+    const R a2 = p.added_mass ? R(p.a2c) : R(0.);
+    R tl_h = R(p.tl_h), tl_v = R(p.tl_v), sigma_h, sigma_v = R(0.);
     if (diffmod == 2 || diffmod == 3) {
-        tl_h = fmax(EPSILON_LSM3, tml_ke);
-        sigma_h = sqrt(C0KOLM * ep);
+        tl_h = R(fmax(EPSILON_LSM3, tml_ke));
+        sigma_h = sqrt(R(C0KOLM) * R(ep));
     } else {
-        sigma_h = sqrt(2. * p.nux) / tl_h;
+        sigma_h = sqrt(R(2.) * R(p.nux)) / tl_h;
     }
     if (DIM == 3) {
         if (diffmod == 3) {
             tl_v = tl_h;
             sigma_v = sigma_h;
         } else {
-            sigma_v = sqrt(2. * p.nuz) / tl_v;
+            sigma_v = sqrt(R(2.) * R(p.nuz)) / tl_v;
         }
     }
     const double mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
-    Lsm3Coef c;
-    double lower[9];
-    if (!lsm3_coefficients(a1, a2, tl_h, dt, edge_opt, c)) { q.err |= ERR_NONFINITE; return; }
+    Lsm3Coef<R> c;
+    R lower[9];
+    if (!lsm3_coefficients<R>(a1, a2, tl_h, R(dt), edge_opt, c)) { q.err |= ERR_NONFINITE; return; }
     bool factored = false;
-    double sigma_s = sigma_h;
+    R sigma_s = sigma_h;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        double tl_k = tl_h;
+        R tl_k = tl_h;
         if (d == 2) {
             tl_k = tl_v;
             sigma_s = sigma_v;
             if (tl_v != tl_h) {
-                if (!lsm3_coefficients(a1, a2, tl_v, dt, edge_opt, c)) {
+                if (!lsm3_coefficients<R>(a1, a2, tl_v, R(dt), edge_opt, c)) {
                     q.err |= ERR_NONFINITE;
                     return;
                 }
                 factored = false;
             }
         }
-        double u_k = mean_flow[d];
-        double Fp = d == 2 ? -GRAV * p.a0c : 0.;
-        double ur0 = up0[d] - a2 * us0[d];
-        double us_mean = (us0[d] * c.phi[0] + u_k * c.flow[0] + mean_acc[d] * tl_k * c.flow[0]);
-        double ur_mean = (ur0 * c.phi[4] + us0[d] * c.phi[3] + u_k * c.flow[1] +
-                          mean_acc[d] * tl_k * c.flow[1] + Fp * c.force[1]);
-        double xp_mean = (xp0[d] + ur0 * c.force[1] + us0[d] * c.phi[6] + u_k * c.flow[2] +
-                          mean_acc[d] * tl_k * c.flow[2] + Fp * c.force[2]);
-        if (sigma_s > 0. && c.q[0] > 0.) {
+        const R u_k = R(mean_flow[d]), acc = R(mean_acc[d]);
+        const R Fp = d == 2 ? -R(GRAV) * R(p.a0c) : R(0.);
+        const R s0 = R(us0[d]);
+        const R ur0 = exact ? R(up0[d] - a2 * us0[d]) : R(up0[d]) - a2 * s0;
+        R us_mean = (s0 * c.phi[0] + u_k * c.flow[0] + acc * tl_k * c.flow[0]);
+        R ur_mean = (ur0 * c.phi[4] + s0 * c.phi[3] + u_k * c.flow[1] +
+                     acc * tl_k * c.flow[1] + Fp * c.force[1]);
+        // position: the mean without x0 in the mixed form (added in FP64 below)
+        R xp_mean;
+        if constexpr (exact)
+            xp_mean = (xp0[d] + ur0 * c.force[1] + s0 * c.phi[6] + u_k * c.flow[2] +
+                       acc * tl_k * c.flow[2] + Fp * c.force[2]);
+        else
+            xp_mean = (ur0 * c.force[1] + s0 * c.phi[6] + u_k * c.flow[2] +
+                       acc * tl_k * c.flow[2] + Fp * c.force[2]);
+        if (sigma_s > R(0.) && c.q[0] > R(0.)) {
             if (!factored) {
                 if (edge_opt == 2) {
-                    lsm3_cholesky_clipped(c.q, lower);
-                } else if (!lsm3_cholesky(c.q, lower)) {
+                    lsm3_cholesky_clipped<R>(c.q, lower);
+                } else if (!lsm3_cholesky<R>(c.q, lower)) {
                     q.err |= ERR_NONFINITE;
                     return;
                 }
                 factored = true;
             }
-            double xix, xiy, xiz;
-            if (lower[4] > 0.) {
-                rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
+            double xixd, xiyd, xizd;
+            if (lower[4] > R(0.)) {
+                rng_pair(q.rng, p.rng_method, q.z, xixd, xiyd);
             } else {
-                xix = rng_single(q.rng, p.rng_method, q.z);
-                xiy = 0.;
+                xixd = rng_single(q.rng, p.rng_method, q.z);
+                xiyd = 0.;
             }
-            xiz = lower[8] > 0. ? rng_single(q.rng, p.rng_method, q.z) : 0.;
+            xizd = lower[8] > R(0.) ? rng_single(q.rng, p.rng_method, q.z) : 0.;
+            const R xix = R(xixd), xiy = R(xiyd), xiz = R(xizd);
             us_mean += sigma_s * lower[0] * xix;
             ur_mean += sigma_s * (lower[3] * xix + lower[4] * xiy);
             xp_mean += sigma_s * (lower[6] * xix + lower[7] * xiy + lower[8] * xiz);
         }
-        q.us[d] = us_mean;
-        q.up[d] = ur_mean + a2 * us_mean;
-        q.x[d] = xp_mean;
+        q.us[d] = double(us_mean);
+        q.up[d] = double(ur_mean + a2 * us_mean);
+        q.x[d] = exact ? double(xp_mean) : xp0[d] + double(xp_mean);
     }
 }
 
