@@ -33,6 +33,10 @@ UNITS = {
     "cg_server.cu": HOST_EXACT,
     "cg_kernels_plain.cu": ["-fmad=false"],
     "cg_kernels_mixed.cu": [],
+    "cg_lsm23_plain.cu": ["-fmad=false"],
+    "cg_lsm23_mixed.cu": [],
+    "cg_serve_plain.cu": ["-fmad=false"],
+    "cg_serve_mixed.cu": [],
     "cg_sort.cu": [],
 }
 

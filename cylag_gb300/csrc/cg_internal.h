@@ -56,6 +56,14 @@ void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
                        int* stats, uint32_t* err, cudaStream_t st);
 
+// The LSM2/LSM3 step kernels (cg_lsm23_plain.cu, cg_lsm23_mixed.cu)
+void launch_lsm23_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                        const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
+                        cudaStream_t st);
+void launch_lsm23_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
+                        const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
+                        cudaStream_t st);
+
 // The same step, mixed-precision form (FP32 node records).
 void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,

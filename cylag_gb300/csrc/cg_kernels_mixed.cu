@@ -5,7 +5,7 @@
 #include <cstdlib>
 
 #include "cg_internal.h"
-#include "cg_serve.cuh"
+#include "cg_step_mixed.cuh"
 
 namespace cg {
 
@@ -22,12 +22,14 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs_, 0);
         return nsm * (per < 1 ? 1 : per);
     };
+    if (p.model != 1) {
+        // LSM2 / LSM3: FP32 node records and Langevin coefficients, inline walk
+        launch_lsm23_mixed(m, fv, p, s, aux, step_index, stats, err, st);
+        return;
+    }
     DevFields<float> f = fv.as<float>();
     WalkQueue none{nullptr, nullptr};
-    if (fv.dim == 2 && p.model >= 2) {
-        // LSM2 / LSM3: FP32 node records, FP64 arithmetic, inline walk
-        launch_step_kernel<2, float>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
-    } else if (fv.dim == 2) {
+    if (fv.dim == 2) {
         // occupancy variant: 3 blocks/SM (80 registers) by default, 4 (64) on request
         static int minb = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
@@ -43,17 +45,8 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                                                                    step_index, stats, err);
     } else {
         // 3D: FP32 node records, FP64 arithmetic
-        launch_step_kernel<3, float>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
+        launch_lsm1_kernel<3, float>(m, f, p, s, none, aux, step_index, stats, err, st);
     }
-}
-
-int serve_grid_mixed() { return resident_blocks(serve_step_kernel<float, true>, 256); }
-
-void launch_serve_mixed(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
-                        const ServeRun* runs, const int2* active, const int* nactive,
-                        ServeClock* clk, uint32_t* run_err, cudaStream_t st) {
-    serve_step_kernel<float, true><<<grid, 256, 0, st>>>(m, fv.as<float>(), pool, runs, active,
-                                                         nactive, clk, run_err);
 }
 
 void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,

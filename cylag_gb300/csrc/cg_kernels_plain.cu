@@ -6,7 +6,7 @@
 #include <cstdio>
 
 #include "cg_internal.h"
-#include "cg_serve.cuh"
+#include "cg_step.cuh"
 
 namespace cg {
 
@@ -73,12 +73,16 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
 void launch_step_plain(const DevMesh& m, const FieldView& fv, const DevParams& p,
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
                        int* stats, uint32_t* err, cudaStream_t st) {
+    if (p.model != 1) {
+        launch_lsm23_plain(m, fv, p, s, aux, step_index, stats, err, st);
+        return;
+    }
     DevFields<double> f = fv.as<double>();
     if (fv.dim == 2) {
-        launch_step_kernel<2, double>(p.model, m, f, p, s, wq, aux, step_index, stats, err, st);
+        launch_lsm1_kernel<2, double>(m, f, p, s, wq, aux, step_index, stats, err, st);
     } else {
         WalkQueue none{nullptr, nullptr};
-        launch_step_kernel<3, double>(p.model, m, f, p, s, none, aux, step_index, stats, err, st);
+        launch_lsm1_kernel<3, double>(m, f, p, s, none, aux, step_index, stats, err, st);
     }
 }
 
@@ -93,18 +97,6 @@ void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p
     int nb = nsm * 8;
     DevFields<double> f = fv.as<double>();
     walk_kernel<double, false><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
-}
-
-// ---------------------------------------------------------------------------
-// serving pool: every admitted run in one launch (FP64 records)
-// ---------------------------------------------------------------------------
-int serve_grid_plain() { return resident_blocks(serve_step_kernel<double, false>, 256); }
-
-void launch_serve_plain(int grid, const DevMesh& m, const FieldView& fv, const DevState& pool,
-                        const ServeRun* runs, const int2* active, const int* nactive,
-                        ServeClock* clk, uint32_t* run_err, cudaStream_t st) {
-    serve_step_kernel<double, false><<<grid, 256, 0, st>>>(m, fv.as<double>(), pool, runs, active,
-                                                           nactive, clk, run_err);
 }
 
 // ---------------------------------------------------------------------------

@@ -32,7 +32,7 @@ __device__ __forceinline__ R cpow_re(R x, R y) {
 
 // lagrangian_particle_set.pyx:790-832.  The Almedeij powers overflow FP32
 // at small Re: that law is evaluated in FP64 in both forms.
-__device__ inline double drag_almedeij(double Re) {
+__device__ __forceinline__ double drag_almedeij(double Re) {
     double phi1 = pow(24. / Re, 10.) + cpow_re(21. * cpow_re(Re, -0.67), 10.) +
                   cpow_re(4. * cpow_re(Re, -0.33), 10.) + pow(0.4, 10.);
     double phi2 = 1. / (cpow_re(0.148 * cpow_re(Re, 0.11), -10.) + pow(0.5, -10.));
@@ -42,7 +42,7 @@ __device__ inline double drag_almedeij(double Re) {
 }
 
 template <typename R>
-__device__ inline R drag_coefficient(const DevParams& p, R U, R dp) {
+__device__ __forceinline__ R drag_coefficient(const DevParams& p, R U, R dp) {
     R Re = fmax(R(EPSILON), U * dp / R(NU0));
     if (p.drag_model == 0) return R(p.drag_coef);
     if (p.drag_model == 1) {
@@ -80,7 +80,7 @@ __device__ __forceinline__ void mean_fields(Particle<DIM, FT>& q, int k, int l, 
 
 // update_state_lsm2.pyx:141-217
 template <int DIM, typename FT>
-__device__ void euler_lsm2(Particle<DIM, FT>& q, double dp) {
+__device__ __forceinline__ void euler_lsm2(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     double dt = p.dt, ux, uy, uz, ax, ay, az;
     double z = DIM == 3 ? q.x[2] : 0.;
@@ -106,7 +106,7 @@ __device__ void euler_lsm2(Particle<DIM, FT>& q, double dp) {
 // that leaves the mesh (or the water column) ends the step with an Euler
 // update from the stage just evaluated.  NST = 2, 3, 4.
 template <int NST, int DIM, typename FT>
-__device__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
+__device__ __forceinline__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     const double dt = p.dt;
     // stage-point and slip coefficients applied to k(s-1) and f(s-1)
@@ -227,7 +227,7 @@ __device__ __forceinline__ double keps_tml(Particle<DIM, FT>& q, int k, int l, d
 
 // update_state_lsm2.pyx:1088-1230
 template <int DIM, typename FT>
-__device__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, double dp) {
+__device__ __forceinline__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     double dt = p.dt, sqrtdt = p.sqrtdt, ux, uy, uz, ax, ay, az;
     const int diffmod = p.diffmod, nuopt = p.nuopt;
@@ -277,7 +277,7 @@ struct Lsm2Coef {
 };
 
 template <typename R>
-__device__ inline bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>& c) {
+__device__ __forceinline__ bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>& c) {
     R r = a1 * dt;
     if (!isfinite(a1) || !isfinite(dt) || a1 < R(0.) || dt < R(0.) || !isfinite(r)) return false;
     c.beta = exp(-r);
@@ -316,7 +316,7 @@ __device__ inline bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>& c) {
 // di_ode_lsm2, 1232-1238).  Mixed form: coefficients, means and increments
 // in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
-__device__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux, double nuz,
+__device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux, double nuz,
                         int nuopt) {
     using R = typename ArithOf<FT>::type;
     const DevParams& p = q.p;
@@ -388,25 +388,23 @@ __device__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux
     }
 }
 
-// update_state_lsm2.pyx:30-139; the final localization is unconditional
-template <int DIM, typename FT>
-__device__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
+// update_state_lsm2.pyx:30-139; the final localization is unconditional.
+// SCHEME: the time scheme, fixed per kernel instantiation
+template <int SCHEME, int DIM, typename FT>
+__device__ __forceinline__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     const int diffmod = p.diffmod, nuopt = p.nuopt;
     int bnd_j = -1;
     if (nuopt == 1 || (nuopt >= 2 && diffmod == 0)) {
-        switch (p.time_scheme) {
-            case 1: euler_lsm2(q, dp); break;
-            case 2: bnd_j = rk_lsm2<2>(q, dp); break;
-            case 3: bnd_j = rk_lsm2<3>(q, dp); break;
-            case 4: bnd_j = rk_lsm2<4>(q, dp); break;
-            case 5: di_lsm2(q, dp, 0, 0., 0., 2); break;
-            default: q.err |= ERR_UNSUPPORTED; return -1;
-        }
+        if constexpr (SCHEME == 1) euler_lsm2(q, dp);
+        else if constexpr (SCHEME == 2) bnd_j = rk_lsm2<2>(q, dp);
+        else if constexpr (SCHEME == 3) bnd_j = rk_lsm2<3>(q, dp);
+        else if constexpr (SCHEME == 4) bnd_j = rk_lsm2<4>(q, dp);
+        else di_lsm2(q, dp, 0, 0., 0., 2);
         if (diffmod != 0) q.diffusion_lsm1(p1_at(q.m, q.tri0, q.x0[0], q.x0[1]));
-    } else if (p.time_scheme == 1) {
+    } else if constexpr (SCHEME == 1) {
         euler_maruyama_lsm2_u(q, dp);
-    } else if (p.time_scheme == 5) {
+    } else if constexpr (SCHEME == 5) {
         di_lsm2(q, dp, diffmod, p.nux, p.nuz, nuopt);
     } else {
         q.err |= ERR_UNSUPPORTED;
@@ -421,7 +419,7 @@ __device__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
 
 // init_lsm2_fluctuations.pyx:28-129: stationary velocity fluctuation
 template <int DIM, typename FT>
-__device__ void lsm2_fluctuations(Particle<DIM, FT>& q, double dp, double* fl) {
+__device__ __forceinline__ void lsm2_fluctuations(Particle<DIM, FT>& q, double dp, double* fl) {
     const DevParams& p = q.p;
     fl[0] = fl[1] = fl[2] = 0.;
     if (p.diffmod == 0) return;
@@ -491,7 +489,7 @@ __device__ __forceinline__ R phi2_(R z) {
 }
 
 template <typename R>
-__device__ inline bool lsm3_check(R a, R a2, R tl, R dt, Lsm3Coef<R>& c) {
+__device__ __forceinline__ bool lsm3_check(R a, R a2, R tl, R dt, Lsm3Coef<R>& c) {
     if (!isfinite(a) || !isfinite(a2) || !isfinite(tl) || !isfinite(dt) || a < R(0.) || tl <= R(0.) ||
         dt < R(0.))
         return false;
@@ -513,7 +511,7 @@ __device__ inline bool lsm3_check(R a, R a2, R tl, R dt, Lsm3Coef<R>& c) {
 }
 
 template <typename R>
-__device__ inline bool lsm3_finite(const Lsm3Coef<R>& c) {
+__device__ __forceinline__ bool lsm3_finite(const Lsm3Coef<R>& c) {
 #pragma unroll
     for (int k = 0; k < 9; ++k)
         if (!isfinite(c.phi[k]) || !isfinite(c.q[k])) return false;
@@ -527,7 +525,7 @@ __device__ inline bool lsm3_finite(const Lsm3Coef<R>& c) {
 // update_state_lsm3.pyx:32-216 (lsm3_edge_opt = 1: normalized Taylor series
 // at max(a h, b h) <= 1/2, then step doublings)
 template <typename R>
-__device__ inline bool lsm3_direct_coefficients(R a, R a2, R tl, R dt,
+__device__ __forceinline__ bool lsm3_direct_coefficients(R a, R a2, R tl, R dt,
                                                 Lsm3Coef<R>& c) {
     if (!lsm3_check(a, a2, tl, dt, c)) return false;
     if (dt == R(0.)) return true;
@@ -629,7 +627,7 @@ __device__ inline bool lsm3_direct_coefficients(R a, R a2, R tl, R dt,
 
 // update_state_lsm3.pyx:235-264
 template <typename R>
-__device__ inline void lsm3_closed_covariance(R a, R b, R a2, R h, R* q) {
+__device__ __forceinline__ void lsm3_closed_covariance(R a, R b, R a2, R h, R* q) {
     R d = a - b;
     R cc = a * (R(1.) - a2) / d;
     R bb = (R(1.) - a2) / d;
@@ -648,7 +646,7 @@ __device__ inline void lsm3_closed_covariance(R a, R b, R a2, R h, R* q) {
 
 // update_state_lsm3.pyx:266-307
 template <typename R>
-__device__ inline void lsm3_clipped_covariance(R a, R b, R a2, R h, R* q) {
+__device__ __forceinline__ void lsm3_clipped_covariance(R a, R b, R a2, R h, R* q) {
     R d = a - b, m = R(0.5) * (a + b), x = m * h, delta;
     if (x > R(1.)) delta = fmin(R(0.5), R(LSM3_CLIP_STEP) * sqrt(x)) / h;
     else delta = fmin(R(0.5), R(LSM3_CLIP_STEP) / sqrt(x)) * m;
@@ -675,7 +673,7 @@ __device__ inline void lsm3_clipped_covariance(R a, R b, R a2, R h, R* q) {
 
 // update_state_lsm3.pyx:309-374 (lsm3_edge_opt = 2, the default)
 template <typename R>
-__device__ inline bool lsm3_clipped_coefficients(R a, R a2, R tl, R dt,
+__device__ __forceinline__ bool lsm3_clipped_coefficients(R a, R a2, R tl, R dt,
                                                  Lsm3Coef<R>& c) {
     if (!lsm3_check(a, a2, tl, dt, c)) return false;
     if (dt == R(0.)) return true;
@@ -707,7 +705,7 @@ __device__ __forceinline__ bool lsm3_coefficients(R a, R a2, R tl, R dt,
 
 // update_state_lsm3.pyx:523-557 (strict: only roundoff-sized negative pivots clip)
 template <typename R>
-__device__ inline bool lsm3_cholesky(const R* q, R* lower) {
+__device__ __forceinline__ bool lsm3_cholesky(const R* q, R* lower) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) lower[k] = R(0.);
 #pragma unroll
@@ -737,7 +735,7 @@ __device__ inline bool lsm3_cholesky(const R* q, R* lower) {
 
 // update_state_lsm3.pyx:559-585
 template <typename R>
-__device__ inline void lsm3_cholesky_clipped(const R* q, R* lower) {
+__device__ __forceinline__ void lsm3_cholesky_clipped(const R* q, R* lower) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) lower[k] = R(0.);
 #pragma unroll
@@ -775,7 +773,7 @@ __device__ __forceinline__ double slip_norm(const double* us, const double* up) 
 
 // update_state_lsm3.pyx:664-820
 template <int DIM, typename FT>
-__device__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double dp) {
+__device__ __forceinline__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     double dt = p.dt, sqrtdt = p.sqrtdt, ux, uy, uz, ax, ay, az;
     const int diffmod = p.diffmod;
@@ -829,7 +827,7 @@ __device__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double dp) {
 // update_state_lsm3.pyx:822-996.  Mixed form: coefficients, Cholesky factor,
 // means and increments in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
-__device__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
+__device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
     using R = typename ArithOf<FT>::type;
     constexpr bool exact = std::is_same<R, double>::value;
     const DevParams& p = q.p;
@@ -930,10 +928,10 @@ __device__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
 }
 
 // update_state_lsm3.pyx:587-662; the final localization is unconditional
-template <int DIM, typename FT>
-__device__ int update_lsm3(Particle<DIM, FT>& q, double dp) {
-    if (q.p.time_scheme == 1) euler_maruyama_lsm3(q, dp);
-    else if (q.p.time_scheme == 5) di_lsm3(q, dp);
+template <int SCHEME, int DIM, typename FT>
+__device__ __forceinline__ int update_lsm3(Particle<DIM, FT>& q, double dp) {
+    if constexpr (SCHEME == 1) euler_maruyama_lsm3(q, dp);
+    else if constexpr (SCHEME == 5) di_lsm3(q, dp);
     else { q.err |= ERR_UNSUPPORTED; return -1; }
     int bnd_j;
     q.ltri = q.tri;
@@ -944,7 +942,7 @@ __device__ int update_lsm3(Particle<DIM, FT>& q, double dp) {
 
 // init_lsm3_fluctuations.pyx:28-90: stationary seen-velocity fluctuation
 template <int DIM, typename FT>
-__device__ void lsm3_fluctuations(Particle<DIM, FT>& q, double* fl) {
+__device__ __forceinline__ void lsm3_fluctuations(Particle<DIM, FT>& q, double* fl) {
     const DevParams& p = q.p;
     fl[0] = fl[1] = fl[2] = 0.;
     double sigma_h;

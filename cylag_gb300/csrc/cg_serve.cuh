@@ -22,6 +22,16 @@ namespace cg {
 
 // ServeRun and ServeClock: cg_internal.h
 
+// one LSM2/LSM3 particle of a served run, out of line: each variant keeps
+// its own register allocation and the kernel's LSM1 path stays lean
+template <typename FT, int MODEL, int SCHEME>
+__device__ __noinline__ void serve_particle(const DevMesh& m, const DevFields<FT>& f,
+                                            const DevParams& p, DevState& pool, int aux, int k,
+                                            uint32_t* err, const ZigTables& zt, int i) {
+    const WalkQueue none{nullptr, nullptr};
+    step_particle<2, FT, MODEL, SCHEME>(m, f, p, pool, none, aux, k, nullptr, err, zt, i);
+}
+
 template <typename FT, bool MIXED>
 __global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT> f, DevState pool,
                                                          const ServeRun* __restrict__ runs,
@@ -59,12 +69,16 @@ __global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT
                 continue;
             }
         }
+        const int ts = R.p.time_scheme, kk = (int)k;
         if (model == 1)
-            step_particle<2, FT, 1>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
-        else if (model == 2)
-            step_particle<2, FT, 2>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
-        else
-            step_particle<2, FT, 3>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, zt, i);
+            step_particle<2, FT, 1>(m, f, R.p, pool, none, aux, kk, nullptr, err, zt, i);
+        else if (model == 2 && ts == 5) serve_particle<FT, 2, 5>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (model == 2 && ts == 1) serve_particle<FT, 2, 1>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (model == 2 && ts == 2) serve_particle<FT, 2, 2>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (model == 2 && ts == 3) serve_particle<FT, 2, 3>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (model == 2) serve_particle<FT, 2, 4>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (ts == 5) serve_particle<FT, 3, 5>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else serve_particle<FT, 3, 1>(m, f, R.p, pool, aux, kk, err, zt, i);
     }
     // the last block to finish advances the global step
     __syncthreads();

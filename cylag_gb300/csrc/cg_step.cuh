@@ -579,7 +579,7 @@ __device__ __forceinline__ void load_zig(ZigTables& zt) {
 // q.e != nullptr (2D): particles leaving their start triangle are queued
 // for walk_kernel instead of walking here.
 // One particle of the step (the body of the particle loop).
-template <int DIM, typename FT, int MODEL>
+template <int DIM, typename FT, int MODEL, int SCHEME = 0>
 __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<FT>& f,
                                               const DevParams& p, DevState& s,
                                               const WalkQueue& wq, int aux, int step_index,
@@ -620,8 +620,8 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
 
     int bnd_j = -1;
     if constexpr (MODEL == 1) bnd_j = q.update_lsm1(dp);
-    else if constexpr (MODEL == 2) bnd_j = update_lsm2(q, dp);
-    else bnd_j = update_lsm3(q, dp);
+    else if constexpr (MODEL == 2) bnd_j = update_lsm2<SCHEME>(q, dp);
+    else bnd_j = update_lsm3<SCHEME>(q, dp);
 
     uint32_t e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
@@ -652,9 +652,11 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
 // wq.e != nullptr (2D): particles leaving their start triangle are queued
 // for walk_kernel instead of walking here.  Persistent grid (one wave of
 // resident blocks) striding over the particles.
-// MODEL: 1, 2 or 3 (LSM1/2/3), one instantiation each so that the LSM1
-// kernels keep their register budget.
-template <int DIM, typename FT, int MODEL = 1>
+// MODEL: 1, 2 or 3 (LSM1/2/3); SCHEME: the LSM2/LSM3 time scheme.  One
+// instantiation per combination, so that each kernel holds one integrator
+// inlined (no particle state in local memory) and the LSM1 kernels keep
+// their register budget.
+template <int DIM, typename FT, int MODEL = 1, int SCHEME = 0>
 __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
@@ -662,7 +664,8 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
     __shared__ ZigTables zt;
     load_zig(zt);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_particle<DIM, FT, MODEL>(m, f, p, s, wq, aux, step_index, stats, err_word, zt, i);
+        step_particle<DIM, FT, MODEL, SCHEME>(m, f, p, s, wq, aux, step_index, stats, err_word,
+                                               zt, i);
 }
 
 // blocks of one wave of resident blocks of `kernel` (persistent grid)
@@ -675,23 +678,44 @@ inline int resident_blocks(K kernel, int bs) {
     return nsm * (per < 1 ? 1 : per);
 }
 
-// step_kernel<DIM, FT, model> over every particle on a persistent grid
+// step_kernel<DIM, FT, 1> (LSM1) over every particle on a persistent grid
 template <int DIM, typename FT>
-void launch_step_kernel(int model, const DevMesh& m, const DevFields<FT>& f, const DevParams& p,
+void launch_lsm1_kernel(const DevMesh& m, const DevFields<FT>& f, const DevParams& p,
                         const DevState& s, const WalkQueue& wq, int aux, int step_index,
                         int* stats, uint32_t* err, cudaStream_t st) {
     const int bs = 256;
     const int need = (s.n + bs - 1) / bs;
     if (need == 0) return;
-    static int wave[3] = {0, 0, 0};
+    static int wave = 0;
+    if (!wave) wave = resident_blocks(step_kernel<DIM, FT, 1>, bs);
+    step_kernel<DIM, FT, 1><<<need < wave ? need : wave, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                      step_index, stats, err);
+}
+
+// step_kernel<DIM, FT, model, time scheme> for LSM2/LSM3 runs (instantiated
+// in cg_lsm23_plain.cu / cg_lsm23_mixed.cu)
+template <int DIM, typename FT>
+void launch_lsm23_kernel(const DevMesh& m, const DevFields<FT>& f, const DevParams& p,
+                         const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
+                         cudaStream_t st) {
+    const int bs = 256;
+    const int need = (s.n + bs - 1) / bs;
+    if (need == 0) return;
+    static int wave[7] = {0, 0, 0, 0, 0, 0, 0};
+    const WalkQueue none{nullptr, nullptr};
     auto go = [&](auto kernel, int idx) {
         if (!wave[idx]) wave[idx] = resident_blocks(kernel, bs);
         int nb = need < wave[idx] ? need : wave[idx];
-        kernel<<<nb, bs, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+        kernel<<<nb, bs, 0, st>>>(m, f, p, s, none, aux, step_index, stats, err);
     };
-    if (model == 1) go(step_kernel<DIM, FT, 1>, 0);
-    else if (model == 2) go(step_kernel<DIM, FT, 2>, 1);
-    else go(step_kernel<DIM, FT, 3>, 2);
+    const int ts = p.time_scheme;
+    if (p.model == 2 && ts == 1) go(step_kernel<DIM, FT, 2, 1>, 0);
+    else if (p.model == 2 && ts == 2) go(step_kernel<DIM, FT, 2, 2>, 1);
+    else if (p.model == 2 && ts == 3) go(step_kernel<DIM, FT, 2, 3>, 2);
+    else if (p.model == 2 && ts == 4) go(step_kernel<DIM, FT, 2, 4>, 3);
+    else if (p.model == 2) go(step_kernel<DIM, FT, 2, 5>, 4);
+    else if (ts == 1) go(step_kernel<DIM, FT, 3, 1>, 5);
+    else go(step_kernel<DIM, FT, 3, 5>, 6);
 }
 
 // Second half of the step for queued (2D) particles: path walk from the
