@@ -68,14 +68,55 @@ __device__ __forceinline__ double lsm2_a1(const DevParams& p, int dim, double dp
     return double(R(p.a1c) * (R(1.5) / d) * Cd * unorm);
 }
 
-template <int DIM, typename FT>
+template <typename FT>
+__host__ __device__ constexpr bool is_mixed() { return std::is_same<FT, float>::value; }
+
+// mean velocity (and, when asked, acceleration) at (k, l, px, py, pz) in the
+// arithmetic V: FP64 interpolation in the plain form, FP32 from the FP32
+// records and barycentrics in the mixed form
+template <typename V, int DIM, typename FT>
 __device__ __forceinline__ void mean_fields(Particle<DIM, FT>& q, int k, int l, double px,
-                                            double py, double pz, bool want_acc, double& ux,
-                                            double& uy, double& uz, double& ax, double& ay,
-                                            double& az) {
-    q.velocity(k, l, px, py, pz, ux, uy, uz);
-    ax = ay = az = 0.;
-    if (want_acc) q.accel(k, l, px, py, pz, ux, uy, uz, ax, ay, az);
+                                            double py, double pz, bool want_acc, V& ux, V& uy,
+                                            V& uz, V& ax, V& ay, V& az) {
+    if constexpr (is_mixed<FT>()) {
+        auto P = q.p1f_at(k, px, py);
+        float u, v, w, a = 0.f, b = 0.f, c = 0.f;
+        q.velocity32(P, l, (float)pz, u, v, w);
+        if (want_acc) q.accel32(P, l, (float)pz, u, v, w, a, b, c);
+        ux = V(u); uy = V(v); uz = V(w);
+        ax = V(a); ay = V(b); az = V(c);
+    } else {
+        double u, v, w, a = 0., b = 0., c = 0.;
+        q.velocity(k, l, px, py, pz, u, v, w);
+        if (want_acc) q.accel(k, l, px, py, pz, u, v, w, a, b, c);
+        ux = V(u); uy = V(v); uz = V(w);
+        ax = V(a); ay = V(b); az = V(c);
+    }
+}
+
+// horizontal localization: the exact predicates in the plain form, the
+// FP32-filtered ones (same decisions) in the mixed form; element -1 (the
+// stage-exit quirk) takes the exact walk in both
+template <int DIM, typename FT>
+__device__ __forceinline__ void localize(Particle<DIM, FT>& q, int k, double p0x, double p0y,
+                                         double x, double y, int& nk, int& bnd) {
+    if constexpr (is_mixed<FT>()) {
+        if (k >= 0) {
+            bnd = -1;
+            Tri32 t = load_tri32(q.m, k);
+            if (in_tri_mixed(q.m, t, k, x, y)) { nk = k; return; }
+            path_walk_mixed(q.m, k, p0x, p0y, x, y, nk, bnd);
+            if (nk == -1 && bnd == -1) nk = grid_locate(q.m, x, y);
+            return;
+        }
+    }
+    xy_localize(q.m, k, p0x, p0y, x, y, nk, bnd);
+}
+
+template <int DIM, typename FT>
+__device__ __forceinline__ int zloc(Particle<DIM, FT>& q, int k, double x, double y, double z) {
+    if constexpr (is_mixed<FT>()) return q.z_localize32(k, x, y, z);
+    else return q.z_localize(k, x, y, z);
 }
 
 // update_state_lsm2.pyx:141-217
@@ -84,7 +125,7 @@ __device__ __forceinline__ void euler_lsm2(Particle<DIM, FT>& q, double dp) {
     const DevParams& p = q.p;
     double dt = p.dt, ux, uy, uz, ax, ay, az;
     double z = DIM == 3 ? q.x[2] : 0.;
-    mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
+    mean_fields<double>(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
     double a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
     q.us[0] = ux;
     q.us[1] = uy;
@@ -118,7 +159,7 @@ __device__ __forceinline__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
     double ux = 0., uy = 0., uz = 0., ax = 0., ay = 0., az = 0., a1 = 0.;
 #pragma unroll
     for (int st = 0; st < NST; ++st) {
-        mean_fields(q, k, l, xs, ys, zs, p.added_mass, ux, uy, uz, ax, ay, az);
+        mean_fields<double>(q, k, l, xs, ys, zs, p.added_mass, ux, uy, uz, ax, ay, az);
         const double cv = st == 0 ? 0. : (st == 1 ? c1 : (st == 2 ? c2 : 1.));
         double vx, vy, vz = 0.;
         if (st == 0) {
@@ -151,8 +192,8 @@ __device__ __forceinline__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
         double zt = DIM == 3 ? q.x[2] + cp * kz[st] : 0.;
         int tt, tl = 0, bnd;
         q.ltri = q.tri;
-        xy_localize(q.m, q.ltri, q.x0[0], q.x0[1], xt, yt, tt, bnd);
-        if (DIM == 3) tl = q.z_localize(tt, xt, yt, zt);
+        localize(q, q.ltri, q.x0[0], q.x0[1], xt, yt, tt, bnd);
+        if (DIM == 3) tl = zloc(q, tt, xt, yt, zt);
         if (bnd != -1 || (DIM == 3 && (tl == -2 || tl == -3))) {
             // Euler step with this stage's U, a and a1 (update_state_lsm2.pyx:315-333)
             q.tri = tt;
@@ -213,11 +254,28 @@ __device__ __forceinline__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
     return -1;
 }
 
+// T_L and eps at the particle from the FP32 records (mixed form)
+template <int DIM, typename FT>
+__device__ __forceinline__ float keps_tml32(Particle<DIM, FT>& q, int k, int l, double px,
+                                            double py, double pz, float& ep) {
+    auto P = q.p1f_at(k, px, py);
+    float kt;
+    q.turb32(P, l, (float)pz, kt, ep);
+    ep = fmaxf(ep, (float)EPSILON);
+    return (kt / ep) / (0.5f + 0.75f * (float)C0KOLM);
+}
+
 // B_k^2 terms of the k-epsilon LSM2 diffusion: T_L and (kt, eps) at the
 // particle (update_state_lsm2.pyx:1161-1173)
 template <int DIM, typename FT>
 __device__ __forceinline__ double keps_tml(Particle<DIM, FT>& q, int k, int l, double px,
                                            double py, double pz, double& ep) {
+    if constexpr (is_mixed<FT>()) {
+        float e;
+        float t = keps_tml32(q, k, l, px, py, pz, e);
+        ep = e;
+        return t;
+    }
     P1 f1 = p1_at(q.m, k, px, py);
     double kt;
     q.turb_q(f1, l, pz, kt, ep);
@@ -232,7 +290,7 @@ __device__ __forceinline__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, doub
     double dt = p.dt, sqrtdt = p.sqrtdt, ux, uy, uz, ax, ay, az;
     const int diffmod = p.diffmod, nuopt = p.nuopt;
     double z = DIM == 3 ? q.x[2] : 0.;
-    mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
+    mean_fields<double>(q, q.tri, q.ll, q.x[0], q.x[1], z, p.added_mass, ux, uy, uz, ax, ay, az);
     double a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
     double xix = 0., xiy = 0., xiz = 0., diffx = 0., diffy = 0., diffz = 0.;
     if (diffmod != 0) {
@@ -328,18 +386,29 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
         up0[d] = q.up[d];
     }
     double z0 = DIM == 3 ? xp0[2] : 0.;
-    double ux, uy, uz, ax, ay, az;
-    mean_fields(q, q.tri, q.ll, xp0[0], xp0[1], z0, p.added_mass, ux, uy, uz, ax, ay, az);
-    const R a1 = R(lsm2_a1<R>(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.));
+    R ux, uy, uz, ax, ay, az;
+    mean_fields<R>(q, q.tri, q.ll, xp0[0], xp0[1], z0, p.added_mass, ux, uy, uz, ax, ay, az);
+    R a1;
+    if constexpr (std::is_same<R, double>::value) {
+        a1 = lsm2_a1<R>(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.);
+    } else {
+        R sx = ux - R(up0[0]), sy = uy - R(up0[1]), sz = DIM == 3 ? uz - R(up0[2]) : R(0.);
+        R unorm = fmax(R(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
+        a1 = R(p.a1c) * (R(1.5) / R(dp)) * drag_coefficient<R>(p, unorm, R(dp)) * unorm;
+    }
     const R rdt = R(dt);
     Lsm2Coef<R> c;
     if (!lsm2_direct_coefficients<R>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return; }
     R um_beta = -expm1(-a1 * rdt);
     R b2[3] = {R(0.), R(0.), R(0.)};
     if (diffmod == 2 || diffmod == 3) {
-        double epd;
-        const R tml = R(keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, epd));
-        const R ep = R(epd), rnuz = R(nuz);
+        R tml, ep;
+        if constexpr (std::is_same<R, double>::value) {
+            tml = keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
+        } else {
+            tml = keps_tml32(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
+        }
+        const R rnuz = R(nuz);
         b2[0] = a1 * a1 * R(C0KOLM) * ep * (tml * tml);
         b2[1] = b2[0];
         if (diffmod == 2) b2[2] = nuopt == 2 ? rnuz * rnuz : R(2.) * rnuz * a1 * a1;
@@ -356,14 +425,14 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
             b2[2] = R(2.) * rnuz * a1 * a1;
         }
     }
-    const double mu[3] = {ux, uy, uz};
-    const double acc[3] = {ax, ay, az};
+    const R mu[3] = {ux, uy, uz};
+    const R acc[3] = {ax, ay, az};
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        const R u_k = R(mu[d]);
-        const R Fp = d == 2 ? R(p.a2c) * R(acc[2]) - R(GRAV) * R(p.a0c) : R(p.a2c) * R(acc[d]);
+        const R u_k = mu[d];
+        const R Fp = d == 2 ? R(p.a2c) * acc[2] - R(GRAV) * R(p.a0c) : R(p.a2c) * acc[d];
         const R v0 = R(up0[d]);
-        q.us[d] = mu[d];
+        q.us[d] = double(mu[d]);
         R Gp = R(0.), Gx = R(0.);
         const bool noise = !(b2[d] == R(0.) || dt == 0.);
         if (noise) {
@@ -401,7 +470,12 @@ __device__ __forceinline__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
         else if constexpr (SCHEME == 3) bnd_j = rk_lsm2<3>(q, dp);
         else if constexpr (SCHEME == 4) bnd_j = rk_lsm2<4>(q, dp);
         else di_lsm2(q, dp, 0, 0., 0., 2);
-        if (diffmod != 0) q.diffusion_lsm1(p1_at(q.m, q.tri0, q.x0[0], q.x0[1]));
+        if (diffmod != 0) {
+            // K and its gradient at the start point only for the k-epsilon models
+            P1 q0{};
+            if (diffmod == 2 || diffmod == 3) q0 = p1_at(q.m, q.tri0, q.x0[0], q.x0[1]);
+            q.diffusion_lsm1(q0);
+        }
     } else if constexpr (SCHEME == 1) {
         euler_maruyama_lsm2_u(q, dp);
     } else if constexpr (SCHEME == 5) {
@@ -412,8 +486,8 @@ __device__ __forceinline__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
     }
     (void)bnd_j;
     q.ltri = q.tri;
-    xy_localize(q.m, q.ltri, q.x0[0], q.x0[1], q.x[0], q.x[1], q.tri, bnd_j);
-    if (DIM == 3) q.ll = q.z_localize(q.tri, q.x[0], q.x[1], q.x[2]);
+    localize(q, q.ltri, q.x0[0], q.x0[1], q.x[0], q.x[1], q.tri, bnd_j);
+    if (DIM == 3) q.ll = zloc(q, q.tri, q.x[0], q.x[1], q.x[2]);
     return bnd_j;
 }
 
@@ -778,7 +852,7 @@ __device__ __forceinline__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double
     double dt = p.dt, sqrtdt = p.sqrtdt, ux, uy, uz, ax, ay, az;
     const int diffmod = p.diffmod;
     double z = DIM == 3 ? q.x[2] : 0.;
-    mean_fields(q, q.tri, q.ll, q.x[0], q.x[1], z, true, ux, uy, uz, ax, ay, az);
+    mean_fields<double>(q, q.tri, q.ll, q.x[0], q.x[1], z, true, ux, uy, uz, ax, ay, az);
     using R = typename ArithOf<FT>::type;
     const double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(q.us, q.up)));
     const double a1 = double(lsm3_a1<R>(p, R(dp), R(unorm)));
@@ -842,16 +916,26 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
         us0[d] = q.us[d];
     }
     double z0 = DIM == 3 ? xp0[2] : 0.;
-    double ux, uy, uz, ax, ay, az, ep = 0., tml_ke = 0.;
-    mean_fields(q, q.tri, q.ll, xp0[0], xp0[1], z0, true, ux, uy, uz, ax, ay, az);
-    if (diffmod == 2 || diffmod == 3) tml_ke = keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
-    double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(us0, up0)));
-    const R a1 = lsm3_a1<R>(p, R(dp), R(unorm));
+    R ux, uy, uz, ax, ay, az, ep = R(0.), tml_ke = R(0.);
+    mean_fields<R>(q, q.tri, q.ll, xp0[0], xp0[1], z0, true, ux, uy, uz, ax, ay, az);
+    if (diffmod == 2 || diffmod == 3) {
+        if constexpr (exact) tml_ke = keps_tml(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
+        else tml_ke = keps_tml32(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
+    }
+    R unorm;
+    if constexpr (exact) {
+        unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(us0, up0)));
+    } else {
+        R sx = R(us0[0]) - R(up0[0]), sy = R(us0[1]) - R(up0[1]);
+        R sz = DIM == 3 ? R(us0[2]) - R(up0[2]) : R(0.);
+        unorm = fmax(R(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
+    }
+    const R a1 = lsm3_a1<R>(p, R(dp), unorm);
     const R a2 = p.added_mass ? R(p.a2c) : R(0.);
     R tl_h = R(p.tl_h), tl_v = R(p.tl_v), sigma_h, sigma_v = R(0.);
     if (diffmod == 2 || diffmod == 3) {
-        tl_h = R(fmax(EPSILON_LSM3, tml_ke));
-        sigma_h = sqrt(R(C0KOLM) * R(ep));
+        tl_h = fmax(R(EPSILON_LSM3), tml_ke);
+        sigma_h = sqrt(R(C0KOLM) * ep);
     } else {
         sigma_h = sqrt(R(2.) * R(p.nux)) / tl_h;
     }
@@ -863,7 +947,7 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
             sigma_v = sqrt(R(2.) * R(p.nuz)) / tl_v;
         }
     }
-    const double mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
+    const R mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
     Lsm3Coef<R> c;
     R lower[9];
     if (!lsm3_coefficients<R>(a1, a2, tl_h, R(dt), edge_opt, c)) { q.err |= ERR_NONFINITE; return; }
@@ -883,7 +967,7 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
                 factored = false;
             }
         }
-        const R u_k = R(mean_flow[d]), acc = R(mean_acc[d]);
+        const R u_k = mean_flow[d], acc = mean_acc[d];
         const R Fp = d == 2 ? -R(GRAV) * R(p.a0c) : R(0.);
         const R s0 = R(us0[d]);
         const R ur0 = exact ? R(up0[d] - a2 * us0[d]) : R(up0[d]) - a2 * s0;
@@ -935,8 +1019,8 @@ __device__ __forceinline__ int update_lsm3(Particle<DIM, FT>& q, double dp) {
     else { q.err |= ERR_UNSUPPORTED; return -1; }
     int bnd_j;
     q.ltri = q.tri;
-    xy_localize(q.m, q.ltri, q.x0[0], q.x0[1], q.x[0], q.x[1], q.tri, bnd_j);
-    if (DIM == 3) q.ll = q.z_localize(q.tri, q.x[0], q.x[1], q.x[2]);
+    localize(q, q.ltri, q.x0[0], q.x0[1], q.x[0], q.x[1], q.tri, bnd_j);
+    if (DIM == 3) q.ll = zloc(q, q.tri, q.x[0], q.x[1], q.x[2]);
     return bnd_j;
 }
 

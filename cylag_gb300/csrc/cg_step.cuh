@@ -259,6 +259,158 @@ struct Particle {
         az = dwdt + ua * dwdx + va * dwdy + wa * dwdz;
     }
 
+    // ---- FP32 field access of the mixed LSM2/LSM3 form ------------------------------
+    // P1 weights from the FP32 offset to the triangle's anchor vertex and the
+    // FP32 gradients of its packed record (no FP64 arithmetic).
+    struct P1f {
+        int i0, i1, i2;
+        float f0, f1, f2, gx0, gx1, gx2, gy0, gy1, gy2;
+    };
+    __device__ P1f p1f_at(int k, double px, double py) const {
+        Tri32 t = load_tri32(m, k);
+        Bary b = bary32(t, px, py);
+        P1f r;
+        r.i0 = t.tv.x; r.i1 = t.tv.y; r.i2 = t.tv.z;
+        r.f0 = b.l0; r.f1 = b.l1; r.f2 = b.l2;
+        r.gx0 = t.g0.x; r.gx1 = t.g0.y; r.gx2 = t.g0.z;
+        r.gy0 = t.g0.w; r.gy1 = t.g1.x; r.gy2 = t.g1.y;
+        return r;
+    }
+    __device__ float nf(const FT* fld, int node, int slot) const {
+        return (float)fld[(size_t)node * Slots<DIM>::NF + slot];
+    }
+    __device__ float ev(const FT* fld, int off, const P1f& q, int slot) const {
+        return nf(fld, off + q.i0, slot) * q.f0 + nf(fld, off + q.i1, slot) * q.f1 +
+               nf(fld, off + q.i2, slot) * q.f2;
+    }
+    // 2D / prism velocity (eulerian_field_set.pyx:1057-1115, 1289-1394)
+    __device__ void velocity32(const P1f& q, int l, float pz, float& ux, float& uy, float& uz) {
+        using S = Slots<DIM>;
+        if (DIM == 2) {
+            ux = ev(f.cur, 0, q, S::UX);
+            uy = ev(f.cur, 0, q, S::UY);
+            uz = 0.f;
+            return;
+        }
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ux = uy = uz = 0.f; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        float zlp = ev(f.cur, jl, q, S::ZS), zup = ev(f.cur, ju, q, S::ZS);
+        float dz = zlp - zup;
+        if (!(fabsf(dz) >= (float)EPSILON)) { err |= ERR_DEGENERATE_LAYER; ux = uy = uz = 0.f; return; }
+        float zf0 = (pz - zup) / dz, zf1 = (zlp - pz) / dz;
+        ux = zf0 * ev(f.cur, jl, q, S::UX) + zf1 * ev(f.cur, ju, q, S::UX);
+        uy = zf0 * ev(f.cur, jl, q, S::UY) + zf1 * ev(f.cur, ju, q, S::UY);
+        uz = zf0 * ev(f.cur, jl, q, Slots<3>::UZ) + zf1 * ev(f.cur, ju, q, Slots<3>::UZ);
+    }
+    // k and eps (2D P1, 3D prism)
+    __device__ void turb32(const P1f& q, int l, float pz, float& kt, float& ep) {
+        const FT* t = f.turb;
+        auto tv = [&](int off, int c) {
+            return (float)t[2 * (size_t)(off + q.i0) + c] * q.f0 +
+                   (float)t[2 * (size_t)(off + q.i1) + c] * q.f1 +
+                   (float)t[2 * (size_t)(off + q.i2) + c] * q.f2;
+        };
+        if (DIM == 2) {
+            kt = tv(0, 0);
+            ep = tv(0, 1);
+            return;
+        }
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; kt = ep = 0.f; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        float zlp = ev(f.cur, jl, q, Slots<DIM>::ZS), zup = ev(f.cur, ju, q, Slots<DIM>::ZS);
+        float dz = zlp - zup;
+        if (!(fabsf(dz) >= (float)EPSILON)) { err |= ERR_DEGENERATE_LAYER; kt = ep = 0.f; return; }
+        float zf0 = (pz - zup) / dz, zf1 = (zlp - pz) / dz;
+        kt = zf0 * tv(jl, 0) + zf1 * tv(ju, 0);
+        ep = zf0 * tv(jl, 1) + zf1 * tv(ju, 1);
+    }
+    __device__ void prism_vg32(const FT* fld, int jl, int ju, int slot, const P1f& q, float s_,
+                               float dz, float zlx, float zly, float zux, float zuy, float& val,
+                               float& ddx, float& ddy, float& ddz) {
+        float a0 = nf(fld, jl + q.i0, slot), a1 = nf(fld, jl + q.i1, slot), a2 = nf(fld, jl + q.i2, slot);
+        float b0 = nf(fld, ju + q.i0, slot), b1 = nf(fld, ju + q.i1, slot), b2 = nf(fld, ju + q.i2, slot);
+        float fl = a0 * q.f0 + a1 * q.f1 + a2 * q.f2;
+        float fu = b0 * q.f0 + b1 * q.f1 + b2 * q.f2;
+        float gxl = a0 * q.gx0 + a1 * q.gx1 + a2 * q.gx2, gyl = a0 * q.gy0 + a1 * q.gy1 + a2 * q.gy2;
+        float gxu = b0 * q.gx0 + b1 * q.gx1 + b2 * q.gx2, gyu = b0 * q.gy0 + b1 * q.gy1 + b2 * q.gy2;
+        float dfdz = (fu - fl) / dz;
+        val = (1.f - s_) * fl + s_ * fu;
+        ddx = (1.f - s_) * gxl + s_ * gxu - dfdz * ((1.f - s_) * zlx + s_ * zux);
+        ddy = (1.f - s_) * gyl + s_ * gyu - dfdz * ((1.f - s_) * zly + s_ * zuy);
+        ddz = dfdz;
+    }
+    // dU/dt along a path (eulerian_field_set.pyx:1396-1579) in FP32
+    __device__ void accel32(const P1f& q, int l, float pz, float ua, float va, float wa,
+                            float& ax, float& ay, float& az) {
+        const float dt = (float)p.dt;
+        if (DIM == 2) {
+            using S = Slots<2>;
+            float u0 = nf(f.cur, q.i0, S::UX), u1 = nf(f.cur, q.i1, S::UX), u2 = nf(f.cur, q.i2, S::UX);
+            float v0 = nf(f.cur, q.i0, S::UY), v1 = nf(f.cur, q.i1, S::UY), v2 = nf(f.cur, q.i2, S::UY);
+            float dudx = u0 * q.gx0 + u1 * q.gx1 + u2 * q.gx2, dudy = u0 * q.gy0 + u1 * q.gy1 + u2 * q.gy2;
+            float dvdx = v0 * q.gx0 + v1 * q.gx1 + v2 * q.gx2, dvdy = v0 * q.gy0 + v1 * q.gy1 + v2 * q.gy2;
+            float dudt = 0.f, dvdt = 0.f;
+            if (f.prev_valid) {
+                dudt = ((u0 - nf(f.prev, q.i0, S::UX)) * q.f0 + (u1 - nf(f.prev, q.i1, S::UX)) * q.f1 +
+                        (u2 - nf(f.prev, q.i2, S::UX)) * q.f2) / dt;
+                dvdt = ((v0 - nf(f.prev, q.i0, S::UY)) * q.f0 + (v1 - nf(f.prev, q.i1, S::UY)) * q.f1 +
+                        (v2 - nf(f.prev, q.i2, S::UY)) * q.f2) / dt;
+            }
+            ax = dudt + ua * dudx + va * dudy;
+            ay = dvdt + ua * dvdx + va * dvdy;
+            az = 0.f;
+            return;
+        }
+        using S = Slots<3>;
+        if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ax = ay = az = 0.f; return; }
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+        float e0 = nf(f.cur, jl + q.i0, S::ZS), e1 = nf(f.cur, jl + q.i1, S::ZS), e2 = nf(f.cur, jl + q.i2, S::ZS);
+        float h0 = nf(f.cur, ju + q.i0, S::ZS), h1 = nf(f.cur, ju + q.i1, S::ZS), h2 = nf(f.cur, ju + q.i2, S::ZS);
+        float zlp = e0 * q.f0 + e1 * q.f1 + e2 * q.f2, zup = h0 * q.f0 + h1 * q.f1 + h2 * q.f2;
+        float dz = zup - zlp;
+        if (!(fabsf(dz) >= (float)EPSILON)) { err |= ERR_DEGENERATE_LAYER; ax = ay = az = 0.f; return; }
+        float s_ = (pz - zlp) / dz;
+        float zlx = e0 * q.gx0 + e1 * q.gx1 + e2 * q.gx2, zly = e0 * q.gy0 + e1 * q.gy1 + e2 * q.gy2;
+        float zux = h0 * q.gx0 + h1 * q.gx1 + h2 * q.gx2, zuy = h0 * q.gy0 + h1 * q.gy1 + h2 * q.gy2;
+        float un, dudx, dudy, dudz, vn, dvdx, dvdy, dvdz, wn, dwdx, dwdy, dwdz, t0, t1, t2, t3;
+        prism_vg32(f.cur, jl, ju, S::UX, q, s_, dz, zlx, zly, zux, zuy, un, dudx, dudy, dudz);
+        prism_vg32(f.cur, jl, ju, S::UY, q, s_, dz, zlx, zly, zux, zuy, vn, dvdx, dvdy, dvdz);
+        prism_vg32(f.cur, jl, ju, S::UZ, q, s_, dz, zlx, zly, zux, zuy, wn, dwdx, dwdy, dwdz);
+        float dudt = 0.f, dvdt = 0.f, dwdt = 0.f;
+        if (f.prev_valid) {
+            prism_vg32(f.prev, jl, ju, S::UX, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dudt = (un - t0) / dt;
+            prism_vg32(f.prev, jl, ju, S::UY, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dvdt = (vn - t0) / dt;
+            prism_vg32(f.prev, jl, ju, S::UZ, q, s_, dz, zlx, zly, zux, zuy, t0, t1, t2, t3);
+            dwdt = (wn - t0) / dt;
+        }
+        ax = dudt + ua * dudx + va * dudy + wa * dudz;
+        ay = dvdt + ua * dvdx + va * dvdy + wa * dvdz;
+        az = dwdt + ua * dwdx + va * dwdy + wa * dwdz;
+    }
+    // layer of (px, py, pz) in element k from FP32 bed/surface elevations
+    // (eulerian_field_set.pyx:1117-1182)
+    __device__ int z_localize32(int k, double px, double py, double pz) {
+        if (k == -1) return PART_LOC_O;
+        P1f q = p1f_at(k, px, py);
+        int nl = f.nlayers;
+        float zbp = ev(f.cur, 0, q, Slots<DIM>::ZS);
+        float zsp = ev(f.cur, (nl - 1) * f.npoints, q, Slots<DIM>::ZS);
+        float z = (float)pz;
+        int l = 0;
+        if (nl > 1) {
+            float hl = (zsp - zbp) / (float)(nl - 1);
+            if (hl > 0.f) {
+                float fi = floorf((z - zbp) / hl);
+                l = !(fi >= 0.f) ? 0 : (!(fi <= (float)(nl - 2)) ? nl - 2 : (int)fi);
+            }
+        }
+        if (z < zbp) l = PART_LOC_B;
+        else if (z > zsp) l = PART_LOC_A;
+        return l;
+    }
+
     // ---- LSM1 (cylag/lsm/update_state_lsm1.pyx) ----------------------------------
     __device__ void set_up_us(double ux, double uy, double uz) {
         up[0] = ux; up[1] = uy; us[0] = ux; us[1] = uy;
