@@ -5,6 +5,7 @@
 // (SimuTime and the field time-interpolation record, cylag/core/simutime.pyx
 // and cylag/core/eulerian_field_set.pyx:845-938), kernel launches and error
 // reporting.  No exception leaves this file.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -463,16 +464,28 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     // deferred 2D walk: LSM1 (its queue entry carries no velocities)
     bool use_queue = c->fdim == 2 && s->n > 0 && p->model == 1;
     size_t queue_bytes = use_queue ? 256 + (size_t)s->n * sizeof(WalkEntry) : 0;
-    // element sort: 2D runs, keys nt + 1 <= 4096 scan tiles of 4096
-    int nkeys = c->mesh.nt + 1;
-    bool use_sort = p->sort_period > 0 && c->fdim == 2 && s->n > 0 &&
-                    scan_scratch_ints(nkeys) <= 4096;
+    // element sort: keys tri * layers + layer (+1 for inactive) within 4096
+    // scan tiles of 4096; the optional working arrays are those the model
+    // reads every step
+    const int nl_key = c->fdim == 3 ? (c->nlayers > 1 ? c->nlayers - 1 : 1) : 1;
+    const int64_t nkeys64 = (int64_t)c->mesh.nt * nl_key + 1;
+    bool use_sort = p->sort_period > 0 && s->n > 0 && nkeys64 < (1ll << 31) &&
+                    scan_scratch_ints((int)std::min<int64_t>(nkeys64, 1ll << 30)) <= 4096;
+    const int nkeys = (int)std::min<int64_t>(nkeys64, 1ll << 30);
+    int work = 0;
+    if (p->model >= 2) work |= W_VEL | W_DIAM;
+    if (p->model == 3) work |= W_FVS;
+    if (p->dim == 3) work |= W_LAYER | W_DIAM;
     size_t n = (size_t)s->n;
+    const int D = p->dim;
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t sort_bytes = 0;
     size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0};
-    const size_t work_bytes = ((n * 16 + 255) & ~(size_t)255) + 4 * ((n * 8 + 255) & ~(size_t)255);
+    const size_t work_bytes = al(n * 8 * D) + 4 * al(n * 8) +
+                              ((work & W_VEL) ? al(n * 8 * D) : 0) +
+                              ((work & W_FVS) ? al(n * 8 * D) : 0) +
+                              ((work & W_LAYER) ? al(n * 4) : 0) + ((work & W_DIAM) ? al(n * 8) : 0);
     if (use_sort) {
-        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
         off_sums = al((size_t)nkeys * 4);
         off_perm = al(off_sums + (size_t)scan_scratch_ints(nkeys) * 4);
         off_w[0] = al(off_perm + n * 4);
@@ -501,22 +514,25 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->use_queue = use_queue;
     if (use_sort) {
         char* b = (char*)r->sortbuf.p;
-        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
         r->sb.count = (int*)b;
         r->sb.block_sums = (int*)(b + off_sums);
         r->sb.perm = (int*)(b + off_perm);
+        r->sb.dim = D;
+        r->sb.nl = nl_key;
+        r->sb.work = work;
         WorkState* ws[2] = {&r->sb.a, &r->sb.b};
         for (int k = 0; k < 2; ++k) {
             char* w = b + off_w[k];
-            ws[k]->pos = (double2*)w;
-            w += al(n * 16);
-            ws[k]->rng = (unsigned long long*)w;
-            w += al(n * 8);
-            ws[k]->tri = (int*)w;
-            w += al(n * 8);
-            ws[k]->tag = (int*)w;
-            w += al(n * 8);
-            ws[k]->slot = (int*)w;
+            auto take = [&](size_t bytes) { char* q = w; w += al(bytes); return q; };
+            ws[k]->pos = (double*)take(n * 8 * D);
+            ws[k]->rng = (unsigned long long*)take(n * 8);
+            ws[k]->tri = (int*)take(n * 8);
+            ws[k]->tag = (int*)take(n * 8);
+            ws[k]->slot = (int*)take(n * 8);
+            ws[k]->vel = (work & W_VEL) ? (double*)take(n * 8 * D) : nullptr;
+            ws[k]->fvs = (work & W_FVS) ? (double*)take(n * 8 * D) : nullptr;
+            ws[k]->layer = (work & W_LAYER) ? (int*)take(n * 4) : nullptr;
+            ws[k]->diam = (work & W_DIAM) ? (double*)take(n * 8) : nullptr;
         }
         r->sort_period = p->sort_period;
     }
@@ -672,11 +688,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             if (s == 0) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
             else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
             launches += 6;   // histogram, 3 scan passes, index scatter, gather
-            ws.pos = (double*)r->sb.a.pos;
-            ws.tri = r->sb.a.tri;
-            ws.tag = r->sb.a.tag;
-            ws.rng = (uint64_t*)r->sb.a.rng;
-            ws.slot = r->sb.a.slot;
+            ws = sorted_view(r->st, r->sb);
         }
         const DevState& run_state = sorted ? ws : r->st;
         // solver.pyx:440: fields at the step-start time

@@ -117,9 +117,18 @@ struct DevState {
     uint64_t* __restrict__ rng;
     // sorted runs: pos/tri/tag/rng are working copies in sorted order and
     // slot[i] is the caller's index of working particle i, where the
-    // remaining arrays (velocities, last_*, diameter, lowerlayer) live
+    // remaining arrays live, except those flagged in `work` (W_*), which are
+    // working copies too (indexed by i)
     const int* __restrict__ slot;
+    int work;
 };
+
+constexpr int W_VEL = 1, W_FVS = 2, W_LAYER = 4, W_DIAM = 8;
+
+// index of particle i in an array that is a working copy when `flag` is set
+__device__ __forceinline__ int widx(const DevState& s, int i, int a, int flag) {
+    return (s.work & flag) ? i : a;
+}
 
 __device__ __forceinline__ int aux_index(const DevState& s, int i) {
     return s.slot ? __ldg(&s.slot[i]) : i;

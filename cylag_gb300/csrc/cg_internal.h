@@ -99,19 +99,29 @@ void launch_serve_mixed(int grid, const DevMesh& m, const FieldView& fv, const D
                         const ServeRun* runs, const int2* active, const int* nactive,
                         ServeClock* clk, uint32_t* run_err, cudaStream_t st);
 
-// Working copies of the per-step state in element order (cg_sort.cu).
+// Working copies of the per-step state in element order (cg_sort.cu):
+// always position, tri, tag, PCG32 state and the caller slot; velocity,
+// fluid velocity seen, layer and diameter as well when the model reads them
+// every step (nullptr otherwise: reached through slot).
 struct WorkState {
-    double2* pos;             // [n]
+    double* pos;              // [n][dim]
     int* tri;                 // [n]
     int* tag;                 // [n]
     unsigned long long* rng;  // [n]
     int* slot;                // [n] caller index of each working particle
+    double* vel;              // [n][dim] or nullptr
+    double* fvs;              // [n][dim] or nullptr
+    int* layer;               // [n] or nullptr
+    double* diam;             // [n] or nullptr
 };
 struct SortBuffers {
-    int* count;          // [nt + 1] histogram, then scan offsets
-    int* block_sums;     // [scan_scratch_ints(nt + 1)]
+    int* count;          // [nkeys] histogram, then scan offsets
+    int* block_sums;     // [scan_scratch_ints(nkeys)]
     int* perm;           // [n] new order -> old order
     WorkState a, b;      // current and spare working copies
+    int dim;             // 2 or 3
+    int nl;              // layers per column (1 in 2D): key = tri * nl + layer
+    int work;            // W_* flags of the optional arrays
 };
 int scan_scratch_ints(int nkeys);
 // caller arrays -> b.a in element order
@@ -120,6 +130,8 @@ void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream
 void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st);
 // b.a -> caller arrays
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st);
+// the run's state with the working copies of b.a in place of the caller's
+DevState sorted_view(const DevState& user, const SortBuffers& b);
 
 // rng[i] = pcg32_seed(seed, tag[i])
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);

@@ -10,8 +10,8 @@
 // caller's slots when it returns.  Every per-particle computation is
 // independent of the order, so results do not depend on the sort.
 //
-// Counting sort on the key tri (inactive and uninitialized particles, tri <
-// 0, get the key nt and go last):
+// Counting sort on the key tri (in 3D tri * layers + layer; inactive and
+// uninitialized particles, tri < 0, get the last key):
 //   1. histogram of the keys (global atomics),
 //   2. exclusive scan of the nt+1 counts (warp-shuffle block scans, then a
 //      scan of the block sums, then the carry-in),
@@ -25,11 +25,18 @@ constexpr int SCAN_BLOCK = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
 
-__device__ __forceinline__ int sort_key(int tri, int nt) { return tri >= 0 ? tri : nt; }
+// key of a particle: its element (and, in 3D, its layer within the
+// column); inactive and uninitialized particles (tri < 0) go last
+__device__ __forceinline__ int sort_key(int tri, int layer, int nt, int nl) {
+    if (tri < 0) return nt * nl;
+    int l = layer < 0 ? 0 : (layer >= nl ? nl - 1 : layer);
+    return tri * nl + l;
+}
 
-__global__ void hist_kernel(const int* __restrict__ tri, int n, int nt, int* __restrict__ count) {
+__global__ void hist_kernel(const int* __restrict__ tri, const int* __restrict__ layer, int n,
+                            int nt, int nl, int* __restrict__ count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&count[sort_key(__ldg(&tri[i]), nt)], 1);
+    if (i < n) atomicAdd(&count[sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl)], 1);
 }
 
 // inclusive warp scan
@@ -108,71 +115,96 @@ __global__ void add_carry_kernel(int* __restrict__ v, int n, const int* __restri
     if (i < n) v[i] += sums[i / SCAN_TILE];
 }
 
-__global__ void scatter_index_kernel(const int* __restrict__ tri, int n, int nt,
-                                     int* __restrict__ offset, int* __restrict__ perm) {
+__global__ void scatter_index_kernel(const int* __restrict__ tri, const int* __restrict__ layer,
+                                     int n, int nt, int nl, int* __restrict__ offset,
+                                     int* __restrict__ perm) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) perm[atomicAdd(&offset[sort_key(__ldg(&tri[i]), nt)], 1)] = i;
+    if (i < n)
+        perm[atomicAdd(&offset[sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl)],
+                       1)] = i;
+}
+
+template <typename T>
+__device__ __forceinline__ void move_rows(const T* __restrict__ src, T* __restrict__ dst, int from,
+                                          int to, int dim) {
+    for (int d = 0; d < dim; ++d) dst[(size_t)to * dim + d] = __ldcs(src + (size_t)from * dim + d);
 }
 
 // dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays
 __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src, WorkState dst,
-                                    int n) {
+                                    int n, int dim) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&perm[j]);
-    dst.pos[j] = __ldcs(src.pos + i);
+    move_rows(src.pos, dst.pos, i, j, dim);
     dst.tri[j] = __ldcs(src.tri + i);
     dst.tag[j] = __ldcs(src.tag + i);
     dst.rng[j] = __ldcs(src.rng + i);
     dst.slot[j] = src.slot ? __ldcs(src.slot + i) : i;
+    if (dst.vel) move_rows(src.vel, dst.vel, i, j, dim);
+    if (dst.fvs) move_rows(src.fvs, dst.fvs, i, j, dim);
+    if (dst.layer) dst.layer[j] = __ldcs(src.layer + i);
+    if (dst.diam) dst.diam[j] = __ldcs(src.diam + i);
 }
 
 // caller[slot[j]] = work[j]
-__global__ void scatter_state_kernel(WorkState w, WorkState user, int n) {
+__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&w.slot[j]);
-    __stcs(user.pos + i, w.pos[j]);
+    for (int d = 0; d < dim; ++d) __stcs(user.pos + (size_t)i * dim + d, w.pos[(size_t)j * dim + d]);
     __stcs(user.tri + i, w.tri[j]);
     __stcs(user.tag + i, w.tag[j]);
     __stcs(user.rng + i, w.rng[j]);
+    if (w.vel)
+        for (int d = 0; d < dim; ++d) __stcs(user.vel + (size_t)i * dim + d, w.vel[(size_t)j * dim + d]);
+    if (w.fvs)
+        for (int d = 0; d < dim; ++d) __stcs(user.fvs + (size_t)i * dim + d, w.fvs[(size_t)j * dim + d]);
+    if (w.layer) __stcs(user.layer + i, w.layer[j]);
+    if (w.diam) __stcs(user.diam + i, w.diam[j]);
 }
 
 int scan_scratch_ints(int nkeys) { return (nkeys + SCAN_TILE - 1) / SCAN_TILE; }
 
-static void sort_perm(const int* tri, int n, int nt, SortBuffers& b, cudaStream_t st) {
-    int nkeys = nt + 1;
+static void sort_perm(const int* tri, const int* layer, int n, int nt, SortBuffers& b,
+                      cudaStream_t st) {
+    int nkeys = nt * b.nl + 1;
     int bs = 256;
     cudaMemsetAsync(b.count, 0, (size_t)nkeys * sizeof(int), st);
-    hist_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, n, nt, b.count);
+    hist_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, layer, n, nt, b.nl, b.count);
     int ntiles = scan_scratch_ints(nkeys);
     scan_tiles_kernel<<<ntiles, SCAN_BLOCK, 0, st>>>(b.count, nkeys, b.block_sums);
     scan_sums_kernel<<<1, SCAN_BLOCK, 0, st>>>(b.block_sums, ntiles);
     add_carry_kernel<<<(nkeys + bs - 1) / bs, bs, 0, st>>>(b.count, nkeys, b.block_sums);
-    scatter_index_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, n, nt, b.count, b.perm);
+    scatter_index_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, layer, n, nt, b.nl, b.count, b.perm);
 }
 
-static WorkState user_view(const DevState& u) {
+// the caller's arrays seen as a working state (only those kept in b.a)
+static WorkState user_view(const DevState& u, const SortBuffers& b) {
     WorkState w;
-    w.pos = reinterpret_cast<double2*>(u.pos);
+    w.pos = u.pos;
     w.tri = u.tri;
     w.tag = u.tag;
     w.rng = reinterpret_cast<unsigned long long*>(u.rng);
     w.slot = nullptr;
+    w.vel = (b.work & W_VEL) ? u.vel : nullptr;
+    w.fvs = (b.work & W_FVS) ? u.fvs : nullptr;
+    w.layer = (b.work & W_LAYER) ? u.lowerlayer : nullptr;
+    w.diam = (b.work & W_DIAM) ? u.diameter : nullptr;
     return w;
 }
 
 void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream_t st) {
     int n = user.n;
     if (n == 0) return;
-    sort_perm(user.tri, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user), b.a, n);
+    sort_perm(user.tri, (b.work & W_LAYER) ? user.lowerlayer : nullptr, n, nt, b, st);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user, b), b.a, n, b.dim);
 }
 
 void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
     if (n == 0) return;
-    sort_perm(b.a.tri, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n);
+    sort_perm(b.a.tri, b.a.layer, n, nt, b, st);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim);
     WorkState t = b.a;
     b.a = b.b;
     b.b = t;
@@ -181,7 +213,22 @@ void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st) {
     int n = user.n;
     if (n == 0) return;
-    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user), n);
+    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user, b), n, b.dim);
+}
+
+DevState sorted_view(const DevState& user, const SortBuffers& b) {
+    DevState w = user;
+    w.pos = b.a.pos;
+    w.tri = b.a.tri;
+    w.tag = b.a.tag;
+    w.rng = reinterpret_cast<uint64_t*>(b.a.rng);
+    w.slot = b.a.slot;
+    if (b.a.vel) w.vel = b.a.vel;
+    if (b.a.fvs) w.fvs = b.a.fvs;
+    if (b.a.layer) w.lowerlayer = b.a.layer;
+    if (b.a.diam) w.diameter = b.a.diam;
+    w.work = b.work;
+    return w;
 }
 
 }  // namespace cg

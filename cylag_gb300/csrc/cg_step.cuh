@@ -567,19 +567,21 @@ struct Particle {
     __device__ void store(DevState& s, int i, int aux, int step_index, const double* lastv) {
         const int D = DIM;
         const int a = aux_index(s, i);   // slot of the per-particle arrays outside the sort
+        const int iv = widx(s, i, a, W_VEL), iu = widx(s, i, a, W_FVS);
+        const int il = widx(s, i, a, W_LAYER), id = widx(s, i, a, W_DIAM);
         if (deleted) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.pos[(size_t)i * D + d] = 0.;
-                s.vel[(size_t)a * D + d] = 0.;
-                s.fvs[(size_t)a * D + d] = 0.;
+                s.vel[(size_t)iv * D + d] = 0.;
+                s.fvs[(size_t)iu * D + d] = 0.;
                 s.last_pos[(size_t)a * D + d] = 0.;
                 s.last_vel[(size_t)a * D + d] = 0.;
             }
-            s.diameter[a] = 0.;
+            s.diameter[id] = 0.;
             s.tri[i] = -1;
             s.last_tri[a] = -1;
-            s.lowerlayer[a] = 0;
+            s.lowerlayer[il] = 0;
             s.tag[i] = -2 - step_index;
             s.rng[i] = rng.state;
             return;
@@ -587,15 +589,15 @@ struct Particle {
 #pragma unroll
         for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = x[d];
         s.tri[i] = tri;
-        if (DIM == 3) s.lowerlayer[a] = ll;
+        if (DIM == 3) s.lowerlayer[il] = ll;
         s.rng[i] = rng.state;
         if (p.model >= 2 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.vel[(size_t)a * D + d] = up[d];
+            for (int d = 0; d < D; ++d) s.vel[(size_t)iv * D + d] = up[d];
         }
         if (p.model == 3 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.fvs[(size_t)a * D + d] = us[d];
+            for (int d = 0; d < D; ++d) s.fvs[(size_t)iu * D + d] = us[d];
         }
         if (aux >= 2) {
 #pragma unroll
@@ -746,7 +748,7 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
     q.tri0 = tri;
     q.ltri = tri;
     const int ai = aux_index(s, i);
-    q.ll = DIM == 3 ? s.lowerlayer[ai] : 0;
+    q.ll = DIM == 3 ? s.lowerlayer[widx(s, i, ai, W_LAYER)] : 0;
     q.ll0 = q.ll;
     q.defer = (DIM == 2) && (wq.e != nullptr) && MODEL == 1;
     const int D = DIM;
@@ -758,17 +760,17 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
     bool need_vel = (MODEL >= 2) || aux >= 2;
     if (need_vel) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)ai * D + d];
+        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)widx(s, i, ai, W_VEL) * D + d];
     }
     double lastv[3] = {q.up[0], q.up[1], DIM == 3 ? q.up[2] : 0.};
     if (MODEL == 3) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)ai * D + d];
+        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)widx(s, i, ai, W_FVS) * D + d];
     }
     q.rng.state = s.rng[i];
     q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
     q.rng.err = 0;
-    double dp = (DIM == 3 || MODEL >= 2) ? s.diameter[ai] : 0.;
+    double dp = (DIM == 3 || MODEL >= 2) ? s.diameter[widx(s, i, ai, W_DIAM)] : 0.;
 
     int bnd_j = -1;
     if constexpr (MODEL == 1) bnd_j = q.update_lsm1(dp);
@@ -899,7 +901,7 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
         q.rng.err = 0;
         double lastv[3] = {0., 0., 0.};
         if (aux >= 2) {
-            double2 v = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
+            double2 v = reinterpret_cast<const double2*>(s.vel)[widx(s, i, aux_index(s, i), W_VEL)];
             lastv[0] = v.x;
             lastv[1] = v.y;
         }
