@@ -311,6 +311,20 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         g32[2 * k] = make_float4((float)gx[0], (float)gx[1], (float)gx[2], (float)gy[0]);
         g32[2 * k + 1] = make_float4((float)gy[1], (float)gy[2], 0.f, 0.f);
     }
+    // neighbour across the edge opposite each vertex
+    std::vector<int4> nbr((size_t)nt);
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        int n[3] = {-1, -1, -1};
+        for (int i = 0; i < 3; ++i) {
+            int eid = d->triedge_map[3 * k + i];
+            int a = d->edges[2 * eid], b = d->edges[2 * eid + 1];
+            int t0 = d->edgetri_map[2 * eid], t1 = d->edgetri_map[2 * eid + 1];
+            for (int j = 0; j < 3; ++j)
+                if (t[j] != a && t[j] != b) n[j] = (t0 == k) ? t1 : t0;
+        }
+        nbr[k] = make_int4(n[0], n[1], n[2], 0);
+    }
     // packed 64-byte mixed-form record (see DevMesh::t64)
     std::vector<int4> t64(4 * (size_t)nt);
     for (int k = 0; k < nt; ++k) {
@@ -346,7 +360,7 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     int rc;
     const double2 *p_xy, *p_basis, *p_geo;
     const float4* p_g32;
-    const int4 *p_tv, *p_edge, *p_t64;
+    const int4 *p_tv, *p_edge, *p_t64, *p_nbr;
     const int *p_lab, *p_gs, *p_gt;
     if ((rc = upload(c, xy, p_xy))) return rc;
     if ((rc = upload(c, tv, p_tv))) return rc;
@@ -355,11 +369,12 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     if ((rc = upload(c, g32, p_g32))) return rc;
     if ((rc = upload(c, t64, p_t64))) return rc;
     if ((rc = upload(c, edge, p_edge))) return rc;
+    if ((rc = upload(c, nbr, p_nbr))) return rc;
     if ((rc = upload(c, lab, p_lab))) return rc;
     if ((rc = upload(c, gstart, p_gs))) return rc;
     if ((rc = upload(c, gtris, p_gt))) return rc;
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
-    m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64;
+    m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64; m.nbr = p_nbr;
     m.gstart = p_gs; m.gtris = p_gt;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;

@@ -60,6 +60,9 @@ struct DevMesh {
     const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
     const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
     const int4* __restrict__ edge;      // [ne]: {n0, n1, t0, t1}
+    // [nt]: the triangle across the edge opposite each vertex {n0, n1, n2, -}
+    // (-1: boundary edge)
+    const int4* __restrict__ nbr;
     const int* __restrict__ elabel;     // [ne]
     double gx0, gy0, ginv;
     int gnx, gny;

@@ -91,6 +91,30 @@ __device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32&
     if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
 }
 
+// One-hop exit.  When the start point is certainly inside the start
+// triangle and the end point certainly beyond exactly one of its edges (the
+// other two barycentric coordinates certainly positive at both points), the
+// segment crosses that edge alone, in its interior: the first edge the
+// reference's path walk finds (xylocalizer.pyx:375-415).  The walk's next
+// test, the point in the neighbour across it, is made here.  Returns the
+// neighbour when the end point is in it, else -1 (the walk kernel decides).
+__device__ __forceinline__ int one_hop(const DevMesh& m, int tri0, const Bary& bs, const Bary& be,
+                                       double xn, double yn) {
+    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
+    const bool n0 = be.l0 < -be.e0, n1 = be.l1 < -be.e1, n2 = be.l2 < -be.e2;
+    const bool p0 = be.l0 > be.e0, p1 = be.l1 > be.e1, p2 = be.l2 > be.e2;
+    int j;
+    if (n0 && p1 && p2) j = 0;
+    else if (n1 && p0 && p2) j = 1;
+    else if (n2 && p0 && p1) j = 2;
+    else return -1;
+    int4 nb = __ldg(&m.nbr[tri0]);
+    int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+    if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
+    Tri32 tn = load_tri32(m, kn);
+    return in_tri_mixed(m, tn, kn, xn, yn) ? kn : -1;
+}
+
 // FP32 P1 interpolation of the packed node record {ux, uy, K, zs}
 struct Node4 {
     float4 n0, n1, n2;
@@ -252,10 +276,12 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (bnd_j == -1) {
         ltri = tri0;
         if (wq.e != nullptr) {
-            // leaves the start triangle: walk + boundary conditions in walk_kernel
-            bool inside = euler ? in_tri_decide(m, bary32_moved(t0, rx0, ry0, dx, dy), tri0, xn, yn)
-                                : in_tri_mixed(m, t0, tri0, xn, yn);
-            if (!inside) {
+            // leaves the start triangle: one hop here, else walk + boundary
+            // conditions in walk_kernel
+            const Bary be = euler ? bary32_moved(t0, rx0, ry0, dx, dy) : bary32(t0, xn, yn);
+            const bool inside = in_tri_decide(m, be, tri0, xn, yn);
+            const int kn = inside ? tri0 : one_hop(m, tri0, b0, be, xn, yn);
+            if (kn < 0) {
                 if (rng.err) atomicOr(err_word, rng.err);
                 int slot = queue_slot(wq);
                 WalkEntry w;
@@ -267,7 +293,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                 wq.e[slot] = w;
                 return;
             }
-            tri = tri0;
+            tri = kn;
         } else {
             xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xn, yn, tri, bnd_j);
         }
