@@ -152,6 +152,9 @@ void make_dev_params(const cg_ctx* c, const cg_params* p, DevParams& d) {
     // update_state_lsm1.pyx:708-713
     d.diffx_const = std::sqrt(2. * d.nux) * d.sqrtdt;
     d.diffz_const = std::sqrt(2. * d.nuz) * d.sqrtdt;
+    d.dt32 = (float)d.dt;
+    d.sqrtdt32 = (float)d.sqrtdt;
+    d.diffx32 = (float)d.diffx_const;
     d.damp = std::fmin(p->rebound_damping_coef, 1.0 - EPSILON_REBOUND);  // compute_bc.pyx:76
     d.strand = p->stranding_probability;
     d.roughness = p->wall_roughness_angle * DEG_TO_RAD;

@@ -100,6 +100,8 @@ struct DevParams {
     double density, rho0, drag_coef;
     // LSM2 / LSM3: particle coefficients (lagrangian_particle_set.pyx:355-375)
     // and model options (parameters.pyx)
+    // FP32 copies for the mixed form (no per-particle conversions)
+    float dt32, sqrtdt32, diffx32;
     int added_mass, drag_model, nuopt, edge_opt;
     double a0c, a1c, a2c, a3c;
     double tl_h, tl_v;               // diffusion_lsm3_tl_horizontal / _vertical

@@ -140,7 +140,7 @@ static __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __r
                                       const DevParams& p, const Tri32& t0, int tri0, double2 x0,
                                       float ux, float uy, double& xn, double& yn, int& tri,
                                       int& bnd_j) {
-    const float dt = (float)p.dt;
+    const float dt = p.dt32;
     const float up0 = ux, up1 = uy;
     const int ns = p.time_scheme == 2 ? 1 : (p.time_scheme == 3 ? 2 : 3);
     float kx[4], ky[4];
@@ -223,7 +223,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     double2 lastv = make_double2(0., 0.);
     if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
 
-    const float dt = (float)p.dt;
+    const float dt = p.dt32;
     Tri32 t0 = load_tri32(m, tri0);
     Node4 n0 = load_nodes(cur, t0);
     const float rx0 = (float)(x0.x - t0.a.x), ry0 = (float)(x0.y - t0.a.y);
@@ -252,11 +252,11 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
             float dKdx = n0.n0.z * t0.g0.x + n0.n1.z * t0.g0.y + n0.n2.z * t0.g0.z;
             float dKdy = n0.n0.z * t0.g0.w + n0.n1.z * t0.g1.x + n0.n2.z * t0.g1.y;
             K = fmaxf(0.f, K);
-            diffx = sqrtf(2.f * K) * (float)p.sqrtdt;
+            diffx = sqrtf(2.f * K) * p.sqrtdt32;
             driftx = dKdx * dt;
             drifty = dKdy * dt;
         } else {
-            diffx = (float)p.diffx_const;
+            diffx = p.diffx32;
         }
         float xix = 0.f, xiy = 0.f;
         if (diffx != 0.f) pair32(rng, p.rng_method, z32, xix, xiy);
