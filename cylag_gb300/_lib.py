@@ -95,6 +95,8 @@ SIGNATURES = [
     ("cg_run_time", C.c_int, [P, C.POINTER(F64), C.POINTER(C.c_int64)]),
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),
+    ("cg_run_resize", C.c_int, [P, C.POINTER(StateDesc)]),
+    ("cg_run_added", C.c_int, [P, C.c_int32]),
     ("cg_server_create", C.c_int, [P, I32, C.c_int64, I32, F64, C.POINTER(P)]),
     ("cg_server_destroy", C.c_int, [P]),
     ("cg_server_admit", C.c_int, [P, C.POINTER(Params), I32, P, F64, P, I32, C.POINTER(I32)]),

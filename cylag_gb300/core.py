@@ -67,6 +67,19 @@ class SimuTime:
             self.is_finished = True
 
 
+class _SimuTimeView:
+    """A copy of a SimuTime's clock that can be moved forward on its own."""
+
+    def __init__(self, st):
+        self.time, self.time_step = st.time, st.time_step
+        self.iteration, self.final_time = st.iteration, st.final_time
+        self.initial_time, self.nt = st.initial_time, st.nt
+
+    def advance(self):
+        self.time += self.time_step
+        self.iteration += 1
+
+
 class EulerianFieldSet:
     """Mirror of cylag.EulerianFieldSet (eulerian_field_set.pyx:125-256)."""
 
@@ -343,6 +356,76 @@ class LagrangianParticleSet:
             self._dev[k].copy_(self._dev[k].index_select(0, ti))
         torch.cuda.synchronize()
 
+    # ---- particles added during the run ---------------------------------------
+    _PAD = {"position": 0., "velocity": 0., "fluid_velocity_seen": 0., "last_position": 0.,
+            "last_velocity": 0., "tri": -1, "last_tri": 0, "lowerlayer": 0, "diameter": 0.}
+
+    def _increase_pool_size(self, size):
+        """lagrangian_particle_set.pyx:522-582: grows every array by
+        max(min_pool_size_update, size) inactive entries (tri -1, last_tri 0,
+        zero state) tagged maxtag+1, maxtag+2, ...; an attached run is
+        pointed at the new arrays."""
+        add = max(int(self.min_pool_size_update), int(size))
+        newtags = np.arange(self.maxtag + 1, self.maxtag + 1 + add, dtype=np.int32)
+        if self._dev is None:
+            for k, v in self._host.items():
+                if k == "tag":
+                    pad = newtags
+                else:
+                    pad = np.full((add,) + v.shape[1:], self._PAD[k], dtype=v.dtype)
+                self._host[k] = np.concatenate([v, pad], axis=0)
+        else:
+            torch = _torch()
+            self._sync()   # nothing of the run may still touch the old arrays
+            for k, v in list(self._dev.items()):
+                if k == "tag":
+                    pad = torch.from_numpy(newtags).to(v.device)
+                elif k == "rng_state":
+                    pad = torch.zeros(add, dtype=v.dtype, device=v.device)
+                else:
+                    pad = torch.full((add,) + tuple(v.shape[1:]), self._PAD[k], dtype=v.dtype,
+                                     device=v.device)
+                self._dev[k] = torch.cat([v, pad], dim=0)
+            torch.cuda.synchronize(v.device)
+        self.maxtag += add
+        self.npart += add
+        solver = getattr(self, "_solver", None)
+        if solver is not None and self._dev is not None:
+            solver._pool_resized()
+
+    def add(self, position):
+        """lagrangian_particle_set.pyx:620-710 (its method 1): the nadd new
+        particles take the inactive entries in index order, after the pool
+        grew by the shortfall; each gets the set's diameter, its position and
+        tri = -2 (initialized by the next step of an attached run, with the
+        PCG32 stream pcg32_seed(seed, tag)).  Velocities are left as they
+        are (zero for a deleted or new entry)."""
+        pos = np.ascontiguousarray(position, dtype=np.float64)
+        nadd = pos.shape[0] if pos.ndim == 2 else 0
+        if nadd == 0:
+            return
+        if pos.shape[1] != self.dim:
+            raise ValueError("dim of position != LagrangianParticleSet.dim")
+        self._retag()   # deleted entries carry their final tags before reuse
+        free = np.flatnonzero(self._get("tri") == -1)
+        if nadd > len(free):
+            self._increase_pool_size(nadd - len(free))
+            free = np.flatnonzero(self._get("tri") == -1)
+        idx = free[:nadd]
+        if self._dev is None:
+            self._host["position"][idx] = pos
+            self._host["diameter"][idx] = self.particle_diameter
+            self._host["tri"][idx] = -2
+        else:
+            torch = _torch()
+            dev = self._dev["tri"].device
+            ti = torch.from_numpy(idx).to(dev)
+            self._dev["position"].index_copy_(0, ti, torch.from_numpy(pos).to(dev))
+            self._dev["diameter"].index_fill_(0, ti, float(self.particle_diameter))
+            self._dev["tri"].index_fill_(0, ti, -2)
+            torch.cuda.synchronize(dev)
+            self._added = True
+
     def delete_single(self, i):
         """lagrangian_particle_set.pyx:754-788"""
         if self._get("tri")[i] == -1:
@@ -437,8 +520,6 @@ class Solver:
         self.parameters.check_values()
         P = self.parameters
         self.simutime = SimuTime(P.listing, P.initial_time, P.final_time, P.time_step)
-        if sources:
-            raise NotImplementedError("particle sources are not built in the GPU step")
         if control_sections:
             raise NotImplementedError("control sections are not built in the GPU step")
         self.sources = sources
@@ -496,14 +577,40 @@ class Solver:
         """solver.pyx:238-379, for every particle awaiting initialization."""
         _lib.check(self._ctx, self.L.cg_run_init(self._run))
 
-    def forward(self, time_step=None, nsteps=1):
-        """solver.pyx:413-585: advances the run by one step (nsteps > 1
-        batches several forward calls into one library call)."""
-        if time_step is not None and time_step != self.simutime.time_step:
-            raise ValueError("forward(time_step) must equal parameters['time_step']")
+    def _pool_resized(self):
+        """The particle set grew its arrays: the run follows them."""
+        sd = self.particle_set._state_desc()
+        _lib.check(self._ctx, self.L.cg_run_resize(self._run, C.byref(sd)))
+
+    def _released(self, clock):
+        """solver.pyx:445-455: asks every source, in order, at the start of
+        the step ``clock`` describes; returns the positions of those that
+        release."""
+        out = []
+        for k, src in enumerate(self.sources or (), start=1):
+            if src.release_condition(clock, self.field_set):
+                pos = np.asarray(src.init_positions(self.field_set, self.particle_set.dim),
+                                 dtype=np.float64)
+                out.append(pos)
+                if self.parameters.listing:
+                    print(f" ~~> Adding {pos.shape[0]} particles from source {k}")
+        return out
+
+    def _add(self, released):
+        """Adds the released positions and tells the run which particles its
+        next step initializes: those below the pool size the step started
+        with (solver.pyx:430, 462-467); entries of a pool grown in this step
+        wait for the following one."""
+        ps = self.particle_set
+        npart0 = ps.npart
+        for pos in released:
+            ps.add(pos)
+        _lib.check(self._ctx, self.L.cg_run_added(self._run, npart0))
+        ps._added = ps.npart > npart0
+
+    def _run_steps(self, nsteps):
         nopen = max(1, self.nopen)
         stats = np.zeros((nsteps, nopen), dtype=np.int32)
-        t0 = self.simutime.time
         rc = self.L.cg_run_step(self._run, nsteps, stats.ctypes.data)
         _lib.check(self._ctx, rc)
         for s in range(nsteps):
@@ -511,6 +618,32 @@ class Solver:
                 self._bnd_stats_times.append(self.simutime.time)
                 self._bnd_stats_data.append(stats[s, : self.nopen].copy())
             self.simutime.increment()
+
+    def forward(self, time_step=None, nsteps=1):
+        """solver.pyx:413-585: advances the run by one step (nsteps > 1
+        batches several forward calls into one library call; a step in which
+        a source releases, or which initializes added particles, starts a
+        new call)."""
+        if time_step is not None and time_step != self.simutime.time_step:
+            raise ValueError("forward(time_step) must equal parameters['time_step']")
+        t0 = self.simutime.time
+        ps = self.particle_set
+        if not self.sources and not getattr(ps, "_added", False):
+            self._run_steps(nsteps)
+        else:
+            clock = _SimuTimeView(self.simutime)
+            batch = 0
+            for _ in range(nsteps):
+                released = self._released(clock)
+                if released or getattr(ps, "_added", False):
+                    if batch:
+                        self._run_steps(batch)
+                        batch = 0
+                    self._add(released)
+                batch += 1
+                clock.advance()
+            if batch:
+                self._run_steps(batch)
         self._last_forward = (t0, nsteps)
 
     def solve(self):

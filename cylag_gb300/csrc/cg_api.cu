@@ -44,6 +44,9 @@ struct cg_run {
     SortBuffers sb{};
     int sort_period = 0;
     uint64_t bytes = 0;
+    uint64_t scratch_bytes = 0;   // walk queue + sort buffers (follow the particle count)
+    bool pending_init = false;    // particles added (tri == -2): initialize at the next step
+    int32_t init_n = 0;           // ... those with an index below init_n
     std::vector<cudaEvent_t> ev;
     int last_launches = 0;
     double last_ms = 0.;
@@ -186,6 +189,103 @@ void make_dev_params(const cg_ctx* c, const cg_params* p, DevParams& d) {
         }
     }
 
+}
+
+// ---------------------------------------------------------------------------
+// per-particle scratch of a run: the walk queue (2D LSM1) and the element-
+// sorted working copies (their size follows the particle count)
+// ---------------------------------------------------------------------------
+// caller-owned particle state counted against the budget: five [n, dim]
+// FP64 arrays, four int32, the diameter and the PCG32 state
+static uint64_t state_bytes_of(int32_t n, int dim) {
+    return (uint64_t)n * (5ull * dim * 8 + 4 * 4 + 8 + 8);
+}
+
+// the particles that the next step initializes: the first init_n
+static DevState added_view(const cg_run* r) {
+    DevState v = r->st;
+    v.n = r->init_n;
+    return v;
+}
+
+struct ScratchPlan {
+    bool use_queue = false, use_sort = false;
+    size_t queue_bytes = 0, sort_bytes = 0;
+    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0};
+    int nkeys = 0, nl_key = 1, work = 0, dim = 2;
+    size_t n = 0;
+};
+
+static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32) {
+    ScratchPlan q;
+    const size_t n = (size_t)(n32 > 0 ? n32 : 0);
+    q.n = n;
+    q.dim = p->dim;
+    // deferred 2D walk: LSM1 (its queue entry carries no velocities)
+    q.use_queue = c->fdim == 2 && n > 0 && p->model == 1;
+    q.queue_bytes = q.use_queue ? 256 + n * sizeof(WalkEntry) : 0;
+    // element sort: keys tri * layers + layer (+1 for inactive) within 4096
+    // scan tiles of 4096; the optional working arrays are those the model
+    // reads every step
+    q.nl_key = c->fdim == 3 ? (c->nlayers > 1 ? c->nlayers - 1 : 1) : 1;
+    const int64_t nkeys64 = (int64_t)c->mesh.nt * q.nl_key + 1;
+    q.use_sort = p->sort_period > 0 && n > 0 && nkeys64 < (1ll << 30) &&
+                 scan_scratch_ints((int)nkeys64) <= 4096;
+    q.nkeys = (int)std::min<int64_t>(nkeys64, 1ll << 30);
+    if (p->model >= 2) q.work |= W_VEL | W_DIAM;
+    if (p->model == 3) q.work |= W_FVS;
+    if (p->dim == 3) q.work |= W_LAYER | W_DIAM;
+    const size_t D = (size_t)p->dim;
+    const size_t work_bytes = al256(n * 8 * D) + 4 * al256(n * 8) +
+                              ((q.work & W_VEL) ? al256(n * 8 * D) : 0) +
+                              ((q.work & W_FVS) ? al256(n * 8 * D) : 0) +
+                              ((q.work & W_LAYER) ? al256(n * 4) : 0) +
+                              ((q.work & W_DIAM) ? al256(n * 8) : 0);
+    if (q.use_sort) {
+        q.off_sums = al256((size_t)q.nkeys * 4);
+        q.off_perm = al256(q.off_sums + (size_t)scan_scratch_ints(q.nkeys) * 4);
+        q.off_w[0] = al256(q.off_perm + n * 4);
+        q.off_w[1] = q.off_w[0] + work_bytes;
+        q.sort_bytes = q.off_w[1] + work_bytes;
+    }
+    return q;
+}
+
+// allocates the planned scratch into r (r->queue and r->sortbuf must be empty)
+static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
+    int rc;
+    if ((rc = dalloc(c, r->queue, q.queue_bytes)) || (rc = dalloc(c, r->sortbuf, q.sort_bytes)))
+        return rc;
+    r->use_queue = q.use_queue;
+    r->sb = SortBuffers{};
+    r->sort_period = 0;
+    if (!q.use_sort) return CG_OK;
+    const size_t n = q.n, D = (size_t)q.dim;
+    char* b = (char*)r->sortbuf.p;
+    r->sb.count = (int*)b;
+    r->sb.block_sums = (int*)(b + q.off_sums);
+    r->sb.perm = (int*)(b + q.off_perm);
+    r->sb.dim = q.dim;
+    r->sb.nl = q.nl_key;
+    r->sb.work = q.work;
+    WorkState* ws[2] = {&r->sb.a, &r->sb.b};
+    for (int k = 0; k < 2; ++k) {
+        char* w = b + q.off_w[k];
+        auto take = [&](size_t bytes) { char* t = w; w += al256(bytes); return t; };
+        ws[k]->pos = (double*)take(n * 8 * D);
+        ws[k]->rng = (unsigned long long*)take(n * 8);
+        ws[k]->tri = (int*)take(n * 8);
+        ws[k]->tag = (int*)take(n * 8);
+        ws[k]->slot = (int*)take(n * 8);
+        ws[k]->vel = (q.work & W_VEL) ? (double*)take(n * 8 * D) : nullptr;
+        ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * 8 * D) : nullptr;
+        ws[k]->layer = (q.work & W_LAYER) ? (int*)take(n * 4) : nullptr;
+        ws[k]->diam = (q.work & W_DIAM) ? (double*)take(n * 8) : nullptr;
+    }
+    r->sort_period = r->prm.sort_period;
+    return CG_OK;
 }
 
 extern "C" {
@@ -478,39 +578,9 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     // LSM2/LSM3 with k-epsilon diffusion read k and eps themselves
     bool need_turb = p->model >= 2 && (p->diffusion_model == 2 || p->diffusion_model == 3);
     size_t turb_bytes = need_turb ? 2 * c->frames.nnodes * (p->precision ? 4 : 8) : 0;
-    uint64_t state_bytes = (uint64_t)s->n * (5ull * p->dim * 8 + 4 * 4 + 8 + 8);
-    // deferred 2D walk: LSM1 (its queue entry carries no velocities)
-    bool use_queue = c->fdim == 2 && s->n > 0 && p->model == 1;
-    size_t queue_bytes = use_queue ? 256 + (size_t)s->n * sizeof(WalkEntry) : 0;
-    // element sort: keys tri * layers + layer (+1 for inactive) within 4096
-    // scan tiles of 4096; the optional working arrays are those the model
-    // reads every step
-    const int nl_key = c->fdim == 3 ? (c->nlayers > 1 ? c->nlayers - 1 : 1) : 1;
-    const int64_t nkeys64 = (int64_t)c->mesh.nt * nl_key + 1;
-    bool use_sort = p->sort_period > 0 && s->n > 0 && nkeys64 < (1ll << 31) &&
-                    scan_scratch_ints((int)std::min<int64_t>(nkeys64, 1ll << 30)) <= 4096;
-    const int nkeys = (int)std::min<int64_t>(nkeys64, 1ll << 30);
-    int work = 0;
-    if (p->model >= 2) work |= W_VEL | W_DIAM;
-    if (p->model == 3) work |= W_FVS;
-    if (p->dim == 3) work |= W_LAYER | W_DIAM;
-    size_t n = (size_t)s->n;
-    const int D = p->dim;
-    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    size_t sort_bytes = 0;
-    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0};
-    const size_t work_bytes = al(n * 8 * D) + 4 * al(n * 8) +
-                              ((work & W_VEL) ? al(n * 8 * D) : 0) +
-                              ((work & W_FVS) ? al(n * 8 * D) : 0) +
-                              ((work & W_LAYER) ? al(n * 4) : 0) + ((work & W_DIAM) ? al(n * 8) : 0);
-    if (use_sort) {
-        off_sums = al((size_t)nkeys * 4);
-        off_perm = al(off_sums + (size_t)scan_scratch_ints(nkeys) * 4);
-        off_w[0] = al(off_perm + n * 4);
-        off_w[1] = off_w[0] + work_bytes;
-        sort_bytes = off_w[1] + work_bytes;
-    }
-    uint64_t need = state_bytes + 2 * rec_bytes + turb_bytes + 64 + queue_bytes + sort_bytes;
+    uint64_t state_bytes = state_bytes_of(s->n, p->dim);
+    const ScratchPlan plan = plan_scratch(c, p, s->n);
+    uint64_t need = state_bytes + 2 * rec_bytes + turb_bytes + 64 + plan.queue_bytes + plan.sort_bytes;
     if (c->budget && c->used + need > c->budget)
         return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
                        (unsigned long long)need, (unsigned long long)c->used,
@@ -522,40 +592,16 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     r->prm = *p;
     int rc;
     if ((rc = dalloc(c, r->cur, rec_bytes)) || (rc = dalloc(c, r->prev, rec_bytes)) ||
-        (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->queue, queue_bytes)) ||
-        (rc = dalloc(c, r->sortbuf, sort_bytes)) || (rc = dalloc(c, r->turb, turb_bytes))) {
+        (rc = dalloc(c, r->errw, 64)) || (rc = dalloc(c, r->turb, turb_bytes)) ||
+        (rc = take_scratch(c, r, plan))) {
         dfree(r->cur); dfree(r->prev); dfree(r->errw); dfree(r->queue); dfree(r->sortbuf);
         dfree(r->turb);
         delete r;
         return rc;
     }
-    r->use_queue = use_queue;
-    if (use_sort) {
-        char* b = (char*)r->sortbuf.p;
-        r->sb.count = (int*)b;
-        r->sb.block_sums = (int*)(b + off_sums);
-        r->sb.perm = (int*)(b + off_perm);
-        r->sb.dim = D;
-        r->sb.nl = nl_key;
-        r->sb.work = work;
-        WorkState* ws[2] = {&r->sb.a, &r->sb.b};
-        for (int k = 0; k < 2; ++k) {
-            char* w = b + off_w[k];
-            auto take = [&](size_t bytes) { char* q = w; w += al(bytes); return q; };
-            ws[k]->pos = (double*)take(n * 8 * D);
-            ws[k]->rng = (unsigned long long*)take(n * 8);
-            ws[k]->tri = (int*)take(n * 8);
-            ws[k]->tag = (int*)take(n * 8);
-            ws[k]->slot = (int*)take(n * 8);
-            ws[k]->vel = (work & W_VEL) ? (double*)take(n * 8 * D) : nullptr;
-            ws[k]->fvs = (work & W_FVS) ? (double*)take(n * 8 * D) : nullptr;
-            ws[k]->layer = (work & W_LAYER) ? (int*)take(n * 4) : nullptr;
-            ws[k]->diam = (work & W_DIAM) ? (double*)take(n * 8) : nullptr;
-        }
-        r->sort_period = p->sort_period;
-    }
     cudaMemsetAsync(r->errw.p, 0, 64, c->stream);
     r->bytes = need;
+    r->scratch_bytes = plan.queue_bytes + plan.sort_bytes;
     c->used += need;
 
     make_dev_params(c, p, r->dp);
@@ -671,7 +717,7 @@ int cg_run_init(cg_run* r) {
     int rc = ensure_fields(r);
     if (rc) return rc;
     launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, r->st,
-                r->prm.particle_velocity_init, (uint32_t*)r->errw.p, c->stream);
+                r->prm.particle_velocity_init, -1, (uint32_t*)r->errw.p, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
 }
@@ -702,6 +748,18 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     DevState ws = r->st;
     int launches = 0;   // kernels launched by this call
     for (int s = 0; s < nsteps; ++s) {
+        // solver.pyx:440: fields at the step-start time
+        if ((rc = time_interpolation(r, r->time))) return rc;
+        if (!r->frozen) launches += 1;   // field blend
+        // particles added since the last step: initialized with this step's
+        // fields, then advanced by it (solver.pyx:443-470)
+        if (s == 0 && r->pending_init) {
+            launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, added_view(r),
+                        r->prm.particle_velocity_init, -2 - (int)r->iteration,
+                        (uint32_t*)r->errw.p, c->stream);
+            r->pending_init = false;
+            launches += 1;
+        }
         if (sorted && s % r->sort_period == 0) {
             if (s == 0) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
             else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
@@ -709,9 +767,6 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             ws = sorted_view(r->st, r->sb);
         }
         const DevState& run_state = sorted ? ws : r->st;
-        // solver.pyx:440: fields at the step-start time
-        if ((rc = time_interpolation(r, r->time))) return rc;
-        if (!r->frozen) launches += 1;   // field blend
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * nopen;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
@@ -763,6 +818,58 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     return CG_OK;
 }
 
+int cg_run_resize(cg_run* r, const cg_state_desc* s) {
+    if (!r || !s || s->n < 0) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (s->n > 0 && (!s->position || !s->velocity || !s->fluid_velocity_seen ||
+                     !s->last_position || !s->last_velocity || !s->tri || !s->last_tri ||
+                     !s->lowerlayer || !s->tag || !s->diameter || !s->rng_state))
+        return set_err(c, CG_EINVAL, "incomplete particle state description");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const ScratchPlan plan = plan_scratch(c, &r->prm, s->n);
+    const uint64_t old_state = state_bytes_of(r->st.n, r->prm.dim);
+    const uint64_t new_state = state_bytes_of(s->n, r->prm.dim);
+    const uint64_t old_bytes = r->bytes;
+    const uint64_t new_bytes = old_bytes - old_state - r->scratch_bytes + new_state +
+                               plan.queue_bytes + plan.sort_bytes;
+    if (c->budget && c->used - old_bytes + new_bytes > c->budget)
+        return set_err(c, CG_ENOMEM_BUDGET, "resized run needs %llu bytes, budget %llu",
+                       (unsigned long long)new_bytes, (unsigned long long)c->budget);
+    dfree(r->queue);
+    dfree(r->sortbuf);
+    int rc = take_scratch(c, r, plan);
+    if (rc) return rc;
+    c->used = c->used - old_bytes + new_bytes;
+    r->bytes = new_bytes;
+    r->scratch_bytes = plan.queue_bytes + plan.sort_bytes;
+    DevState& st = r->st;
+    st.n = s->n;
+    st.pos = s->position;
+    st.vel = s->velocity;
+    st.fvs = s->fluid_velocity_seen;
+    st.last_pos = s->last_position;
+    st.last_vel = s->last_velocity;
+    st.tri = s->tri;
+    st.last_tri = s->last_tri;
+    st.lowerlayer = s->lowerlayer;
+    st.tag = s->tag;
+    st.diameter = s->diameter;
+    st.rng = s->rng_state;
+    return CG_OK;
+}
+
+int cg_run_added(cg_run* r, int32_t n_init) {
+    if (!r || n_init < 0) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_seed_added(r->st.tri, r->st.tag, r->st.rng, r->st.n, r->prm.seed, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    r->pending_init = n_init > 0;
+    r->init_n = n_init < r->st.n ? n_init : r->st.n;
+    return CG_OK;
+}
+
 int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
     if (!r) return CG_EINVAL;
     if (time) *time = r->time;
@@ -787,6 +894,12 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
     if ((rc = ensure_fields(r))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         if ((rc = time_interpolation(r, r->time))) return rc;
+        if (s == 0 && r->pending_init) {
+            launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, added_view(r),
+                        r->prm.particle_velocity_init, -2 - (int)r->iteration,
+                        (uint32_t*)r->errw.p, c->stream);
+            r->pending_init = false;
+        }
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         WalkQueue wq{nullptr, nullptr};
         if (r->use_queue) {

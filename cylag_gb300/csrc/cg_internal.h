@@ -70,9 +70,12 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                        int* stats, uint32_t* err, cudaStream_t st);
 
 // Solver.initialize_particle_state for particles with tri == -2 (FP64
-// arithmetic; node records FP64 or FP32 by precision).
+// arithmetic; node records FP64 or FP32 by precision).  A particle outside
+// the mesh is deleted with tag = del_mark (-1 at the run's creation, -2 - it
+// when added particles are initialized in iteration it).
 void launch_init(int precision, const DevMesh& m, const FieldView& fv, const DevParams& p,
-                 const DevState& s, int velocity_init, uint32_t* err, cudaStream_t st);
+                 const DevState& s, int velocity_init, int del_mark, uint32_t* err,
+                 cudaStream_t st);
 
 // Serving pool (cg_serve.cuh): one launch steps every admitted run.
 // Device run table entry:
@@ -135,6 +138,9 @@ DevState sorted_view(const DevState& user, const SortBuffers& b);
 
 // rng[i] = pcg32_seed(seed, tag[i])
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);
+// the same for the particles awaiting initialization (tri == -2)
+void launch_seed_added(const int* tri, const int* tag, uint64_t* rng, int n, uint64_t seed,
+                       cudaStream_t st);
 
 // values in one packed node record, and its bytes by precision
 inline int record_values(int dim) { return dim == 2 ? Slots<2>::NF : Slots<3>::NF; }

@@ -104,7 +104,7 @@ void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p
 // ---------------------------------------------------------------------------
 template <int DIM, typename FT>
 __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s, int vinit,
-                            uint32_t* err) {
+                            int del_mark, uint32_t* err) {
     __shared__ ZigTables zt;
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
         zt.kn[t] = g_zig.kn[t];
@@ -132,7 +132,7 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
         s.tri[i] = -1;
         s.last_tri[i] = -1;
         s.lowerlayer[i] = 0;
-        s.tag[i] = -1;  // deleted during initialization
+        s.tag[i] = del_mark;  // deleted during initialization (new tag given on the host)
         return;
     }
     int ll = 0;
@@ -184,19 +184,19 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
 }
 
 void launch_init(int precision, const DevMesh& m, const FieldView& fv, const DevParams& p,
-                 const DevState& s, int vinit, uint32_t* err, cudaStream_t st) {
+                 const DevState& s, int vinit, int del_mark, uint32_t* err, cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
     if (precision != 0) {
         DevFields<float> f = fv.as<float>();
-        if (fv.dim == 2) init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-        else init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+        if (fv.dim == 2) init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
+        else init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
         return;
     }
     DevFields<double> f = fv.as<double>();
-    if (fv.dim == 2) init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
-    else init_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, err);
+    if (fv.dim == 2) init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
+    else init_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -215,6 +215,22 @@ void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream
     int bs = 256;
     int nb = (n + bs - 1) / bs;
     if (nb) seed_kernel<<<nb, bs, 0, st>>>(tag, rng, n, seed);
+}
+
+__global__ void seed_added_kernel(const int* __restrict__ tri, const int* __restrict__ tag,
+                                  uint64_t* __restrict__ rng, int n, uint64_t seed) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || tri[i] != -2) return;
+    uint64_t st, inc;
+    pcg_seed(seed, (uint64_t)(uint32_t)tag[i], st, inc);
+    rng[i] = st;
+}
+
+void launch_seed_added(const int* tri, const int* tag, uint64_t* rng, int n, uint64_t seed,
+                       cudaStream_t st) {
+    int bs = 256;
+    int nb = (n + bs - 1) / bs;
+    if (nb) seed_added_kernel<<<nb, bs, 0, st>>>(tri, tag, rng, n, seed);
 }
 
 }  // namespace cg

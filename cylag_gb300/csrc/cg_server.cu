@@ -360,7 +360,7 @@ int cg_server_admit(cg_server* s, const cg_params* prm, int32_t n, const double*
     serve_prepare_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(v, diameter ? 0. : particle_diameter);
     launch_seed(v.tag, v.rng, n, prm->seed, c->stream);
     CUDA_TRY(c, cudaMemsetAsync((uint32_t*)s->err_buf.p + id, 0, 4, c->stream));
-    launch_init(s->precision, c->mesh, server_view(s), dp, v, prm->particle_velocity_init,
+    launch_init(s->precision, c->mesh, server_view(s), dp, v, prm->particle_velocity_init, -1,
                 (uint32_t*)s->err_buf.p + id, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     // run table entry: step 0 at the next launched step (the pinned slot's

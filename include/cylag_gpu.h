@@ -196,6 +196,25 @@ int cg_run_errors(cg_run *run, uint32_t *flags);
 /* Number of active particles and deleted-this-call counts are derived by the
  * caller from tri (tri == -1 inactive). */
 
+/* ---- particles added during a run -------------------------------------- */
+/* Points the run at a new (larger) particle state after the caller grew
+ * its arrays (LagrangianParticleSet._increase_pool_size,
+ * lagrangian_particle_set.pyx:522-582); scratch follows the new count.
+ * Synchronous. */
+int cg_run_resize(cg_run *run, const cg_state_desc *state);
+/* Particles the caller set to tri == -2 (LagrangianParticleSet.add,
+ * lagrangian_particle_set.pyx:620-710: released by a source) get their
+ * PCG32 streams, pcg32_seed(seed, tag); those with an index below n_init are
+ * initialized (Solver.initialize_particle_state, solver.pyx:238-379) with the
+ * fields of the next step, which then advances them (solver.pyx:443-470).
+ * The reference's step loop covers the pool size it had before the sources
+ * added (solver.pyx:430, 462): particles placed in a grown pool wait one
+ * step, which the caller reproduces with n_init = that size and a second
+ * call before the following step.  One deleted in its initialization
+ * (outside the mesh) gets tag -2 - iteration, like a particle deleted in
+ * that step. */
+int cg_run_added(cg_run *run, int32_t n_init);
+
 /* ---- serving pool ----------------------------------------------------- */
 /* Many dispersion runs on one context's mesh and frozen fields, stepped
  * together: one launch per step advances every admitted run (continuous

@@ -171,7 +171,8 @@ class OracleSolver:
     """
 
     def __init__(self, mesh, fields, params, position, pset=None, seed=0,
-                 tags=None, nthreads=1, diameter=None):
+                 tags=None, nthreads=1, diameter=None, sources=None, initial_pool_size=None,
+                 min_pool_size_update=1000):
         from cylag_gb300.parameters import Parameters
         L = lib()
         self.L = L
@@ -219,31 +220,38 @@ class OracleSolver:
         if not self.frozen:
             self.record = self._lower_index(P.initial_time, 0)
         # ---- particles ------------------------------------------------------
-        pos = np.ascontiguousarray(position, dtype=np.float64)
-        n, pd = pos.shape
+        # lagrangian_particle_set.pyx:158-261: a pool of initial_pool_size
+        # entries (default: the positions given), the first ones active
+        pos0 = np.ascontiguousarray(position, dtype=np.float64)
+        na, pd = pos0.shape
+        n = na if initial_pool_size is None else int(initial_pool_size)
+        if n < na:
+            raise ValueError("size of position > initial_pool_size")
         self.n, self.pd = n, pd
-        self.pos = pos.copy()
+        self.seed = seed
+        self.sources = list(sources or [])
+        self.min_pool_size_update = int(min_pool_size_update)
+        self.pos = np.zeros((n, pd))
+        self.pos[:na] = pos0
         self.vel = np.zeros((n, pd))
         self.fvs = np.zeros((n, pd))
-        self.last_pos = pos.copy()
+        self.last_pos = self.pos.copy()
         self.last_vel = np.zeros((n, pd))
         self.tri = -np.ones(n, np.int32)
         self.last_tri = -np.ones(n, np.int32)
         self.lowerlayer = np.zeros(n, np.int32)
-        self.inactive = np.zeros(n, np.int32)
+        self.inactive = np.ones(n, np.int32)
+        self.inactive[:na] = 0
         self.tag = (np.arange(n, dtype=np.int32) if tags is None
                     else np.asarray(tags, dtype=np.int32).copy())
         self.maxtag = int(self.tag.max()) if n else -1
         dp = pset.get("particle_diameter", 0.01)
+        self.dp = dp
         self.diameter = (np.full(n, dp) if diameter is None
                          else np.asarray(diameter, dtype=np.float64).copy())
         self.volume = np.pi * (self.diameter ** 3) / 6.
         self.rng_state, self.rng_inc = seed_streams(seed, self.tag)
-        self._s = Particles(n, _p(self.pos), _p(self.vel), _p(self.fvs), _p(self.last_pos),
-                            _p(self.last_vel), _p(self.tri), _p(self.last_tri),
-                            _p(self.lowerlayer), _p(self.inactive), _p(self.tag),
-                            _p(self.diameter), _p(self.volume), _p(self.rng_state),
-                            _p(self.rng_inc))
+        self._bind()
         # ---- params ----------------------------------------------------------
         rho0 = P.water_density
         rhop = pset.get("particle_density", 1000.)
@@ -268,6 +276,7 @@ class OracleSolver:
             a0c, a1c, a2c, a3c)
         self.time = P.initial_time
         self.dt = P.time_step
+        self.time_step = P.time_step
         self.nopen = int(getattr(mesh, "nopen", 0))
         self.bnd_stats = []
         if not self.frozen:
@@ -277,6 +286,58 @@ class OracleSolver:
                               C.byref(self._s), 0, n)
         self._raise_errors("initialization")
         self.maxtag = self.L.cgo_retag(C.byref(self._s), self.maxtag)
+        self.iteration = 0
+        self.final_time = P.final_time
+
+    def _bind(self, n=None):
+        """The C view of the particle arrays (its first n entries)."""
+        self._s = Particles(self.n if n is None else n, _p(self.pos), _p(self.vel),
+                            _p(self.fvs), _p(self.last_pos), _p(self.last_vel), _p(self.tri),
+                            _p(self.last_tri), _p(self.lowerlayer), _p(self.inactive),
+                            _p(self.tag), _p(self.diameter), _p(self.volume),
+                            _p(self.rng_state), _p(self.rng_inc))
+
+    # ---- particles added during the run (lagrangian_particle_set.pyx) ------------
+    def _increase_pool_size(self, size):
+        """lagrangian_particle_set.pyx:522-582"""
+        add = max(self.min_pool_size_update, int(size))
+        z = lambda *sh, dt=np.float64: np.zeros(sh, dtype=dt)
+        cat = lambda a, b: np.ascontiguousarray(np.concatenate([a, b], axis=0))
+        self.inactive = cat(self.inactive, np.ones(add, np.int32))
+        self.diameter = cat(self.diameter, z(add))
+        self.volume = cat(self.volume, z(add))
+        for k in ("pos", "vel", "fvs", "last_pos", "last_vel"):
+            setattr(self, k, cat(getattr(self, k), z(add, self.pd)))
+        self.tag = cat(self.tag, np.arange(self.maxtag + 1, self.maxtag + 1 + add, dtype=np.int32))
+        self.maxtag += add
+        self.tri = cat(self.tri, -np.ones(add, np.int32))
+        self.lowerlayer = cat(self.lowerlayer, z(add, dt=np.int32))
+        self.last_tri = cat(self.last_tri, z(add, dt=np.int32))
+        self.rng_state = cat(self.rng_state, z(add, dt=self.rng_state.dtype))
+        self.rng_inc = cat(self.rng_inc, z(add, dt=self.rng_inc.dtype))
+        self.n += add
+        self._bind()
+
+    def add(self, position):
+        """lagrangian_particle_set.pyx:620-710 (method 1), plus the stream of
+        each added particle: pcg32_seed(seed, tag)."""
+        pos = np.asarray(position, dtype=np.float64)
+        nadd = pos.shape[0] if pos.ndim == 2 else 0
+        if nadd == 0:
+            return
+        free = np.flatnonzero(self.inactive == 1)
+        if nadd > len(free):
+            self._increase_pool_size(nadd - len(free))
+            free = np.flatnonzero(self.inactive == 1)
+        idx = free[:nadd]
+        self.inactive[idx] = 0
+        self.diameter[idx] = self.dp
+        self.volume[idx] = np.pi * (self.dp ** 3) / 6.
+        self.pos[idx] = pos
+        self.tri[idx] = -2
+        st, inc = seed_streams(self.seed, self.tag[idx])
+        self.rng_state[idx] = st
+        self.rng_inc[idx] = inc
 
     def _raise_errors(self, where):
         e = self.L.cgo_take_errors()
@@ -321,16 +382,27 @@ class OracleSolver:
         return f
 
     def forward(self):
-        """solver.pyx:413-585 (no sources, no control sections)."""
+        """solver.pyx:413-585 (no control sections).  The sources are asked
+        at the step's start (``self`` serves as the SimuTime: time,
+        time_step, iteration, final_time); the step covers the pool size it
+        started with (solver.pyx:430), so entries of a pool grown by this
+        step's releases wait for the next step."""
         self._time_interpolation(self.time)
+        npart = self.n
+        for src in self.sources:
+            if src.release_condition(self, None):
+                self.add(src.init_positions(None, self.pd))
+        self._bind(npart)
         self._p.time = self.time
         stats = np.zeros(max(1, self.nopen), np.int32)
         self.L.cgo_step(C.byref(self._m), C.byref(self._fields()), C.byref(self._p),
                         C.byref(self._s), _p(stats), self.nthreads)
         self._raise_errors(f"the step at t={self.time}")
         self.maxtag = self.L.cgo_retag(C.byref(self._s), self.maxtag)
+        self._bind()
         self.bnd_stats.append(stats[: self.nopen].copy())
         self.time += self.dt
+        self.iteration += 1
 
     def solve(self, nsteps):
         for _ in range(nsteps):

@@ -46,6 +46,38 @@ def load_golden(name):
     return case, meta, out
 
 
+def source_names():
+    return sorted(p.stem[len("src_"):] for p in GOLDEN.glob("src_*.npz"))
+
+
+def load_source(name):
+    """A fixture of a reference run with particle sources: (case, meta, out);
+    meta["sources"] describes the sources (see make_sources)."""
+    z = np.load(GOLDEN / f"src_{name}.npz", allow_pickle=False)
+    meta = json.loads(str(z["meta"]))
+    case = dict(meta["case"])
+    for k in z.files:
+        if k.startswith("in_"):
+            case[k[3:]] = z[k]
+    out = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return case, meta, out
+
+
+def make_sources(spec):
+    """ParticleSource objects (cylag_gb300.extra) from a fixture's JSON
+    description: {"scheduler": schedules() keywords, "poly": [[x, y], ...],
+    "kwargs": ParticleSource keywords}."""
+    from cylag_gb300 import extra
+    out = []
+    for d in spec:
+        kw = dict(d.get("kwargs", {}))
+        if "grid_res" in kw:
+            kw["grid_res"] = np.array(kw["grid_res"], dtype=np.int32)
+        out.append(extra.ParticleSource(extra.schedules(**d["scheduler"]),
+                                        np.array(d["poly"], dtype=np.float64), **kw))
+    return out
+
+
 def mesh_from_case(case):
     from cylag_gb300.mesh import TriangularMesh
     return TriangularMesh(case["x"], case["y"], case["triangles"],

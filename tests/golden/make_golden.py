@@ -344,8 +344,121 @@ def lsm23_fixtures():
         save_traj(name, case, p, 50 if p["time_step"] >= 0.5 else 100, seed=8, pset_kw=pkw)
 
 
+# ---------------------------------------------------------------------------
+# particle sources: one reference Solver for the whole pool (no diffusion,
+# so no draws), sources releasing into a pool that reuses deleted entries and
+# grows by min_pool_size_update
+# ---------------------------------------------------------------------------
+def make_sources(cy, spec):
+    """Sources from their JSON description, with the reference's classes."""
+    out = []
+    for d in spec:
+        sch = cy.schedules(**d["scheduler"])
+        kw = dict(d.get("kwargs", {}))
+        if "grid_res" in kw:
+            kw["grid_res"] = np.array(kw["grid_res"], dtype=np.int32)
+        out.append(cy.ParticleSource(sch, np.array(d["poly"], dtype=np.float64), **kw))
+    return out
+
+
+def run_reference_sources(case, params, nsteps, spec, pset_kw):
+    cy = _cylag()
+    dim = case.get("dim", 2)
+    mesh = cy.TriangularMesh(case["x"], case["y"], case["triangles"],
+                             boundary_points=case.get("boundary_points"),
+                             nopen=case.get("nopen", 0))
+    fset = cy.EulerianFieldSet(
+        mesh, dim=dim, nlayers=case.get("nlayers", 1), times=case["times"],
+        elevation=case["elevation"], velocity_x=case["velocity_x"], velocity_y=case["velocity_y"],
+        velocity_z=case.get("velocity_z"), opt_fields=case.get("opt_fields"),
+        opt_fields_names=case.get("opt_fields_names"))
+    params = dict(params, output_rep=tempfile.mkdtemp(prefix="cylag_golden_"))
+    ps = cy.LagrangianParticleSet(case["position"], dim=dim, **pset_kw)
+    s = cy.Solver(fset, ps, params, sources=make_sources(cy, spec))
+    npart = []
+    for _ in range(nsteps):
+        s.forward(s.simutime.time_step)
+        npart.append(ps.npart)
+    out = {k: np.asarray(getattr(ps, k)).copy() for k in
+           ("position", "velocity", "fluid_velocity_seen", "last_position", "last_velocity",
+            "tri", "last_tri", "lowerlayer", "inactive", "tag", "diameter")}
+    out["npart"] = np.array(npart, dtype=np.int64)
+    out["maxtag"] = np.array(ps.maxtag)
+    return out
+
+
+def save_sources(name, case, params, nsteps, spec, pset_kw):
+    res = run_reference_sources(case, params, nsteps, spec, pset_kw)
+    inputs = {k: v for k, v in case.items() if isinstance(v, np.ndarray)}
+    meta = {k: v for k, v in case.items() if not isinstance(v, np.ndarray)}
+    np.savez_compressed(
+        OUT / f"src_{name}.npz",
+        meta=json.dumps({"params": params, "nsteps": nsteps, "sources": spec,
+                         "pset": pset_kw, "case": meta}),
+        **{f"in_{k}": v for k, v in inputs.items()},
+        **{f"out_{k}": v for k, v in res.items()})
+    na = int((res["inactive"] == 0).sum())
+    print(f"src_{name}: pool {res['npart'][0]}..{res['npart'][-1]}, {na} active after "
+          f"{nsteps} steps, maxtag {int(res['maxtag'])}")
+
+
+def source_fixtures():
+    # 2D open channel, two field records (time interpolation), LSM1 RK4
+    # without diffusion: exits free entries, three sources refill them
+    x, y, tri, bp, nopen = open_channel()
+    u0 = 0.4 + 0.3 * y / 100.0
+    v0 = 0.05 * np.sin(2 * np.pi * x / 400.0)
+    rng = np.random.default_rng(21)
+    pos = np.stack([rng.uniform(250.0, 395.0, 20), rng.uniform(2.0, 98.0, 20)], 1)
+    case = dict(x=x, y=y, triangles=tri, boundary_points=bp, nopen=nopen,
+                times=np.array([0.0, 200.0]), elevation=np.ones((2, len(x))),
+                velocity_x=np.stack([u0, 1.3 * u0]), velocity_y=np.stack([v0, -v0]),
+                position=pos)
+    p = dict(model=1, diffusion_model=0, time_scheme=4, frozen_eulerian_fields=False,
+             time_step=2.0, final_time=200.0, bnd_statistics=True)
+    spec = [
+        # 6 particles every 4 iterations
+        dict(scheduler=dict(iteration_delta=4),
+             poly=[[10., 10.], [60., 10.], [60., 40.], [10., 40.]],
+             kwargs=dict(grid_res=[3, 2, 1])),
+        # triangle by density; 41.0 and 41.5 fall in the same step: one release
+        dict(scheduler=dict(times=[3.0, 17.0, 41.0, 41.5]),
+             poly=[[100., 60.], [180., 70.], [120., 95.]],
+             kwargs=dict(xy_method=2, xy_density=0.01)),
+        # half outside the mesh: those particles are deleted at initialization
+        dict(scheduler=dict(count=5),
+             poly=[[300., 80.], [340., 80.], [340., 130.], [300., 130.]],
+             kwargs=dict(grid_res=[2, 5, 1])),
+    ]
+    save_sources("open_lsm1_rk4", case, p, 90, spec,
+                 dict(initial_pool_size=24, min_pool_size_update=7))
+    # same with Euler and a release every 6 s by time_delta, npart-based grid
+    p1 = dict(p, time_scheme=1)
+    spec1 = [dict(scheduler=dict(time_delta=6.0, ini_time=1.0),
+                  poly=[[20., 20.], [90., 25.], [80., 80.], [30., 70.]],
+                  kwargs=dict(xy_method=1, xy_npart=9)),
+             spec[2]]
+    save_sources("open_lsm1_euler", case, p1, 90, spec1,
+                 dict(initial_pool_size=20, min_pool_size_update=5))
+
+    # 3D log-law, LSM2 RK4 without diffusion, settling particles, a 3D
+    # source every 5 iterations
+    c = synth.loglaw_case(nx=21, ny=11, lx=400.0, ly=200.0, nplanes=6, npart=30)
+    case3 = {k: c[k] for k in ("x", "y", "triangles", "times", "elevation", "velocity_x",
+                               "velocity_y", "velocity_z", "opt_fields", "position")}
+    case3.update(dim=3, nlayers=6, opt_fields_names=c["opt_fields_names"])
+    hmin = float(c["bathymetry"].min())
+    p3 = dict(model=2, time_scheme=4, diffusion_model=0, frozen_eulerian_fields=True,
+              time_step=0.1, final_time=100.0)
+    spec3 = [dict(scheduler=dict(iteration_delta=5),
+                  poly=[[50., 50.], [150., 50.], [150., 120.], [50., 120.]],
+                  kwargs=dict(grid_res=[3, 2, 2], zmin=-0.9 * hmin, zmax=-0.1 * hmin))]
+    save_sources("loglaw3d_lsm2_rk4", case3, p3, 40, spec3,
+                 dict(min_pool_size_update=10, particle_density=1200.))
+
+
 GROUPS = {"rng": rng_fixture, "mesh": mesh_fixture, "lsm1": traj_fixtures,
-          "lsm23": lsm23_fixtures}
+          "lsm23": lsm23_fixtures, "sources": source_fixtures}
 
 if __name__ == "__main__":
     for g in (sys.argv[1:] or list(GROUPS)):
