@@ -33,6 +33,19 @@ _OPT_NAMES = {
 }
 
 
+def lower_index(times, value, last=0):
+    """zlocalizer.pyx:125-151: i with times[i] <= value < times[i+1],
+    searched from ``last``; the last interval at or past the end; 0 before
+    the start."""
+    n = len(times)
+    for i in range(int(last), n - 1):
+        if times[i] <= value < times[i + 1]:
+            return i
+    if n > 1 and value >= times[-1]:
+        return n - 2
+    return 0
+
+
 def _torch():
     import torch
     if not torch.cuda.is_available():
@@ -140,6 +153,39 @@ class EulerianFieldSet:
                         break
         self.friction_model = friction_model
         self.friction_coefficient = friction_coefficient
+
+    def _get_field_from_id(self, field_id):
+        """eulerian_field_set.pyx:673-720: 0 elevation, 1-3 velocity, 4+ the
+        optional fields in the given order ([ntimes, npoints*nlayers])."""
+        if field_id == 0:
+            return self.elevation
+        if field_id == 1:
+            return self.velocity_x
+        if field_id == 2:
+            return self.velocity_y
+        if field_id == 3 and self.velocity_z is not None:
+            return self.velocity_z
+        if 4 <= field_id < 4 + self.nopt:
+            return self.opt_fields[field_id - 4]
+        raise ValueError(f"Invalid field id {field_id}")
+
+    def _get_field_slice(self, field, k, l):
+        """eulerian_field_set.pyx:623-648: record k, layer l (-1: all)."""
+        if self.dim == 2:
+            return field[k, 0:self.npoints]
+        if l != -1:
+            return field[k, l * self.npoints:(l + 1) * self.npoints]
+        return field[k, :]
+
+    def _set_record(self, time, follow=True):
+        """eulerian_field_set.pyx:845-864: the record whose [t_r, t_r+1)
+        holds ``time`` (searched from the current one when following); 0
+        when the fields are frozen.  The device run keeps its own copy; this
+        one is what the sources see."""
+        if not self.frozen_hydro:
+            self.record = lower_index(self.times, time, self.record if follow else 0)
+        else:
+            self.record = 0
 
     def check_regular_layers(self, rtol=1e-3):
         """eulerian_field_set.pyx:258-294 (uniform sigma layers)."""
@@ -587,6 +633,7 @@ class Solver:
         the step ``clock`` describes; returns the positions of those that
         release."""
         out = []
+        self.field_set._set_record(clock.time)   # solver.pyx:440 precedes the sources
         for k, src in enumerate(self.sources or (), start=1):
             if src.release_condition(clock, self.field_set):
                 pos = np.asarray(src.init_positions(self.field_set, self.particle_set.dim),

@@ -299,3 +299,121 @@ class ParticleSource:
         return init_positions_3d(self.poly, self.poly_area, self.xy_method, self.grid_res,
                                  self.xy_npart, self.xy_density, self.z_method, self.z_npart,
                                  self.z_density, self.zmin, self.zmax)
+
+
+# ---------------------------------------------------------------------------
+# release where a field meets a criterion (particle_source.pyx:114-339)
+# ---------------------------------------------------------------------------
+INTERN_REF = -1          # vertex label of an interior node (constants.pyx:29)
+_M64 = (1 << 64) - 1
+
+
+class HostPCG32:
+    """PCG32 (XSH-RR output, 64-bit LCG with multiplier 6364136223846793005;
+    M. O'Neill's published generator) on the host, for release positions:
+    the same seeding and uniform draw as random_utils.pyx:22-67."""
+
+    def __init__(self, seed=0, stream=0):
+        self.state = 0
+        self.inc = ((int(stream) << 1) | 1) & _M64
+        self.next_u32()
+        self.state = (self.state + int(seed)) & _M64
+        self.next_u32()
+
+    def next_u32(self):
+        old = self.state
+        self.state = (old * 6364136223846793005 + self.inc) & _M64
+        xs = (((old >> 18) ^ old) >> 27) & 0xFFFFFFFF
+        rot = old >> 59
+        return ((xs >> rot) | (xs << ((32 - rot) & 31))) & 0xFFFFFFFF
+
+    def uniform(self):
+        return self.next_u32() * (1.0 / 4294967296.0)
+
+
+_CMP = {"eq": np.equal, "neq": np.not_equal, "geq": np.greater_equal,
+        "leq": np.less_equal, "gt": np.greater, "lt": np.less}
+
+
+class ParticleSourceFromField:
+    """particle_source.pyx:114-339: releases around the interior nodes where
+    a field's value (``val_*``) or its variation to the next record
+    (``var_*``) meets ``criteria`` against ``threshold``; each such node gets
+    max(1, int(density * dual_area)) particles uniform in the disc of its
+    dual-cell area (density = the density field / virtual_mass).
+
+    The reference draws the disc positions from its one global PCG32; here
+    the source owns a stream, pcg32_seed(``seed``, ``stream``), or shares the
+    HostPCG32 ``rng`` given, so releases do not depend on the particle draws
+    (and equal the reference's when the global stream is seeded the same way
+    and nothing else draws from it)."""
+
+    def __init__(self, scheduler, field_id_criteria, field_id_density, criteria, threshold,
+                 virtual_mass=1., single_release=False, seed=0, stream=0, rng=None):
+        self.scheduler = scheduler
+        self.field_id_criteria = field_id_criteria
+        self.field_id_density = field_id_density
+        self.criteria = criteria
+        self.threshold = threshold
+        self.virtual_mass = virtual_mass
+        self.loc = np.empty(0, dtype=np.int64)
+        self.single_release = single_release
+        self.release_rec = -1
+        self.rng = rng if rng is not None else HostPCG32(seed, stream)
+
+    def release_condition(self, simutime, fset):
+        rec = fset.record
+        if not self.scheduler.now(simutime):
+            return 0
+        kind, _, op = self.criteria.partition("_")
+        if kind not in ("var", "val") or op not in _CMP:
+            if kind in ("var", "val"):
+                raise ValueError("Unkwown criteria")
+            return 0
+        field = fset._get_field_from_id(self.field_id_criteria)
+        f0 = np.asarray(fset._get_field_slice(field, rec, -1))
+        if kind == "var":
+            f1 = np.asarray(fset._get_field_slice(field, rec + 1, -1))
+            values = f1 - f0
+        else:
+            values = f0
+        self.loc = np.nonzero(_CMP[op](values, self.threshold))[0]
+        if len(self.loc) > 0:
+            if not self.single_release or rec != self.release_rec:
+                self.release_rec = rec
+                return 1
+        return 0
+
+    def init_positions(self, fset, dim=-1):
+        if fset.dim != 2:
+            raise ValueError("Dimension must be 2")
+        if dim == 3:
+            raise ValueError("ParticleSourceFromField only generates 2D positions, "
+                             "it cannot be used with a 3D LagrangianParticleSet")
+        m = fset.triangular_mesh
+        rec = fset.record
+        dens = np.asarray(fset._get_field_slice(fset._get_field_from_id(self.field_id_density),
+                                                rec, -1))
+        va = m.vertex_adjacency
+        out = []
+        for k in self.loc:
+            if m.vertex_labels[k] != INTERN_REF:
+                continue
+            area = 0.0
+            for itri in va[k]:
+                if itri != -1:
+                    area += abs(float(m.signed_area[itri])) / 3.
+            density = float(dens[k]) / self.virtual_mass
+            r0 = math.sqrt(area / np.pi)
+            if density == 0.:
+                continue
+            n = max(1, int(density * area))
+            x0, y0 = float(m.x[k]), float(m.y[k])
+            p = np.zeros((n, 2))
+            for j in range(n):
+                r = r0 * math.sqrt(self.rng.uniform())
+                a = 2. * np.pi * self.rng.uniform()
+                p[j, 0] = x0 + r * np.cos(a)
+                p[j, 1] = y0 + r * np.sin(a)
+            out.append(p)
+        return np.concatenate(out, axis=0) if out else np.zeros((0, 2))

@@ -62,7 +62,8 @@ class TriangularMesh:
         else:
             self.edgetri_map = np.ascontiguousarray(edgetri_map, dtype=np.int32)
             self.triedge_map = np.ascontiguousarray(triedge_map, dtype=np.int32)
-        self.vertex_adjacency = vertex_adjacency
+        self.vertex_adjacency = (self._init_vertex_adjacency() if vertex_adjacency is None
+                                 else np.ascontiguousarray(vertex_adjacency, dtype=np.int32))
         self.triangle_adjacency = triangle_adjacency
         self.triangle_neighbors = triangle_neighbors
 
@@ -95,6 +96,23 @@ class TriangularMesh:
         return np.ascontiguousarray(np.unique(e, axis=0), dtype=np.int32)
 
     # -- triangular_mesh.pyx:311-367 (overflow check only) ---------------------
+    # -- triangular_mesh.pyx:311-367 ------------------------------------------
+    def _init_vertex_adjacency(self):
+        """[nv, MAX_VERTEX_ADJACENCY] triangles around each vertex in
+        increasing triangle index, -1 padded."""
+        self._check_vertex_adjacency()
+        va = -np.ones((self.nv, MAX_VERTEX_ADJACENCY), dtype=np.int32)
+        if self.nt == 0:
+            return va
+        v = self.triangles.reshape(-1).astype(np.int64)
+        k = np.repeat(np.arange(self.nt, dtype=np.int64), 3)
+        order = np.lexsort((k, v))
+        v, k = v[order], k[order]
+        start = np.searchsorted(v, np.arange(self.nv))
+        slot = np.arange(len(v)) - start[v]
+        va[v, slot] = k
+        return va
+
     def _check_vertex_adjacency(self):
         cnt = np.bincount(self.triangles.reshape(-1), minlength=self.nv)
         if self.nv and cnt.max() > MAX_VERTEX_ADJACENCY:

@@ -172,7 +172,7 @@ class OracleSolver:
 
     def __init__(self, mesh, fields, params, position, pset=None, seed=0,
                  tags=None, nthreads=1, diameter=None, sources=None, initial_pool_size=None,
-                 min_pool_size_update=1000):
+                 min_pool_size_update=1000, field_set=None):
         from cylag_gb300.parameters import Parameters
         L = lib()
         self.L = L
@@ -230,6 +230,8 @@ class OracleSolver:
         self.n, self.pd = n, pd
         self.seed = seed
         self.sources = list(sources or [])
+        # what the sources see as the field set (record kept in step here)
+        self.field_set = field_set
         self.min_pool_size_update = int(min_pool_size_update)
         self.pos = np.zeros((n, pd))
         self.pos[:na] = pos0
@@ -386,12 +388,16 @@ class OracleSolver:
         at the step's start (``self`` serves as the SimuTime: time,
         time_step, iteration, final_time); the step covers the pool size it
         started with (solver.pyx:430), so entries of a pool grown by this
-        step's releases wait for the next step."""
+        step's releases wait for the next step.  ``field_set`` (given at
+        construction) is handed to the sources with this run's record."""
         self._time_interpolation(self.time)
         npart = self.n
+        fs = self.field_set
+        if fs is not None:
+            fs.record = self.record
         for src in self.sources:
-            if src.release_condition(self, None):
-                self.add(src.init_positions(None, self.pd))
+            if src.release_condition(self, fs):
+                self.add(src.init_positions(fs, self.pd))
         self._bind(npart)
         self._p.time = self.time
         stats = np.zeros(max(1, self.nopen), np.int32)

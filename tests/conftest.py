@@ -63,13 +63,21 @@ def load_source(name):
     return case, meta, out
 
 
-def make_sources(spec):
+def make_sources(spec, rng_stream=None):
     """ParticleSource objects (cylag_gb300.extra) from a fixture's JSON
     description: {"scheduler": schedules() keywords, "poly": [[x, y], ...],
-    "kwargs": ParticleSource keywords}."""
+    "kwargs": ParticleSource keywords}, or {"kind": "field", "scheduler",
+    "kwargs": ParticleSourceFromField keywords} whose disc positions draw
+    from pcg32_seed(*rng_stream) (one stream shared by the field sources, as
+    the reference's global stream is)."""
     from cylag_gb300 import extra
     out = []
+    shared = extra.HostPCG32(*(rng_stream if rng_stream is not None else (0, 0)))
     for d in spec:
+        if d.get("kind") == "field":
+            out.append(extra.ParticleSourceFromField(extra.schedules(**d["scheduler"]),
+                                                     rng=shared, **d["kwargs"]))
+            continue
         kw = dict(d.get("kwargs", {}))
         if "grid_res" in kw:
             kw["grid_res"] = np.array(kw["grid_res"], dtype=np.int32)

@@ -96,7 +96,7 @@ def mesh_fixture():
     m = cy.TriangularMesh(x, y, tri, boundary_points=bp, nopen=nopen)
     out = dict(x=x, y=y, triangles=tri, boundary_points=bp, nopen=nopen)
     for a in ("edges", "triedge_map", "edgetri_map", "edges_labels", "vertex_labels",
-              "gradx", "grady", "det", "signed_area"):
+              "gradx", "grady", "det", "signed_area", "vertex_adjacency"):
         out[a] = np.asarray(getattr(m, a)).copy()
     np.savez_compressed(OUT / "mesh_open.npz", **out)
 
@@ -354,6 +354,9 @@ def make_sources(cy, spec):
     out = []
     for d in spec:
         sch = cy.schedules(**d["scheduler"])
+        if d.get("kind") == "field":
+            out.append(cy.ParticleSourceFromField(sch, **d["kwargs"]))
+            continue
         kw = dict(d.get("kwargs", {}))
         if "grid_res" in kw:
             kw["grid_res"] = np.array(kw["grid_res"], dtype=np.int32)
@@ -361,7 +364,7 @@ def make_sources(cy, spec):
     return out
 
 
-def run_reference_sources(case, params, nsteps, spec, pset_kw):
+def run_reference_sources(case, params, nsteps, spec, pset_kw, rng_stream=None):
     cy = _cylag()
     dim = case.get("dim", 2)
     mesh = cy.TriangularMesh(case["x"], case["y"], case["triangles"],
@@ -375,6 +378,9 @@ def run_reference_sources(case, params, nsteps, spec, pset_kw):
     params = dict(params, output_rep=tempfile.mkdtemp(prefix="cylag_golden_"))
     ps = cy.LagrangianParticleSet(case["position"], dim=dim, **pset_kw)
     s = cy.Solver(fset, ps, params, sources=make_sources(cy, spec))
+    if rng_stream is not None:
+        # the field sources' disc positions are the only draws of these runs
+        cy.random_utils.pcg32_seed(*rng_stream)
     npart = []
     for _ in range(nsteps):
         s.forward(s.simutime.time_step)
@@ -387,14 +393,14 @@ def run_reference_sources(case, params, nsteps, spec, pset_kw):
     return out
 
 
-def save_sources(name, case, params, nsteps, spec, pset_kw):
-    res = run_reference_sources(case, params, nsteps, spec, pset_kw)
+def save_sources(name, case, params, nsteps, spec, pset_kw, rng_stream=None):
+    res = run_reference_sources(case, params, nsteps, spec, pset_kw, rng_stream)
     inputs = {k: v for k, v in case.items() if isinstance(v, np.ndarray)}
     meta = {k: v for k, v in case.items() if not isinstance(v, np.ndarray)}
     np.savez_compressed(
         OUT / f"src_{name}.npz",
         meta=json.dumps({"params": params, "nsteps": nsteps, "sources": spec,
-                         "pset": pset_kw, "case": meta}),
+                         "pset": pset_kw, "case": meta, "rng_stream": rng_stream}),
         **{f"in_{k}": v for k, v in inputs.items()},
         **{f"out_{k}": v for k, v in res.items()})
     na = int((res["inactive"] == 0).sum())
@@ -440,6 +446,32 @@ def source_fixtures():
              spec[2]]
     save_sources("open_lsm1_euler", case, p1, 90, spec1,
                  dict(initial_pool_size=20, min_pool_size_update=5))
+
+    # releases where a field meets a criterion: three field records (the
+    # record changes at t = 60 s), a density field in kg/m2 and a source
+    # field; interior nodes only; disc positions from the global stream,
+    # seeded (5, 77) once the solver exists
+    nv = len(x)
+    srng = np.random.default_rng(31)
+    src_field = np.zeros((3, nv))
+    for r in range(3):
+        src_field[r, srng.choice(nv, 6, replace=False)] = 1.0
+    dens = np.stack([0.01 + 0.008 * (1 + np.sin(2 * np.pi * x / 150.0))] * 3)
+    casef = dict(case, times=np.array([0.0, 60.0, 200.0]), elevation=np.ones((3, nv)),
+                 velocity_x=np.stack([u0, 1.2 * u0, 1.3 * u0]),
+                 velocity_y=np.stack([v0, 0.5 * v0, -v0]),
+                 opt_fields=np.stack([dens, src_field]),
+                 opt_fields_names=["DENSITY", "SOURCE"], position=pos[:8])
+    specf = [
+        dict(kind="field", scheduler=dict(iteration_delta=2),
+             kwargs=dict(field_id_criteria=5, field_id_density=4, criteria="val_gt",
+                         threshold=0.5, virtual_mass=2.0, single_release=True)),
+        dict(kind="field", scheduler=dict(times=[10.0, 70.0, 71.0]),
+             kwargs=dict(field_id_criteria=5, field_id_density=4, criteria="var_geq",
+                         threshold=0.5)),
+    ]
+    save_sources("field_open_lsm1", casef, dict(p, time_scheme=2), 60, specf,
+                 dict(initial_pool_size=8, min_pool_size_update=16), rng_stream=[5, 77])
 
     # 3D log-law, LSM2 RK4 without diffusion, settling particles, a 3D
     # source every 5 iterations

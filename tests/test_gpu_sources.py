@@ -30,10 +30,10 @@ def _field_set(case):
 
 
 def _gpu(case, params, nsteps, spec, pset, precision="fp64", seed=0, sort_period=0,
-         batch=None):
+         batch=None, rng_stream=None):
     import cylag_gb300 as cg
     ps = cg.LagrangianParticleSet(case["position"], dim=case.get("dim", 2), **pset)
-    s = cg.Solver(_field_set(case), ps, params, sources=make_sources(spec),
+    s = cg.Solver(_field_set(case), ps, params, sources=make_sources(spec, rng_stream),
                   precision=precision, seed=seed, sort_period=sort_period)
     done = 0
     while done < nsteps:
@@ -48,11 +48,11 @@ def _gpu(case, params, nsteps, spec, pset, precision="fp64", seed=0, sort_period
     return out
 
 
-def _oracle(case, params, nsteps, spec, pset, seed=0):
+def _oracle(case, params, nsteps, spec, pset, seed=0, rng_stream=None):
     import oracle
     o = oracle.OracleSolver(mesh_from_case(case), fields_from_case(case), params,
                             case["position"], pset=pset, seed=seed, nthreads=8,
-                            sources=make_sources(spec),
+                            sources=make_sources(spec, rng_stream),
                             initial_pool_size=pset.get("initial_pool_size"),
                             min_pool_size_update=pset.get("min_pool_size_update", 1000))
     o.solve(nsteps)
@@ -75,7 +75,7 @@ def _check(got, want, what, rtol=RTOL):
 def test_gpu_sources_match_reference(name, sort_period, batch):
     case, meta, want = load_source(name)
     got = _gpu(case, meta["params"], meta["nsteps"], meta["sources"], meta["pset"],
-               sort_period=sort_period, batch=batch)
+               sort_period=sort_period, batch=batch, rng_stream=meta.get("rng_stream"))
     _check(got, want, f"{name} sort={sort_period} batch={batch}")
 
 
@@ -141,11 +141,11 @@ def test_gpu_manual_add_between_forward_calls():
     s.close()
 
 
-@pytest.mark.parametrize("name", ["open_lsm1_rk4", "loglaw3d_lsm2_rk4"])
+@pytest.mark.parametrize("name", ["open_lsm1_rk4", "field_open_lsm1", "loglaw3d_lsm2_rk4"])
 def test_mixed_sources_follow_plain(name):
     case, meta, want = load_source(name)
     got = _gpu(case, meta["params"], meta["nsteps"], meta["sources"], meta["pset"],
-               precision="mixed", sort_period=5)
+               precision="mixed", sort_period=5, rng_stream=meta.get("rng_stream"))
     assert got["npart"] == int(want["npart"][-1])
     both = (got["inactive"] == 0) & (want["inactive"] == 0)
     assert both.sum() >= 0.97 * (want["inactive"] == 0).sum()

@@ -5,8 +5,9 @@
   particles in the step that releases them, the one-step wait of entries of
   a pool grown in that step) reproduces the reference's runs recorded in
   tests/golden/src_*.npz: every pool entry, its tag and the pool size;
-* the schedulers and the release grids (cylag_gb300.extra) give the
-  reference's answers, step by step, when the compiled reference is present.
+* the schedulers, the release grids and the field-criterion releases
+  (cylag_gb300.extra) give the reference's answers, step by step, when the
+  compiled reference is present.
 """
 import numpy as np
 import pytest
@@ -15,14 +16,22 @@ from conftest import (X86, assert_state_close, fields_from_case, load_source, ma
                       mesh_from_case, source_names)
 
 
+def host_field_set(case):
+    """The host-side EulerianFieldSet that sources query (no device use)."""
+    import cylag_gb300 as cg
+    f = fields_from_case(case)
+    return cg.EulerianFieldSet(mesh_from_case(case), **f)
+
+
 def _oracle_run(case, meta, nthreads=1):
     import oracle
     pk = dict(meta["pset"])
     o = oracle.OracleSolver(mesh_from_case(case), fields_from_case(case), meta["params"],
                             case["position"], pset=pk, seed=0, nthreads=nthreads,
-                            sources=make_sources(meta["sources"]),
+                            sources=make_sources(meta["sources"], meta.get("rng_stream")),
                             initial_pool_size=pk.get("initial_pool_size"),
-                            min_pool_size_update=pk.get("min_pool_size_update", 1000))
+                            min_pool_size_update=pk.get("min_pool_size_update", 1000),
+                            field_set=host_field_set(case))
     sizes = []
     for _ in range(meta["nsteps"]):
         o.forward()
@@ -106,3 +115,21 @@ def test_release_grids_match_the_reference(poly, kw):
         b = cy.ParticleSource(cy.schedules(always=True), P, **kk)
         np.testing.assert_array_equal(a.init_positions(None, dim),
                                       np.asarray(b.init_positions(None, dim)))
+
+
+def test_vertex_adjacency_matches_reference():
+    from conftest import GOLDEN
+    z = np.load(GOLDEN / "mesh_open.npz")
+    from cylag_gb300.mesh import TriangularMesh
+    m = TriangularMesh(z["x"], z["y"], z["triangles"], boundary_points=z["boundary_points"],
+                       nopen=int(z["nopen"]))
+    np.testing.assert_array_equal(m.vertex_adjacency, z["vertex_adjacency"])
+
+
+def test_host_pcg32_matches_reference_streams():
+    from conftest import GOLDEN
+    from cylag_gb300.extra import HostPCG32
+    z = np.load(GOLDEN / "rng.npz")
+    for j, (seed, stream) in enumerate(z["pairs"]):
+        g = HostPCG32(int(seed), int(stream))
+        np.testing.assert_array_equal([g.uniform() for _ in range(512)], z[f"uniform_{j}"])
