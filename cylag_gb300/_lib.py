@@ -95,6 +95,10 @@ SIGNATURES = [
     ("cg_run_time", C.c_int, [P, C.POINTER(F64), C.POINTER(C.c_int64)]),
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),
+    ("cg_run_set_stranding_output", C.c_int, [P, C.c_int32]),
+    ("cg_run_stranded", C.c_int, [P, P, C.POINTER(C.c_int32)]),
+    ("cg_run_set_sections", C.c_int, [P, C.c_int32, P]),
+    ("cg_run_section_stats", C.c_int, [P, P, C.POINTER(C.c_int32)]),
     ("cg_run_resize", C.c_int, [P, C.POINTER(StateDesc)]),
     ("cg_run_added", C.c_int, [P, C.c_int32]),
     ("cg_server_create", C.c_int, [P, I32, C.c_int64, I32, F64, C.POINTER(P)]),

@@ -248,6 +248,7 @@ class LagrangianParticleSet:
             raise NotImplementedError("compute_depth is not built in the GPU step")
         self.max_stranded = max_stranded if max_stranded is not None else self.npart
         self.stranded_count = 0
+        self.stranded_positions = np.zeros((self.max_stranded, 3))
         n, d = self.npart, self.dim
         h = {}
         h["position"] = np.zeros((n, d))
@@ -401,6 +402,17 @@ class LagrangianParticleSet:
         for k in self._dev:  # in place: the run keeps pointing at these buffers
             self._dev[k].copy_(self._dev[k].index_select(0, ti))
         torch.cuda.synchronize()
+
+    def _append_stranded(self, xyz):
+        """compute_bc.pyx:109-121: appends stranded positions while the
+        buffer (max_stranded) has room."""
+        for row in np.asarray(xyz).reshape(-1, 3):
+            if self.stranded_count < self.max_stranded:
+                self.stranded_positions[self.stranded_count] = row
+                self.stranded_count += 1
+            else:
+                print("Warning: stranded particle buffer is full"
+                      "                       Increase max_stranded in LagrangianParticleSet")
 
     # ---- particles added during the run ---------------------------------------
     _PAD = {"position": 0., "velocity": 0., "fluid_velocity_seen": 0., "last_position": 0.,
@@ -566,10 +578,11 @@ class Solver:
         self.parameters.check_values()
         P = self.parameters
         self.simutime = SimuTime(P.listing, P.initial_time, P.final_time, P.time_step)
-        if control_sections:
-            raise NotImplementedError("control sections are not built in the GPU step")
         self.sources = sources
         self.control_sections = control_sections
+        # solver.pyx:97-103
+        P.control_sections = control_sections is not None
+        P.ncsec = len(control_sections) if control_sections is not None else 0
         self.particle_set = particle_set
         self.field_set = field_set
         fs, ps = field_set, particle_set
@@ -607,9 +620,26 @@ class Solver:
         _lib.check(self._ctx, self.L.cg_run_seed(self._run))
         self.initialize_particle_state()
         nopen = fs.triangular_mesh.nopen
-        self._bnd_stats_times = []
-        self._bnd_stats_data = []
         self.nopen = nopen
+        self._bnd_stats_times = []     # every step's exit counts (bnd_statistics())
+        self._bnd_stats_data = []
+        self._bnd_buf = 0              # how many of them flush_statistics has not written
+        self._csec_stats_times = []
+        self._csec_stats_data = []
+        self._csec_buf = 0
+        if P.ncsec:
+            from .extra import section_segments
+            seg = np.ascontiguousarray(section_segments(control_sections))
+            _lib.check(self._ctx, self.L.cg_run_set_sections(self._run, P.ncsec,
+                                                             seg.ctypes.data))
+        if P.stranding_output:
+            _lib.check(self._ctx, self.L.cg_run_set_stranding_output(self._run, 1))
+        # solver.pyx:209-220
+        if P.bnd_statistics or P.control_sections:
+            from .statistics import prepare_secstats_output
+            prepare_secstats_output(bool(P.bnd_statistics), nopen, P.output_rep,
+                                    P.bnd_statistics_file_name, bool(P.control_sections),
+                                    P.ncsec, P.control_sections_file_name)
 
     def _upload_mesh_fields(self):
         self._keep = upload_mesh_fields(self.L, self._ctx, self.field_set)
@@ -656,14 +686,33 @@ class Solver:
         ps._added = ps.npart > npart0
 
     def _run_steps(self, nsteps):
+        P = self.parameters
         nopen = max(1, self.nopen)
         stats = np.zeros((nsteps, nopen), dtype=np.int32)
         rc = self.L.cg_run_step(self._run, nsteps, stats.ctypes.data)
         _lib.check(self._ctx, rc)
+        csec = None
+        if P.ncsec:
+            csec = np.zeros((nsteps, P.ncsec), dtype=np.int32)
+            k = C.c_int32()
+            _lib.check(self._ctx, self.L.cg_run_section_stats(self._run, csec.ctypes.data,
+                                                              C.byref(k)))
+        if P.stranding_output:
+            cnt = C.c_int32()
+            _lib.check(self._ctx, self.L.cg_run_stranded(self._run, None, C.byref(cnt)))
+            xyz = np.zeros((cnt.value, 3))
+            _lib.check(self._ctx, self.L.cg_run_stranded(self._run, xyz.ctypes.data,
+                                                         C.byref(cnt)))
+            self.particle_set._append_stranded(xyz)
         for s in range(nsteps):
-            if self.parameters.bnd_statistics:
+            if P.bnd_statistics:
                 self._bnd_stats_times.append(self.simutime.time)
                 self._bnd_stats_data.append(stats[s, : self.nopen].copy())
+                self._bnd_buf += 1
+            if csec is not None:
+                self._csec_stats_times.append(self.simutime.time)
+                self._csec_stats_data.append(csec[s].copy())
+                self._csec_buf += 1
             self.simutime.increment()
 
     def forward(self, time_step=None, nsteps=1):
@@ -703,14 +752,41 @@ class Solver:
         self.flush_statistics()
 
     def flush_statistics(self):
-        """solver.pyx:587-630 (kept in memory: see bnd_statistics())."""
-        return None
+        """solver.pyx:587-630: appends the steps not yet written to the
+        boundary and control-section statistics files, writes the stranded
+        positions, and empties those buffers."""
+        from .statistics import write_secstats_buffer, write_stranded_particles_txt_2d
+        P = self.parameters
+        if P.bnd_statistics and self._bnd_buf > 0:
+            k = self._bnd_buf
+            write_secstats_buffer(self._bnd_stats_times[-k:], np.stack(self._bnd_stats_data[-k:]),
+                                  k, self.nopen, P.output_rep, P.bnd_statistics_file_name)
+            self._bnd_buf = 0
+        if P.stranding_output:
+            ps = self.particle_set
+            write_stranded_particles_txt_2d(P.output_rep, P.stranding_output_file_name,
+                                            ps.stranded_positions, ps.stranded_count)
+            ps.stranded_count = 0
+        if P.control_sections and self._csec_buf > 0:
+            k = self._csec_buf
+            write_secstats_buffer(self._csec_stats_times[-k:],
+                                  np.stack(self._csec_stats_data[-k:]), k, P.ncsec,
+                                  P.output_rep, P.control_sections_file_name)
+            self._csec_buf = 0
 
     def bnd_statistics(self):
-        """Per-step open-boundary exit counts, [nsteps, nopen]."""
+        """Per-step open-boundary exit counts, [nsteps, nopen] (every step
+        since the Solver was made)."""
         if not self._bnd_stats_data:
             return np.zeros((0, self.nopen), dtype=np.int32)
         return np.stack(self._bnd_stats_data)
+
+    def section_statistics(self):
+        """Per-step control-section crossing counts, [nsteps, ncsec] (every
+        step since the Solver was made)."""
+        if not self._csec_stats_data:
+            return np.zeros((0, self.parameters.ncsec), dtype=np.int32)
+        return np.stack(self._csec_stats_data)
 
     def last_kernel_ms(self):
         ms, n = C.c_double(), C.c_int32()

@@ -37,6 +37,13 @@ struct cg_run {
     DevBuf turb;          // {k, eps} per node (LSM2/LSM3 k-epsilon runs)
     DevBuf stats;
     int stats_rows = 0;
+    int stats_cols = 0;
+    DevBuf csec;                     // control-section segments {x0, y0, x1, y1}
+    std::vector<int32_t> csec_counts;  // [nsteps, ncsec] of the last cg_run_step
+    int csec_steps = 0;
+    DevBuf strand;                   // stranding output: count (first 256 B) + n records
+    bool strand_on = false;
+    std::vector<StrandRec> strand_host;  // the last cg_run_step's, in the reference's order
     DevBuf errw;
     DevBuf queue;          // walk queue: count (first 256 B) + one entry per particle
     bool use_queue = false;
@@ -641,6 +648,8 @@ int cg_run_destroy(cg_run* r) {
     dfree(r->prev);
     dfree(r->turb);
     dfree(r->stats);
+    dfree(r->csec);
+    dfree(r->strand);
     dfree(r->errw);
     dfree(r->queue);
     dfree(r->sortbuf);
@@ -729,13 +738,18 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = ensure_fields(r);
     if (rc) return rc;
-    int nopen = c->nopen > 0 ? c->nopen : 1;
-    if (r->stats_rows < nsteps) {
+    // a step's statistics row: max(1, nopen) exit counts, then the control
+    // sections' counts
+    const int nopen = c->nopen > 0 ? c->nopen : 1;
+    const int row = nopen + r->dp.ncsec;
+    if (r->stats_rows < nsteps || r->stats_cols != row) {
         dfree(r->stats);
-        if ((rc = dalloc(c, r->stats, (size_t)nsteps * nopen * sizeof(int)))) return rc;
+        if ((rc = dalloc(c, r->stats, (size_t)nsteps * row * sizeof(int)))) return rc;
         r->stats_rows = nsteps;
+        r->stats_cols = row;
     }
-    CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * nopen * sizeof(int), c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * row * sizeof(int), c->stream));
+    if (r->strand_on) CUDA_TRY(c, cudaMemsetAsync(r->strand.p, 0, sizeof(int), c->stream));
     int nev = 2 * nsteps;
     while ((int)r->ev.size() < nev) {
         cudaEvent_t e;
@@ -768,7 +782,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         }
         const DevState& run_state = sorted ? ws : r->st;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
-        int* stats = (int*)r->stats.p + (size_t)s * nopen;
+        int* stats = (int*)r->stats.p + (size_t)s * row;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
         WalkQueue wq{nullptr, nullptr};
         if (r->use_queue) {
@@ -810,11 +824,103 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     r->last_ms = tot / nsteps;
     r->last_launches = launches;
     if (bnd_stats_host && c->nopen > 0)
-        CUDA_TRY(c, cudaMemcpy(bnd_stats_host, r->stats.p, (size_t)nsteps * c->nopen * sizeof(int),
-                               cudaMemcpyDeviceToHost));
+        CUDA_TRY(c, cudaMemcpy2D(bnd_stats_host, (size_t)c->nopen * sizeof(int), r->stats.p,
+                                 (size_t)row * sizeof(int), (size_t)c->nopen * sizeof(int),
+                                 nsteps, cudaMemcpyDeviceToHost));
+    if (r->strand_on) {
+        int cnt = 0;
+        CUDA_TRY(c, cudaMemcpy(&cnt, r->strand.p, sizeof(int), cudaMemcpyDeviceToHost));
+        cnt = std::min(cnt, r->dp.strand_cap);
+        r->strand_host.resize(cnt);
+        if (cnt)
+            CUDA_TRY(c, cudaMemcpy(r->strand_host.data(), r->dp.strand_rec,
+                                   (size_t)cnt * sizeof(StrandRec), cudaMemcpyDeviceToHost));
+        // the reference appends in its particle loop: by step, then index
+        std::sort(r->strand_host.begin(), r->strand_host.end(),
+                  [](const StrandRec& a, const StrandRec& b) {
+                      return a.step != b.step ? a.step < b.step : a.index < b.index;
+                  });
+    }
+    if (r->dp.ncsec > 0) {
+        r->csec_counts.resize((size_t)nsteps * r->dp.ncsec);
+        CUDA_TRY(c, cudaMemcpy2D(r->csec_counts.data(), (size_t)r->dp.ncsec * sizeof(int),
+                                 (const int*)r->stats.p + nopen, (size_t)row * sizeof(int),
+                                 (size_t)r->dp.ncsec * sizeof(int), nsteps,
+                                 cudaMemcpyDeviceToHost));
+        r->csec_steps = nsteps;
+    }
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
     if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
+    return CG_OK;
+}
+
+int cg_run_set_sections(cg_run* r, int32_t ncsec, const double* segments) {
+    if (!r || ncsec < 0 || (ncsec > 0 && !segments)) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (ncsec > CG_MAX_SECTIONS)
+        return set_err(c, CG_EINVAL, "%d control sections, at most %d", ncsec, CG_MAX_SECTIONS);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    dfree(r->csec);
+    r->dp.ncsec = 0;
+    r->dp.csec = nullptr;
+    r->csec_counts.clear();
+    r->csec_steps = 0;
+    if (ncsec == 0) return CG_OK;
+    int rc = dalloc(c, r->csec, (size_t)ncsec * sizeof(double4));
+    if (rc) return rc;
+    CUDA_TRY(c, cudaMemcpy(r->csec.p, segments, (size_t)ncsec * sizeof(double4),
+                           cudaMemcpyHostToDevice));
+    r->dp.ncsec = ncsec;
+    r->dp.csec = (const double4*)r->csec.p;
+    return CG_OK;
+}
+
+// stranding record buffer for r->st.n particles (a stranded particle is
+// deleted, so one call records each particle at most once)
+static int alloc_strand(cg_ctx* c, cg_run* r) {
+    dfree(r->strand);
+    r->dp.strand_cap = 0;
+    r->dp.strand_count = nullptr;
+    r->dp.strand_rec = nullptr;
+    r->strand_host.clear();
+    if (!r->strand_on) return CG_OK;
+    const size_t cap = r->st.n > 0 ? (size_t)r->st.n : 1;
+    int rc = dalloc(c, r->strand, 256 + cap * sizeof(StrandRec));
+    if (rc) return rc;
+    r->dp.strand_cap = (int)cap;
+    r->dp.strand_count = (int*)r->strand.p;
+    r->dp.strand_rec = (StrandRec*)((char*)r->strand.p + 256);
+    return CG_OK;
+}
+
+int cg_run_set_stranding_output(cg_run* r, int32_t on) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    r->strand_on = on != 0;
+    return alloc_strand(c, r);
+}
+
+int cg_run_stranded(const cg_run* r, double* xyz, int32_t* count) {
+    if (!r) return CG_EINVAL;
+    if (count) *count = (int32_t)r->strand_host.size();
+    if (xyz)
+        for (size_t k = 0; k < r->strand_host.size(); ++k) {
+            xyz[3 * k] = r->strand_host[k].x;
+            xyz[3 * k + 1] = r->strand_host[k].y;
+            xyz[3 * k + 2] = r->strand_host[k].z;
+        }
+    return CG_OK;
+}
+
+int cg_run_section_stats(const cg_run* r, int32_t* counts, int32_t* nsteps) {
+    if (!r) return CG_EINVAL;
+    if (nsteps) *nsteps = r->csec_steps;
+    if (counts && !r->csec_counts.empty())
+        std::memcpy(counts, r->csec_counts.data(), r->csec_counts.size() * sizeof(int32_t));
     return CG_OK;
 }
 
@@ -856,7 +962,7 @@ int cg_run_resize(cg_run* r, const cg_state_desc* s) {
     st.tag = s->tag;
     st.diameter = s->diameter;
     st.rng = s->rng_state;
-    return CG_OK;
+    return alloc_strand(c, r);
 }
 
 int cg_run_added(cg_run* r, int32_t n_init) {

@@ -88,6 +88,14 @@ struct DevFields {
     const FT* __restrict__ turb;   // [nnodes][2]
 };
 
+// one stranded particle (compute_bc.pyx:109-121): its position when it
+// stranded, with the step and the particle's index, which order the records
+// as the reference's particle loop appends them
+struct StrandRec {
+    int step, index;
+    double x, y, z;
+};
+
 struct DevParams {
     int model, time_scheme, rng_method, diffmod;
     int bc_on, bc_type, max_rebounds, bnd_statistics, nopen;
@@ -105,7 +113,22 @@ struct DevParams {
     int added_mass, drag_model, nuopt, edge_opt;
     double a0c, a1c, a2c, a3c;
     double tl_h, tl_v;               // diffusion_lsm3_tl_horizontal / _vertical
+    // control sections: one segment {x0, y0, x1, y1} each; their per-step
+    // counts follow the nopen exit counts in a step's statistics row
+    int ncsec;
+    const double4* csec;
+    // stranding output: records of this call's stranded particles
+    int strand_cap;
+    int* strand_count;
+    StrandRec* strand_rec;
 };
+
+__device__ __forceinline__ void record_strand(const DevParams& p, int step, int index, double x,
+                                              double y, double z) {
+    if (p.strand_rec == nullptr) return;
+    const int k = atomicAdd(p.strand_count, 1);
+    if (k < p.strand_cap) p.strand_rec[k] = StrandRec{step, index, x, y, z};
+}
 
 struct DevState {
     int n;
@@ -338,6 +361,24 @@ __device__ inline bool intersec2d(double p0x, double p0y, double p1x, double p1y
     if (o3 == 0 && on_segment(s0x, s0y, s1x, s1y, p0x, p0y)) return true;
     if (o4 == 0 && on_segment(s0x, s0y, s1x, s1y, p1x, p1y)) return true;
     return false;
+}
+
+// Control sections (solver.pyx:542-549, control_shapes.pyx:74-101,
+// intersections.pyx:150-192): once a particle's step is over, each section
+// whose segment meets the step's segment (step-start position -> final
+// position; both (0, 0) when the step deleted the particle, as the reference
+// tests the zeroed arrays) counts it once.  The reference's ControlSection
+// tests only its first segment (nseg = poly.shape[1] - 1 = 1), so a section
+// is that one segment here.  stats: the step's row, max(1, nopen) exit
+// counts then the sections'.
+__device__ __forceinline__ void count_sections(const DevParams& p, int* stats, double x0,
+                                               double y0, double x1, double y1) {
+    if (p.ncsec == 0 || stats == nullptr) return;
+    int* row = stats + (p.nopen > 0 ? p.nopen : 1);
+    for (int c = 0; c < p.ncsec; ++c) {
+        const double4 g = p.csec[c];
+        if (intersec2d(x0, y0, x1, y1, g.x, g.y, g.z, g.w)) atomicAdd(&row[c], 1);
+    }
 }
 
 // Global point location: first triangle (lowest id) in the point's grid

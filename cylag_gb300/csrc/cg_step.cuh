@@ -30,6 +30,7 @@ struct Particle {
     double up[3];     // velocity
     double us[3];     // fluid velocity seen
     int tri, tri0, ltri, ll, ll0;
+    int pidx = 0, pstep = 0;   // caller's particle index and step (stranding records)
     uint32_t err;
     bool deleted;
     bool defer;       // in: 2D final localization may be deferred to the walk queue
@@ -650,6 +651,7 @@ struct Particle {
         if (bnd_j != -1) {
             int lab = __ldg(&m.elabel[bnd_j]);
             if (lab == BND_WALL_REF && p.strand > 0.) strand_condition = rng_uniform(rng) < p.strand;
+            if (strand_condition) record_strand(p, pstep, pidx, x[0], x[1], DIM == 3 ? x[2] : 0.);
             if (lab == BND_WALL_REF && !strand_condition) {
                 int bnd_jj = bnd_j;
                 for (int rc = 0; tri == PART_LOC_O && rc < p.max_rebounds; ++rc) {
@@ -757,6 +759,7 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
         q.x[d] = s.pos[(size_t)i * D + d];
         q.x0[d] = q.x[d];
     }
+    const double sx = q.x[0], sy = q.x[1];   // last_position of the step
     bool need_vel = (MODEL >= 2) || aux >= 2;
     if (need_vel) {
 #pragma unroll
@@ -791,6 +794,8 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
         return;
     }
     if (p.bc_on) {
+        q.pidx = ai;
+        q.pstep = step_index;
         q.compute_bc(bnd_j, stats);
     } else if (q.tri == PART_LOC_O || q.ll == PART_LOC_B || q.ll == PART_LOC_A) {
         q.deleted = true;
@@ -798,6 +803,11 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
     e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
     q.store(s, i, aux, step_index, lastv);
+    if (p.ncsec) {
+        const bool del = q.deleted;
+        count_sections(p, stats, del ? 0. : sx, del ? 0. : sy, del ? 0. : q.x[0],
+                       del ? 0. : q.x[1]);
+    }
 }
 
 // aux: 0 = state only; 1 = also write velocity / fluid velocity seen;
@@ -917,11 +927,18 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
         else path_walk(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
         if (nk == -1 && bnd == -1) nk = grid_locate(m, w.xn, w.yn);
         q.tri = nk;
+        q.pidx = aux_index(s, i);
+        q.pstep = step_index;
         if (p.bc_on) q.compute_bc(bnd, stats);
         else if (q.tri == PART_LOC_O) q.deleted = true;
         uint32_t e = q.err | q.rng.err;
         if (e) atomicOr(err_word, e);
         q.store(s, i, aux, step_index, lastv);
+        if (p.ncsec) {
+            const bool del = q.deleted;
+            count_sections(p, stats, del ? 0. : x0.x, del ? 0. : x0.y, del ? 0. : q.x[0],
+                           del ? 0. : q.x[1]);
+        }
     }
 }
 

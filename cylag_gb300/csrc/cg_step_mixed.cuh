@@ -184,8 +184,10 @@ static __device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<f
                                       const DevParams& p, const ZigTables& z64, Rng& rng,
                                       double2 x0, float up0, float up1, int tri0, int ltri,
                                       int bnd_j, int* stats, double& xn, double& yn, int& tri,
-                                      bool& deleted) {
+                                      bool& deleted, int pidx, int pstep) {
     Particle<2, float> q(m, f, p, z64);
+    q.pidx = pidx;
+    q.pstep = pstep;
     q.rng = rng;
     q.x[0] = xn; q.x[1] = yn;
     q.x0[0] = x0.x; q.x0[1] = x0.y;
@@ -301,7 +303,8 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
     bool deleted = false;
     if (bnd_j != -1 || tri == PART_LOC_O)
-        bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted);
+        bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted,
+                 aux_index(s, i), step_index);
     if (rng.err) atomicOr(err_word, rng.err);
 
     if (deleted) {
@@ -317,8 +320,10 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         s.lowerlayer[a] = 0;
         s.tag[i] = -2 - step_index;
         s.rng[i] = rng.state;
+        if (p.ncsec) count_sections(p, stats, 0., 0., 0., 0.);
         return;
     }
+    if (p.ncsec) count_sections(p, stats, x0.x, x0.y, xn, yn);
     __stcs(reinterpret_cast<double2*>(s.pos) + i, make_double2(xn, yn));
     __stcs(&s.tri[i], tri);
     __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);

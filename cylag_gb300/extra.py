@@ -417,3 +417,70 @@ class ParticleSourceFromField:
                 p[j, 1] = y0 + r * np.sin(a)
             out.append(p)
         return np.concatenate(out, axis=0) if out else np.zeros((0, 2))
+
+
+# ---------------------------------------------------------------------------
+# control sections (cylag/extra/control_shapes.pyx)
+# ---------------------------------------------------------------------------
+class ControlSection:
+    """control_shapes.pyx:7-101: counts the particles whose step crosses the
+    section.  As in the reference, ``nseg = poly.shape[1] - 1``, which for an
+    (npoint, 2) polyline is 1: only the first segment poly[0] -> poly[1] is
+    tested.  The counting itself runs in the GPU step."""
+
+    def __init__(self, poly):
+        self.poly = np.asarray(poly, dtype=np.float64)
+        self.nseg = self.poly.shape[1] - 1
+
+    def cross(self, pos_0, pos_1):
+        for i in range(self.nseg):
+            if segments_intersect(pos_0[0], pos_0[1], pos_1[0], pos_1[1],
+                                  self.poly[i, 0], self.poly[i, 1],
+                                  self.poly[i + 1, 0], self.poly[i + 1, 1]):
+                return 1
+        return 0
+
+
+def _orientation(ax, ay, bx, by, cx, cy):
+    """geom/utils.pyx:254-280: 0 collinear, 1 clockwise, 2 counter-clockwise."""
+    d = (ay - by) * (cx - ax) - (ax - bx) * (cy - ay)
+    return 0 if d == 0. else (1 if d > 0. else 2)
+
+
+def _on_segment(ax, ay, bx, by, cx, cy):
+    return min(ax, bx) <= cx <= max(ax, bx) and min(ay, by) <= cy <= max(ay, by)
+
+
+def segments_intersect(p0x, p0y, p1x, p1y, s0x, s0y, s1x, s1y):
+    """intersections.pyx:150-192: segment p0-p1 meets segment s0-s1."""
+    o1 = _orientation(p0x, p0y, p1x, p1y, s0x, s0y)
+    o2 = _orientation(p0x, p0y, p1x, p1y, s1x, s1y)
+    o3 = _orientation(s0x, s0y, s1x, s1y, p0x, p0y)
+    o4 = _orientation(s0x, s0y, s1x, s1y, p1x, p1y)
+    if o1 != o2 and o3 != o4:
+        return 1
+    if o1 == 0 and _on_segment(p0x, p0y, p1x, p1y, s0x, s0y):
+        return 1
+    if o2 == 0 and _on_segment(p0x, p0y, p1x, p1y, s1x, s1y):
+        return 1
+    if o3 == 0 and _on_segment(s0x, s0y, s1x, s1y, p0x, p0y):
+        return 1
+    if o4 == 0 and _on_segment(s0x, s0y, s1x, s1y, p1x, p1y):
+        return 1
+    return 0
+
+
+def section_segments(sections):
+    """[ncsec, 4] {x0, y0, x1, y1} of each section's tested segment, for the
+    GPU step; a section with no segment gets NaNs (never crosses)."""
+    out = np.full((len(sections), 4), np.nan)
+    for c, cs in enumerate(sections):
+        poly = np.asarray(cs.poly, dtype=np.float64)
+        nseg = poly.shape[1] - 1
+        if nseg > 1:
+            raise NotImplementedError(
+                "control section polygon of shape (n, >2): the reference's nseg = "
+                "poly.shape[1] - 1 would test rows as segments")
+        if nseg == 1 and poly.shape[0] >= 2:
+            out[c] = [poly[0, 0], poly[0, 1], poly[1, 0], poly[1, 1]]
+    return out

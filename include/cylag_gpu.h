@@ -196,6 +196,31 @@ int cg_run_errors(cg_run *run, uint32_t *flags);
 /* Number of active particles and deleted-this-call counts are derived by the
  * caller from tri (tri == -1 inactive). */
 
+/* ---- control sections ---------------------------------------------------- */
+#define CG_MAX_SECTIONS 4096
+/* Solver(control_sections=[...]) (solver.pyx:97-103, 542-549): each step
+ * counts, per section, the particles whose step segment (step-start
+ * position -> final position, both (0, 0) after a deletion in that step)
+ * meets the section (ControlSection.c_cross, control_shapes.pyx:74-101).
+ * The reference's ControlSection tests its first segment only
+ * (nseg = poly.shape[1] - 1 = 1): segments[4*c .. 4*c+3] = x0, y0, x1, y1
+ * of section c's first segment.  ncsec = 0 removes them.  Synchronous. */
+int cg_run_set_sections(cg_run *run, int32_t ncsec, const double *segments);
+/* The counts of the last cg_run_step: counts[nsteps][ncsec] (caller-sized
+ * from *nsteps; pass counts = NULL to ask for nsteps first).  Host copy,
+ * no device work. */
+int cg_run_section_stats(const cg_run *run, int32_t *counts, int32_t *nsteps);
+
+/* ---- stranding output --------------------------------------------------- */
+/* parameters['stranding_output'] (compute_bc.pyx:109-121): on, each
+ * cg_run_step records the position of every particle that strands on a wall
+ * (its end-of-step position; z = 0 in 2D). */
+int cg_run_set_stranding_output(cg_run *run, int32_t on);
+/* The last cg_run_step's stranded positions, xyz[count][3], in the order the
+ * reference's particle loop appends them (by step, then particle index);
+ * xyz = NULL asks for the count only.  Host copy, no device work. */
+int cg_run_stranded(const cg_run *run, double *xyz, int32_t *count);
+
 /* ---- particles added during a run -------------------------------------- */
 /* Points the run at a new (larger) particle state after the caller grew
  * its arrays (LagrangianParticleSet._increase_pool_size,

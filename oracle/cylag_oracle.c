@@ -1760,6 +1760,65 @@ static void reflect_velocity(ctx_t *c, double *vel, double ex0, double ey0,
     }
 }
 
+/* control sections (control_shapes.pyx:74-101): the first segment
+ * {x0, y0, x1, y1} of each; counts of the current cgo_step call */
+static int g_ncsec = 0;
+static double g_csec[4 * 64];
+static int32_t g_csec_counts[64];
+
+int cgo_set_sections(int n, const double *seg) {
+    if (n < 0 || n > 64) return -1;
+    g_ncsec = n;
+    if (n) memcpy(g_csec, seg, (size_t)n * 4 * sizeof(double));
+    memset(g_csec_counts, 0, sizeof g_csec_counts);
+    return 0;
+}
+
+void cgo_take_section_counts(int32_t *out) {
+    memcpy(out, g_csec_counts, (size_t)g_ncsec * sizeof(int32_t));
+    memset(g_csec_counts, 0, sizeof g_csec_counts);
+}
+
+/* stranding output (compute_bc.pyx:109-121): {index, x, y, z} of each
+ * stranded particle of the current cgo_step call, in any order (the caller
+ * sorts by index, the reference's loop order) */
+static int g_strand_on = 0;
+static double *g_strand = NULL;
+static int g_strand_n = 0, g_strand_cap = 0;
+
+void cgo_set_stranding(int on) {
+    g_strand_on = on;
+    g_strand_n = 0;
+}
+
+int cgo_take_stranded(double *out, int cap) {
+    int n = g_strand_n < cap ? g_strand_n : cap;
+    if (out) memcpy(out, g_strand, (size_t)n * 4 * sizeof(double));
+    g_strand_n = 0;
+    return n;
+}
+
+static void record_strand(int i, double x, double y, double z) {
+#pragma omp critical(cgo_strand)
+    {
+        if (g_strand_n == g_strand_cap) {
+            int cap = g_strand_cap ? 2 * g_strand_cap : 256;
+            double *b = (double *)realloc(g_strand, (size_t)cap * 4 * sizeof(double));
+            if (b) {
+                g_strand = b;
+                g_strand_cap = cap;
+            }
+        }
+        if (g_strand_n < g_strand_cap) {
+            double *r = g_strand + 4 * (size_t)g_strand_n++;
+            r[0] = i;
+            r[1] = x;
+            r[2] = y;
+            r[3] = z;
+        }
+    }
+}
+
 static void compute_bc(ctx_t *c, int bnd_j, int32_t *bnd_stats) {
     const cgo_params *p = c->p;
     const cgo_mesh *m = c->m;
@@ -1775,6 +1834,8 @@ static void compute_bc(ctx_t *c, int bnd_j, int32_t *bnd_stats) {
         int lab = m->edge_labels[bnd_j];
         if (lab == BND_WALL_REF && strand > 0.)
             strand_condition = rng_uniform(&c->rng) < strand;
+        if (strand_condition && g_strand_on)
+            record_strand(i, POS(c, 0), POS(c, 1), c->pd == 3 ? POS(c, 2) : 0.0);
         if (lab == BND_WALL_REF && strand_condition == 0) {
             int bnd_jj = bnd_j, rebound_count = 0;
             while (s->tri[i] == PART_LOC_O && rebound_count < p->max_wall_rebounds) {
@@ -1973,6 +2034,16 @@ int cgo_step_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
                 if (s->tri[i] == PART_LOC_O) delete_single(s, c.pd, i);
                 if (s->lowerlayer[i] == PART_LOC_B) delete_single(s, c.pd, i);
                 if (s->lowerlayer[i] == PART_LOC_A) delete_single(s, c.pd, i);
+            }
+            /* control sections, solver.pyx:542-549 (zeroed arrays when the
+             * step deleted the particle) */
+            for (int cs = 0; cs < g_ncsec; cs++) {
+                const double *g = g_csec + 4 * cs;
+                if (intersec2d(s->last_pos[i * c.pd], s->last_pos[i * c.pd + 1],
+                               s->pos[i * c.pd], s->pos[i * c.pd + 1], g[0], g[1], g[2], g[3])) {
+#pragma omp atomic
+                    g_csec_counts[cs] += 1;
+                }
             }
         }
         ctx_end(&c);

@@ -126,6 +126,10 @@ int cgo_init_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
  * (interpolation outside the mesh or the column, non-finite LSM2/LSM3
  * coefficients, ...); their state is then unspecified.  Resets the count. */
 int cgo_take_errors(void);
+void cgo_set_stranding(int on);
+int cgo_set_sections(int n, const double *seg);
+void cgo_take_section_counts(int32_t *out);
+int cgo_take_stranded(double *out, int cap);
 
 #ifdef __cplusplus
 }

@@ -111,6 +111,12 @@ def lib():
             L.cgo_init_range.restype = C.c_int
             L.cgo_take_errors.argtypes = []
             L.cgo_take_errors.restype = C.c_int
+            L.cgo_set_stranding.argtypes = [C.c_int]
+            L.cgo_take_stranded.argtypes = [P, C.c_int]
+            L.cgo_take_stranded.restype = C.c_int
+            L.cgo_set_sections.argtypes = [C.c_int, P]
+            L.cgo_set_sections.restype = C.c_int
+            L.cgo_take_section_counts.argtypes = [P]
             L.cgo_retag.argtypes = [P, C.c_int]
             L.cgo_retag.restype = C.c_int
             L.cgo_xy_localize.argtypes = [P, C.c_int, C.c_double, C.c_double,
@@ -172,7 +178,8 @@ class OracleSolver:
 
     def __init__(self, mesh, fields, params, position, pset=None, seed=0,
                  tags=None, nthreads=1, diameter=None, sources=None, initial_pool_size=None,
-                 min_pool_size_update=1000, field_set=None):
+                 min_pool_size_update=1000, field_set=None, control_sections=None,
+                 max_stranded=None):
         from cylag_gb300.parameters import Parameters
         L = lib()
         self.L = L
@@ -283,6 +290,16 @@ class OracleSolver:
         self.bnd_stats = []
         if not self.frozen:
             self._time_interpolation(P.initial_time)
+        # control sections: first segment of each (control_shapes.pyx:17-19)
+        self.sections = []
+        for cs in control_sections or []:
+            poly = np.asarray(cs.poly if hasattr(cs, "poly") else cs, dtype=np.float64)
+            self.sections.append([poly[0, 0], poly[0, 1], poly[1, 0], poly[1, 1]])
+        self.section_stats = []
+        # stranding output buffer (lagrangian_particle_set.pyx:225-228)
+        self.stranding = bool(P.stranding_output)
+        self.max_stranded = n if max_stranded is None else int(max_stranded)
+        self.stranded = []
         self.L.cgo_take_errors()
         self.L.cgo_init_range(C.byref(self._m), C.byref(self._fields()), C.byref(self._p),
                               C.byref(self._s), 0, n)
@@ -401,8 +418,24 @@ class OracleSolver:
         self._bind(npart)
         self._p.time = self.time
         stats = np.zeros(max(1, self.nopen), np.int32)
+        seg = np.ascontiguousarray(np.array(self.sections, dtype=np.float64).reshape(-1, 4))
+        self.L.cgo_set_sections(len(self.sections), _p(seg))
+        self.L.cgo_set_stranding(int(self.stranding))
         self.L.cgo_step(C.byref(self._m), C.byref(self._fields()), C.byref(self._p),
                         C.byref(self._s), _p(stats), self.nthreads)
+        if self.sections:
+            cnt = np.zeros(len(self.sections), np.int32)
+            self.L.cgo_take_section_counts(_p(cnt))
+            self.section_stats.append(cnt)
+        if self.stranding:
+            buf = np.zeros((npart, 4))
+            k = self.L.cgo_take_stranded(_p(buf), npart)
+            rec = buf[:k][np.argsort(buf[:k, 0], kind="stable")]
+            for r in rec:   # compute_bc.pyx:109-121: kept while the buffer has room
+                if len(self.stranded) < self.max_stranded:
+                    self.stranded.append(r[1:].copy())
+        self.L.cgo_set_sections(0, None)
+        self.L.cgo_set_stranding(0)
         self._raise_errors(f"the step at t={self.time}")
         self.maxtag = self.L.cgo_retag(C.byref(self._s), self.maxtag)
         self._bind()

@@ -35,8 +35,12 @@ def golden_names():
     return sorted(p.stem[len("traj_"):] for p in GOLDEN.glob("traj_*.npz"))
 
 
-def load_golden(name):
-    z = np.load(GOLDEN / f"traj_{name}.npz", allow_pickle=False)
+def section_names():
+    return sorted(p.stem[len("sec_"):] for p in GOLDEN.glob("sec_*.npz"))
+
+
+def load_golden(name, prefix="traj"):
+    z = np.load(GOLDEN / f"{prefix}_{name}.npz", allow_pickle=False)
     meta = json.loads(str(z["meta"]))
     case = dict(meta["case"])
     for k in z.files:
@@ -104,7 +108,8 @@ def run_oracle(case, meta, nthreads=1, nsteps=None, seed=None):
     import oracle
     o = oracle.OracleSolver(mesh_from_case(case), fields_from_case(case), meta["params"],
                             case["position"], pset=meta.get("pset"),
-                            seed=meta["seed"] if seed is None else seed, nthreads=nthreads)
+                            seed=meta["seed"] if seed is None else seed, nthreads=nthreads,
+                            control_sections=[np.array(q) for q in meta.get("sections") or []])
     o.solve(meta["nsteps"] if nsteps is None else nsteps)
     return o
 

@@ -101,9 +101,13 @@ def mesh_fixture():
     np.savez_compressed(OUT / "mesh_open.npz", **out)
 
 
-def run_reference(case, params, nsteps, seed=0, pset_kw=None):
+def run_reference(case, params, nsteps, seed=0, pset_kw=None, sections=None):
     """Run every particle through its own reference Solver with
-    pcg32_seed(seed, tag) and return the stacked final state."""
+    pcg32_seed(seed, tag) and return the stacked final state.  With
+    ``sections`` (polylines), also the control-section counts summed over
+    the particles ([nsteps, ncsec]); with stranding output on, the stranded
+    positions in the order one Solver over all particles appends them (by
+    step, then particle index)."""
     cy = _cylag()
     R = cy.random_utils
     pset_kw = dict(pset_kw or {})
@@ -123,15 +127,25 @@ def run_reference(case, params, nsteps, seed=0, pset_kw=None):
     res = {k: [] for k in keys + ("tri", "last_tri", "lowerlayer", "inactive")}
     nopen = case.get("nopen", 0)
     stats = np.zeros((nsteps, max(1, nopen)), dtype=np.int64)
+    ncsec = len(sections or [])
+    csec = np.zeros((nsteps, max(1, ncsec)), dtype=np.int64)
+    stranded = []
     for i, p in enumerate(case["position"]):
         R.pcg32_seed(seed, i)
         ps = cy.LagrangianParticleSet(np.array(p, dtype=np.float64)[None, :], dim=dim, **pset_kw)
         if "diameter" in case:
             ps.diameter[0] = case["diameter"][i]
             ps.volume[0] = np.pi * case["diameter"][i] ** 3 / 6.
-        s = cy.Solver(fset, ps, params)
-        for _ in range(nsteps):
+        cs = None if sections is None else [cy.ControlSection(np.array(q, dtype=np.float64))
+                                            for q in sections]
+        s = cy.Solver(fset, ps, params, control_sections=cs)
+        for it in range(nsteps):
+            before = ps.stranded_count
             s.forward(s.simutime.time_step)
+            for k in range(before, ps.stranded_count):
+                stranded.append((it, i, *np.asarray(ps.stranded_positions)[k]))
+        if ncsec:
+            csec[:, :ncsec] += np.asarray(s._csec_stats_data)[:nsteps, :ncsec]
         for k in keys:
             res[k].append(np.asarray(getattr(ps, k))[0].copy())
         res["tri"].append(ps.tri[0])
@@ -142,21 +156,31 @@ def run_reference(case, params, nsteps, seed=0, pset_kw=None):
             stats += np.asarray(s._bnd_stats_data)[:nsteps]
     out = {k: np.array(v) for k, v in res.items()}
     out["bnd_stats"] = stats[:, :nopen]
+    if ncsec:
+        out["csec_stats"] = csec[:, :ncsec]
+    if params.get("stranding_output"):
+        stranded.sort(key=lambda r: (r[0], r[1]))
+        out["stranded"] = np.array([r[2:] for r in stranded], dtype=np.float64).reshape(-1, 3)
     return out
 
 
-def save_traj(name, case, params, nsteps, seed=0, pset_kw=None):
-    res = run_reference(case, params, nsteps, seed, pset_kw)
+def save_traj(name, case, params, nsteps, seed=0, pset_kw=None, sections=None, prefix="traj"):
+    res = run_reference(case, params, nsteps, seed, pset_kw, sections)
     inputs = {k: v for k, v in case.items() if isinstance(v, np.ndarray)}
     meta = {k: v for k, v in case.items() if not isinstance(v, np.ndarray)}
     np.savez_compressed(
-        OUT / f"traj_{name}.npz",
+        OUT / f"{prefix}_{name}.npz",
         meta=json.dumps({"params": params, "nsteps": nsteps, "seed": seed,
-                         "pset": pset_kw or {}, "case": meta}),
+                         "pset": pset_kw or {}, "case": meta, "sections": sections}),
         **{f"in_{k}": v for k, v in inputs.items()},
         **{f"out_{k}": v for k, v in res.items()})
     na = int((res["inactive"] == 0).sum())
-    print(f"traj_{name}: {len(case['position'])} particles x {nsteps} steps, {na} active")
+    extra = ""
+    if "csec_stats" in res:
+        extra += f", crossings {res['csec_stats'].sum(0).tolist()}"
+    if "stranded" in res:
+        extra += f", {len(res['stranded'])} stranded"
+    print(f"{prefix}_{name}: {len(case['position'])} particles x {nsteps} steps, {na} active{extra}")
 
 
 def traj_fixtures():
@@ -489,8 +513,44 @@ def source_fixtures():
                  dict(min_pool_size_update=10, particle_density=1200.))
 
 
+# ---------------------------------------------------------------------------
+# control sections and stranding output
+# ---------------------------------------------------------------------------
+def section_fixtures():
+    # 2D open channel, LSM1 diffusion, walls with stranding, open exits
+    x, y, tri, bp, nopen = open_channel()
+    u = 0.4 + 0.0 * x
+    v = 0.05 * np.sin(2 * np.pi * x / 400.0)
+    rng = np.random.default_rng(12)
+    pos = np.stack([rng.uniform(5.0, 395.0, 80), rng.uniform(0.5, 99.5, 80)], 1)
+    case = dict(x=x, y=y, triangles=tri, boundary_points=bp, nopen=nopen, times=np.zeros(1),
+                elevation=np.ones((1, len(x))), velocity_x=u[None, :], velocity_y=v[None, :],
+                position=pos)
+    p = dict(model=1, diffusion_model=1, horizontal_diffusivity=0.8, time_scheme=1,
+             frozen_eulerian_fields=True, time_step=2.0, final_time=400.0,
+             bnd_statistics=True, stranding_probability=0.3, stranding_output=True)
+    sections = [
+        [[200.0, -10.0], [200.0, 110.0]],                  # across the channel
+        [[100.0, 20.0], [300.0, 80.0], [350.0, 0.0]],      # first segment only counts
+        [[50.0, 50.0], [380.0, 50.0]],                     # along the flow
+        [[0.0, 0.0], [0.0, 100.0]],                        # the inlet line (and the origin)
+    ]
+    save_traj("open_lsm1", case, p, 150, seed=3, sections=sections, prefix="sec")
+    # RK4 without diffusion: deterministic crossings
+    p2 = dict(p, diffusion_model=0, time_scheme=4, stranding_probability=0.5)
+    save_traj("open_lsm1_rk4", case, p2, 150, seed=3, sections=sections, prefix="sec")
+
+    # 3D sigma layers, LSM2 DI with k-epsilon: walls strand, sections in (x, y)
+    c3 = _loglaw3d(npart=60)
+    p3 = dict(model=2, time_scheme=5, diffusion_model=3, diffusion_lsm2_option=2,
+              frozen_eulerian_fields=True, time_step=1.0, final_time=100.0,
+              stranding_probability=0.4, stranding_output=True)
+    sec3 = [[[0.0, 100.0], [400.0, 100.0]], [[150.0, -5.0], [250.0, 205.0]]]
+    save_traj("loglaw3d_lsm2", c3, p3, 60, seed=8, sections=sec3, prefix="sec")
+
+
 GROUPS = {"rng": rng_fixture, "mesh": mesh_fixture, "lsm1": traj_fixtures,
-          "lsm23": lsm23_fixtures, "sources": source_fixtures}
+          "lsm23": lsm23_fixtures, "sources": source_fixtures, "sections": section_fixtures}
 
 if __name__ == "__main__":
     for g in (sys.argv[1:] or list(GROUPS)):
