@@ -38,6 +38,7 @@ UNITS = {
     "cg_serve_plain.cu": ["-fmad=false"],
     "cg_serve_mixed.cu": [],
     "cg_sort.cu": [],
+    "cg_snapshot.cpp": ["-Xcompiler", "-pthread"],
 }
 
 
@@ -49,7 +50,8 @@ def nvcc() -> str:
 
 
 def _sources_newest() -> float:
-    files = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+    files = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) +
+             list(CSRC.glob("*.cpp")))
     files += list(INCLUDE.glob("*.h")) + [Path(__file__)]
     return max(f.stat().st_mtime for f in files)
 
@@ -75,7 +77,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 1)) as ex:
         objs = list(ex.map(one, UNITS.items()))
     tmp = LIB.with_suffix(f".so.{os.getpid()}")
-    cmd = [exe, *ARCH, "-shared", *map(str, objs), "-o", str(tmp), "-lcudart"]
+    cmd = [exe, *ARCH, "-shared", *map(str, objs), "-o", str(tmp), "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -286,6 +286,7 @@ class LagrangianParticleSet:
         h["tag"] = np.arange(n, dtype=np.int32)
         h["diameter"] = np.full(n, float(particle_diameter))
         self.maxtag = n - 1
+        self._added = False     # entries set to tri = -2 since the run's last step
         self._host = h
         self._dev = None
         self._ctx = None
@@ -640,6 +641,13 @@ class Solver:
             prepare_secstats_output(bool(P.bnd_statistics), nopen, P.output_rep,
                                     P.bnd_statistics_file_name, bool(P.control_sections),
                                     P.ncsec, P.control_sections_file_name)
+        # solver.pyx:199-224: particle output header and the initial snapshot
+        self._snapshots = None
+        if P.output_file:
+            from .output import SnapshotWriter, prepare_output
+            prepare_output(ps, P.output_rep, P.output_file_format, P.output_file_name, P.model)
+            self._snapshots = SnapshotWriter(P, P.model)
+            self._snapshots.take(ps, self.simutime.time, 0)
 
     def _upload_mesh_fields(self):
         self._keep = upload_mesh_fields(self.L, self._ctx, self.field_set)
@@ -724,20 +732,28 @@ class Solver:
             raise ValueError("forward(time_step) must equal parameters['time_step']")
         t0 = self.simutime.time
         ps = self.particle_set
-        if not self.sources and not getattr(ps, "_added", False):
+        P = self.parameters
+        period = P.output_printout_period if self._snapshots is not None else 0
+        if not self.sources and not ps._added and not period:
             self._run_steps(nsteps)
         else:
             clock = _SimuTimeView(self.simutime)
             batch = 0
             for _ in range(nsteps):
-                released = self._released(clock)
-                if released or getattr(ps, "_added", False):
+                released = self._released(clock) if self.sources else []
+                if released or ps._added:
                     if batch:
                         self._run_steps(batch)
                         batch = 0
                     self._add(released)
                 batch += 1
                 clock.advance()
+                # solver.pyx:557-566: snapshot after iterations that are
+                # multiples of output_printout_period
+                if period and clock.iteration % period == 0:
+                    self._run_steps(batch)
+                    batch = 0
+                    self._snapshots.take(ps, self.simutime.time, self.simutime.iteration)
             if batch:
                 self._run_steps(batch)
         self._last_forward = (t0, nsteps)
@@ -748,6 +764,8 @@ class Solver:
         remaining = self.simutime.nt - self.simutime.iteration
         if remaining > 0 and not self.simutime.is_finished:
             self.forward(nsteps=remaining)
+        if self._snapshots is not None:
+            self._snapshots.wait()
         self.wall_time = _time.time() - start
         self.flush_statistics()
 
@@ -794,6 +812,9 @@ class Solver:
         return ms.value, n.value
 
     def close(self):
+        if getattr(self, "_snapshots", None) is not None:
+            self._snapshots.close()
+            self._snapshots = None
         if getattr(self, "_run", None):
             self.L.cg_run_destroy(self._run)
             self._run = None

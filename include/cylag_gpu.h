@@ -221,6 +221,23 @@ int cg_run_set_stranding_output(cg_run *run, int32_t on);
  * xyz = NULL asks for the count only.  Host copy, no device work. */
 int cg_run_stranded(const cg_run *run, double *xyz, int32_t *count);
 
+/* ---- particle snapshots (host only) ------------------------------------- */
+/* parameters['output_file'] every output_printout_period iterations
+ * (write_particles.pyx:52-91).  Host arrays of the whole pool (n entries;
+ * an entry is written when tri != -1, i.e. active); fvs is read when
+ * model >= 2, diameter (may be NULL) adds the polydisperse column.
+ * cg_snapshot_txt appends one block to <path> (writer_txt.pyx:25-180);
+ * cg_snapshot_vtk writes <path> (writer_vtk.pyx:25-304).  Byte-identical to
+ * the reference's files; formatted on all host threads.  No device work. */
+int cg_snapshot_txt(const char *path, int32_t dim, int32_t model, double time,
+                    int64_t iteration, int32_t n, const int32_t *tri, const int32_t *tag,
+                    const double *pos, const double *vel, const double *fvs,
+                    const double *diameter);
+int cg_snapshot_vtk(const char *path, int32_t dim, int32_t model, double time,
+                    int64_t iteration, int32_t n, const int32_t *tri, const int32_t *tag,
+                    const double *pos, const double *vel, const double *fvs,
+                    const double *diameter);
+
 /* ---- particles added during a run -------------------------------------- */
 /* Points the run at a new (larger) particle state after the caller grew
  * its arrays (LagrangianParticleSet._increase_pool_size,

@@ -75,3 +75,47 @@ def test_mixed_sections_follow_plain(tmp_path):
     got = _run(case, meta, tmp_path, precision="mixed", sort_period=10)
     tot, ref = got["csec"].sum(0), want["csec_stats"].sum(0)
     assert np.all(np.abs(tot - ref) <= np.maximum(2, 0.05 * ref)), (tot, ref)
+
+
+def _read_txt_blocks(path):
+    lines = path.read_text().splitlines()
+    assert lines[0] == "cylag particles result file"
+    blocks, k = [], 2
+    while k < len(lines):
+        head = lines[k]
+        t = float(head.split("Time =")[1].split(",")[0])
+        it = int(head.split("Iter =")[1].split(",")[0])
+        n = int(head.split("Npart =")[1])
+        rows = np.array([[float(v) for v in ln.split(",")[:-1]] for ln in lines[k + 1:k + 1 + n]])
+        blocks.append((t, it, rows.reshape(n, -1)))
+        k += 1 + n
+    return blocks
+
+
+def test_solver_snapshots(tmp_path):
+    """output_file: the initial snapshot and one every output_printout_period
+    iterations, in one forward call that the snapshots split; the last
+    block is the final state (tags, positions to 1e-10 of the reference)."""
+    import cylag_gb300 as cg
+    from conftest import golden_names  # noqa: F401
+    case, meta, want = load_golden("couette")
+    f = fields_from_case(case)
+    fs = cg.EulerianFieldSet(mesh_from_case(case), **f)
+    ps = cg.LagrangianParticleSet(case["position"], dim=2)
+    params = dict(meta["params"], output_file=True, output_file_format="all",
+                  output_printout_period=50, output_rep=str(tmp_path))
+    s = cg.Solver(fs, ps, params, seed=meta["seed"], sort_period=20)
+    s.forward(nsteps=meta["nsteps"])
+    s.flush_statistics()
+    s._snapshots.wait()
+    blocks = _read_txt_blocks(tmp_path / "particles.txt")
+    its = [b[1] for b in blocks]
+    assert its == list(range(0, meta["nsteps"] + 1, 50))
+    t, it, rows = blocks[-1]
+    assert it == meta["nsteps"]
+    act = want["inactive"] == 0
+    np.testing.assert_array_equal(rows[:, 0].astype(int), ps.tag[act])
+    np.testing.assert_allclose(rows[:, 1:3], want["position"][act], rtol=RTOL, atol=1e-9)
+    for k in its:
+        assert (tmp_path / f"particles_{k}.vtk").exists()
+    s.close()
