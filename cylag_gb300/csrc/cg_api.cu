@@ -244,6 +244,8 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     if (p->model >= 2) q.work |= W_VEL | W_DIAM;
     if (p->model == 3) q.work |= W_FVS;
     if (p->dim == 3) q.work |= W_LAYER | W_DIAM;
+    // mixed LSM1 2D: working positions as split FP32 pairs (same 16 bytes)
+    if (p->precision == CG_PRECISION_MIXED && p->dim == 2 && p->model == 1) q.work |= W_SPLIT;
     const size_t D = (size_t)p->dim;
     const size_t work_bytes = al256(n * 8 * D) + 4 * al256(n * 8) +
                               ((q.work & W_VEL) ? al256(n * 8 * D) : 0) +
@@ -456,6 +458,18 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         t64[4 * k + 2] = gi0;
         t64[4 * k + 3] = gi1;
     }
+    // the same records with vertex a as FP32 pairs hi + lo
+    std::vector<int4> t64s(t64);
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        double xa = d->x[t[0]], ya = d->y[t[0]];
+        float q[4];
+        q[0] = (float)xa;
+        q[1] = (float)ya;
+        q[2] = (float)(xa - (double)q[0]);
+        q[3] = (float)(ya - (double)q[1]);
+        memcpy(&t64s[4 * k + 1], q, 16);
+    }
     std::vector<int4> edge(ne);
     std::vector<int> lab(ne);
     for (int j = 0; j < ne; ++j) {
@@ -470,7 +484,7 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     int rc;
     const double2 *p_xy, *p_basis, *p_geo;
     const float4* p_g32;
-    const int4 *p_tv, *p_edge, *p_t64, *p_nbr;
+    const int4 *p_tv, *p_edge, *p_t64, *p_t64s, *p_nbr;
     const int *p_lab, *p_gs, *p_gt;
     if ((rc = upload(c, xy, p_xy))) return rc;
     if ((rc = upload(c, tv, p_tv))) return rc;
@@ -478,13 +492,14 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     if ((rc = upload(c, geo, p_geo))) return rc;
     if ((rc = upload(c, g32, p_g32))) return rc;
     if ((rc = upload(c, t64, p_t64))) return rc;
+    if ((rc = upload(c, t64s, p_t64s))) return rc;
     if ((rc = upload(c, edge, p_edge))) return rc;
     if ((rc = upload(c, nbr, p_nbr))) return rc;
     if ((rc = upload(c, lab, p_lab))) return rc;
     if ((rc = upload(c, gstart, p_gs))) return rc;
     if ((rc = upload(c, gtris, p_gt))) return rc;
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
-    m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64; m.nbr = p_nbr;
+    m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64; m.t64s = p_t64s; m.nbr = p_nbr;
     m.gstart = p_gs; m.gtris = p_gt;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;

@@ -57,6 +57,9 @@ struct DevMesh {
     // [4*nt] packed 64-byte record per triangle for the mixed form:
     // {v0, v1, v2, e0} | {xa, ya} (FP64) | {gx0, gx1, gx2, gy0} | {gy1, gy2, e1, e2}
     const int4* __restrict__ t64;
+    // [4*nt] the same with {xa_hi, ya_hi, xa_lo, ya_lo} (FP32 pairs) as the
+    // second quarter (split working positions)
+    const int4* __restrict__ t64s;
     const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
     const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
     const int4* __restrict__ edge;      // [ne]: {n0, n1, t0, t1}
@@ -152,6 +155,39 @@ struct DevState {
 };
 
 constexpr int W_VEL = 1, W_FVS = 2, W_LAYER = 4, W_DIAM = 8;
+// working positions held as float4 {x_hi, y_hi, x_lo, y_lo}, the unevaluated
+// sums x_hi + x_lo (mixed LSM1 2D step over sorted working copies)
+constexpr int W_SPLIT = 16;
+
+// An FP64 position as a pair of FP32 values hi + lo (|lo| <= ulp(hi)/2):
+// 48 significant bits, so the step's arithmetic on it stays in FP32.
+__device__ __forceinline__ float4 split_pos(double x, double y) {
+    const float hx = (float)x, hy = (float)y;
+    return make_float4(hx, hy, (float)(x - (double)hx), (float)(y - (double)hy));
+}
+
+// the FP64 value of a split position (rounded to nearest double)
+__device__ __forceinline__ double2 join_pos(float4 p) {
+    return make_double2((double)p.x + (double)p.z, (double)p.y + (double)p.w);
+}
+
+// hi + lo + d as a new normalized pair: TwoSum(hi, d) (Knuth), the low
+// parts added, then Fast2Sum; the result is within about ulp(lo) of the
+// exact sum.  No multiplications, so no contraction can change it.
+__device__ __forceinline__ void split_add1(float& hi, float& lo, float d) {
+    const float s = hi + d;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (d - bb);
+    const float t = e + lo;
+    hi = s + t;
+    lo = t - (hi - s);
+}
+
+__device__ __forceinline__ float4 split_add(float4 p, float dx, float dy) {
+    split_add1(p.x, p.z, dx);
+    split_add1(p.y, p.w, dy);
+    return p;
+}
 
 // index of particle i in an array that is a working copy when `flag` is set
 __device__ __forceinline__ int widx(const DevState& s, int i, int a, int flag) {
@@ -558,6 +594,33 @@ struct Tri32 {
     float4 g1;    // gy1 gy2 - -
 };
 
+// the same record with vertex a as a split pair {xa_hi, ya_hi, xa_lo, ya_lo}
+// (DevMesh::t64s), for split working positions
+struct Tri32S {
+    int4 tv;
+    float4 as;
+    float4 g0;
+    float4 g1;
+};
+
+__device__ __forceinline__ Tri32S load_tri32s(const DevMesh& m, int k) {
+    Tri32S t;
+    const float4* r = reinterpret_cast<const float4*>(m.t64s + 4 * (size_t)k);
+    t.tv = __ldg(&m.t64s[4 * (size_t)k]);
+    t.as = __ldg(&r[1]);
+    t.g0 = __ldg(&r[2]);
+    t.g1 = __ldg(&r[3]);
+    return t;
+}
+
+// offset of a split position to the record's vertex a, in FP32:
+// (x_hi - xa_hi) + (x_lo - xa_lo); within 2^-23 relative of the exact
+// offset (the hi difference is exact when both are within a factor 2, as
+// they are near the triangle; else one rounding), inside bary32_off's bounds
+__device__ __forceinline__ float2 split_offset(const Tri32S& t, float4 p) {
+    return make_float2((p.x - t.as.x) + (p.z - t.as.z), (p.y - t.as.y) + (p.w - t.as.w));
+}
+
 __device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
     Tri32 t;
     const int4* r = m.t64 + 4 * (size_t)k;
@@ -573,7 +636,8 @@ __device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
     return t;
 }
 
-__device__ __forceinline__ int tri32_edge(const Tri32& t, int i) {
+template <typename T>
+__device__ __forceinline__ int tri32_edge(const T& t, int i) {
     return i == 0 ? t.tv.w : (i == 1 ? __float_as_int(t.g1.z) : __float_as_int(t.g1.w));
 }
 
@@ -585,7 +649,8 @@ struct Bary {
 // barycentric coordinates from the FP32 offset (rx, ry) to vertex a:
 // l_j = gx_j rx + gy_j ry.  The bounds cover the offset rounding (relative
 // 2^-24), the FP32 gradients and products: <= ~4 ulp of the terms.
-__device__ __forceinline__ Bary bary32_off(const Tri32& t, float rx, float ry) {
+template <typename T>
+__device__ __forceinline__ Bary bary32_off(const T& t, float rx, float ry) {
     Bary b;
     float p1 = t.g0.y * rx, q1 = t.g1.x * ry;
     float p2 = t.g0.z * rx, q2 = t.g1.y * ry;
@@ -606,7 +671,8 @@ __device__ __forceinline__ Bary bary32(const Tri32& t, double x, double y) {
 // Offset of an FP64 position advanced by an FP32 increment, (x0 + d) - a,
 // formed in FP32 as (x0 - a) + d: one more rounding of the start offset
 // (relative 2^-24 of |x0 - a|), so the bounds get that term added.
-__device__ __forceinline__ Bary bary32_moved(const Tri32& t, float rx0, float ry0, float dx,
+template <typename T>
+__device__ __forceinline__ Bary bary32_moved(const T& t, float rx0, float ry0, float dx,
                                              float dy) {
     Bary b = bary32_off(t, rx0 + dx, ry0 + dy);
     float s1 = 1.2e-7f * (fabsf(t.g0.y * rx0) + fabsf(t.g1.x * ry0));

@@ -30,15 +30,25 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
     DevFields<float> f = fv.as<float>();
     WalkQueue none{nullptr, nullptr};
     if (fv.dim == 2) {
-        // occupancy variant: 3 blocks/SM (80 registers) by default, 4 (64) on request
+        // occupancy variant: 3 blocks/SM (80 registers) by default; 2 (128)
+        // or 4 (64) on request
         static int minb = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
-            return (e && atoi(e) == 4) ? 4 : 3;
+            int v = e ? atoi(e) : 3;
+            return (v == 2 || v == 4) ? v : 3;
         }();
         // persistent grid: one wave of resident blocks
-        static int w3 = wave(step_mixed2d_kernel<3>, bs), w4 = wave(step_mixed2d_kernel<4>, bs);
-        if (minb == 3)
+        static int w2 = wave(step_mixed2d_kernel<2>, bs), w3 = wave(step_mixed2d_kernel<3>, bs),
+                   w4 = wave(step_mixed2d_kernel<4>, bs),
+                   w3s = wave(step_mixed2d_kernel<3, true>, bs);
+        if (s.work & W_SPLIT)   // sorted working copies with split positions
+            step_mixed2d_kernel<3, true><<<nb < w3s ? nb : w3s, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                           step_index, stats, err);
+        else if (minb == 3)
             step_mixed2d_kernel<3><<<nb < w3 ? nb : w3, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                   step_index, stats, err);
+        else if (minb == 2)
+            step_mixed2d_kernel<2><<<nb < w2 ? nb : w2, bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                    step_index, stats, err);
         else
             step_mixed2d_kernel<4><<<nb < w4 ? nb : w4, bs, 0, st>>>(m, f, p, s, wq, aux,

@@ -130,13 +130,20 @@ __device__ __forceinline__ void move_rows(const T* __restrict__ src, T* __restri
     for (int d = 0; d < dim; ++d) dst[(size_t)to * dim + d] = __ldcs(src + (size_t)from * dim + d);
 }
 
-// dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays
+// dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays.
+// split: working positions are split FP32 pairs (W_SPLIT), made from the
+// caller's FP64 positions here and moved as they are between working copies
 __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src, WorkState dst,
-                                    int n, int dim) {
+                                    int n, int dim, bool split) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&perm[j]);
-    move_rows(src.pos, dst.pos, i, j, dim);
+    if (split && src.slot == nullptr) {
+        const double2 x = __ldcs(reinterpret_cast<const double2*>(src.pos) + i);
+        reinterpret_cast<float4*>(dst.pos)[j] = split_pos(x.x, x.y);
+    } else {
+        move_rows(src.pos, dst.pos, i, j, dim);
+    }
     dst.tri[j] = __ldcs(src.tri + i);
     dst.tag[j] = __ldcs(src.tag + i);
     dst.rng[j] = __ldcs(src.rng + i);
@@ -148,11 +155,16 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
 }
 
 // caller[slot[j]] = work[j]
-__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim) {
+__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim, bool split) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&w.slot[j]);
-    for (int d = 0; d < dim; ++d) __stcs(user.pos + (size_t)i * dim + d, w.pos[(size_t)j * dim + d]);
+    if (split)
+        __stcs(reinterpret_cast<double2*>(user.pos) + i,
+               join_pos(reinterpret_cast<const float4*>(w.pos)[j]));
+    else
+        for (int d = 0; d < dim; ++d)
+            __stcs(user.pos + (size_t)i * dim + d, w.pos[(size_t)j * dim + d]);
     __stcs(user.tri + i, w.tri[j]);
     __stcs(user.tag + i, w.tag[j]);
     __stcs(user.rng + i, w.rng[j]);
@@ -198,13 +210,15 @@ void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream
     int n = user.n;
     if (n == 0) return;
     sort_perm(user.tri, (b.work & W_LAYER) ? user.lowerlayer : nullptr, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user, b), b.a, n, b.dim);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user, b), b.a, n, b.dim,
+                                                         (b.work & W_SPLIT) != 0);
 }
 
 void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
     if (n == 0) return;
     sort_perm(b.a.tri, b.a.layer, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim,
+                                                         (b.work & W_SPLIT) != 0);
     WorkState t = b.a;
     b.a = b.b;
     b.b = t;
@@ -213,7 +227,8 @@ void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st) {
     int n = user.n;
     if (n == 0) return;
-    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user, b), n, b.dim);
+    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user, b), n, b.dim,
+                                                          (b.work & W_SPLIT) != 0);
 }
 
 DevState sorted_view(const DevState& user, const SortBuffers& b) {

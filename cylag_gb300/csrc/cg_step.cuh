@@ -587,8 +587,12 @@ struct Particle {
             s.rng[i] = rng.state;
             return;
         }
+        if (DIM == 2 && (s.work & W_SPLIT)) {
+            reinterpret_cast<float4*>(s.pos)[i] = split_pos(x[0], x[1]);
+        } else {
 #pragma unroll
-        for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = x[d];
+            for (int d = 0; d < D; ++d) s.pos[(size_t)i * D + d] = x[d];
+        }
         s.tri[i] = tri;
         if (DIM == 3) s.lowerlayer[il] = ll;
         s.rng[i] = rng.state;
@@ -898,7 +902,8 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
         int i = w.i;
         Particle<2, FT> q(m, f, p, zt);
         int tri0 = s.tri[i];
-        double2 x0 = reinterpret_cast<const double2*>(s.pos)[i];
+        double2 x0 = (s.work & W_SPLIT) ? join_pos(reinterpret_cast<const float4*>(s.pos)[i])
+                                        : reinterpret_cast<const double2*>(s.pos)[i];
         q.tri0 = tri0;
         q.ltri = tri0;
         q.ll = q.ll0 = 0;

@@ -120,7 +120,8 @@ struct Node4 {
     float4 n0, n1, n2;
 };
 
-__device__ __forceinline__ Node4 load_nodes(const float4* __restrict__ f, const Tri32& t) {
+template <typename T>
+__device__ __forceinline__ Node4 load_nodes(const float4* __restrict__ f, const T& t) {
     Node4 r;
     r.n0 = __ldg(&f[t.tv.x]);
     r.n1 = __ldg(&f[t.tv.y]);
@@ -204,8 +205,43 @@ static __device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<f
     deleted = q.deleted;
 }
 
+// in-element decision from FP32 barycentrics: 1 certainly inside, 0
+// certainly outside, -1 within the rounding band (exact test needed)
+__device__ __forceinline__ int decide32(const Bary& b) {
+    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return 1;
+    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return 0;
+    return -1;
+}
+
+// one_hop for a split end position: the neighbour's record with its split
+// vertex, so that the test stays in FP32 outside the band
+__device__ __forceinline__ int one_hop_split(const DevMesh& m, int tri0, const Bary& bs,
+                                            const Bary& be, float4 pn) {
+    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
+    const bool n0 = be.l0 < -be.e0, n1 = be.l1 < -be.e1, n2 = be.l2 < -be.e2;
+    const bool p0 = be.l0 > be.e0, p1 = be.l1 > be.e1, p2 = be.l2 > be.e2;
+    int j;
+    if (n0 && p1 && p2) j = 0;
+    else if (n1 && p0 && p2) j = 1;
+    else if (n2 && p0 && p1) j = 2;
+    else return -1;
+    int4 nb = __ldg(&m.nbr[tri0]);
+    int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+    if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
+    const Tri32S tn = load_tri32s(m, kn);
+    const float2 r = split_offset(tn, pn);
+    const int d = decide32(bary32_off(tn, r.x, r.y));
+    if (d >= 0) return d ? kn : -1;
+    const double2 x = join_pos(pn);
+    return in_tri(m, kn, x.x, x.y) ? kn : -1;
+}
+
 // LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
 // diffusion 658-726) with the boundary conditions of compute_bc.pyx.
+// SPLIT: the working position is a split pair (W_SPLIT); the Euler step then
+// runs without FP64 arithmetic outside the rounding bands, the walk and the
+// boundary conditions (which work on its FP64 value).
+template <bool SPLIT>
 __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
                                                     const DevParams& p, DevState& s,
                                                     const WalkQueue& wq, int aux, int step_index,
@@ -217,7 +253,10 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     int tri0 = __ldcs(&s.tri[i]);
     if (tri0 < 0) return;
     const float4* __restrict__ cur = reinterpret_cast<const float4*>(f.cur);
-    double2 x0 = __ldcs(reinterpret_cast<const double2*>(s.pos) + i);
+    float4 xs = make_float4(0.f, 0.f, 0.f, 0.f);   // SPLIT: the start position
+    double2 x0 = make_double2(0., 0.);
+    if constexpr (SPLIT) xs = __ldcs(reinterpret_cast<const float4*>(s.pos) + i);
+    else x0 = __ldcs(reinterpret_cast<const double2*>(s.pos) + i);
     Rng rng;
     rng.state = __ldcs(reinterpret_cast<const unsigned long long*>(s.rng) + i);
     rng.inc = ((uint64_t)(uint32_t)__ldcs(&s.tag[i]) << 1) | 1ULL;
@@ -226,19 +265,39 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
 
     const float dt = p.dt32;
-    Tri32 t0 = load_tri32(m, tri0);
-    Node4 n0 = load_nodes(cur, t0);
-    const float rx0 = (float)(x0.x - t0.a.x), ry0 = (float)(x0.y - t0.a.y);
-    Bary b0 = bary32_off(t0, rx0, ry0);
+    const bool euler = p.time_scheme == 1;
+    // start record and offset to its vertex a
+    Tri32 t0;
+    Tri32S t0s;
+    float rx0, ry0;
+    Node4 n0;
+    Bary b0;
+    if constexpr (SPLIT) {
+        t0s = load_tri32s(m, tri0);
+        const float2 r = split_offset(t0s, xs);
+        rx0 = r.x;
+        ry0 = r.y;
+        n0 = load_nodes(cur, t0s);
+        b0 = bary32_off(t0s, rx0, ry0);
+        if (!euler) {   // the Runge-Kutta stages work on the FP64 value
+            x0 = join_pos(xs);
+            t0 = load_tri32(m, tri0);
+        }
+    } else {
+        t0 = load_tri32(m, tri0);
+        rx0 = (float)(x0.x - t0.a.x);
+        ry0 = (float)(x0.y - t0.a.y);
+        n0 = load_nodes(cur, t0);
+        b0 = bary32_off(t0, rx0, ry0);
+    }
     float ux, uy;
     vel32(n0, b0, ux, uy);
     float up0 = ux, up1 = uy;   // velocity = fluid velocity seen = U(x0)
     double xn = x0.x, yn = x0.y;
     int tri = tri0, ltri = tri0, bnd_j = -1;
     // Euler: the whole step's increment is accumulated in FP32 and added to
-    // the FP64 position once
+    // the position once
     float dx = 0.f, dy = 0.f;
-    const bool euler = p.time_scheme == 1;
     if (euler) {
         dx = ux * dt;
         dy = uy * dt;
@@ -250,9 +309,10 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (p.diffmod != 0) {
         float diffx, driftx = 0.f, drifty = 0.f;
         if (p.diffmod == 2 || p.diffmod == 3) {
+            const float4 g0 = SPLIT ? t0s.g0 : t0.g0, g1 = SPLIT ? t0s.g1 : t0.g1;
             float K = b0.l0 * n0.n0.z + b0.l1 * n0.n1.z + b0.l2 * n0.n2.z;
-            float dKdx = n0.n0.z * t0.g0.x + n0.n1.z * t0.g0.y + n0.n2.z * t0.g0.z;
-            float dKdy = n0.n0.z * t0.g0.w + n0.n1.z * t0.g1.x + n0.n2.z * t0.g1.y;
+            float dKdx = n0.n0.z * g0.x + n0.n1.z * g0.y + n0.n2.z * g0.z;
+            float dKdy = n0.n0.z * g0.w + n0.n1.z * g1.x + n0.n2.z * g1.y;
             K = fmaxf(0.f, K);
             diffx = sqrtf(2.f * K) * p.sqrtdt32;
             driftx = dKdx * dt;
@@ -270,20 +330,56 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
             yn += (double)(drifty + diffx * xiy);
         }
     }
+    float4 xe = xs;   // SPLIT: the end position
     if (euler) {
-        xn = x0.x + (double)dx;
-        yn = x0.y + (double)dy;
+        if constexpr (SPLIT) {
+            xe = split_add(xs, dx, dy);
+        } else {
+            xn = x0.x + (double)dx;
+            yn = x0.y + (double)dy;
+        }
+    } else if constexpr (SPLIT) {
+        xe = split_pos(xn, yn);
     }
+    // SPLIT: FP64 values of the start and end positions, formed where needed
+    bool have64 = !SPLIT || !euler;
+    auto need64 = [&]() {
+        if constexpr (SPLIT) {
+            if (!have64) {
+                x0 = join_pos(xs);
+                const double2 e = join_pos(xe);
+                xn = e.x;
+                yn = e.y;
+                have64 = true;
+            }
+        }
+    };
 
     if (bnd_j == -1) {
         ltri = tri0;
         if (wq.e != nullptr) {
             // leaves the start triangle: one hop here, else walk + boundary
             // conditions in walk_kernel
-            const Bary be = euler ? bary32_moved(t0, rx0, ry0, dx, dy) : bary32(t0, xn, yn);
-            const bool inside = in_tri_decide(m, be, tri0, xn, yn);
-            const int kn = inside ? tri0 : one_hop(m, tri0, b0, be, xn, yn);
+            int kn;
+            if constexpr (SPLIT) {
+                const Bary be = euler ? bary32_moved(t0s, rx0, ry0, dx, dy)
+                                      : [&] {
+                                            const float2 r = split_offset(t0s, xe);
+                                            return bary32_off(t0s, r.x, r.y);
+                                        }();
+                int d = decide32(be);
+                if (d < 0) {
+                    need64();
+                    d = in_tri(m, tri0, xn, yn) ? 1 : 0;
+                }
+                kn = d ? tri0 : one_hop_split(m, tri0, b0, be, xe);
+            } else {
+                const Bary be = euler ? bary32_moved(t0, rx0, ry0, dx, dy) : bary32(t0, xn, yn);
+                const bool inside = in_tri_decide(m, be, tri0, xn, yn);
+                kn = inside ? tri0 : one_hop(m, tri0, b0, be, xn, yn);
+            }
             if (kn < 0) {
+                need64();
                 if (rng.err) atomicOr(err_word, rng.err);
                 int slot = queue_slot(wq);
                 WalkEntry w;
@@ -297,14 +393,19 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
             }
             tri = kn;
         } else {
+            need64();
+            if constexpr (SPLIT) t0 = load_tri32(m, tri0);
             xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xn, yn, tri, bnd_j);
         }
     }
 
     bool deleted = false;
-    if (bnd_j != -1 || tri == PART_LOC_O)
+    if (bnd_j != -1 || tri == PART_LOC_O) {
+        need64();
         bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted,
                  aux_index(s, i), step_index);
+        if constexpr (SPLIT) xe = split_pos(xn, yn);
+    }
     if (rng.err) atomicOr(err_word, rng.err);
 
     if (deleted) {
@@ -323,8 +424,12 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         if (p.ncsec) count_sections(p, stats, 0., 0., 0., 0.);
         return;
     }
-    if (p.ncsec) count_sections(p, stats, x0.x, x0.y, xn, yn);
-    __stcs(reinterpret_cast<double2*>(s.pos) + i, make_double2(xn, yn));
+    if (p.ncsec) {
+        need64();
+        count_sections(p, stats, x0.x, x0.y, xn, yn);
+    }
+    if constexpr (SPLIT) __stcs(reinterpret_cast<float4*>(s.pos) + i, xe);
+    else __stcs(reinterpret_cast<double2*>(s.pos) + i, make_double2(xn, yn));
     __stcs(&s.tri[i], tri);
     __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);
     if (aux >= 1) {
@@ -332,6 +437,9 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         reinterpret_cast<double2*>(s.vel)[a] = make_double2(up0, up1);
         reinterpret_cast<double2*>(s.fvs)[a] = make_double2(up0, up1);
         if (aux >= 2) {
+            if constexpr (SPLIT) {
+                if (!have64) x0 = join_pos(xs);
+            }
             reinterpret_cast<double2*>(s.last_pos)[a] = x0;
             reinterpret_cast<double2*>(s.last_vel)[a] = lastv;
             s.last_tri[a] = ltri;
@@ -340,7 +448,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 }
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
-template <int MINB>
+template <int MINB, bool SPLIT = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -355,7 +463,7 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     }
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_mixed_particle(m, f, p, s, wq, aux, step_index, stats, err_word, z32, i);
+        step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, i);
 }
 
 }  // namespace cg
