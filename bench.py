@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--serve-chunk", type=int, default=32, help="steps queued per loop (serve)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-chunk", type=int, default=0,
+                    help="particles per copy/step chunk of the end-to-end steps (0: about n/8)")
     return ap.parse_args()
 
 
@@ -326,26 +328,25 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
            "position": ps.position, "velocity": ps.velocity, "inactive": ps.inactive,
            "nt": int(mesh.nt)}
     if do_e2e:
-        # end to end: host state (pinned) -> device, one step through the C
-        # ABI, device -> host, every step
+        # end to end: the particle state lives in pinned host memory; every
+        # step, one C-ABI call copies it in, steps and copies it back
+        # (cg_run_step_host: chunked, copies overlapping the step)
         log("end-to-end region")
         d = ps._dev
-        keys_in = ["position", "tri", "tag", "rng_state"]
-        keys_out = ["position", "tri", "rng_state"]
+        keys = ["position", "tri", "tag", "rng_state"]
         if c["dim"] == 3:
-            keys_in.append("lowerlayer")
-            keys_out.append("lowerlayer")
+            keys.append("lowerlayer")
         if params["model"] >= 2:
-            keys_in.append("velocity")
-            keys_out.append("velocity")
+            keys.append("velocity")
         if params["model"] == 3:
-            keys_in.append("fluid_velocity_seen")
-            keys_out.append("fluid_velocity_seen")
-        host = {k: torch.empty_like(d[k], device="cpu").pin_memory() for k in keys_in}
-        for k in keys_in:
+            keys.append("fluid_velocity_seen")
+        host = {k: torch.empty_like(d[k], device="cpu").pin_memory() for k in keys}
+        for k in keys:
             host[k].copy_(d[k])
-        h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
-        d2h = sum(host[k].numel() * host[k].element_size() for k in keys_out)
+        h2d = d2h = sum(host[k].numel() * host[k].element_size() for k in keys)
+        ptr = lambda k: host[k].data_ptr() if k in host else None
+        arr = _lib.HostArrays(ptr("position"), ptr("velocity"), ptr("fluid_velocity_seen"),
+                              ptr("tri"), ptr("lowerlayer"), ptr("tag"), ptr("rng_state"))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -353,14 +354,10 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
         e1 = torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record(stream)
-        with torch.cuda.stream(stream):
-            for _ in range(args.steps):
-                for k in keys_in:
-                    d[k].copy_(host[k], non_blocking=True)
-                rc = L.cg_run_step(solver._run, 1, None)
-                _lib.check(solver._ctx, rc)
-                for k in keys_out:
-                    host[k].copy_(d[k], non_blocking=True)
+        for _ in range(args.steps):
+            rc = L.cg_run_step_host(solver._run, 1, C.byref(arr), C.byref(arr), args.e2e_chunk,
+                                    None)
+            _lib.check(solver._ctx, rc)
         e1.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0

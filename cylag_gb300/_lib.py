@@ -76,6 +76,11 @@ class StateDesc(C.Structure):
                 ("lowerlayer", P), ("tag", P), ("diameter", P), ("rng_state", P)]
 
 
+class HostArrays(C.Structure):
+    _fields_ = [("position", P), ("velocity", P), ("fluid_velocity_seen", P), ("tri", P),
+                ("lowerlayer", P), ("tag", P), ("rng_state", P)]
+
+
 # (name, restype, argtypes) for every symbol include/cylag_gpu.h declares
 SIGNATURES = [
     ("cg_ctx_create", C.c_int, [I32, C.c_uint64, C.POINTER(P)]),
@@ -99,6 +104,7 @@ SIGNATURES = [
                                   C.c_int32, P, P, P, P, P, P]),
     ("cg_snapshot_vtk", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                   C.c_int32, P, P, P, P, P, P]),
+    ("cg_run_step_host", C.c_int, [P, I32, C.POINTER(HostArrays), C.POINTER(HostArrays), I32, P]),
     ("cg_run_set_stranding_output", C.c_int, [P, C.c_int32]),
     ("cg_run_stranded", C.c_int, [P, P, C.POINTER(C.c_int32)]),
     ("cg_run_set_sections", C.c_int, [P, C.c_int32, P]),

@@ -41,6 +41,8 @@ struct cg_run {
     DevBuf csec;                     // control-section segments {x0, y0, x1, y1}
     std::vector<int32_t> csec_counts;  // [nsteps, ncsec] of the last cg_run_step
     int csec_steps = 0;
+    cudaStream_t h2d = nullptr, d2h = nullptr;   // cg_run_step_host copy streams
+    std::vector<cudaEvent_t> hev;                // ... and its per-chunk events
     DevBuf strand;                   // stranding output: count (first 256 B) + n records
     bool strand_on = false;
     std::vector<StrandRec> strand_host;  // the last cg_run_step's, in the reference's order
@@ -669,6 +671,9 @@ int cg_run_destroy(cg_run* r) {
     dfree(r->queue);
     dfree(r->sortbuf);
     for (auto e : r->ev) cudaEventDestroy(e);
+    for (auto e : r->hev) cudaEventDestroy(e);
+    if (r->h2d) cudaStreamDestroy(r->h2d);
+    if (r->d2h) cudaStreamDestroy(r->d2h);
     c->used -= r->bytes;
     delete r;
     return CG_OK;
@@ -743,6 +748,25 @@ int cg_run_init(cg_run* r) {
     launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, r->st,
                 r->prm.particle_velocity_init, -1, (uint32_t*)r->errw.p, c->stream);
     CUDA_TRY(c, cudaGetLastError());
+    return CG_OK;
+}
+
+// the stranding records of the call just finished, in the reference's order
+static int collect_stranded(cg_run* r) {
+    if (!r->strand_on) return CG_OK;
+    cg_ctx* c = r->ctx;
+    int cnt = 0;
+    CUDA_TRY(c, cudaMemcpy(&cnt, r->strand.p, sizeof(int), cudaMemcpyDeviceToHost));
+    cnt = std::min(cnt, r->dp.strand_cap);
+    r->strand_host.resize(cnt);
+    if (cnt)
+        CUDA_TRY(c, cudaMemcpy(r->strand_host.data(), r->dp.strand_rec,
+                               (size_t)cnt * sizeof(StrandRec), cudaMemcpyDeviceToHost));
+    // the reference appends in its particle loop: by step, then index
+    std::sort(r->strand_host.begin(), r->strand_host.end(),
+              [](const StrandRec& a, const StrandRec& b) {
+                  return a.step != b.step ? a.step < b.step : a.index < b.index;
+              });
     return CG_OK;
 }
 
@@ -842,20 +866,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaMemcpy2D(bnd_stats_host, (size_t)c->nopen * sizeof(int), r->stats.p,
                                  (size_t)row * sizeof(int), (size_t)c->nopen * sizeof(int),
                                  nsteps, cudaMemcpyDeviceToHost));
-    if (r->strand_on) {
-        int cnt = 0;
-        CUDA_TRY(c, cudaMemcpy(&cnt, r->strand.p, sizeof(int), cudaMemcpyDeviceToHost));
-        cnt = std::min(cnt, r->dp.strand_cap);
-        r->strand_host.resize(cnt);
-        if (cnt)
-            CUDA_TRY(c, cudaMemcpy(r->strand_host.data(), r->dp.strand_rec,
-                                   (size_t)cnt * sizeof(StrandRec), cudaMemcpyDeviceToHost));
-        // the reference appends in its particle loop: by step, then index
-        std::sort(r->strand_host.begin(), r->strand_host.end(),
-                  [](const StrandRec& a, const StrandRec& b) {
-                      return a.step != b.step ? a.step < b.step : a.index < b.index;
-                  });
-    }
+    if ((rc = collect_stranded(r))) return rc;
     if (r->dp.ncsec > 0) {
         r->csec_counts.resize((size_t)nsteps * r->dp.ncsec);
         CUDA_TRY(c, cudaMemcpy2D(r->csec_counts.data(), (size_t)r->dp.ncsec * sizeof(int),
@@ -1048,6 +1059,153 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
         r->iteration += 1;
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    uint32_t flags = 0;
+    CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
+    return CG_OK;
+}
+
+// entries [a, a + m) of the particle state, as a state of m particles
+static DevState slice_state(const DevState& s, int a, int m, int dim) {
+    DevState v = s;
+    const size_t av = (size_t)a * dim;
+    v.n = m;
+    v.pos += av;
+    v.vel += av;
+    v.fvs += av;
+    v.last_pos += av;
+    v.last_vel += av;
+    v.tri += a;
+    v.last_tri += a;
+    v.lowerlayer += a;
+    v.tag += a;
+    v.diameter += a;
+    v.rng += a;
+    v.slot = nullptr;
+    v.work = 0;
+    v.base = s.base + a;
+    return v;
+}
+
+// copies of entries [a, a + m) between the host arrays h and the run's state
+static cudaError_t copy_chunk(const cg_run* r, const cg_host_arrays* h, bool to_device, int a,
+                              int m, cudaStream_t st) {
+    const int D = r->prm.dim;
+    const DevState& d = r->st;
+    struct A {
+        void* host;
+        void* dev;
+        size_t elem;
+    } arr[] = {{h->position, d.pos, 8u * D},       {h->velocity, d.vel, 8u * D},
+               {h->fluid_velocity_seen, d.fvs, 8u * D}, {h->tri, d.tri, 4},
+               {h->lowerlayer, d.lowerlayer, 4},   {h->tag, d.tag, 4},
+               {h->rng_state, d.rng, 8}};
+    for (const A& x : arr) {
+        if (!x.host) continue;
+        char* hp = (char*)x.host + (size_t)a * x.elem;
+        char* dp = (char*)x.dev + (size_t)a * x.elem;
+        cudaError_t e = to_device
+            ? cudaMemcpyAsync(dp, hp, (size_t)m * x.elem, cudaMemcpyHostToDevice, st)
+            : cudaMemcpyAsync(hp, dp, (size_t)m * x.elem, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
+                     const cg_host_arrays* out, int32_t chunk, int32_t* bnd_stats_host) {
+    if (!r || nsteps < 0 || !in || !out || chunk < 0) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (nsteps == 0) return CG_OK;
+    if (r->pending_init)
+        return set_err(c, CG_ESTATE, "particles await initialization: step them with cg_run_step");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = ensure_fields(r);
+    if (rc) return rc;
+    const int n = r->st.n, D = r->prm.dim;
+    if (chunk == 0) chunk = std::max(1 << 16, ((n + 7) / 8 + 255) / 256 * 256);
+    const int nch = n > 0 ? (n + chunk - 1) / chunk : 0;
+    if (!r->h2d) CUDA_TRY(c, cudaStreamCreateWithFlags(&r->h2d, cudaStreamNonBlocking));
+    if (!r->d2h) CUDA_TRY(c, cudaStreamCreateWithFlags(&r->d2h, cudaStreamNonBlocking));
+    while ((int)r->hev.size() < 3 * nch + 1) {
+        cudaEvent_t e;
+        CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        r->hev.push_back(e);
+    }
+    cudaEvent_t* ev_in = r->hev.data();
+    cudaEvent_t* ev_comp = ev_in + nch;
+    cudaEvent_t* ev_out = ev_comp + nch;
+    cudaEvent_t ev_start = r->hev[3 * nch];
+    const int nopen = c->nopen > 0 ? c->nopen : 1;
+    const int row = nopen + r->dp.ncsec;
+    if (r->stats_rows < nsteps || r->stats_cols != row) {
+        dfree(r->stats);
+        if ((rc = dalloc(c, r->stats, (size_t)nsteps * row * sizeof(int)))) return rc;
+        r->stats_rows = nsteps;
+        r->stats_cols = row;
+    }
+    CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * row * sizeof(int), c->stream));
+    if (r->strand_on) CUDA_TRY(c, cudaMemsetAsync(r->strand.p, 0, sizeof(int), c->stream));
+    // the copy streams start after what is queued on the run's stream
+    CUDA_TRY(c, cudaEventRecord(ev_start, c->stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(r->h2d, ev_start, 0));
+    CUDA_TRY(c, cudaStreamWaitEvent(r->d2h, ev_start, 0));
+    uint32_t* errw = (uint32_t*)r->errw.p;
+    for (int s = 0; s < nsteps; ++s) {
+        if ((rc = time_interpolation(r, r->time))) return rc;
+        const int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
+        int* stats = (int*)r->stats.p + (size_t)s * row;
+        const FieldView fv = field_view(r);
+        const int it = (int)r->iteration;
+        for (int j = 0; j < nch; ++j) {
+            const int a = j * chunk, m = std::min(chunk, n - a);
+            // in: after the previous step's copy out of this chunk (the host
+            // arrays may be the same)
+            if (s > 0) CUDA_TRY(c, cudaStreamWaitEvent(r->h2d, ev_out[j], 0));
+            CUDA_TRY(c, copy_chunk(r, in, true, a, m, r->h2d));
+            CUDA_TRY(c, cudaEventRecord(ev_in[j], r->h2d));
+            // step
+            CUDA_TRY(c, cudaStreamWaitEvent(c->stream, ev_in[j], 0));
+            const DevState v = slice_state(r->st, a, m, D);
+            WalkQueue wq{nullptr, nullptr};
+            if (r->use_queue) {
+                wq.count = (int*)r->queue.p;
+                wq.e = (WalkEntry*)((char*)r->queue.p + 256);
+                CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
+            }
+            if (r->prm.precision == CG_PRECISION_MIXED) {
+                launch_step_mixed(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);
+                if (wq.e) launch_walk_mixed(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);
+            } else {
+                launch_step_plain(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);
+                if (wq.e) launch_walk_plain(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);
+            }
+            CUDA_TRY(c, cudaGetLastError());
+            CUDA_TRY(c, cudaEventRecord(ev_comp[j], c->stream));
+            // out
+            CUDA_TRY(c, cudaStreamWaitEvent(r->d2h, ev_comp[j], 0));
+            CUDA_TRY(c, copy_chunk(r, out, false, a, m, r->d2h));
+            CUDA_TRY(c, cudaEventRecord(ev_out[j], r->d2h));
+        }
+        r->time += r->prm.time_step;
+        r->iteration += 1;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(r->d2h));
+    CUDA_TRY(c, cudaStreamSynchronize(r->h2d));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (bnd_stats_host && c->nopen > 0)
+        CUDA_TRY(c, cudaMemcpy2D(bnd_stats_host, (size_t)c->nopen * sizeof(int), r->stats.p,
+                                 (size_t)row * sizeof(int), (size_t)c->nopen * sizeof(int),
+                                 nsteps, cudaMemcpyDeviceToHost));
+    if (r->dp.ncsec > 0) {
+        r->csec_counts.resize((size_t)nsteps * r->dp.ncsec);
+        CUDA_TRY(c, cudaMemcpy2D(r->csec_counts.data(), (size_t)r->dp.ncsec * sizeof(int),
+                                 (const int*)r->stats.p + nopen, (size_t)row * sizeof(int),
+                                 (size_t)r->dp.ncsec * sizeof(int), nsteps,
+                                 cudaMemcpyDeviceToHost));
+        r->csec_steps = nsteps;
+    }
+    if ((rc = collect_stranded(r))) return rc;
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
     if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);

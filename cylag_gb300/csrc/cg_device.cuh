@@ -152,6 +152,7 @@ struct DevState {
     // working copies too (indexed by i)
     const int* __restrict__ slot;
     int work;
+    int base;   // index of entry 0 in the whole pool (a chunk of it: its offset)
 };
 
 constexpr int W_VEL = 1, W_FVS = 2, W_LAYER = 4, W_DIAM = 8;

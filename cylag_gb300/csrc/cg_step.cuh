@@ -798,7 +798,7 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
         return;
     }
     if (p.bc_on) {
-        q.pidx = ai;
+        q.pidx = ai + s.base;
         q.pstep = step_index;
         q.compute_bc(bnd_j, stats);
     } else if (q.tri == PART_LOC_O || q.ll == PART_LOC_B || q.ll == PART_LOC_A) {
@@ -932,7 +932,7 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
         else path_walk(m, tri0, x0.x, x0.y, w.xn, w.yn, nk, bnd);
         if (nk == -1 && bnd == -1) nk = grid_locate(m, w.xn, w.yn);
         q.tri = nk;
-        q.pidx = aux_index(s, i);
+        q.pidx = aux_index(s, i) + s.base;
         q.pstep = step_index;
         if (p.bc_on) q.compute_bc(bnd, stats);
         else if (q.tri == PART_LOC_O) q.deleted = true;

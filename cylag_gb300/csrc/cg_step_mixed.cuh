@@ -403,7 +403,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (bnd_j != -1 || tri == PART_LOC_O) {
         need64();
         bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted,
-                 aux_index(s, i), step_index);
+                 aux_index(s, i) + s.base, step_index);
         if constexpr (SPLIT) xe = split_pos(xn, yn);
     }
     if (rng.err) atomicOr(err_word, rng.err);

@@ -196,6 +196,30 @@ int cg_run_errors(cg_run *run, uint32_t *flags);
 /* Number of active particles and deleted-this-call counts are derived by the
  * caller from tri (tri == -1 inactive). */
 
+/* ---- particle state in host memory ---------------------------------------- */
+/* Host arrays of the whole pool (pinned: cudaHostAlloc / torch pin_memory);
+ * NULL arrays are not transferred. */
+typedef struct {
+    double *position;             /* [n, dim] */
+    double *velocity;             /* [n, dim] */
+    double *fluid_velocity_seen;  /* [n, dim] */
+    int32_t *tri;
+    int32_t *lowerlayer;
+    int32_t *tag;
+    uint64_t *rng_state;
+} cg_host_arrays;
+
+/* nsteps x Solver.forward with the particle state kept in host memory, the
+ * drop-in for a caller whose arrays are the reference's host arrays: every
+ * step copies the `in` arrays into the run's device arrays, steps, and copies
+ * the device arrays back into the `out` arrays, chunk by chunk (`chunk`
+ * particles; 0 = about n/8), so that the copies of one chunk overlap the
+ * step of another (a host->device stream, the run's stream, a device->host
+ * stream).  Same results as copying in, cg_run_step(run, 1), copying out, per
+ * step.  Refused (CG_ESTATE) while added particles await initialization. */
+int cg_run_step_host(cg_run *run, int32_t nsteps, const cg_host_arrays *in,
+                     const cg_host_arrays *out, int32_t chunk, int32_t *bnd_stats);
+
 /* ---- control sections ---------------------------------------------------- */
 #define CG_MAX_SECTIONS 4096
 /* Solver(control_sections=[...]) (solver.pyx:97-103, 542-549): each step
