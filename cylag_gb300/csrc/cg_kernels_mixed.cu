@@ -40,10 +40,37 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         // persistent grid: one wave of resident blocks
         static int w2 = wave(step_mixed2d_kernel<2>, bs), w3 = wave(step_mixed2d_kernel<3>, bs),
                    w4 = wave(step_mixed2d_kernel<4>, bs),
-                   w3s = wave(step_mixed2d_kernel<3, true>, bs);
-        if (s.work & W_SPLIT)   // sorted working copies with split positions
+                   w3s = wave(step_mixed2d_kernel<3, true>, bs),
+                   w2st = wave(step_mixed2d_kernel<2, true, true>, bs),
+                   w3st = wave(step_mixed2d_kernel<3, true, true>, bs),
+                   w3t = wave(step_mixed2d_kernel<3, false, true>, bs);
+        // bulk-copy staging of the state tiles: 16-byte aligned arrays
+        // (0: off, the default; 2 or 3: resident blocks per SM of the staged
+        // kernel).  Measured on the default 1e7-particle LSM1 case: 0.495 ms
+        // off, 0.567 ms at 2 blocks/SM (no spills), 0.640 ms at 3 (spills):
+        // the state's HBM latency is not what bounds the step, and the staged
+        // kernel's extra registers cost resident warps
+        static const int stage_minb = [] {
+            const char* e = getenv("CYLAG_MIXED_STAGE");
+            int v = e ? atoi(e) : 0;
+            return (v == 2 || v == 3) ? v : 0;
+        }();
+        const bool stage_on = stage_minb != 0;
+        auto a16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+        const bool staged = stage_on && s.n >= 32 && a16(s.pos) && a16(s.rng) && a16(s.tri) &&
+                            a16(s.tag);
+        if ((s.work & W_SPLIT) && staged && stage_minb == 2)
+            step_mixed2d_kernel<2, true, true><<<nb < w2st ? nb : w2st, bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && staged)
+            step_mixed2d_kernel<3, true, true><<<nb < w3st ? nb : w3st, bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if (s.work & W_SPLIT)   // sorted working copies with split positions
             step_mixed2d_kernel<3, true><<<nb < w3s ? nb : w3s, bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                            step_index, stats, err);
+        else if (staged && minb == 3)
+            step_mixed2d_kernel<3, false, true><<<nb < w3t ? nb : w3t, bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
         else if (minb == 3)
             step_mixed2d_kernel<3><<<nb < w3 ? nb : w3, bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                    step_index, stats, err);

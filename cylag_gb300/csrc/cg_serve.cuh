@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT
         const int model = R.p.model;
         if constexpr (MIXED) {
             if (model == 1) {
-                step_mixed_particle<false>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, z32, i);
+                step_mixed_particle<false>(m, f, R.p, pool, none, aux, (int)k, nullptr, err, z32,
+                                           load_mixed_in(pool, i), i);
                 continue;
             }
         }

@@ -15,6 +15,7 @@
 // position; only the positions themselves differ (FP32 increments).
 #pragma once
 
+#include "cg_stage.cuh"
 #include "cg_step.cuh"
 
 namespace cg {
@@ -236,6 +237,28 @@ __device__ __forceinline__ int one_hop_split(const DevMesh& m, int tri0, const B
     return in_tri(m, kn, x.x, x.y) ? kn : -1;
 }
 
+// the per-particle state the mixed LSM1 step streams in
+struct MixedIn {
+    int tri;
+    int tag;
+    uint64_t rng;
+    float4 pos;   // split pair (W_SPLIT) or the bits of the FP64 pair
+};
+
+__device__ __forceinline__ MixedIn load_mixed_in(const DevState& s, int i) {
+    MixedIn in;
+    in.tri = __ldcs(&s.tri[i]);
+    in.pos = __ldcs(reinterpret_cast<const float4*>(s.pos) + i);
+    in.rng = __ldcs(reinterpret_cast<const unsigned long long*>(s.rng) + i);
+    in.tag = __ldcs(&s.tag[i]);
+    return in;
+}
+
+__device__ __forceinline__ double2 double2_from_bits(float4 r) {
+    return make_double2(__hiloint2double(__float_as_int(r.y), __float_as_int(r.x)),
+                        __hiloint2double(__float_as_int(r.w), __float_as_int(r.z)));
+}
+
 // LSM1 2D, mixed precision.  update_state_lsm1.pyx:30-133 (schemes 135-656,
 // diffusion 658-726) with the boundary conditions of compute_bc.pyx.
 // SPLIT: the working position is a split pair (W_SPLIT); the Euler step then
@@ -247,19 +270,19 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                                                     const WalkQueue& wq, int aux, int step_index,
                                                     int* __restrict__ stats,
                                                     uint32_t* __restrict__ err_word,
-                                                    const Zig32& z32, int i) {
-    // particle state streams through L2 once per step: evict-first loads and
-    // stores keep the mesh and node records resident in L2
-    int tri0 = __ldcs(&s.tri[i]);
+                                                    const Zig32& z32, const MixedIn& in, int i) {
+    // particle state streams through L2 once per step (evict-first loads or
+    // bulk copies, evict-first stores): the mesh and node records stay in L2
+    const int tri0 = in.tri;
     if (tri0 < 0) return;
     const float4* __restrict__ cur = reinterpret_cast<const float4*>(f.cur);
     float4 xs = make_float4(0.f, 0.f, 0.f, 0.f);   // SPLIT: the start position
     double2 x0 = make_double2(0., 0.);
-    if constexpr (SPLIT) xs = __ldcs(reinterpret_cast<const float4*>(s.pos) + i);
-    else x0 = __ldcs(reinterpret_cast<const double2*>(s.pos) + i);
+    if constexpr (SPLIT) xs = in.pos;
+    else x0 = double2_from_bits(in.pos);
     Rng rng;
-    rng.state = __ldcs(reinterpret_cast<const unsigned long long*>(s.rng) + i);
-    rng.inc = ((uint64_t)(uint32_t)__ldcs(&s.tag[i]) << 1) | 1ULL;
+    rng.state = in.rng;
+    rng.inc = ((uint64_t)(uint32_t)in.tag << 1) | 1ULL;
     rng.err = 0;
     double2 lastv = make_double2(0., 0.);
     if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
@@ -448,7 +471,11 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 }
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
-template <int MINB, bool SPLIT = false>
+// STAGED: each warp steps 32-particle tiles whose state the bulk-copy engine
+// staged in shared memory one tile ahead (cg_stage.cuh); the tail of fewer
+// than 32 particles is read directly.  The state arrays must be 16-byte
+// aligned (checked on the host).
+template <int MINB, bool SPLIT = false, bool STAGED = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -461,9 +488,56 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
         z32.wn[t] = (float)g_zig.wn[t];
         z32.fn[t] = (float)g_zig.fn[t];
     }
-    __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, i);
+    if constexpr (!STAGED) {
+        __syncthreads();
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
+            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
+                                       load_mixed_in(s, i), i);
+    } else {
+        constexpr int WPB = 256 / 32;
+        __shared__ WarpTile tiles[WPB][2];
+        __shared__ alignas(8) uint64_t bars[WPB][2];
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) {
+            mbar_init(&bars[w][0], 1);
+            mbar_init(&bars[w][1], 1);
+            fence_proxy_async_smem();   // the initialized barriers, to the copy engine
+        }
+        __syncthreads();
+        const int nfull = s.n >> 5;
+        const int gw = blockIdx.x * WPB + w, nw = gridDim.x * WPB;
+        if (lane == 0 && gw < nfull)
+            stage_tile(tiles[w][0], &bars[w][0], s.pos, s.rng, s.tri, s.tag, gw);
+        int k = 0;
+        for (int tile = gw; tile < nfull; tile += nw, ++k) {
+            const int st = k & 1;
+            const int next = tile + nw;
+            if (lane == 0 && next < nfull)
+                stage_tile(tiles[w][st ^ 1], &bars[w][st ^ 1], s.pos, s.rng, s.tri, s.tag, next);
+            if (!__all_sync(0xffffffffu, mbar_wait(&bars[w][st], (k >> 1) & 1))) {
+                // copies that do not complete: flag, wait (bounded) for the
+                // other stage's copy in flight, leave
+                if (lane == 0) atomicOr(err_word, ERR_ASYNC_TIMEOUT);
+                if (next < nfull) mbar_wait(&bars[w][st ^ 1], ((k + 1) >> 1) & 1);
+                return;
+            }
+            const WarpTile& t = tiles[w][st];
+            MixedIn in;
+            in.tri = t.tri[lane];
+            in.tag = t.tag[lane];
+            in.rng = t.rng[lane];
+            in.pos = t.pos[lane];
+            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, in,
+                                       tile * 32 + lane);
+            __syncwarp();   // the tile is read before lane 0 stages into it again
+        }
+        if (gw == 0) {
+            const int i = (nfull << 5) + lane;
+            if (i < s.n)
+                step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
+                                           load_mixed_in(s, i), i);
+        }
+    }
 }
 
 }  // namespace cg
