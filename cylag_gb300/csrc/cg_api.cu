@@ -325,6 +325,7 @@ int cg_ctx_destroy(cg_ctx* c) {
     cudaStreamSynchronize(c->stream);
     for (auto& b : c->mesh_bufs) dfree(b);
     dfree(c->frames_buf);
+    dfree(c->frames32_buf);
     cudaStreamSynchronize(c->own_stream);
     cudaStreamDestroy(c->own_stream);
     delete c;
@@ -548,12 +549,27 @@ int cg_fields_upload(cg_ctx* c, const cg_fields_desc* d) {
             memcpy(&h[((size_t)t * fr.nraw + fr.raw_slot[f]) * per], src[f] + (size_t)t * per,
                    per * sizeof(double));
         }
+    // a re-upload replaces the frames (and their budget share)
+    if (c->frames32_buf.p) c->used -= c->frames32_buf.bytes;
+    if (c->frames_buf.p) c->used -= c->frames_buf.bytes;
+    dfree(c->frames32_buf);
     dfree(c->frames_buf);
     int rc = dalloc(c, c->frames_buf, h.size() * sizeof(double));
     if (rc) return rc;
     CUDA_TRY(c, cudaMemcpy(c->frames_buf.p, h.data(), c->frames_buf.bytes, cudaMemcpyHostToDevice));
     c->used += c->frames_buf.bytes;
     fr.frames = (const double*)c->frames_buf.p;
+    // FP32 copy for the mixed form's per-step blend
+    {
+        std::vector<float> h32(h.size());
+        for (size_t k = 0; k < h.size(); ++k) h32[k] = (float)h[k];
+        dfree(c->frames32_buf);
+        if ((rc = dalloc(c, c->frames32_buf, h32.size() * sizeof(float)))) return rc;
+        CUDA_TRY(c, cudaMemcpy(c->frames32_buf.p, h32.data(), c->frames32_buf.bytes,
+                               cudaMemcpyHostToDevice));
+        c->used += c->frames32_buf.bytes;
+        fr.frames32 = (const float*)c->frames32_buf.p;
+    }
     c->frames = fr;
     c->times.assign(d->times, d->times + d->ntimes);
     c->fdim = d->dim;

@@ -34,6 +34,7 @@ struct cg_ctx {
     bool have_fields = false;
     DevFrames frames{};
     DevBuf frames_buf;
+    DevBuf frames32_buf;
     std::vector<double> times;
     int fdim = 2, nlayers = 1, npoints = 0;
     bool has_keps = false;

@@ -15,6 +15,7 @@ enum RawField { RF_ZS = 0, RF_UX, RF_UY, RF_UZ, RF_KT, RF_EP, RF_ZB, RF_COUNT };
 
 struct DevFrames {
     const double* frames;   // [ntimes][nraw][nnodes]
+    const float* frames32;  // the same rounded to FP32 (mixed form), or nullptr
     int nraw;
     int raw_slot[RF_COUNT]; // position of each raw field in a frame, -1 if absent
     int64_t nnodes;         // npoints * nlayers

@@ -51,6 +51,43 @@ __global__ void blend_kernel(DevFrames fr, int rec, double tf, int frozen, doubl
     }
 }
 
+// the mixed form's blend: FP32 frames and FP32 arithmetic (the record is
+// FP32 either way; interpolation and K add a few FP32 roundings)
+template <int DIM>
+__global__ void blend32_kernel(DevFrames fr, int rec, float tf, int frozen, float fac,
+                               float* __restrict__ cur, float* __restrict__ turb) {
+    using S = Slots<DIM>;
+    const int64_t n = fr.nnodes;
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= n) return;
+    const float* f0 = fr.frames32 + (int64_t)rec * fr.nraw * n;
+    const float* f1 = f0 + (int64_t)fr.nraw * n;
+    auto val = [&](int rf) -> float {
+        const int sl = fr.raw_slot[rf];
+        if (sl < 0) return 0.f;
+        const float a = __ldg(&f0[(int64_t)sl * n + node]);
+        if (frozen) return a;
+        const float b = __ldg(&f1[(int64_t)sl * n + node]);
+        return tf * a + (1.f - tf) * b;
+    };
+    float* r = cur + node * S::NF;
+    const float kt = val(RF_KT), ep = val(RF_EP);
+    r[S::ZS] = val(RF_ZS);
+    r[S::UX] = val(RF_UX);
+    r[S::UY] = val(RF_UY);
+    r[S::K] = fac * kt * kt / fmaxf(ep, 1e-16f);   // eulerian_field_set.pyx:1995-1997
+    if (DIM == 3) {
+        r[Slots<3>::UZ] = val(RF_UZ);
+        r[5] = 0.f;
+        r[6] = 0.f;
+        r[7] = 0.f;
+    }
+    if (turb) {
+        turb[2 * node] = kt;
+        turb[2 * node + 1] = ep;
+    }
+}
+
 void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac, void* cur,
                   void* turb, int precision, cudaStream_t st) {
     int bs = 256;
@@ -59,6 +96,12 @@ void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double f
         double *c = (double*)cur, *t = (double*)turb;
         if (fr.dim == 2) blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
         else blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
+    } else if (fr.frames32) {
+        float *c = (float*)cur, *t = (float*)turb;
+        if (fr.dim == 2)
+            blend32_kernel<2><<<nb, bs, 0, st>>>(fr, rec, (float)tf, frozen, (float)fac, c, t);
+        else
+            blend32_kernel<3><<<nb, bs, 0, st>>>(fr, rec, (float)tf, frozen, (float)fac, c, t);
     } else {
         // FP64 interpolation, rounded once to the FP32 record
         float *c = (float*)cur, *t = (float*)turb;

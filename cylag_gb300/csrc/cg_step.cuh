@@ -894,9 +894,12 @@ __global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, D
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
+    const int count = *wq.count;
+    // blocks beyond the queue leave before loading the tables (the grid is
+    // sized for any count; most steps queue few particles)
+    if ((long long)blockIdx.x * blockDim.x >= count) return;
     __shared__ ZigTables zt;
     load_zig(zt);
-    const int count = *wq.count;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
         WalkEntry w = wq.e[j];
         int i = w.i;
