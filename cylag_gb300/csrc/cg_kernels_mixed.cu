@@ -41,6 +41,8 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         static int w2 = wave(step_mixed2d_kernel<2>, bs), w3 = wave(step_mixed2d_kernel<3>, bs),
                    w4 = wave(step_mixed2d_kernel<4>, bs),
                    w3s = wave(step_mixed2d_kernel<3, true>, bs),
+                   w2s = wave(step_mixed2d_kernel<2, true>, bs),
+                   w4s = wave(step_mixed2d_kernel<4, true>, bs),
                    w2st = wave(step_mixed2d_kernel<2, true, true>, bs),
                    w3st = wave(step_mixed2d_kernel<3, true, true>, bs),
                    w3t = wave(step_mixed2d_kernel<3, false, true>, bs);
@@ -65,6 +67,12 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         else if ((s.work & W_SPLIT) && staged)
             step_mixed2d_kernel<3, true, true><<<nb < w3st ? nb : w3st, bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && minb == 2)
+            step_mixed2d_kernel<2, true><<<nb < w2s ? nb : w2s, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                           step_index, stats, err);
+        else if ((s.work & W_SPLIT) && minb == 4)
+            step_mixed2d_kernel<4, true><<<nb < w4s ? nb : w4s, bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                           step_index, stats, err);
         else if (s.work & W_SPLIT)   // sorted working copies with split positions
             step_mixed2d_kernel<3, true><<<nb < w3s ? nb : w3s, bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                            step_index, stats, err);
