@@ -154,6 +154,52 @@ class EulerianFieldSet:
         self.friction_model = friction_model
         self.friction_coefficient = friction_coefficient
 
+    @staticmethod
+    def from_telemac2d(file_name, main_var_names=("FREE SURFACE", "VELOCITY U", "VELOCITY V"),
+                       bnd_file=None, optional_fields=None, init_trifinder=True,
+                       friction_model=1, friction_coefficient=40.):
+        """eulerian_field_set.pyx:316-398 from a TELEMAC-2D result file
+        (cylag_gb300.telemac reads the Selafin format); times start at 0 at
+        the first record.  ``init_trifinder`` is accepted and unused: the
+        grid locator replaces matplotlib's trifinder."""
+        from .telemac import SelafinFile, read_cli
+        res = SelafinFile(file_name)
+        bnd_pts, nopen = read_cli(bnd_file) if bnd_file is not None else (None, 0)
+        mesh = TriangularMesh(res.x, res.y, res.ikle2, boundary_points=bnd_pts, nopen=nopen)
+        nt, n = res.ntimestep, res.npoin2
+        get = lambda name: np.stack([res.get_data_value(name, k)[:n] for k in range(nt)])
+        opt = None
+        if optional_fields is not None:
+            opt = np.stack([get(nm) for nm in optional_fields])
+        return EulerianFieldSet(mesh, 2, 1, res.times - res.times[0], get(main_var_names[0]),
+                                get(main_var_names[1]), get(main_var_names[2]), None, opt,
+                                None if optional_fields is None else list(optional_fields),
+                                None, friction_model=friction_model,
+                                friction_coefficient=friction_coefficient)
+
+    @staticmethod
+    def from_telemac3d(file_name,
+                       main_var_names=("ELEVATION Z", "VELOCITY U", "VELOCITY V", "VELOCITY W"),
+                       bnd_file=None, optional_fields=None, init_trifinder=True,
+                       friction_model=1, friction_coefficient=40.):
+        """eulerian_field_set.pyx:400-484 from a TELEMAC-3D result file:
+        nplan layers of npoin2 nodes (the file's node order)."""
+        from .telemac import SelafinFile, read_cli
+        res = SelafinFile(file_name)
+        bnd_pts, nopen = read_cli(bnd_file) if bnd_file is not None else (None, 0)
+        mesh = TriangularMesh(res.x, res.y, res.ikle2, boundary_points=bnd_pts, nopen=nopen)
+        nt = res.ntimestep
+        get = lambda name: np.stack([res.get_data_value(name, k) for k in range(nt)])
+        opt = None
+        if optional_fields is not None:
+            opt = np.stack([get(nm) for nm in optional_fields])
+        return EulerianFieldSet(mesh, 3, res.nplan, res.times - res.times[0],
+                                get(main_var_names[0]), get(main_var_names[1]),
+                                get(main_var_names[2]), get(main_var_names[3]), opt,
+                                None if optional_fields is None else list(optional_fields),
+                                None, friction_model=friction_model,
+                                friction_coefficient=friction_coefficient)
+
     def _get_field_from_id(self, field_id):
         """eulerian_field_set.pyx:673-720: 0 elevation, 1-3 velocity, 4+ the
         optional fields in the given order ([ntimes, npoints*nlayers])."""

@@ -83,3 +83,35 @@ def test_gpu_keps_larger_vs_oracle():
     assert_state_close(dict(position=ps.position, tri=ps.tri, inactive=ps.inactive), want,
                        rtol=RTOL, what="keps20k")
     s.close()
+
+
+def test_gpu_run_from_telemac_files(tmp_path):
+    """The open-channel fixture's mesh, boundary and fields written as a
+    TELEMAC-2D result file (FP64) and a .cli file, read back through
+    EulerianFieldSet.from_telemac2d: same trajectories as the reference's,
+    exit counts per open boundary (numbered in .cli order)."""
+    import cylag_gb300 as cg
+    from cylag_gb300.telemac import write_selafin
+    case, meta, want = load_golden("open")
+    bp = case["boundary_points"]
+    lines = []
+    for vid, lab in bp:
+        code = "2 2 2" if lab == 0 else "5 4 4"
+        lines.append(f"{code} 0.0 0.0 0.0 0.0 2 0.0 0.0 0.0 {vid + 1} 0")
+    (tmp_path / "open.cli").write_text("\n".join(lines) + "\n")
+    nv = len(case["x"])
+    vals = [[case["elevation"][0], case["velocity_x"][0], case["velocity_y"][0]]]
+    write_selafin(tmp_path / "open.slf", case["x"], case["y"], case["triangles"], [0.0], vals,
+                  ["FREE SURFACE", "VELOCITY U", "VELOCITY V"], double=True)
+    fs = cg.EulerianFieldSet.from_telemac2d(str(tmp_path / "open.slf"),
+                                            bnd_file=str(tmp_path / "open.cli"))
+    assert fs.triangular_mesh.nopen == 2 and fs.npoints == nv
+    ps = cg.LagrangianParticleSet(case["position"], dim=2, **meta.get("pset", {}))
+    s = cg.Solver(fs, ps, meta["params"], seed=meta["seed"])
+    s.forward(nsteps=meta["nsteps"])
+    assert_state_close(state(ps), want, rtol=RTOL, what="from telemac")
+    # .cli order numbers the right side 1 and the left side 2
+    order = [2, 1] if bp[[i for i in range(len(bp)) if bp[i, 1]][0], 1] == 2 else [1, 2]
+    got = s.bnd_statistics()
+    np.testing.assert_array_equal(got[:, [o - 1 for o in order]], want["bnd_stats"])
+    s.close()
