@@ -44,24 +44,30 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                    w2s = wave(step_mixed2d_kernel<2, true>, bs),
                    w4s = wave(step_mixed2d_kernel<4, true>, bs),
                    w2st = wave(step_mixed2d_kernel<2, true, true>, bs),
+                   w3sa = wave(step_mixed2d_kernel<3, true, true, true>, bs),
                    w3st = wave(step_mixed2d_kernel<3, true, true>, bs),
                    w3t = wave(step_mixed2d_kernel<3, false, true>, bs);
         // bulk-copy staging of the state tiles: 16-byte aligned arrays
-        // (0: off, the default; 2 or 3: resident blocks per SM of the staged
-        // kernel).  Measured on the default 1e7-particle LSM1 case: 0.495 ms
-        // off, 0.567 ms at 2 blocks/SM (no spills), 0.640 ms at 3 (spills):
-        // the state's HBM latency is not what bounds the step, and the staged
-        // kernel's extra registers cost resident warps
+        // (0: off, the default; 2 or 3: bulk copies per warp tile at 2 or 3
+        // resident blocks per SM; 4: per-thread cp.async one particle ahead).
+        // Measured on the default 1e7-particle LSM1 case (kernels per step):
+        // 0.478-0.495 ms off, 0.567 ms bulk at 2 blocks/SM (no spills),
+        // 0.640 ms bulk at 3 (spills), 0.521 ms per-thread cp.async: the
+        // state's HBM latency is not what bounds the step, and staging costs
+        // registers and instructions
         static const int stage_minb = [] {
             const char* e = getenv("CYLAG_MIXED_STAGE");
             int v = e ? atoi(e) : 0;
-            return (v == 2 || v == 3) ? v : 0;
+            return (v == 2 || v == 3 || v == 4) ? v : 0;
         }();
         const bool stage_on = stage_minb != 0;
         auto a16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
         const bool staged = stage_on && s.n >= 32 && a16(s.pos) && a16(s.rng) && a16(s.tri) &&
                             a16(s.tag);
-        if ((s.work & W_SPLIT) && staged && stage_minb == 2)
+        if ((s.work & W_SPLIT) && staged && stage_minb == 4)   // per-thread cp.async prefetch
+            step_mixed2d_kernel<3, true, true, true><<<nb < w3sa ? nb : w3sa, bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && staged && stage_minb == 2)
             step_mixed2d_kernel<2, true, true><<<nb < w2st ? nb : w2st, bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && staged)

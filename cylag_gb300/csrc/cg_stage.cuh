@@ -92,4 +92,47 @@ __device__ __forceinline__ void stage_tile(WarpTile& t, uint64_t* bar, const voi
     bulk_copy_g2s(t.tag, tag + (size_t)tile * 32, 128, bar);
 }
 
+// ---------------------------------------------------------------------------
+// per-thread asynchronous copies (cp.async): each thread prefetches its next
+// particle's state into its own shared-memory slot one iteration ahead; the
+// slot is private, so the thread's own wait_group is the only
+// synchronization
+// ---------------------------------------------------------------------------
+struct ThreadSlot {
+    float4 pos;
+    uint64_t rng;
+    int tri;
+    int tag;
+};
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// all but the most recent `N` groups of this thread are complete
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// particle i's state into slot t (one group)
+__device__ __forceinline__ void prefetch_slot(ThreadSlot& t, const void* pos, const uint64_t* rng,
+                                              const int* tri, const int* tag, int i) {
+    cp_async16(&t.pos, (const char*)pos + (size_t)i * 16);
+    cp_async8(&t.rng, rng + i);
+    cp_async4(&t.tri, tri + i);
+    cp_async4(&t.tag, tag + i);
+}
+
 }  // namespace cg

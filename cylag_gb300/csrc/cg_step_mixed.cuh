@@ -475,7 +475,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 // staged in shared memory one tile ahead (cg_stage.cuh); the tail of fewer
 // than 32 particles is read directly.  The state arrays must be 16-byte
 // aligned (checked on the host).
-template <int MINB, bool SPLIT = false, bool STAGED = false>
+template <int MINB, bool SPLIT = false, bool STAGED = false, bool ASYNC = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -493,6 +493,30 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
             step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
                                        load_mixed_in(s, i), i);
+    } else if constexpr (ASYNC) {
+        // per-thread cp.async prefetch of the next particle's state
+        __shared__ ThreadSlot slots[2][256];
+        __syncthreads();
+        const int stride = gridDim.x * blockDim.x;
+        int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < s.n) prefetch_slot(slots[0][threadIdx.x], s.pos, s.rng, s.tri, s.tag, i);
+        cp_async_commit();
+        for (int k = 0; i < s.n; i += stride, ++k) {
+            const int nx = i + stride;
+            if (nx < s.n)
+                prefetch_slot(slots[(k + 1) & 1][threadIdx.x], s.pos, s.rng, s.tri, s.tag, nx);
+            cp_async_commit();
+            cp_async_wait<1>();
+            const ThreadSlot& t = slots[k & 1][threadIdx.x];
+            MixedIn in;
+            in.tri = t.tri;
+            in.tag = t.tag;
+            in.rng = t.rng;
+            in.pos = t.pos;
+            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, in,
+                                       i);
+        }
+        cp_async_wait<0>();
     } else {
         constexpr int WPB = 256 / 32;
         __shared__ WarpTile tiles[WPB][2];

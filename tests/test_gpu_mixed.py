@@ -127,7 +127,7 @@ s.close()
 """
 
 
-@pytest.mark.parametrize("stage", ["2", "3"])
+@pytest.mark.parametrize("stage", ["2", "3", "4"])
 def test_staged_state_tiles_same_results(tmp_path, stage):
     """The bulk-copy staged variant of the mixed step (opt-in through
     CYLAG_MIXED_STAGE; a ragged tail of 7 particles) gives bit-identical
