@@ -325,6 +325,141 @@ __device__ inline double rng_single(Rng& r, int method, const ZigTables& z) {
     return a;
 }
 
+// FP32 samplers of the mixed form (tables in shared memory)
+struct Zig32 {
+    uint32_t kn[128];
+    float wn[128];
+    float fn[128];
+};
+
+// random_utils.pyx:55-67 in FP32
+__device__ __forceinline__ float uniform32(Rng& r) {
+    return (float)pcg_next(r) * 2.3283064365386963e-10f;
+}
+
+// random_utils.pyx:154-194 in FP32 (same stream consumption as the FP64
+// version except where an FP32 wedge/tail test rounds the other way)
+__device__ inline float zig32(Rng& r, const Zig32& z) {
+    for (int tries = 0; tries < RNG_MAX_TRIES; ++tries) {
+        int32_t hz = (int32_t)pcg_next(r);
+        uint32_t iz = (uint32_t)hz & 127u;
+        uint32_t ahz = hz < 0 ? 0u - (uint32_t)hz : (uint32_t)hz;
+        if (ahz < z.kn[iz]) return (float)hz * z.wn[iz];
+        if (iz == 0) {
+            for (int t2 = 0; t2 < RNG_MAX_TRIES; ++t2) {
+                float x = -__logf(uniform32(r)) * 0.2904764f;
+                float y = -__logf(uniform32(r));
+                if (y + y >= x * x) return hz > 0 ? 3.442619855899f + x : -3.442619855899f - x;
+            }
+            r.err |= ERR_RNG_LIMIT;
+            return 0.f;
+        }
+        float x = (float)hz * z.wn[iz];
+        if (z.fn[iz] + uniform32(r) * (z.fn[iz - 1] - z.fn[iz]) < __expf(-0.5f * x * x)) return x;
+    }
+    r.err |= ERR_RNG_LIMIT;
+    return 0.f;
+}
+
+__device__ inline void polar32(Rng& r, float& a, float& b) {
+    float x1 = 0.f, x2 = 0.f, w = 2.f;
+    int tries = 0;
+    while ((w >= 1.f || w == 0.f) && tries < RNG_MAX_TRIES) {
+        x1 = 2.f * uniform32(r) - 1.f;
+        x2 = 2.f * uniform32(r) - 1.f;
+        w = x1 * x1 + x2 * x2;
+        ++tries;
+    }
+    if (tries == RNG_MAX_TRIES) { r.err |= ERR_RNG_LIMIT; a = b = 0.f; return; }
+    w = sqrtf((-2.f * __logf(w)) / w);
+    a = x1 * w;
+    b = x2 * w;
+}
+
+__device__ inline void pair32(Rng& r, int method, const Zig32& z, float& a, float& b) {
+    if (method == 1) {
+        a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+        b = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+    } else if (method == 2) {
+        a = zig32(r, z);
+        b = zig32(r, z);
+    } else {
+        polar32(r, a, b);
+    }
+}
+
+// Outlined draws for the large LSM2/LSM3 integrators: one copy of the
+// sampler per kernel instead of one per call site (their per-dimension
+// loops are unrolled), which keeps their instruction footprint down.  The
+// stream state goes in and out by value, so no particle state needs an
+// address (it stays in registers).
+template <typename T>
+struct DrawOut {
+    uint64_t state;
+    uint32_t err;
+    T a, b;
+};
+
+static __device__ __noinline__ DrawOut<double> rng_draws_ol(uint64_t st, uint64_t inc, int method,
+                                                           const ZigTables& z, int two) {
+    Rng r{st, inc, 0};
+    DrawOut<double> o;
+    o.b = 0.;
+    if (two) rng_pair(r, method, z, o.a, o.b);
+    else o.a = rng_single(r, method, z);
+    o.state = r.state;
+    o.err = r.err;
+    return o;
+}
+
+static __device__ __noinline__ DrawOut<float> draws32_ol(uint64_t st, uint64_t inc, int method,
+                                                        const Zig32& z, int two) {
+    Rng r{st, inc, 0};
+    DrawOut<float> o;
+    o.b = 0.f;
+    if (two) {
+        pair32(r, method, z, o.a, o.b);
+    } else if (method == 1) {
+        o.a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+    } else if (method == 2) {
+        o.a = zig32(r, z);
+    } else {
+        float b;
+        polar32(r, o.a, b);
+    }
+    o.state = r.state;
+    o.err = r.err;
+    return o;
+}
+
+__device__ __forceinline__ void rng_pair_ol(Rng& r, int method, const ZigTables& z, double& a,
+                                            double& b) {
+    const DrawOut<double> o = rng_draws_ol(r.state, r.inc, method, z, 1);
+    r.state = o.state;
+    r.err |= o.err;
+    a = o.a;
+    b = o.b;
+}
+__device__ __forceinline__ double rng_single_ol(Rng& r, int method, const ZigTables& z) {
+    const DrawOut<double> o = rng_draws_ol(r.state, r.inc, method, z, 0);
+    r.state = o.state;
+    r.err |= o.err;
+    return o.a;
+}
+__device__ __forceinline__ void pair32_ol(Rng& r, int method, const Zig32& z, float& a, float& b) {
+    const DrawOut<float> o = draws32_ol(r.state, r.inc, method, z, 1);
+    r.state = o.state;
+    r.err |= o.err;
+    a = o.a;
+    b = o.b;
+}
+__device__ __forceinline__ float single32_ol(Rng& r, int method, const Zig32& z) {
+    const DrawOut<float> o = draws32_ol(r.state, r.inc, method, z, 0);
+    r.state = o.state;
+    r.err |= o.err;
+    return o.a;
+}
+
 // ---------------------------------------------------------------------------
 // geometry (cylag/geom/utils.pyx, intersections.pyx, xylocalizer.pyx)
 // ---------------------------------------------------------------------------

@@ -294,8 +294,8 @@ __device__ __forceinline__ void euler_maruyama_lsm2_u(Particle<DIM, FT>& q, doub
     double a1 = lsm2_a1<typename ArithOf<FT>::type>(p, DIM, dp, ux - q.up[0], uy - q.up[1], DIM == 3 ? uz - q.up[2] : 0.);
     double xix = 0., xiy = 0., xiz = 0., diffx = 0., diffy = 0., diffz = 0.;
     if (diffmod != 0) {
-        rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
-        if (DIM == 3) xiz = rng_single(q.rng, p.rng_method, q.z);
+        rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
+        if (DIM == 3) xiz = rng_single_ol(q.rng, p.rng_method, q.z);
     }
     if (diffmod == 2 || diffmod == 3) {
         double ep;
@@ -440,10 +440,14 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
             R L_pp = sqrt(fmax(R(0.), var_gp));
             R L_xp = L_pp > R(0.) ? cov / L_pp : R(0.);
             R L_xx = sqrt(fmax(R(0.), var_gx - L_xp * L_xp));
-            double xix, xiy;
-            rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
-            Gp = L_pp * R(xix);
-            Gx = L_xp * R(xix) + L_xx * R(xiy);
+            R xix, xiy;
+            if constexpr (std::is_same<R, double>::value) {
+                rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
+            } else {
+                pair32_ol(q.rng, p.rng_method, *q.z32, xix, xiy);   // FP32 draws (mixed)
+            }
+            Gp = L_pp * xix;
+            Gx = L_xp * xix + L_xx * xiy;
         }
         if constexpr (std::is_same<R, double>::value) {
             double up_mean = up0[d] * c.beta + u_k * um_beta + Fp * c.D1;
@@ -526,11 +530,11 @@ __device__ __forceinline__ void lsm2_fluctuations(Particle<DIM, FT>& q, double d
     }
     if (b0 > 0.) {
         double xix, xiy;
-        rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
+        rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
         fl[0] = sqrt(0.5 * b0) * xix;
         fl[1] = sqrt(0.5 * b1) * xiy;
     }
-    if (DIM == 3 && b2 > 0.) fl[2] = sqrt(0.5 * b2) * rng_single(q.rng, p.rng_method, q.z);
+    if (DIM == 3 && b2 > 0.) fl[2] = sqrt(0.5 * b2) * rng_single_ol(q.rng, p.rng_method, q.z);
 }
 
 // ---------------------------------------------------------------------------
@@ -770,11 +774,29 @@ __device__ __forceinline__ bool lsm3_clipped_coefficients(R a, R a2, R tl, R dt,
     return lsm3_finite(c);
 }
 
+// out of line: called for the horizontal and (when T_L differs) the
+// vertical time scale, one copy of the code; the coefficients come back by
+// value (no caller state needs an address)
 template <typename R>
-__device__ __forceinline__ bool lsm3_coefficients(R a, R a2, R tl, R dt,
-                                                  int edge_opt, Lsm3Coef<R>& c) {
-    return edge_opt == 2 ? lsm3_clipped_coefficients(a, a2, tl, dt, c)
-                         : lsm3_direct_coefficients(a, a2, tl, dt, c);
+struct Lsm3CoefOut {
+    Lsm3Coef<R> c;
+    bool ok;
+};
+
+template <typename R>
+__device__ __noinline__ Lsm3CoefOut<R> lsm3_coefficients_ol(R a, R a2, R tl, R dt, int edge_opt) {
+    Lsm3CoefOut<R> o;
+    o.ok = edge_opt == 2 ? lsm3_clipped_coefficients(a, a2, tl, dt, o.c)
+                         : lsm3_direct_coefficients(a, a2, tl, dt, o.c);
+    return o;
+}
+
+template <typename R>
+__device__ __forceinline__ bool lsm3_coefficients(R a, R a2, R tl, R dt, int edge_opt,
+                                                  Lsm3Coef<R>& c) {
+    const Lsm3CoefOut<R> o = lsm3_coefficients_ol<R>(a, a2, tl, dt, edge_opt);
+    c = o.c;
+    return o.ok;
 }
 
 // update_state_lsm3.pyx:523-557 (strict: only roundoff-sized negative pivots clip)
@@ -857,8 +879,8 @@ __device__ __forceinline__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double
     const double unorm = fmax(EPSILON_LSM2, sqrt(slip_norm<DIM>(q.us, q.up)));
     const double a1 = double(lsm3_a1<R>(p, R(dp), R(unorm)));
     double xix, xiy, xiz = 0.;
-    rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
-    if (DIM == 3) xiz = rng_single(q.rng, p.rng_method, q.z);
+    rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
+    if (DIM == 3) xiz = rng_single_ol(q.rng, p.rng_method, q.z);
     double ep = 0., tml = 0., unstml, diffx;
     if (diffmod == 2 || diffmod == 3) {
         tml = keps_tml(q, q.tri, q.ll, q.x[0], q.x[1], z, ep);
@@ -992,15 +1014,16 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
                 }
                 factored = true;
             }
-            double xixd, xiyd, xizd;
-            if (lower[4] > R(0.)) {
-                rng_pair(q.rng, p.rng_method, q.z, xixd, xiyd);
-            } else {
-                xixd = rng_single(q.rng, p.rng_method, q.z);
-                xiyd = 0.;
+            R xix, xiy = R(0.), xiz = R(0.);
+            if constexpr (exact) {
+                if (lower[4] > R(0.)) rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
+                else xix = rng_single_ol(q.rng, p.rng_method, q.z);
+                if (lower[8] > R(0.)) xiz = rng_single_ol(q.rng, p.rng_method, q.z);
+            } else {   // FP32 draws (mixed)
+                if (lower[4] > R(0.)) pair32_ol(q.rng, p.rng_method, *q.z32, xix, xiy);
+                else xix = single32_ol(q.rng, p.rng_method, *q.z32);
+                if (lower[8] > R(0.)) xiz = single32_ol(q.rng, p.rng_method, *q.z32);
             }
-            xizd = lower[8] > R(0.) ? rng_single(q.rng, p.rng_method, q.z) : 0.;
-            const R xix = R(xixd), xiy = R(xiyd), xiz = R(xizd);
             us_mean += sigma_s * lower[0] * xix;
             ur_mean += sigma_s * (lower[3] * xix + lower[4] * xiy);
             xp_mean += sigma_s * (lower[6] * xix + lower[7] * xiy + lower[8] * xiz);
@@ -1040,13 +1063,13 @@ __device__ __forceinline__ void lsm3_fluctuations(Particle<DIM, FT>& q, double* 
     }
     if (sigma_h > 0.) {
         double xix, xiy;
-        rng_pair(q.rng, p.rng_method, q.z, xix, xiy);
+        rng_pair_ol(q.rng, p.rng_method, q.z, xix, xiy);
         fl[0] = sigma_h * xix;
         fl[1] = sigma_h * xiy;
     }
     if (DIM == 3) {
         double sigma_v = p.diffmod == 3 ? sigma_h : sqrt(p.nuz / p.tl_v);
-        if (sigma_v > 0.) fl[2] = sigma_v * rng_single(q.rng, p.rng_method, q.z);
+        if (sigma_v > 0.) fl[2] = sigma_v * rng_single_ol(q.rng, p.rng_method, q.z);
     }
 }
 

@@ -27,9 +27,10 @@ namespace cg {
 template <typename FT, int MODEL, int SCHEME>
 __device__ __noinline__ void serve_particle(const DevMesh& m, const DevFields<FT>& f,
                                             const DevParams& p, DevState& pool, int aux, int k,
-                                            uint32_t* err, const ZigTables& zt, int i) {
+                                            uint32_t* err, const ZigTables& zt, int i,
+                                            const Zig32* z32) {
     const WalkQueue none{nullptr, nullptr};
-    step_particle<2, FT, MODEL, SCHEME>(m, f, p, pool, none, aux, k, nullptr, err, zt, i);
+    step_particle<2, FT, MODEL, SCHEME>(m, f, p, pool, none, aux, k, nullptr, err, zt, i, z32);
 }
 
 template <typename FT, bool MIXED>
@@ -49,6 +50,7 @@ __global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT
         }
     }
     load_zig(zt);   // ends with __syncthreads
+    const Zig32* z32p = MIXED ? &z32 : nullptr;
     const unsigned long long g = *(volatile unsigned long long*)&clk->gstep;
     const int na = *nactive;
     const int lane = threadIdx.x & 31;
@@ -73,13 +75,13 @@ __global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT
         const int ts = R.p.time_scheme, kk = (int)k;
         if (model == 1)
             step_particle<2, FT, 1>(m, f, R.p, pool, none, aux, kk, nullptr, err, zt, i);
-        else if (model == 2 && ts == 5) serve_particle<FT, 2, 5>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else if (model == 2 && ts == 1) serve_particle<FT, 2, 1>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else if (model == 2 && ts == 2) serve_particle<FT, 2, 2>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else if (model == 2 && ts == 3) serve_particle<FT, 2, 3>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else if (model == 2) serve_particle<FT, 2, 4>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else if (ts == 5) serve_particle<FT, 3, 5>(m, f, R.p, pool, aux, kk, err, zt, i);
-        else serve_particle<FT, 3, 1>(m, f, R.p, pool, aux, kk, err, zt, i);
+        else if (model == 2 && ts == 5) serve_particle<FT, 2, 5>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else if (model == 2 && ts == 1) serve_particle<FT, 2, 1>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else if (model == 2 && ts == 2) serve_particle<FT, 2, 2>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else if (model == 2 && ts == 3) serve_particle<FT, 2, 3>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else if (model == 2) serve_particle<FT, 2, 4>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else if (ts == 5) serve_particle<FT, 3, 5>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
+        else serve_particle<FT, 3, 1>(m, f, R.p, pool, aux, kk, err, zt, i, z32p);
     }
     // the last block to finish advances the global step
     __syncthreads();

@@ -31,6 +31,7 @@ struct Particle {
     double us[3];     // fluid velocity seen
     int tri, tri0, ltri, ll, ll0;
     int pidx = 0, pstep = 0;   // caller's particle index and step (stranding records)
+    const Zig32* z32 = nullptr;   // FP32 tables (mixed LSM2/LSM3 direct integrators)
     uint32_t err;
     bool deleted;
     bool defer;       // in: 2D final localization may be deferred to the walk queue
@@ -745,11 +746,13 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
                                               const WalkQueue& wq, int aux, int step_index,
                                               int* __restrict__ stats,
                                               uint32_t* __restrict__ err_word,
-                                              const ZigTables& zt, int i) {
+                                              const ZigTables& zt, int i,
+                                              const Zig32* z32 = nullptr) {
     int tri = s.tri[i];
     if (tri < 0) return;  // inactive (-1) or awaiting initialization (-2)
 
     Particle<DIM, FT> q(m, f, p, zt);
+    q.z32 = z32;
     q.tri = tri;
     q.tri0 = tri;
     q.ltri = tri;
@@ -830,10 +833,20 @@ __global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, D
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
     __shared__ ZigTables zt;
-    load_zig(zt);
+    // the mixed LSM2/LSM3 direct integrators draw from FP32 tables
+    constexpr bool z32_on = std::is_same<FT, float>::value && MODEL >= 2;
+    __shared__ Zig32 z32[1];
+    if constexpr (z32_on) {
+        for (int t = threadIdx.x; t < 128; t += blockDim.x) {
+            z32[0].kn[t] = g_zig.kn[t];
+            z32[0].wn[t] = (float)g_zig.wn[t];
+            z32[0].fn[t] = (float)g_zig.fn[t];
+        }
+    }
+    load_zig(zt);   // ends with __syncthreads
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
         step_particle<DIM, FT, MODEL, SCHEME>(m, f, p, s, wq, aux, step_index, stats, err_word,
-                                               zt, i);
+                                               zt, i, z32_on ? &z32[0] : nullptr);
 }
 
 // blocks of one wave of resident blocks of `kernel` (persistent grid)

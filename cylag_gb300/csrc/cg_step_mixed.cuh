@@ -20,68 +20,6 @@
 
 namespace cg {
 
-struct Zig32 {
-    uint32_t kn[128];
-    float wn[128];
-    float fn[128];
-};
-
-// random_utils.pyx:55-67 in FP32
-__device__ __forceinline__ float uniform32(Rng& r) {
-    return (float)pcg_next(r) * 2.3283064365386963e-10f;
-}
-
-// random_utils.pyx:154-194 in FP32 (same stream consumption as the FP64
-// version except where an FP32 wedge/tail test rounds the other way)
-__device__ inline float zig32(Rng& r, const Zig32& z) {
-    for (int tries = 0; tries < RNG_MAX_TRIES; ++tries) {
-        int32_t hz = (int32_t)pcg_next(r);
-        uint32_t iz = (uint32_t)hz & 127u;
-        uint32_t ahz = hz < 0 ? 0u - (uint32_t)hz : (uint32_t)hz;
-        if (ahz < z.kn[iz]) return (float)hz * z.wn[iz];
-        if (iz == 0) {
-            for (int t2 = 0; t2 < RNG_MAX_TRIES; ++t2) {
-                float x = -__logf(uniform32(r)) * 0.2904764f;
-                float y = -__logf(uniform32(r));
-                if (y + y >= x * x) return hz > 0 ? 3.442619855899f + x : -3.442619855899f - x;
-            }
-            r.err |= ERR_RNG_LIMIT;
-            return 0.f;
-        }
-        float x = (float)hz * z.wn[iz];
-        if (z.fn[iz] + uniform32(r) * (z.fn[iz - 1] - z.fn[iz]) < __expf(-0.5f * x * x)) return x;
-    }
-    r.err |= ERR_RNG_LIMIT;
-    return 0.f;
-}
-
-__device__ inline void polar32(Rng& r, float& a, float& b) {
-    float x1 = 0.f, x2 = 0.f, w = 2.f;
-    int tries = 0;
-    while ((w >= 1.f || w == 0.f) && tries < RNG_MAX_TRIES) {
-        x1 = 2.f * uniform32(r) - 1.f;
-        x2 = 2.f * uniform32(r) - 1.f;
-        w = x1 * x1 + x2 * x2;
-        ++tries;
-    }
-    if (tries == RNG_MAX_TRIES) { r.err |= ERR_RNG_LIMIT; a = b = 0.f; return; }
-    w = sqrtf((-2.f * __logf(w)) / w);
-    a = x1 * w;
-    b = x2 * w;
-}
-
-__device__ inline void pair32(Rng& r, int method, const Zig32& z, float& a, float& b) {
-    if (method == 1) {
-        a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
-        b = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
-    } else if (method == 2) {
-        a = zig32(r, z);
-        b = zig32(r, z);
-    } else {
-        polar32(r, a, b);
-    }
-}
-
 // xylocalizer.pyx:27-124 method 3, first test through the FP32 filter
 __device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32& t, int k,
                                                   double p0x, double p0y, double x, double y,
