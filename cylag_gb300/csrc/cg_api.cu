@@ -1139,8 +1139,27 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
     int rc = ensure_fields(r);
     if (rc) return rc;
     const int n = r->st.n, D = r->prm.dim;
-    if (chunk == 0) chunk = std::max(1 << 16, ((n + 7) / 8 + 255) / 256 * 256);
-    const int nch = n > 0 ? (n + chunk - 1) / chunk : 0;
+    // chunk boundaries: `chunk` particles each, or (chunk == 0) a ramp of
+    // 1/32, 2/32, then 4/32 of the pool, down to 2/32, 2/32, 1/32 at the end,
+    // so that the copies in and out overlap from early on and the last
+    // chunk's copy out is short
+    std::vector<int> bounds{0};
+    if (chunk > 0) {
+        for (int a = chunk; a < n; a += chunk) bounds.push_back(a);
+    } else if (n >= (1 << 20)) {
+        static const int ramp[] = {1, 2, 4, 4, 4, 4, 4, 4, 2, 2, 1};
+        int acc = 0;
+        for (int w : ramp) {
+            acc += w;
+            const int b = (int)((int64_t)n * acc / 32) / 256 * 256;
+            if (b > bounds.back() && b < n) bounds.push_back(b);
+        }
+    } else {
+        const int c8 = std::max(1 << 16, ((n + 7) / 8 + 255) / 256 * 256);
+        for (int a = c8; a < n; a += c8) bounds.push_back(a);
+    }
+    if (n > 0) bounds.push_back(n);
+    const int nch = (int)bounds.size() - 1;
     if (!r->h2d) CUDA_TRY(c, cudaStreamCreateWithFlags(&r->h2d, cudaStreamNonBlocking));
     if (!r->d2h) CUDA_TRY(c, cudaStreamCreateWithFlags(&r->d2h, cudaStreamNonBlocking));
     while ((int)r->hev.size() < 3 * nch + 1) {
@@ -1174,7 +1193,7 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
         const FieldView fv = field_view(r);
         const int it = (int)r->iteration;
         for (int j = 0; j < nch; ++j) {
-            const int a = j * chunk, m = std::min(chunk, n - a);
+            const int a = bounds[j], m = bounds[j + 1] - bounds[j];
             // in: after the previous step's copy out of this chunk (the host
             // arrays may be the same)
             if (s > 0) CUDA_TRY(c, cudaStreamWaitEvent(r->h2d, ev_out[j], 0));

@@ -65,11 +65,13 @@ def _by_device_steps(s, ps, h, nsteps, nopen):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("chunk,calls", [(7001, [5, 1, 14]), (0, [20])])
-def test_host_state_step_equals_device_steps(precision, chunk, calls):
+@pytest.mark.parametrize("npart,chunk,calls", [(50_000, 7001, [5, 1, 14]), (50_000, 0, [20]),
+                                               (1_100_000, 0, [3, 2])])
+def test_host_state_step_equals_device_steps(precision, npart, chunk, calls):
+    """chunk 0 at 1.1e6 particles: the ramp of chunk sizes"""
     from test_gpu_mixed import keps_case
     from cylag_gb300 import _lib
-    case, p = keps_case(50_000)
+    case, p = keps_case(npart)
     sa, pa = _solver(case, p, precision, 4)
     sb, pb = _solver(case, p, precision, 4)
     ha = _pinned(pa, KEYS)
