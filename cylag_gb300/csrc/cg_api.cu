@@ -267,11 +267,12 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
 // allocates the planned scratch into r (r->queue and r->sortbuf must be empty)
 static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
     int rc;
+    r->use_queue = false;
+    r->sb = SortBuffers{};
+    r->sort_period = 0;
     if ((rc = dalloc(c, r->queue, q.queue_bytes)) || (rc = dalloc(c, r->sortbuf, q.sort_bytes)))
         return rc;
     r->use_queue = q.use_queue;
-    r->sb = SortBuffers{};
-    r->sort_period = 0;
     if (!q.use_sort) return CG_OK;
     const size_t n = q.n, D = (size_t)q.dim;
     char* b = (char*)r->sortbuf.p;
@@ -987,7 +988,11 @@ int cg_run_resize(cg_run* r, const cg_state_desc* s) {
     dfree(r->queue);
     dfree(r->sortbuf);
     int rc = take_scratch(c, r, plan);
-    if (rc) return rc;
+    if (rc) {
+        // the caller's old arrays are gone: the run keeps no particles
+        r->st = DevState{};
+        return rc;
+    }
     c->used = c->used - old_bytes + new_bytes;
     r->bytes = new_bytes;
     r->scratch_bytes = plan.queue_bytes + plan.sort_bytes;
