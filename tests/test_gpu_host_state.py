@@ -130,3 +130,52 @@ def test_host_state_statistics_sections_stranding():
     assert a_st.sum() > 0 and a_cs.sum() > 0 and len(a_sd) > 0
     for k in KEYS:
         np.testing.assert_array_equal(a_h[k], b_h[k], err_msg=k)
+
+
+@pytest.mark.parametrize("model", [2, 3])
+def test_host_state_lsm23_3d(model):
+    """3D LSM2/LSM3 with the velocity (and fluid velocity seen) and layer
+    index kept in host memory: equal to the device-state steps."""
+    import cylag_gb300 as cg
+    import torch
+    from cylag_gb300 import _lib, synth
+    from cylag_gb300.mesh import TriangularMesh
+    mk = synth.lsm2_loglaw_workload if model == 2 else synth.lsm3_taylor_green_workload
+    c = mk(npart=20000, nx=81, ny=41, nplanes=11, seed=2)
+    p = dict(c["parameters"], final_time=1e6)
+    keys = ["position", "tri", "tag", "rng_state", "lowerlayer", "velocity"]
+    if model == 3:
+        keys.append("fluid_velocity_seen")
+    res = []
+    for mode in ("device", "host"):
+        mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+        fs = cg.EulerianFieldSet(mesh, dim=3, nlayers=c["nlayers"], times=c["times"],
+                                 elevation=c["elevation"], velocity_x=c["velocity_x"],
+                                 velocity_y=c["velocity_y"], velocity_z=c["velocity_z"],
+                                 opt_fields=c.get("opt_fields"),
+                                 opt_fields_names=c.get("opt_fields_names"))
+        ps = cg.LagrangianParticleSet(c["position"], dim=3, **c.get("pset", {}))
+        if "diameter" in c:
+            ps.diameter = c["diameter"]
+        s = cg.Solver(fs, ps, p, precision="mixed", seed=5, sort_period=0)
+        d = ps._dev
+        h = {k: torch.empty_like(d[k], device="cpu").pin_memory() for k in keys}
+        for k in keys:
+            h[k].copy_(d[k])
+        for _ in range(12):
+            if mode == "device":
+                for k in keys:
+                    d[k].copy_(h[k])
+                torch.cuda.synchronize()
+                _lib.check(s._ctx, s.L.cg_run_step(s._run, 1, None))
+                for k in keys:
+                    h[k].copy_(d[k])
+                torch.cuda.synchronize()
+            else:
+                arr = _arrays(h)
+                _lib.check(s._ctx, s.L.cg_run_step_host(s._run, 1, C.byref(arr), C.byref(arr),
+                                                        3001, None))
+        res.append({k: h[k].numpy().copy() for k in keys})
+        s.close()
+    for k in keys:
+        np.testing.assert_array_equal(res[0][k], res[1][k], err_msg=k)
