@@ -152,28 +152,58 @@ __device__ __forceinline__ int decide32(const Bary& b) {
     return -1;
 }
 
-// one_hop for a split end position: the neighbour's record with its split
-// vertex, so that the test stays in FP32 outside the band
-__device__ __forceinline__ int one_hop_split(const DevMesh& m, int tri0, const Bary& bs,
-                                            const Bary& be, float4 pn) {
-    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
-    const bool n0 = be.l0 < -be.e0, n1 = be.l1 < -be.e1, n2 = be.l2 < -be.e2;
-    const bool p0 = be.l0 > be.e0, p1 = be.l1 > be.e1, p2 = be.l2 > be.e2;
-    int j;
-    if (n0 && p1 && p2) j = 0;
-    else if (n1 && p0 && p2) j = 1;
-    else if (n2 && p0 && p1) j = 2;
-    else return -1;
-    int4 nb = __ldg(&m.nbr[tri0]);
-    int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
-    if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
-    const Tri32S tn = load_tri32s(m, kn);
-    const float2 r = split_offset(tn, pn);
-    const int d = decide32(bary32_off(tn, r.x, r.y));
-    if (d >= 0) return d ? kn : -1;
-    const double2 x = join_pos(pn);
-    return in_tri(m, kn, x.x, x.y) ? kn : -1;
+// index of the one edge (opposite vertex j) that the point is certainly
+// beyond while certainly inside the other two; -1 otherwise
+__device__ __forceinline__ int single_exit(const Bary& b) {
+    const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
+    const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
+    if (n0 && p1 && p2) return 0;
+    if (n1 && p0 && p2) return 1;
+    if (n2 && p0 && p1) return 2;
+    return -1;
 }
+
+// The walk's first hops for a split end position, decided in FP32 where the
+// signs are certain.  From the start triangle (start point certainly
+// inside) the segment crosses exactly the edge the end point is certainly
+// beyond, as one_hop argues; in each triangle entered, a straight segment
+// that came in through one edge and ends certainly beyond exactly one other
+// edge (and certainly inside the third's half-plane) leaves through that
+// edge, the only one the reference's walk finds there
+// (xylocalizer.pyx:375-415).  After each crossing the walk's test of the end
+// point in the new triangle is made here (exact in the rounding band).
+// Returns the triangle holding the end point within HOPS crossings, else -1
+// (the walk kernel decides: more hops, boundary edges, uncertain signs).
+template <int HOPS>
+__device__ __forceinline__ int hop_walk_split(const DevMesh& m, int tri0, const Bary& bs,
+                                              const Bary& be, float4 pn) {
+    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
+    int k = tri0;
+    Bary b = be;
+#pragma unroll 1
+    for (int h = 0; h < HOPS; ++h) {
+        const int j = single_exit(b);
+        if (j < 0) return -1;
+        const int4 nb = __ldg(&m.nbr[k]);
+        const int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+        if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
+        const Tri32S tn = load_tri32s(m, kn);
+        const float2 r = split_offset(tn, pn);
+        b = bary32_off(tn, r.x, r.y);
+        const int d = decide32(b);
+        if (d == 1) return kn;
+        if (d < 0) {
+            const double2 x = join_pos(pn);
+            return in_tri(m, kn, x.x, x.y) ? kn : -1;
+        }
+        k = kn;
+    }
+    return -1;
+}
+
+#ifndef MIXED_HOPS
+#define MIXED_HOPS 3
+#endif
 
 // the per-particle state the mixed LSM1 step streams in
 struct MixedIn {
@@ -333,7 +363,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                     need64();
                     d = in_tri(m, tri0, xn, yn) ? 1 : 0;
                 }
-                kn = d ? tri0 : one_hop_split(m, tri0, b0, be, xe);
+                kn = d ? tri0 : hop_walk_split<MIXED_HOPS>(m, tri0, b0, be, xe);
             } else {
                 const Bary be = euler ? bary32_moved(t0, rx0, ry0, dx, dy) : bary32(t0, xn, yn);
                 const bool inside = in_tri_decide(m, be, tri0, xn, yn);
