@@ -35,23 +35,35 @@ __device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32&
 // other two barycentric coordinates certainly positive at both points), the
 // segment crosses that edge alone, in its interior: the first edge the
 // reference's path walk finds (xylocalizer.pyx:375-415).  The walk's next
-// test, the point in the neighbour across it, is made here.  Returns the
-// neighbour when the end point is in it, else -1 (the walk kernel decides).
+// test, the point in the neighbour across it, is made here, and so are up
+// to two further crossings of the same kind (see hop_walk_split).  Returns
+// the triangle holding the end point, else -1 (the walk kernel decides).
 __device__ __forceinline__ int one_hop(const DevMesh& m, int tri0, const Bary& bs, const Bary& be,
                                        double xn, double yn) {
     if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
-    const bool n0 = be.l0 < -be.e0, n1 = be.l1 < -be.e1, n2 = be.l2 < -be.e2;
-    const bool p0 = be.l0 > be.e0, p1 = be.l1 > be.e1, p2 = be.l2 > be.e2;
-    int j;
-    if (n0 && p1 && p2) j = 0;
-    else if (n1 && p0 && p2) j = 1;
-    else if (n2 && p0 && p1) j = 2;
-    else return -1;
-    int4 nb = __ldg(&m.nbr[tri0]);
-    int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
-    if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
-    Tri32 tn = load_tri32(m, kn);
-    return in_tri_mixed(m, tn, kn, xn, yn) ? kn : -1;
+    int k = tri0;
+    Bary b = be;
+    // further crossings as hop_walk_split argues (up to three in all)
+#pragma unroll 1
+    for (int h = 0; h < 3; ++h) {
+        const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
+        const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
+        int j;
+        if (n0 && p1 && p2) j = 0;
+        else if (n1 && p0 && p2) j = 1;
+        else if (n2 && p0 && p1) j = 2;
+        else return -1;
+        int4 nb = __ldg(&m.nbr[k]);
+        int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+        if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
+        Tri32 tn = load_tri32(m, kn);
+        b = bary32(tn, xn, yn);
+        if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return kn;
+        if (!(b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2))   // rounding band
+            return in_tri(m, kn, xn, yn) ? kn : -1;
+        k = kn;
+    }
+    return -1;
 }
 
 // FP32 P1 interpolation of the packed node record {ux, uy, K, zs}
