@@ -30,12 +30,13 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
     DevFields<float> f = fv.as<float>();
     WalkQueue none{nullptr, nullptr};
     if (fv.dim == 2) {
-        // occupancy variant: 3 blocks/SM (80 registers) by default; 2 (128)
-        // or 4 (64) on request
-        static int minb = [] {
+        // occupancy variant (resident blocks of 256 per SM): by default 4 (64
+        // registers) for the Euler-with-queue form, which has no out-of-line
+        // calls, and 3 (80) for the others; 2, 3 or 4 on request
+        static int minb_env = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
-            int v = e ? atoi(e) : 3;
-            return (v == 2 || v == 4) ? v : 3;
+            int v = e ? atoi(e) : 0;
+            return (v == 2 || v == 3 || v == 4) ? v : 0;
         }();
         // persistent grid: one wave of resident blocks
         static int w2 = wave(step_mixed2d_kernel<2>, bs), w3 = wave(step_mixed2d_kernel<3>, bs),
@@ -64,36 +65,64 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         auto a16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
         const bool staged = stage_on && s.n >= 32 && a16(s.pos) && a16(s.rng) && a16(s.tri) &&
                             a16(s.tag);
+        // EQ: the Euler scheme with a walk queue, no out-of-line calls
+        const bool eq = p.time_scheme == 1 && wq.e != nullptr;
+        const int minb = minb_env ? minb_env : (eq ? 4 : 3);
+        static int w2e = wave(step_mixed2d_kernel<2, false, false, false, true>, bs),
+                   w3e = wave(step_mixed2d_kernel<3, false, false, false, true>, bs),
+                   w4e = wave(step_mixed2d_kernel<4, false, false, false, true>, bs),
+                   w2se = wave(step_mixed2d_kernel<2, true, false, false, true>, bs),
+                   w3se = wave(step_mixed2d_kernel<3, true, false, false, true>, bs),
+                   w4se = wave(step_mixed2d_kernel<4, true, false, false, true>, bs);
+        auto grid = [nb](int w) { return nb < w ? nb : w; };
         if ((s.work & W_SPLIT) && staged && stage_minb == 4)   // per-thread cp.async prefetch
-            step_mixed2d_kernel<3, true, true, true><<<nb < w3sa ? nb : w3sa, bs, 0, st>>>(
+            step_mixed2d_kernel<3, true, true, true><<<grid(w3sa), bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && staged && stage_minb == 2)
-            step_mixed2d_kernel<2, true, true><<<nb < w2st ? nb : w2st, bs, 0, st>>>(
+            step_mixed2d_kernel<2, true, true><<<grid(w2st), bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && staged)
-            step_mixed2d_kernel<3, true, true><<<nb < w3st ? nb : w3st, bs, 0, st>>>(
+            step_mixed2d_kernel<3, true, true><<<grid(w3st), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && eq && minb == 2)
+            step_mixed2d_kernel<2, true, false, false, true><<<grid(w2se), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && eq && minb == 4)
+            step_mixed2d_kernel<4, true, false, false, true><<<grid(w4se), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if ((s.work & W_SPLIT) && eq)
+            step_mixed2d_kernel<3, true, false, false, true><<<grid(w3se), bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && minb == 2)
-            step_mixed2d_kernel<2, true><<<nb < w2s ? nb : w2s, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                           step_index, stats, err);
+            step_mixed2d_kernel<2, true><<<grid(w2s), bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                  step_index, stats, err);
         else if ((s.work & W_SPLIT) && minb == 4)
-            step_mixed2d_kernel<4, true><<<nb < w4s ? nb : w4s, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                           step_index, stats, err);
+            step_mixed2d_kernel<4, true><<<grid(w4s), bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                  step_index, stats, err);
         else if (s.work & W_SPLIT)   // sorted working copies with split positions
-            step_mixed2d_kernel<3, true><<<nb < w3s ? nb : w3s, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                           step_index, stats, err);
+            step_mixed2d_kernel<3, true><<<grid(w3s), bs, 0, st>>>(m, f, p, s, wq, aux,
+                                                                  step_index, stats, err);
         else if (staged && minb == 3)
-            step_mixed2d_kernel<3, false, true><<<nb < w3t ? nb : w3t, bs, 0, st>>>(
+            step_mixed2d_kernel<3, false, true><<<grid(w3t), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if (eq && minb == 2)
+            step_mixed2d_kernel<2, false, false, false, true><<<grid(w2e), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if (eq && minb == 3)
+            step_mixed2d_kernel<3, false, false, false, true><<<grid(w3e), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
+        else if (eq)
+            step_mixed2d_kernel<4, false, false, false, true><<<grid(w4e), bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if (minb == 3)
-            step_mixed2d_kernel<3><<<nb < w3 ? nb : w3, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                   step_index, stats, err);
+            step_mixed2d_kernel<3><<<grid(w3), bs, 0, st>>>(m, f, p, s, wq, aux, step_index,
+                                                           stats, err);
         else if (minb == 2)
-            step_mixed2d_kernel<2><<<nb < w2 ? nb : w2, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                   step_index, stats, err);
+            step_mixed2d_kernel<2><<<grid(w2), bs, 0, st>>>(m, f, p, s, wq, aux, step_index,
+                                                           stats, err);
         else
-            step_mixed2d_kernel<4><<<nb < w4 ? nb : w4, bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                   step_index, stats, err);
+            step_mixed2d_kernel<4><<<grid(w4), bs, 0, st>>>(m, f, p, s, wq, aux, step_index,
+                                                           stats, err);
     } else {
         // 3D: FP32 node records, FP64 arithmetic
         launch_lsm1_kernel<3, float>(m, f, p, s, none, aux, step_index, stats, err, st);

@@ -87,11 +87,19 @@ __device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, 
 
 // Runge-Kutta stages of update_state_lsm1.pyx:179-656 in the mixed form:
 // each stage point is localized from (tri0, x0); a stage leaving the domain
-// stops the scheme with an Euler step.  Kept out of line (cold path).
-static __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __restrict__ cur,
-                                      const DevParams& p, const Tri32& t0, int tri0, double2 x0,
-                                      float ux, float uy, double& xn, double& yn, int& tri,
-                                      int& bnd_j) {
+// stops the scheme with an Euler step.  Kept out of line (cold path); the
+// particle's values go in and out by value, so none of the caller's locals
+// takes an address (they stay in registers).
+struct RkOut {
+    double xn, yn;
+    int tri, bnd;
+};
+
+static __device__ __noinline__ RkOut rk_mixed(const DevMesh& m, const float4* __restrict__ cur,
+                                              const DevParams& p, int tri0, double x0x,
+                                              double x0y, float ux, float uy) {
+    const Tri32 t0 = load_tri32(m, tri0);
+    RkOut o{x0x, x0y, tri0, -1};
     const float dt = p.dt32;
     const float up0 = ux, up1 = uy;
     const int ns = p.time_scheme == 2 ? 1 : (p.time_scheme == 3 ? 2 : 3);
@@ -105,15 +113,15 @@ static __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __r
         else cst = st < 2 ? 0.5f : 1.f;
         float fx = (p.time_scheme == 2) ? 0.5f * ux * dt : cst * kx[st];
         float fy = (p.time_scheme == 2) ? 0.5f * uy * dt : cst * ky[st];
-        double xt = x0.x + (double)fx, yt = x0.y + (double)fy;
+        double xt = x0x + (double)fx, yt = x0y + (double)fy;
         int tt, bnd;
-        xy_localize_mixed(m, t0, tri0, x0.x, x0.y, xt, yt, tt, bnd);
+        xy_localize_mixed(m, t0, tri0, x0x, x0y, xt, yt, tt, bnd);
         if (bnd != -1) {
-            tri = tt;
-            xn = x0.x + (double)(up0 * dt);
-            yn = x0.y + (double)(up1 * dt);
-            bnd_j = bnd;
-            return;
+            o.tri = tt;
+            o.xn = x0x + (double)(up0 * dt);
+            o.yn = x0y + (double)(up1 * dt);
+            o.bnd = bnd;
+            return o;
         }
         Tri32 ts = load_tri32(m, tt);
         Node4 ns4 = load_nodes(cur, ts);
@@ -126,34 +134,48 @@ static __device__ __noinline__ void rk_mixed(const DevMesh& m, const float4* __r
     if (p.time_scheme == 2) { dxs = kx[1]; dys = ky[1]; }
     else if (p.time_scheme == 3) { dxs = 0.25f * kx[0] + 0.75f * kx[2]; dys = 0.25f * ky[0] + 0.75f * ky[2]; }
     else { dxs = (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) / 6.f; dys = (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) / 6.f; }
-    xn += (double)dxs;
-    yn += (double)dys;
+    o.xn += (double)dxs;
+    o.yn += (double)dys;
+    return o;
 }
 
 // Boundary conditions (compute_bc.pyx:35-395) with the FP64 mirror and the
-// exact walk of the plain form.  Out of line (cold path).
-static __device__ __noinline__ void bc_mixed(const DevMesh& m, const DevFields<float>& f,
-                                      const DevParams& p, const ZigTables& z64, Rng& rng,
-                                      double2 x0, float up0, float up1, int tri0, int ltri,
-                                      int bnd_j, int* stats, double& xn, double& yn, int& tri,
-                                      bool& deleted, int pidx, int pstep) {
+// exact walk of the plain form.  Out of line (cold path), values in and out.
+struct BcOut {
+    double xn, yn;
+    uint64_t rng;
+    uint32_t err;
+    int tri;
+    bool deleted;
+};
+
+static __device__ __noinline__ BcOut bc_mixed(const DevMesh& m, const DevFields<float>& f,
+                                              const DevParams& p, const ZigTables& z64,
+                                              uint64_t rng_state, uint64_t rng_inc, double x0x,
+                                              double x0y, float up0, float up1, int tri0, int ltri,
+                                              int bnd_j, int* stats, double xn, double yn, int tri,
+                                              int pidx, int pstep) {
     Particle<2, float> q(m, f, p, z64);
     q.pidx = pidx;
     q.pstep = pstep;
-    q.rng = rng;
+    q.rng.state = rng_state;
+    q.rng.inc = rng_inc;
+    q.rng.err = 0;
     q.x[0] = xn; q.x[1] = yn;
-    q.x0[0] = x0.x; q.x0[1] = x0.y;
+    q.x0[0] = x0x; q.x0[1] = x0y;
     q.up[0] = up0; q.up[1] = up1;
     q.us[0] = up0; q.us[1] = up1;
     q.tri = tri; q.tri0 = tri0; q.ltri = ltri; q.ll = 0; q.ll0 = 0;
     if (p.bc_on) q.compute_bc(bnd_j, stats);
     else if (q.tri == PART_LOC_O) q.deleted = true;
-    rng = q.rng;
-    rng.err |= q.err;
-    xn = q.x[0];
-    yn = q.x[1];
-    tri = q.tri;
-    deleted = q.deleted;
+    BcOut o;
+    o.rng = q.rng.state;
+    o.err = q.rng.err | q.err;
+    o.xn = q.x[0];
+    o.yn = q.x[1];
+    o.tri = q.tri;
+    o.deleted = q.deleted;
+    return o;
 }
 
 // in-element decision from FP32 barycentrics: 1 certainly inside, 0
@@ -244,7 +266,10 @@ __device__ __forceinline__ double2 double2_from_bits(float4 r) {
 // SPLIT: the working position is a split pair (W_SPLIT); the Euler step then
 // runs without FP64 arithmetic outside the rounding bands, the walk and the
 // boundary conditions (which work on its FP64 value).
-template <bool SPLIT>
+// EQ: the Euler scheme with a walk queue (the caller guarantees both): every
+// particle that does not end in a triangle reached here goes to the queue,
+// so this form has no out-of-line calls and no deletions.
+template <bool SPLIT, bool EQ = false>
 __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
                                                     const DevParams& p, DevState& s,
                                                     const WalkQueue& wq, int aux, int step_index,
@@ -268,7 +293,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
 
     const float dt = p.dt32;
-    const bool euler = p.time_scheme == 1;
+    const bool euler = EQ || p.time_scheme == 1;
     // start record and offset to its vertex a
     Tri32 t0;
     Tri32S t0s;
@@ -282,10 +307,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         ry0 = r.y;
         n0 = load_nodes(cur, t0s);
         b0 = bary32_off(t0s, rx0, ry0);
-        if (!euler) {   // the Runge-Kutta stages work on the FP64 value
-            x0 = join_pos(xs);
-            t0 = load_tri32(m, tri0);
-        }
+        if (!euler) x0 = join_pos(xs);   // the Runge-Kutta stages work on the FP64 value
     } else {
         t0 = load_tri32(m, tri0);
         rx0 = (float)(x0.x - t0.a.x);
@@ -304,8 +326,12 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (euler) {
         dx = ux * dt;
         dy = uy * dt;
-    } else {
-        rk_mixed(m, cur, p, t0, tri0, x0, ux, uy, xn, yn, tri, bnd_j);
+    } else if constexpr (!EQ) {
+        const RkOut r = rk_mixed(m, cur, p, tri0, x0.x, x0.y, ux, uy);
+        xn = r.xn;
+        yn = r.yn;
+        tri = r.tri;
+        bnd_j = r.bnd;
     }
 
     // diffusion (update_state_lsm1.pyx:658-726), K at the start point
@@ -360,7 +386,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
     if (bnd_j == -1) {
         ltri = tri0;
-        if (wq.e != nullptr) {
+        if (EQ || wq.e != nullptr) {
             // leaves the start triangle: one hop here, else walk + boundary
             // conditions in walk_kernel
             int kn;
@@ -403,10 +429,17 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     }
 
     bool deleted = false;
-    if (bnd_j != -1 || tri == PART_LOC_O) {
+    if (!EQ && (bnd_j != -1 || tri == PART_LOC_O)) {
         need64();
-        bc_mixed(m, f, p, g_zig, rng, x0, up0, up1, tri0, ltri, bnd_j, stats, xn, yn, tri, deleted,
-                 aux_index(s, i) + s.base, step_index);
+        const BcOut o = bc_mixed(m, f, p, g_zig, rng.state, rng.inc, x0.x, x0.y, up0, up1, tri0,
+                                 ltri, bnd_j, stats, xn, yn, tri, aux_index(s, i) + s.base,
+                                 step_index);
+        rng.state = o.rng;
+        rng.err |= o.err;
+        xn = o.xn;
+        yn = o.yn;
+        tri = o.tri;
+        deleted = o.deleted;
         if constexpr (SPLIT) xe = split_pos(xn, yn);
     }
     if (rng.err) atomicOr(err_word, rng.err);
@@ -455,7 +488,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 // staged in shared memory one tile ahead (cg_stage.cuh); the tail of fewer
 // than 32 particles is read directly.  The state arrays must be 16-byte
 // aligned (checked on the host).
-template <int MINB, bool SPLIT = false, bool STAGED = false, bool ASYNC = false>
+template <int MINB, bool SPLIT = false, bool STAGED = false, bool ASYNC = false, bool EQ = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -471,7 +504,7 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     if constexpr (!STAGED) {
         __syncthreads();
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
+            step_mixed_particle<SPLIT, EQ>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
                                        load_mixed_in(s, i), i);
     } else if constexpr (ASYNC) {
         // per-thread cp.async prefetch of the next particle's state
