@@ -878,4 +878,21 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
     bnd = -1;
 }
 
+// xy_localize (xylocalizer.pyx:27-124, method 3) with the FP32-filtered
+// in-element and walk tests of the mixed form: the same decisions, with the
+// FP64 arithmetic only inside the rounding bands.  A start index below 0 (a
+// Runge-Kutta stage that left the mesh) takes the plain path.
+__device__ inline void xy_localize_filtered(const DevMesh& m, int k, double p0x, double p0y,
+                                            double x, double y, int& new_k, int& bnd) {
+    if (k < 0) {
+        xy_localize(m, k, p0x, p0y, x, y, new_k, bnd);
+        return;
+    }
+    bnd = -1;
+    const Tri32 t = load_tri32(m, k);
+    if (in_tri_mixed(m, t, k, x, y)) { new_k = k; return; }
+    path_walk_mixed(m, k, p0x, p0y, x, y, new_k, bnd);
+    if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
+}
+
 }  // namespace cg

@@ -133,13 +133,15 @@ void launch_walk_plain(const DevMesh& m, const FieldView& fv, const DevParams& p
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
                        int* stats, uint32_t* err, cudaStream_t st) {
     // grid-stride over the (device-side) entry count: a fixed grid of
-    // 8 blocks per SM covers any count without a host round trip
+    // 32 blocks of 64 per SM covers any count without a host round trip;
+    // small blocks spread a short queue (a few thousand boundary and
+    // multi-hop entries) over every SM instead of a few dozen
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    int nb = nsm * 8;
     DevFields<double> f = fv.as<double>();
-    walk_kernel<double, false><<<nb, 256, 0, st>>>(m, f, p, s, wq, aux, step_index, stats, err);
+    walk_kernel<double, false><<<nsm * WALK_BLOCKS_PER_SM, WALK_BLOCK, 0, st>>>(
+        m, f, p, s, wq, aux, step_index, stats, err);
 }
 
 // ---------------------------------------------------------------------------

@@ -100,17 +100,8 @@ __device__ __forceinline__ void mean_fields(Particle<DIM, FT>& q, int k, int l, 
 template <int DIM, typename FT>
 __device__ __forceinline__ void localize(Particle<DIM, FT>& q, int k, double p0x, double p0y,
                                          double x, double y, int& nk, int& bnd) {
-    if constexpr (is_mixed<FT>()) {
-        if (k >= 0) {
-            bnd = -1;
-            Tri32 t = load_tri32(q.m, k);
-            if (in_tri_mixed(q.m, t, k, x, y)) { nk = k; return; }
-            path_walk_mixed(q.m, k, p0x, p0y, x, y, nk, bnd);
-            if (nk == -1 && bnd == -1) nk = grid_locate(q.m, x, y);
-            return;
-        }
-    }
-    xy_localize(q.m, k, p0x, p0y, x, y, nk, bnd);
+    if constexpr (is_mixed<FT>()) xy_localize_filtered(q.m, k, p0x, p0y, x, y, nk, bnd);
+    else xy_localize(q.m, k, p0x, p0y, x, y, nk, bnd);
 }
 
 template <int DIM, typename FT>

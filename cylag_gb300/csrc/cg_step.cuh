@@ -671,7 +671,12 @@ struct Particle {
                     double py = x[1] - 2. * ((dist * coef) / norm2) * ny;
                     x[0] = px;
                     x[1] = py;
-                    xy_localize(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
+                    // the mixed form's filtered tests: same decisions, FP64
+                    // only inside the rounding bands
+                    if constexpr (std::is_same<FT, float>::value)
+                        xy_localize_filtered(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
+                    else
+                        xy_localize(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
                     if (tri == PART_LOC_O && bnd_jj != -1) {
                         int lj = __ldg(&m.elabel[bnd_jj]);
                         if (lj >= BND_OPEN_REF) {
@@ -899,11 +904,14 @@ void launch_lsm23_kernel(const DevMesh& m, const DevFields<FT>& f, const DevPara
     else go(step_kernel<DIM, FT, 3, 5>, 6);
 }
 
+// walk kernel launch shape: blocks of 64, 32 per SM (grid-stride beyond)
+constexpr int WALK_BLOCK = 64, WALK_BLOCKS_PER_SM = 32;
+
 // Second half of the step for queued (2D) particles: path walk from the
 // start triangle (xylocalizer.pyx:338-435, then the global fallback) and the
 // boundary conditions.  Grid-stride over the entries of this step.
 template <typename FT, bool MIXED>
-__global__ void __launch_bounds__(256) walk_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+__global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<FT> f, DevParams p,
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
