@@ -50,7 +50,10 @@ WORKLOADS = {
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 1000 for lsm1_2d, one call over half of its "
+                         "2,000-step horizon, so that warm-up, timed and end-to-end steps stay "
+                         "within its field records; 100 for the others)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["both", "fp64", "mixed"], default="both")
@@ -68,7 +71,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=0,
                     help="particles per copy/step chunk of the end-to-end steps (0: about n/8)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 1000 if args.workload == "lsm1_2d" else 100
+    return args
 
 
 _T0 = time.perf_counter()

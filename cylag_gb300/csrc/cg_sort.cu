@@ -33,10 +33,15 @@ __device__ __forceinline__ int sort_key(int tri, int layer, int nt, int nl) {
     return tri * nl + l;
 }
 
+// Keys of neighbouring particles mostly agree (the particles are sorted but
+// for the last period's moves): the lanes of a warp with the same key add
+// their count with one atomic.
 __global__ void hist_kernel(const int* __restrict__ tri, const int* __restrict__ layer, int n,
                             int nt, int nl, int* __restrict__ count) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&count[sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl)], 1);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int key = i < n ? sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&count[key], __popc(peers));
 }
 
 // inclusive warp scan
@@ -118,10 +123,16 @@ __global__ void add_carry_kernel(int* __restrict__ v, int n, const int* __restri
 __global__ void scatter_index_kernel(const int* __restrict__ tri, const int* __restrict__ layer,
                                      int n, int nt, int nl, int* __restrict__ offset,
                                      int* __restrict__ perm) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        perm[atomicAdd(&offset[sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl)],
-                       1)] = i;
+    // one atomic per key and warp; the lanes of a key keep their order
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int key = i < n ? sort_key(__ldg(&tri[i]), layer ? __ldg(&layer[i]) : 0, nt, nl) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&offset[key], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key >= 0) perm[base + __popc(peers & ((1u << lane) - 1u))] = i;
 }
 
 template <typename T>
