@@ -671,9 +671,10 @@ struct Particle {
                     double py = x[1] - 2. * ((dist * coef) / norm2) * ny;
                     x[0] = px;
                     x[1] = py;
-                    // the mixed form's filtered tests: same decisions, FP64
-                    // only inside the rounding bands
-                    if constexpr (std::is_same<FT, float>::value)
+                    // the mixed form's filtered tests (same decisions, FP64
+                    // only inside the rounding bands); 2D only: in the 3D
+                    // kernels they cost more registers than they save
+                    if constexpr (std::is_same<FT, float>::value && DIM == 2)
                         xy_localize_filtered(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
                     else
                         xy_localize(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
