@@ -462,7 +462,9 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         t64[4 * k + 2] = gi0;
         t64[4 * k + 3] = gi1;
     }
-    // the same records with vertex a as FP32 pairs hi + lo
+    // the same records with vertex a as FP32 pairs hi + lo, and the
+    // neighbour across each edge in place of the edge ids (the split step's
+    // hops read them from the record they already hold)
     std::vector<int4> t64s(t64);
     for (int k = 0; k < nt; ++k) {
         const int32_t* t = d->triangles + 3 * k;
@@ -473,6 +475,9 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         q[2] = (float)(xa - (double)q[0]);
         q[3] = (float)(ya - (double)q[1]);
         memcpy(&t64s[4 * k + 1], q, 16);
+        t64s[4 * k].w = nbr[k].x;
+        t64s[4 * k + 3].z = nbr[k].y;
+        t64s[4 * k + 3].w = nbr[k].z;
     }
     std::vector<int4> edge(ne);
     std::vector<int> lab(ne);

@@ -58,7 +58,8 @@ struct DevMesh {
     // {v0, v1, v2, e0} | {xa, ya} (FP64) | {gx0, gx1, gx2, gy0} | {gy1, gy2, e1, e2}
     const int4* __restrict__ t64;
     // [4*nt] the same with {xa_hi, ya_hi, xa_lo, ya_lo} (FP32 pairs) as the
-    // second quarter (split working positions)
+    // second quarter and the three neighbours in place of the edge ids
+    // (split working positions, Tri32S)
     const int4* __restrict__ t64s;
     const int4* __restrict__ tv;        // [2*nt]: {v0,v1,v2,e0}, {e1,e2,-,-}
     const double2* __restrict__ basis;  // [5*nt]: det0..2, gx0..2, gy0..2, pad
@@ -731,13 +732,19 @@ struct Tri32 {
 };
 
 // the same record with vertex a as a split pair {xa_hi, ya_hi, xa_lo, ya_lo}
-// (DevMesh::t64s), for split working positions
+// (DevMesh::t64s), for split working positions; in place of the edge ids it
+// holds the triangles across the edges opposite vertices 0, 1, 2 (DevMesh::nbr):
+// tv.w, g1.z, g1.w (as int bits)
 struct Tri32S {
     int4 tv;
     float4 as;
     float4 g0;
     float4 g1;
 };
+
+__device__ __forceinline__ int tri32s_nbr(const Tri32S& t, int j) {
+    return j == 0 ? t.tv.w : (j == 1 ? __float_as_int(t.g1.z) : __float_as_int(t.g1.w));
+}
 
 __device__ __forceinline__ Tri32S load_tri32s(const DevMesh& m, int k) {
     Tri32S t;

@@ -209,17 +209,17 @@ __device__ __forceinline__ int single_exit(const Bary& b) {
 // Returns the triangle holding the end point within HOPS crossings, else -1
 // (the walk kernel decides: more hops, boundary edges, uncertain signs).
 template <int HOPS>
-__device__ __forceinline__ int hop_walk_split(const DevMesh& m, int tri0, const Bary& bs,
+__device__ __forceinline__ int hop_walk_split(const DevMesh& m, const Tri32S& t0, const Bary& bs,
                                               const Bary& be, float4 pn) {
     if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
-    int k = tri0;
+    // neighbours of the current triangle, from its record
+    int n0 = t0.tv.w, n1 = __float_as_int(t0.g1.z), n2 = __float_as_int(t0.g1.w);
     Bary b = be;
 #pragma unroll 1
     for (int h = 0; h < HOPS; ++h) {
         const int j = single_exit(b);
         if (j < 0) return -1;
-        const int4 nb = __ldg(&m.nbr[k]);
-        const int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+        const int kn = j == 0 ? n0 : (j == 1 ? n1 : n2);
         if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
         const Tri32S tn = load_tri32s(m, kn);
         const float2 r = split_offset(tn, pn);
@@ -230,7 +230,9 @@ __device__ __forceinline__ int hop_walk_split(const DevMesh& m, int tri0, const 
             const double2 x = join_pos(pn);
             return in_tri(m, kn, x.x, x.y) ? kn : -1;
         }
-        k = kn;
+        n0 = tn.tv.w;
+        n1 = __float_as_int(tn.g1.z);
+        n2 = __float_as_int(tn.g1.w);
     }
     return -1;
 }
@@ -401,7 +403,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                     need64();
                     d = in_tri(m, tri0, xn, yn) ? 1 : 0;
                 }
-                kn = d ? tri0 : hop_walk_split<MIXED_HOPS>(m, tri0, b0, be, xe);
+                kn = d ? tri0 : hop_walk_split<MIXED_HOPS>(m, t0s, b0, be, xe);
             } else {
                 const Bary be = euler ? bary32_moved(t0, rx0, ry0, dx, dy) : bary32(t0, xn, yn);
                 const bool inside = in_tri_decide(m, be, tri0, xn, yn);
