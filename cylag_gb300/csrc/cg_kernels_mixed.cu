@@ -36,7 +36,7 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         static int minb_env = [] {
             const char* e = getenv("CYLAG_MIXED_MINB");
             int v = e ? atoi(e) : 0;
-            return (v >= 2 && v <= 5) ? v : 0;
+            return (v >= 2 && v <= 4) ? v : 0;
         }();
         // persistent grid: one wave of resident blocks
         static int w2 = wave(step_mixed2d_kernel<2>, bs), w3 = wave(step_mixed2d_kernel<3>, bs),
@@ -59,7 +59,7 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         static const int stage_minb = [] {
             const char* e = getenv("CYLAG_MIXED_STAGE");
             int v = e ? atoi(e) : 0;
-            return (v >= 2 && v <= 5) ? v : 0;
+            return (v >= 2 && v <= 4) ? v : 0;
         }();
         const bool stage_on = stage_minb != 0;
         auto a16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
@@ -73,8 +73,7 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                    w4e = wave(step_mixed2d_kernel<4, false, false, false, true>, bs),
                    w2se = wave(step_mixed2d_kernel<2, true, false, false, true>, bs),
                    w3se = wave(step_mixed2d_kernel<3, true, false, false, true>, bs),
-                   w4se = wave(step_mixed2d_kernel<4, true, false, false, true>, bs),
-                   w5se = wave(step_mixed2d_kernel<5, true, false, false, true>, bs);
+                   w4se = wave(step_mixed2d_kernel<4, true, false, false, true>, bs);
         auto grid = [nb](int w) { return nb < w ? nb : w; };
         if ((s.work & W_SPLIT) && staged && stage_minb == 4)   // per-thread cp.async prefetch
             step_mixed2d_kernel<3, true, true, true><<<grid(w3sa), bs, 0, st>>>(
@@ -87,9 +86,6 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && eq && minb == 2)
             step_mixed2d_kernel<2, true, false, false, true><<<grid(w2se), bs, 0, st>>>(
-                m, f, p, s, wq, aux, step_index, stats, err);
-        else if ((s.work & W_SPLIT) && eq && minb == 5)
-            step_mixed2d_kernel<5, true, false, false, true><<<grid(w5se), bs, 0, st>>>(
                 m, f, p, s, wq, aux, step_index, stats, err);
         else if ((s.work & W_SPLIT) && eq && minb == 4)
             step_mixed2d_kernel<4, true, false, false, true><<<grid(w4se), bs, 0, st>>>(
