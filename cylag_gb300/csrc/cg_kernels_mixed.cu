@@ -51,8 +51,10 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         // bulk-copy staging of the state tiles: 16-byte aligned arrays
         // (0: off, the default; 2 or 3: bulk copies per warp tile at 2 or 3
         // resident blocks per SM; 4: per-thread cp.async one particle ahead).
-        // Measured on the default 1e7-particle LSM1 case (kernels per step):
-        // 0.478-0.495 ms off, 0.567 ms bulk at 2 blocks/SM (no spills),
+        // Measured on the default 1e7-particle LSM1 case (kernels per step,
+        // before the call-free Euler-with-queue form, which the staged
+        // variants do not have): 0.478-0.495 ms off, 0.567 ms bulk at 2
+        // blocks/SM (no spills),
         // 0.640 ms bulk at 3 (spills), 0.521 ms per-thread cp.async: the
         // state's HBM latency is not what bounds the step, and staging costs
         // registers and instructions
