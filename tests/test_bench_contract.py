@@ -1,0 +1,33 @@
+"""bench.py's reference arm (the CPU implementation of the step on the host
+cores) prints one JSON line with the metric, unit and config of the GPU
+arm, a cpu_baseline block describing the run, and an e2e block with no
+host-device bytes.  Runs on CPU, on a small workload."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+
+def test_reference_arm_json_line():
+    env = dict(os.environ, CYLAG_REF_SAMPLE="2000")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--steps", "2", "--warmup", "1", "--npart", "5000", "--nx", "101",
+                        "--ny", "26"], capture_output=True, text=True, env=env, timeout=600,
+                       cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"].startswith("particle-steps/s")
+    assert d["unit"] == "particle-steps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1
+    assert d["config"]["workload"].startswith("lsm1_2d")
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference")
+    assert cb["cores"] >= 1 and "2000" in cb["sample"]
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
