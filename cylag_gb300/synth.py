@@ -123,24 +123,26 @@ def couette_channel(npart: int = 10_000, seed: int = 0):
 
 def keps_drift_channel(npart: int = 10_000_000, nx: int = 1001, ny: int = 251,
                        lx: float = 4000.0, ly: float = 1000.0, seed: int = 0,
-                       nsteps: int = 2000, dt: float = 0.5):
+                       nsteps: int = 2000, dt: float = 0.5, horizon: float = 1200.0):
     """LSM1 2D with diffusivity-gradient drift: 4 km x 1 km, 1001x251 jittered
     vertices (+-0.3 spacing), random diagonals (~5e5 triangles); frames A, B
     600 s apart, each a sum of 8 Fourier modes (amplitude 0.5 m/s,
     wavelengths 100-1000 m); the record sequence is A, B, A at t = 0, 600,
-    1200 s so that the 1,000 s horizon never extrapolates; K(x,y) periodic,
-    passed as nodal k-epsilon (eps = 1e-3, sigc = 0.72); particles uniform in
-    the domain; dt = 0.5 s, 2,000 steps."""
+    1200 s so that the 1,000 s horizon never extrapolates (continued A, B,
+    ... every 600 s up to `horizon` when a longer one is asked for); K(x,y)
+    periodic, passed as nodal k-epsilon (eps = 1e-3, sigc = 0.72); particles
+    uniform in the domain; dt = 0.5 s, 2,000 steps."""
     x, y, tri = channel_mesh(lx, ly, nx, ny, seed=seed, jitter=0.3)
     uA, vA = fourier_velocity(x, y, seed + 1)
     uB, vB = fourier_velocity(x, y, seed + 2)
     K = periodic_K(x, y)
     k, eps = keps_from_K(K)
-    times = np.array([0.0, 600.0, 1200.0])
-    vx = np.stack([uA, uB, uA])
-    vy = np.stack([vA, vB, vA])
-    elev = np.ones((3, len(x)))
-    opt = np.stack([np.stack([k, k, k]), np.stack([eps, eps, eps])])
+    nrec = max(3, int(np.ceil(horizon / 600.0)) + 1)
+    times = 600.0 * np.arange(nrec, dtype=np.float64)
+    vx = np.stack([uA if r % 2 == 0 else uB for r in range(nrec)])
+    vy = np.stack([vA if r % 2 == 0 else vB for r in range(nrec)])
+    elev = np.ones((nrec, len(x)))
+    opt = np.stack([np.stack([k] * nrec), np.stack([eps] * nrec)])
     pos = uniform_in_box(npart, 0.0, lx, 0.0, ly, seed=seed + 3)
     params = {"model": 1, "diffusion_model": 2, "time_scheme": 1,
               "schmidt_number": 0.72, "frozen_eulerian_fields": False,
