@@ -31,3 +31,19 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_lsm1_workload_records_cover_the_horizon():
+    """The k-eps drift workload's field records: A, B, A at 0 / 600 / 1200 s
+    by default, continued A, B, ... every 600 s for longer horizons, so that
+    warm-up, timed and end-to-end steps never extrapolate in time."""
+    import numpy as np
+    from cylag_gb300 import synth
+    a = synth.keps_drift_channel(npart=10, nx=21, ny=6, seed=0)
+    np.testing.assert_array_equal(a["times"], [0.0, 600.0, 1200.0])
+    b = synth.keps_drift_channel(npart=10, nx=21, ny=6, seed=0, horizon=3000.0)
+    np.testing.assert_array_equal(b["times"], 600.0 * np.arange(6))
+    np.testing.assert_array_equal(b["velocity_x"][:3], a["velocity_x"])
+    for r in range(6):
+        np.testing.assert_array_equal(b["velocity_x"][r], a["velocity_x"][r % 2])
+        np.testing.assert_array_equal(b["opt_fields"][:, r], a["opt_fields"][:, 0])
