@@ -185,9 +185,10 @@ class DispersionServer:
                     self.step(min(chunk, min(todo)))
                 # runs finished by earlier queues: their copies overlap these steps
                 results.extend(self.collect(done, clock))
+            elif pending:
+                # nothing runs, so nothing will free room for it
+                raise RuntimeError(f"request {pending[0].rid} does not fit in an empty pool")
             elif i < len(reqs):
-                if pending:
-                    raise RuntimeError(f"request {pending[0].rid} does not fit in an empty pool")
                 time.sleep(max(0.0, min(reqs[i].arrival - now(), 0.05)))
             if log and results and len(results) % 50 == 0:
                 log(f"{len(results)} done, {len(self.runs)} active, {len(pending)} waiting")
