@@ -183,3 +183,52 @@ def test_field_set_validation():
                              opt_fields=np.ones((2, 1, nv)),
                              opt_fields_names=["DISSIPATION", "TURBULENT ENERG."])
     assert fs.fid_dissip == 4 and fs.fid_turbeng == 5
+
+
+# ---------------------------------------------------------------------------
+# host helpers of the step: retagging, record search, error reports
+# ---------------------------------------------------------------------------
+def test_retag_follows_deletion_order():
+    """Markers -1 (deleted at initialization, before the call's steps) and
+    -2-it (deleted in iteration it) become maxtag+1, ... in deletion order,
+    index order within one iteration (lagrangian_particle_set.pyx:786-788)."""
+    from cylag_gb300.core import retag
+    tag = np.array([0, -7, 2, -2, -1, 5, -2, -7, -1], dtype=np.int32)
+    got, mx = retag(tag, 10)
+    #             init (-1): idx 4, 8 -> 11, 12; it 0 (-2): idx 3, 6 -> 13, 14;
+    #             it 5 (-7): idx 1, 7 -> 15, 16
+    np.testing.assert_array_equal(got, [0, 15, 2, 13, 11, 5, 14, 16, 12])
+    assert mx == 16
+    same, mx2 = retag(np.array([3, 4], np.int32), 4)
+    np.testing.assert_array_equal(same, [3, 4])
+    assert mx2 == 4
+
+
+def test_lower_index_intervals():
+    """zlocalizer.pyx:125-151: the record interval holding a time."""
+    from cylag_gb300.core import lower_index
+    t = np.array([0.0, 600.0, 1200.0, 1800.0])
+    assert lower_index(t, -5.0) == 0
+    assert lower_index(t, 0.0) == 0
+    assert lower_index(t, 599.9) == 0
+    assert lower_index(t, 600.0) == 1
+    assert lower_index(t, 1799.0, last=1) == 2
+    assert lower_index(t, 1800.0) == 2 and lower_index(t, 5000.0) == 2
+    assert lower_index(np.array([0.0]), 10.0) == 0
+
+
+def test_error_reports_known_answers():
+    from cylag_gb300.stats import diffusion_report, displacement_report
+    x0 = np.zeros((4, 2))
+    xb = np.array([[1.0, 0.0], [-1.0, 0.0], [0.0, 2.0], [0.0, -2.0]])
+    xa = xb * 1.1
+    rep = displacement_report(x0, xa, xb)
+    assert rep["n"] == 4
+    np.testing.assert_allclose(rep["var_rel_err"], [0.21, 0.21])   # (1.1^2 - 1)
+    np.testing.assert_allclose(rep["mean_rel_err"], [0.0, 0.0], atol=1e-15)
+    np.testing.assert_allclose(rep["rms_displacement_diff"], np.sqrt((0.01 + 0.01 + 0.04 + 0.04) / 4))
+    rng = np.random.default_rng(1)
+    K, t, n = 0.5, 100.0, 200_000
+    x = rng.normal(0.0, np.sqrt(2 * K * t), (n, 2))
+    d = diffusion_report(np.zeros((n, 2)), x, K, t)
+    assert d["var_exact"] == 100.0 and max(abs(z) for z in d["z"]) < 5
