@@ -47,3 +47,33 @@ def test_lsm1_workload_records_cover_the_horizon():
     for r in range(6):
         np.testing.assert_array_equal(b["velocity_x"][r], a["velocity_x"][r % 2])
         np.testing.assert_array_equal(b["opt_fields"][:, r], a["opt_fields"][:, 0])
+
+
+def test_clock_record_parsing():
+    """The clocks block of a bench line: median SM clock under load, the
+    maximum, and every throttle reason seen active during the timed region."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    class Done:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    cs = bench.ClockSampler(0)
+    cs.proc = Done()
+    cs.lines = [
+        "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2055, 2070, 1350.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1320.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbled",
+        "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active",
+    ]
+    got = cs.stop()
+    assert got["sm_mhz"] == 2070.0 and got["sm_max_mhz"] == 2070.0
+    assert got["reasons"] == ["sw_power_cap"] and got["samples"] == 3
+    assert bench.ClockSampler(0).stop()["reasons"] == ["nvidia-smi unavailable"]
