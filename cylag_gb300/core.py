@@ -533,22 +533,41 @@ class LagrangianParticleSet:
 
     def delete_single(self, i):
         """lagrangian_particle_set.pyx:754-788"""
-        if self._get("tri")[i] == -1:
+        self.delete(np.array([i]))
+
+    def delete(self, particles_id):
+        """lagrangian_particle_set.pyx:712-750: deactivates the listed
+        particles that are active (an index listed twice is deleted once),
+        zeroing their state, and gives them the tags maxtag+1, maxtag+2, ...
+        in the order listed.  Particles deleted by earlier steps get their
+        tags first (they were deleted before)."""
+        ids = np.asarray(particles_id, dtype=np.int64).ravel()
+        if len(ids) == 0:
             return
+        self._retag()
+        gone = self._get("tri") == -1
+        order = []
+        for i in ids:
+            if not gone[i]:
+                gone[i] = True
+                order.append(i)
+        if not order:
+            return
+        idx = np.array(order, dtype=np.int64)
         for k in ("position", "velocity", "fluid_velocity_seen", "last_position", "last_velocity"):
             a = self._get(k)
-            a[i] = 0.
+            a[idx] = 0.
             self._set(k, a)
         for k, v in (("tri", -1), ("last_tri", -1), ("lowerlayer", 0)):
             a = self._get(k)
-            a[i] = v
+            a[idx] = v
             self._set(k, a)
         d = self._get("diameter")
-        d[i] = 0.
+        d[idx] = 0.
         self._set("diameter", d)
         t = self._get("tag")
-        self.maxtag += 1
-        t[i] = self.maxtag
+        t[idx] = self.maxtag + 1 + np.arange(len(idx), dtype=np.int32)
+        self.maxtag += len(idx)
         self._set("tag", t)
 
 

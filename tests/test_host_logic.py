@@ -232,3 +232,23 @@ def test_error_reports_known_answers():
     x = rng.normal(0.0, np.sqrt(2 * K * t), (n, 2))
     d = diffusion_report(np.zeros((n, 2)), x, K, t)
     assert d["var_exact"] == 100.0 and max(abs(z) for z in d["z"]) < 5
+
+
+def test_particle_set_delete_like_the_reference():
+    """lagrangian_particle_set.pyx:712-788: delete() deactivates the listed
+    active particles in the order listed (once each), zeroes their state and
+    retags them maxtag+1, ...; delete_single is the one-particle case."""
+    import cylag_gb300 as cg
+    pos = np.arange(12, dtype=np.float64).reshape(6, 2) + 1.0
+    ps = cg.LagrangianParticleSet(pos, dim=2)
+    assert ps.maxtag == 5 and ps.npart_active == 6
+    ps.delete(np.array([4, 1, 4, 0], dtype=np.int32))
+    np.testing.assert_array_equal(ps.tag, [8, 7, 2, 3, 6, 5])
+    assert ps.maxtag == 8 and ps.npart_active == 3
+    np.testing.assert_array_equal(ps.inactive, [1, 1, 0, 0, 1, 0])
+    assert not ps.position[[0, 1, 4]].any() and (ps.position[[2, 3, 5]] == pos[[2, 3, 5]]).all()
+    np.testing.assert_array_equal(ps.last_tri[[0, 1, 4]], -1)
+    ps.delete_single(2)
+    ps.delete_single(2)          # already inactive: nothing happens
+    ps.delete([])
+    assert ps.tag[2] == 9 and ps.maxtag == 9 and ps.npart_active == 2
