@@ -290,8 +290,11 @@ class LagrangianParticleSet:
         self.additional_velocity = False
         self.additional_force = False
         self.compute_depth = compute_depth
+        if compute_depth and dim != 3:
+            raise ValueError("compute_depth can only be True for 3D pset")
         if compute_depth:
             raise NotImplementedError("compute_depth is not built in the GPU step")
+        self.depth = None   # as the reference without compute_depth
         self.max_stranded = max_stranded if max_stranded is not None else self.npart
         self.stranded_count = 0
         self.stranded_positions = np.zeros((self.max_stranded, 3))

@@ -252,3 +252,15 @@ def test_particle_set_delete_like_the_reference():
     ps.delete_single(2)          # already inactive: nothing happens
     ps.delete([])
     assert ps.tag[2] == 9 and ps.maxtag == 9 and ps.npart_active == 2
+
+
+def test_particle_set_depth_like_the_reference():
+    """compute_depth: the reference refuses it for 2D sets (ValueError) and
+    leaves depth None without it; the 3D depth output is not built here."""
+    import cylag_gb300 as cg
+    ps = cg.LagrangianParticleSet(np.zeros((3, 2)) + 1.0, dim=2)
+    assert ps.depth is None
+    with pytest.raises(ValueError):
+        cg.LagrangianParticleSet(np.zeros((3, 2)) + 1.0, dim=2, compute_depth=True)
+    with pytest.raises(NotImplementedError):
+        cg.LagrangianParticleSet(np.zeros((3, 3)) + 1.0, dim=3, compute_depth=True)
