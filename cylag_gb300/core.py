@@ -233,6 +233,102 @@ class EulerianFieldSet:
         else:
             self.record = 0
 
+    # ---- pre- and post-processing (eulerian_field_set.pyx:606-1886) ---------
+    def get_field_list(self):
+        """Field names and ids: the main fields, then the optional ones."""
+        names = self.field_names + list(self.opt_fields_names or [])
+        return names, list(range(len(names)))
+
+    def _field_at(self, field_id, time):
+        """A field's node values at `time` (eulerian_field_set.pyx:940-993):
+        linear in time between the records holding it, record 0 when the
+        fields are frozen.  The record is searched from the first one and
+        the set's own record is left as it is."""
+        if self.dim == 2 and field_id == 3:
+            raise ValueError("Wrong field id")
+        f = self._get_field_from_id(field_id)
+        if f is None:
+            raise ValueError(f"no field with id {field_id}")
+        if self.frozen_hydro:
+            return np.asarray(f[0], dtype=np.float64)
+        rec = lower_index(self.times, time, 0)
+        dt = self.times[rec] - self.times[rec + 1]
+        if abs(dt) < EPSILON:
+            raise ValueError(f"Time interpolation failed: duplicate times at record {rec}")
+        tf = (time - self.times[rec + 1]) / dt
+        return tf * f[rec] + (1. - tf) * f[rec + 1]
+
+    def get_field(self, field_id, time, layer=-1):
+        """eulerian_field_set.pyx:1770-1795: a field at `time`, one layer
+        (3D, layer >= 0) or all."""
+        v = self._field_at(field_id, time)
+        if self.dim == 2:
+            return v[:self.npoints]
+        if layer != -1:
+            return v[layer * self.npoints:(layer + 1) * self.npoints]
+        return v
+
+    def _locate(self, point, k):
+        if k is None:
+            k = (self.trifinder(point[0], point[1]) if self.trifinder is not None
+                 else self.triangular_mesh.find_triangle(float(point[0]), float(point[1])))
+        return int(k)
+
+    def _interp(self, values, k, point):
+        """P1 interpolation on triangle k (eulerian_field_set.pyx:994-1055);
+        in 3D between the P1 values on the layers below and above the point,
+        linear in z between their elevations (1184-1287)."""
+        m = self.triangular_mesh
+        x, y = float(point[0]), float(point[1])
+        i0, i1, i2 = (int(i) for i in m.triangles[k])
+        f = [m.det[k, j] + x * m.gradx[k, j] + y * m.grady[k, j] for j in range(3)]
+
+        def p1(v, off=0):
+            return v[off + i0] * f[0] + v[off + i1] * f[1] + v[off + i2] * f[2]
+
+        if self.dim == 2:
+            return p1(values)
+        return self._interp_z(values, p1, float(point[2]))
+
+    def _interp_z(self, values, p1, z):
+        nl, npt = self.nlayers, self.npoints
+        elev = self._elev_now
+        zb, zs = p1(elev, 0), p1(elev, (nl - 1) * npt)
+        # zlocalizer.pyx:51-71
+        ll = 0
+        if nl > 1:
+            hl = (zs - zb) / (nl - 1)
+            if hl > 0.:
+                fi = (z - zb) // hl
+                ll = 0 if not fi >= 0. else (nl - 2 if not fi <= nl - 2 else int(fi))
+        jl, ju = ll * npt, (ll + 1) * npt
+        zl, zu = p1(elev, jl), p1(elev, ju)
+        dz = zl - zu
+        if abs(dz) < EPSILON:
+            raise ValueError(f"3D interpolation failed: degenerate vertical layer {ll}")
+        return ((z - zu) / dz) * p1(values, jl) + ((zl - z) / dz) * p1(values, ju)
+
+    def interpolate_field(self, field_id, point, time, k=None):
+        """eulerian_field_set.pyx:1842-1886: a field at a point and time;
+        k, the triangle holding the point, is located when not given."""
+        values = self._field_at(field_id, time)
+        k = self._locate(point, k)
+        if k == -1:
+            raise ValueError("Failed interpolation (5), point not in triangulation")
+        if self.dim == 3:
+            self._elev_now = self._field_at(self.fid_zs, time)
+        return self._interp(values, k, point)
+
+    def interpolate_velocity(self, point, time, k=None):
+        """eulerian_field_set.pyx:1797-1840: (u, v) in 2D, (u, v, w) in 3D."""
+        k = self._locate(point, k)
+        if k == -1:
+            raise ValueError("Failed interpolation (4), point not in triangulation")
+        ids = (self.fid_ux, self.fid_uy) + ((self.fid_uz,) if self.dim == 3 else ())
+        if self.dim == 3:
+            self._elev_now = self._field_at(self.fid_zs, time)
+        return tuple(self._interp(self._field_at(i, time), k, point) for i in ids)
+
     def check_regular_layers(self, rtol=1e-3):
         """eulerian_field_set.pyx:258-294 (uniform sigma layers)."""
         nl = self.nlayers

@@ -245,3 +245,40 @@ class TriangularMesh:
         self._grid = (x0, y0, inv, nx, ny, start.astype(np.int32),
                       tid.astype(np.int32))
         return self._grid
+
+    def find_triangle(self, x: float, y: float) -> int:
+        """The lowest-id triangle containing (x, y) under the reference's
+        point-in-triangle test (utils.pyx:332-385: for each vertex v with
+        outgoing edge eo and incoming edge ei, the cross products of eo and
+        ei with p - v have one sign or one of them is zero), searched in the
+        point's bucket of ``locator_grid``; -1 when none contains it.  The
+        host counterpart of the device's global fallback, for pre- and
+        post-processing."""
+        x0, y0, inv, nx, ny, start, tris = self.locator_grid()
+        fx = np.floor((x - x0) * inv)
+        fy = np.floor((y - y0) * inv)
+        cx = 0 if not fx >= 0. else (nx - 1 if fx > nx - 1 else int(fx))
+        cy = 0 if not fy >= 0. else (ny - 1 if fy > ny - 1 else int(fy))
+        c = cy * nx + cx
+        cand = tris[start[c]:start[c + 1]]
+        if len(cand) == 0:
+            return -1
+        t = self.triangles[cand]
+        ax, ay = self.x[t[:, 0]], self.y[t[:, 0]]
+        bx, by = self.x[t[:, 1]], self.y[t[:, 1]]
+        qx, qy = self.x[t[:, 2]], self.y[t[:, 2]]
+
+        def rot(vx, vy, eox, eoy, eix, eiy):
+            wx, wy = x - vx, y - vy
+            t1 = eox * wy - wx * eoy
+            t2 = eix * wy - wx * eiy
+            ok = (t1 == 0.) | (t2 == 0.) | (np.signbit(t1) == np.signbit(t2))
+            return ok & ~np.isnan(t1) & ~np.isnan(t2)
+
+        abx, aby = bx - ax, by - ay
+        bcx, bcy = qx - bx, qy - by
+        cax, cay = ax - qx, ay - qy
+        inside = (rot(ax, ay, abx, aby, cax, cay) & rot(bx, by, bcx, bcy, abx, aby) &
+                  rot(qx, qy, cax, cay, bcx, bcy))
+        hit = np.flatnonzero(inside)
+        return int(cand[hit[0]]) if len(hit) else -1

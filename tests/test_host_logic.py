@@ -264,3 +264,91 @@ def test_particle_set_depth_like_the_reference():
         cg.LagrangianParticleSet(np.zeros((3, 2)) + 1.0, dim=2, compute_depth=True)
     with pytest.raises(NotImplementedError):
         cg.LagrangianParticleSet(np.zeros((3, 3)) + 1.0, dim=3, compute_depth=True)
+
+
+# ---------------------------------------------------------------------------
+# pre- and post-processing helpers (eulerian_field_set.pyx:606-1886)
+# ---------------------------------------------------------------------------
+def _inside_all(mesh, x, y):
+    """Brute force: every triangle under the reference's point-in-triangle
+    test (utils.pyx:332-385)."""
+    t = mesh.triangles
+    a = np.stack([mesh.x[t[:, 0]], mesh.y[t[:, 0]]])
+    b = np.stack([mesh.x[t[:, 1]], mesh.y[t[:, 1]]])
+    c = np.stack([mesh.x[t[:, 2]], mesh.y[t[:, 2]]])
+
+    def rot(v, eo, ei):
+        wx, wy = x - v[0], y - v[1]
+        t1 = eo[0] * wy - wx * eo[1]
+        t2 = ei[0] * wy - wx * ei[1]
+        return (t1 == 0) | (t2 == 0) | (np.signbit(t1) == np.signbit(t2))
+
+    return np.flatnonzero(rot(a, b - a, a - c) & rot(b, c - b, b - a) & rot(c, a - c, c - b))
+
+
+def test_find_triangle_is_the_lowest_index_containing_triangle():
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    x, y, tri = synth.channel_mesh(100.0, 40.0, 21, 9, seed=3, jitter=0.3)
+    mesh = TriangularMesh(x, y, tri)
+    rng = np.random.default_rng(4)
+    pts = np.concatenate([np.stack([rng.uniform(-5, 105, 400), rng.uniform(-5, 45, 400)], 1),
+                          np.stack([x[:40], y[:40]], 1)])        # vertices: shared by several
+    for px, py in pts:
+        allk = _inside_all(mesh, px, py)
+        assert mesh.find_triangle(px, py) == (allk[0] if len(allk) else -1)
+
+
+def _linear_fieldset(dim=2, nl=1):
+    import cylag_gb300 as cg
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    x, y, tri = synth.channel_mesh(100.0, 40.0, 21, 9, seed=3, jitter=0.3)
+    mesh = TriangularMesh(x, y, tri)
+    n = len(x)
+    lin = 2.0 * x - 3.0 * y + 5.0
+    if dim == 2:
+        rec = lambda s: (s * lin)[None, :]
+        zs = np.zeros((2, n))
+        return cg.EulerianFieldSet(mesh, dim=2, nlayers=1, times=np.array([0.0, 10.0]),
+                                   elevation=zs, velocity_x=np.concatenate([rec(1), rec(2)]),
+                                   velocity_y=np.concatenate([rec(-1), rec(-1)])), lin
+    planes = np.concatenate([-10.0 + 2.5 * l + 0.0 * x for l in range(nl)])
+    lin3 = np.concatenate([lin] * nl)
+    return cg.EulerianFieldSet(mesh, dim=3, nlayers=nl, times=np.array([0.0]),
+                               elevation=planes[None, :], velocity_x=lin3[None, :],
+                               velocity_y=planes[None, :], velocity_z=np.zeros((1, nl * n))), lin
+
+
+def test_field_interpolation_helpers_2d():
+    fs, lin = _linear_fieldset()
+    names, ids = fs.get_field_list()
+    assert names[:3] == ["ELEVATION", "VELOCITY U", "VELOCITY V"] and ids[:3] == [0, 1, 2]
+    # time interpolation between records: 0.75 * rec0 + 0.25 * rec1 at t = 2.5
+    np.testing.assert_allclose(fs.get_field(1, 2.5), 1.25 * lin, rtol=1e-14)
+    rng = np.random.default_rng(5)
+    for px, py in np.stack([rng.uniform(1, 99, 50), rng.uniform(1, 39, 50)], 1):
+        want = 2.0 * px - 3.0 * py + 5.0
+        got = fs.interpolate_field(1, np.array([px, py]), 2.5)
+        assert abs(got - 1.25 * want) <= 1e-10 * max(1.0, abs(want))
+        u, v = fs.interpolate_velocity(np.array([px, py]), 10.0)
+        assert abs(u - 2.0 * want) <= 1e-10 * max(1.0, abs(want))
+        assert abs(v + want) <= 1e-10 * max(1.0, abs(want))
+    with pytest.raises(ValueError):
+        fs.interpolate_field(1, np.array([500.0, 500.0]), 0.0)
+    with pytest.raises(ValueError):
+        fs.get_field(3, 0.0)
+    assert fs.record == 0   # the set's own record is left alone
+
+
+def test_field_interpolation_helpers_3d():
+    fs, lin = _linear_fieldset(dim=3, nl=5)
+    np.testing.assert_allclose(fs.get_field(0, 0.0, layer=2), -5.0)
+    rng = np.random.default_rng(6)
+    for px, py, pz in np.stack([rng.uniform(1, 99, 40), rng.uniform(1, 39, 40),
+                                rng.uniform(-10, 0, 40)], 1):
+        pt = np.array([px, py, pz])
+        # VELOCITY V holds the layer elevations: linear in z between them
+        assert abs(fs.interpolate_field(2, pt, 0.0) - pz) <= 1e-9
+        u, v, w = fs.interpolate_velocity(pt, 0.0)
+        assert abs(u - (2.0 * px - 3.0 * py + 5.0)) <= 1e-9 and abs(v - pz) <= 1e-9 and w == 0.0
