@@ -88,6 +88,15 @@ class TriangularMesh:
         self._grid = None
 
     # -- edges (triangular_mesh.pyx:288-309) --------------------------------
+    @staticmethod
+    def from_matplotlib(tri, boundary_points=None, boundary_edges=None, nopen=0):
+        """triangular_mesh.pyx:182-201: a mesh from a triangulation object
+        with ``x``, ``y``, ``triangles`` and ``edges`` (a matplotlib
+        Triangulation or anything shaped like one)."""
+        return TriangularMesh(tri.x, tri.y, tri.triangles, edges=tri.edges,
+                              boundary_points=boundary_points, boundary_edges=boundary_edges,
+                              nopen=nopen)
+
     def _init_edges(self):
         t = self.triangles
         a = t.reshape(-1)

@@ -352,3 +352,16 @@ def test_field_interpolation_helpers_3d():
         assert abs(fs.interpolate_field(2, pt, 0.0) - pz) <= 1e-9
         u, v, w = fs.interpolate_velocity(pt, 0.0)
         assert abs(u - (2.0 * px - 3.0 * py + 5.0)) <= 1e-9 and abs(v - pz) <= 1e-9 and w == 0.0
+
+
+def test_mesh_from_a_triangulation_object():
+    """triangular_mesh.pyx:182-201: TriangularMesh.from_matplotlib takes any
+    object with x, y, triangles and edges; same arrays as the constructor."""
+    from types import SimpleNamespace
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    x, y, tri = synth.channel_mesh(50.0, 20.0, 11, 5, seed=1, jitter=0.2)
+    ref = TriangularMesh(x, y, tri)
+    got = TriangularMesh.from_matplotlib(SimpleNamespace(x=x, y=y, triangles=tri, edges=ref.edges))
+    for k in ("edges", "triedge_map", "edgetri_map", "edges_labels", "gradx", "grady", "det"):
+        np.testing.assert_array_equal(getattr(got, k), getattr(ref, k), err_msg=k)
