@@ -233,6 +233,14 @@ class EulerianFieldSet:
         else:
             self.record = 0
 
+    def check_dim(self, field):
+        """eulerian_field_set.pyx:258-279: ValueError unless the field has
+        the set's record shape."""
+        ref = (self.ntimes, self.npoints) if self.dim == 2 else \
+            (self.ntimes, self.npoints * self.nlayers)
+        if np.shape(field) != ref:
+            raise ValueError(f"Field have wrong dimension, expected {ref}, found {np.shape(field)}")
+
     # ---- pre- and post-processing (eulerian_field_set.pyx:606-1886) ---------
     def get_field_list(self):
         """Field names and ids: the main fields, then the optional ones."""

@@ -365,3 +365,10 @@ def test_mesh_from_a_triangulation_object():
     got = TriangularMesh.from_matplotlib(SimpleNamespace(x=x, y=y, triangles=tri, edges=ref.edges))
     for k in ("edges", "triedge_map", "edgetri_map", "edges_labels", "gradx", "grady", "det"):
         np.testing.assert_array_equal(getattr(got, k), getattr(ref, k), err_msg=k)
+
+
+def test_field_set_check_dim():
+    fs, _ = _linear_fieldset()
+    fs.check_dim(np.zeros((2, fs.npoints)))
+    with pytest.raises(ValueError):
+        fs.check_dim(np.zeros((1, fs.npoints)))
