@@ -25,6 +25,17 @@ from .mesh import TriangularMesh
 from .parameters import Parameters
 
 EPSILON = 1.0e-16
+NU0 = 1.3e-6        # constants.pyx: kinematic viscosity of water, m2/s
+GRAV = 9.80665      # constants.pyx: gravity, m/s2
+
+
+def _cpow_re(x, y):
+    """x**y for x > 0 as the compiled reference evaluates a double power:
+    the real part of the C library's complex power, exp(y log x) with the
+    complex logarithm's real part log1p((x-1)(x+1))/2 for 0.5 <= x < 2."""
+    import math
+    L = math.log1p((x - 1.) * (x + 1.)) / 2. if 0.5 <= x < 2. else math.log(x)
+    return math.exp(y * L)
 DEFAULT_INITIAL_POOL_SIZE = 10000
 _OPT_NAMES = {
     "turbulent_energy": ("TURBULENT ENERG.", "TURBULENT ENERGY", "ENERGIE TURBUL."),
@@ -637,6 +648,58 @@ class LagrangianParticleSet:
             self._dev["tri"].index_fill_(0, ti, -2)
             torch.cuda.synchronize(dev)
             self._added = True
+
+    def show_status(self, i):
+        """lagrangian_particle_set.pyx:377-396: prints particle i's state."""
+        print("~~~~~~~~~~~~~~~~~~~~~")
+        print("Particle n°", i)
+        for k in ("position", "velocity", "fluid_velocity_seen"):
+            print(f"{k:<20}=", np.asarray(self._get(k)[i]))
+        print("tag                 =", self.tag[i])
+        print("inactive            =", self.inactive[i])
+        for k in ("tri", "lowerlayer", "last_tri"):
+            print(f"{k:<20}=", self._get(k)[i])
+        print("last_position       =", np.asarray(self._get("last_position")[i]))
+
+    def drag_coefficient(self, U, dp):
+        """lagrangian_particle_set.pyx:790-832 on the host: the constant,
+        Schiller-Naumann (1935) or Almedeij (2008) drag coefficient at
+        relative speed U and diameter dp, with the powers evaluated as the
+        compiled reference and the device do (_cpow_re)."""
+        Re = max(EPSILON, U * dp / NU0)
+        if self.drag_coef_model == 0:
+            return float(self.drag_coef)
+        if self.drag_coef_model == 1:
+            return (24. / Re) * (1. + 0.15 * _cpow_re(Re, 0.687)) if Re <= 1000. else 0.44
+        if self.drag_coef_model == 2:
+            phi1 = (24. / Re) ** 10. + _cpow_re(21. * _cpow_re(Re, -0.67), 10.) + \
+                _cpow_re(4. * _cpow_re(Re, -0.33), 10.) + 0.4 ** 10.
+            phi2 = 1. / (_cpow_re(0.148 * _cpow_re(Re, 0.11), -10.) + 0.5 ** -10.)
+            phi3 = _cpow_re(1.57 * _cpow_re(Re, -1.625) * 1.e8, 10.)
+            phi4 = 1. / (_cpow_re(6e-17 * _cpow_re(Re, 2.63), -10.) + 0.2 ** -10.)
+            return (1. / ((phi1 + phi2) ** -1. + phi3 ** -1.) + phi4) ** (1. / 10.)
+        return 0.44
+
+    def buoyancy_velocity(self, dp, model_hr, rho0):
+        """lagrangian_particle_set.pyx:834-890 on the host: the user's
+        constant, or the settling velocity of Stokes (dp < 1e-4 m), Ruby and
+        Zanke (1977, in between), constant-drag turbulent (model_hr 0) or
+        Van Rijn (1985) (dp > 1e-3 m); negative for particles denser than
+        the fluid."""
+        if self.buoyancy_velocity_model == 0:
+            return float(self.buoyancy_velocity_value)
+        s = self.density / rho0
+        if dp < 1.e-4:
+            wb = abs(s - 1.) * (GRAV * (dp * dp)) / (18. * NU0)
+        elif dp > 1.e-3:
+            if model_hr == 0:
+                wb = np.sqrt(abs(s - 1.) * (4. * dp * GRAV) / (3. * self.drag_coef))
+            else:
+                wb = 1.1 * np.sqrt((s - 1.) * GRAV * dp)
+        else:
+            wb = (10. * NU0 / dp) * (np.sqrt(1. + abs(s - 1.) * GRAV * dp ** 3.0 /
+                                             (100. * (NU0 * NU0))) - 1.)
+        return float(-wb if s > 1. else wb)
 
     def delete_single(self, i):
         """lagrangian_particle_set.pyx:754-788"""

@@ -372,3 +372,45 @@ def test_field_set_check_dim():
     fs.check_dim(np.zeros((2, fs.npoints)))
     with pytest.raises(ValueError):
         fs.check_dim(np.zeros((1, fs.npoints)))
+
+
+def test_particle_set_drag_and_buoyancy_like_the_reference(capsys):
+    """lagrangian_particle_set.pyx:790-890 on the host: the three drag laws
+    (double powers as complex powers, as the compiled reference evaluates
+    them) and the settling-velocity laws across their diameter ranges."""
+    import cylag_gb300 as cg
+    nu, g = 1.3e-6, 9.80665
+    cp = lambda x, y: (complex(x) ** y).real
+    for model in (0, 1, 2):
+        ps = cg.LagrangianParticleSet(np.ones((2, 2)), dim=2, drag_coefficient_model=model,
+                                      drag_coefficient=0.5)
+        for U, dp in ((1e-3, 1e-4), (0.2, 1e-3), (2.0, 5e-3), (50.0, 0.05)):
+            Re = max(1e-16, U * dp / nu)
+            if model == 0:
+                want = 0.5
+            elif model == 1:
+                want = (24. / Re) * (1. + 0.15 * cp(Re, 0.687)) if Re <= 1000. else 0.44
+            else:
+                p1 = (24. / Re) ** 10 + cp(21. * cp(Re, -0.67), 10.) + cp(4. * cp(Re, -0.33), 10.) \
+                    + 0.4 ** 10
+                p2 = 1. / (cp(0.148 * cp(Re, 0.11), -10.) + 0.5 ** -10)
+                p3 = cp(1.57 * cp(Re, -1.625) * 1e8, 10.)
+                p4 = 1. / (cp(6e-17 * cp(Re, 2.63), -10.) + 0.2 ** -10)
+                want = (1. / (1. / (p1 + p2) + 1. / p3) + p4) ** 0.1
+            got = ps.drag_coefficient(U, dp)
+            assert abs(got - want) <= 1e-13 * abs(want), (model, U, dp, got, want)
+    ps = cg.LagrangianParticleSet(np.ones((2, 2)), dim=2, particle_density=2650.,
+                                  buoyancy_velocity_model=1, drag_coefficient=0.44)
+    s = 2.65
+    assert np.isclose(ps.buoyancy_velocity(5e-5, 0, 1000.), -(s - 1) * g * 5e-5 ** 2 / (18 * nu))
+    assert np.isclose(ps.buoyancy_velocity(5e-4, 0, 1000.),
+                      -(10 * nu / 5e-4) * (np.sqrt(1 + (s - 1) * g * 5e-4 ** 3 / (100 * nu ** 2)) - 1))
+    assert np.isclose(ps.buoyancy_velocity(2e-3, 0, 1000.), -np.sqrt((s - 1) * 4 * 2e-3 * g / (3 * 0.44)))
+    assert np.isclose(ps.buoyancy_velocity(2e-3, 1, 1000.), -1.1 * np.sqrt((s - 1) * g * 2e-3))
+    light = cg.LagrangianParticleSet(np.ones((2, 2)), dim=2, particle_density=900.,
+                                     buoyancy_velocity_model=1)
+    assert light.buoyancy_velocity(5e-5, 0, 1000.) > 0
+    const = cg.LagrangianParticleSet(np.ones((2, 2)), dim=2, buoyancy_velocity=-0.01)
+    assert const.buoyancy_velocity(1e-3, 0, 1000.) == -0.01
+    const.show_status(1)
+    assert "Particle n° 1" in capsys.readouterr().out
