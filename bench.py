@@ -192,9 +192,9 @@ def bytes_per_particle_step(workload, precision):
     return b + 48 if workload == "lsm3_3d" else b
 
 
-# DRAM bytes per particle-step of one step's kernels (step + walk), from the
-# ncu captures summarised in profiles/step_{mixed,fp64}_lsm1_2d_keps_4M.md
-# (4e6 particles, element-sorted; traffic grows with the particles processed)
+# DRAM bytes per particle-step of one step's kernels (step + walk), from ncu
+# captures of the same kernels at 4e6 particles (element-sorted; traffic
+# grows with the particles processed)
 NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 58.9, ("lsm1_2d", "fp64"): 147.0}
 
 

@@ -474,8 +474,16 @@ class LagrangianParticleSet:
                               p("lowerlayer"), p("tag"), p("diameter"), p("rng_state"))
 
     def _sync(self):
+        """Makes the device arrays the whole particle state and waits for
+        the library's queued work: an element-sorted run keeps its newest
+        state in working copies between steps (cg_run_writeback)."""
         if self._ctx is not None:
-            _lib.check(self._ctx, _lib.load().cg_ctx_sync(self._ctx))
+            L = _lib.load()
+            solver = getattr(self, "_solver", None)
+            run = getattr(solver, "_run", None) if solver is not None else None
+            if run:
+                _lib.check(self._ctx, L.cg_run_writeback(run))
+            _lib.check(self._ctx, L.cg_ctx_sync(self._ctx))
 
     def _get(self, key):
         if self._dev is None:
@@ -1051,6 +1059,10 @@ class Solver:
             self._snapshots.close()
             self._snapshots = None
         if getattr(self, "_run", None):
+            # the particle set outlives the run: its arrays get the state
+            # held in the run's working copies
+            self.L.cg_run_writeback(self._run)
+            self.L.cg_ctx_sync(self._ctx)
             self.L.cg_run_destroy(self._run)
             self._run = None
         if getattr(self, "_ctx", None):

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/cylag_gpu.h"
 #include "cg_host.h"
 
@@ -52,6 +54,11 @@ struct cg_run {
     DevBuf sortbuf;        // element-order working copies (cg_sort.cu)
     SortBuffers sb{};
     int sort_period = 0;
+    // the working copies hold the newest position, element, tag and PCG32
+    // state (and the model's working arrays): the caller's copies of those
+    // are stale until cg_run_writeback
+    bool resident = false;
+    int since_sort = 0;    // steps taken on the working copies since their last sort
     uint64_t bytes = 0;
     uint64_t scratch_bytes = 0;   // walk queue + sort buffers (follow the particle count)
     bool pending_init = false;    // particles added (tri == -2): initialize at the next step
@@ -86,24 +93,53 @@ struct NoallocScratch {
 };
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
-// Device address of g_noalloc_scratch per device ordinal, looked up once per
-// device with that device current (in host code the symbol's name is only a
-// stand-in for the device array, never an address a kernel may use).
+// Device address of g_noalloc_scratch per device ordinal, looked up with that
+// device current (in host code the symbol's name is only a stand-in for the
+// device array, never an address a kernel may use).  The address belongs to
+// the context the module was loaded into: it is cached with that context's
+// id and looked up again when the device's current context is a new one
+// (after cudaDeviceReset or a reset of the primary context).
 static std::mutex g_noalloc_mutex;
 static NoallocScratch* g_noalloc_ptr[64] = {nullptr};
+static unsigned long long g_noalloc_ctx[64] = {0};
 
 static int noalloc_scratch(cg_ctx* c, NoallocScratch** out) {
     if (c->device < 0 || c->device >= 64)
         return set_err(c, CG_EINVAL, "cg_run_step_noalloc: device ordinal %d out of range",
                        c->device);
+    // driver entry points through the runtime (the library does not link
+    // libcuda, so that it loads on machines without a driver)
+    static CUresult (*get_current)(CUcontext*) = nullptr;
+    static CUresult (*get_id)(CUcontext, unsigned long long*) = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!get_current || !get_id) {
+            void *f0 = nullptr, *f1 = nullptr;
+            cudaDriverEntryPointQueryResult q0, q1;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault,
+                                                 &q0) != cudaSuccess ||
+                cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault,
+                                                 &q1) != cudaSuccess ||
+                q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess)
+                return set_err(c, CG_ECUDA, "cg_run_step_noalloc: driver context queries unavailable");
+            get_current = (CUresult(*)(CUcontext*))f0;
+            get_id = (CUresult(*)(CUcontext, unsigned long long*))f1;
+        }
+    }
+    CUcontext cu = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&cu) != CUDA_SUCCESS || cu == nullptr || get_id(cu, &id) != CUDA_SUCCESS)
+        return set_err(c, CG_ECUDA, "cg_run_step_noalloc: no current CUDA context on device %d",
+                       c->device);
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[c->device]) {
+    if (!g_noalloc_ptr[c->device] || g_noalloc_ctx[c->device] != id) {
         void* ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess || !ptr)
             return set_err(c, CG_ECUDA, "cudaGetSymbolAddress(g_noalloc_scratch) failed: %s",
                            cudaGetErrorString(e));
         g_noalloc_ptr[c->device] = (NoallocScratch*)ptr;
+        g_noalloc_ctx[c->device] = id;
     }
     *out = g_noalloc_ptr[c->device];
     return CG_OK;
@@ -220,7 +256,7 @@ static DevState added_view(const cg_run* r) {
 struct ScratchPlan {
     bool use_queue = false, use_sort = false;
     size_t queue_bytes = 0, sort_bytes = 0;
-    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0};
+    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0}, off_aux = 0;
     int nkeys = 0, nl_key = 1, work = 0, dim = 2;
     size_t n = 0;
 };
@@ -243,7 +279,11 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     q.use_sort = p->sort_period > 0 && n > 0 && nkeys64 < (1ll << 30) &&
                  scan_scratch_ints((int)nkeys64) <= 4096;
     q.nkeys = (int)std::min<int64_t>(nkeys64, 1ll << 30);
-    if (p->model >= 2) q.work |= W_VEL | W_DIAM;
+    // velocity: read by the next call's last step (LSM1: the last velocity)
+    // or every step (LSM2/LSM3); the outputs no step reads (W_AUXW) in
+    // element order too, so that no step writes through the caller's slots
+    q.work |= W_VEL | W_AUXW;
+    if (p->model >= 2) q.work |= W_DIAM;
     if (p->model == 3) q.work |= W_FVS;
     if (p->dim == 3) q.work |= W_LAYER | W_DIAM;
     // mixed LSM1 2D: working positions as split FP32 pairs (same 16 bytes)
@@ -253,13 +293,18 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
                               ((q.work & W_VEL) ? al256(n * 8 * D) : 0) +
                               ((q.work & W_FVS) ? al256(n * 8 * D) : 0) +
                               ((q.work & W_LAYER) ? al256(n * 4) : 0) +
-                              ((q.work & W_DIAM) ? al256(n * 8) : 0);
+                              ((q.work & W_DIAM) ? al256(n * 8) : 0) +
+                              ((q.work & W_AUXW) ? al256(n * 4) : 0);
+    // the outputs the re-sort does not move: one set shared by both copies
+    const size_t aux_bytes = (q.work & W_AUXW)
+        ? 2 * al256(n * 8 * D) + ((q.work & W_FVS) ? 0 : al256(n * 8 * D)) : 0;
     if (q.use_sort) {
         q.off_sums = al256((size_t)q.nkeys * 4);
         q.off_perm = al256(q.off_sums + (size_t)scan_scratch_ints(q.nkeys) * 4);
         q.off_w[0] = al256(q.off_perm + n * 4);
         q.off_w[1] = q.off_w[0] + work_bytes;
-        q.sort_bytes = q.off_w[1] + work_bytes;
+        q.off_aux = q.off_w[1] + work_bytes;
+        q.sort_bytes = q.off_aux + aux_bytes;
     }
     return q;
 }
@@ -270,6 +315,8 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
     r->use_queue = false;
     r->sb = SortBuffers{};
     r->sort_period = 0;
+    r->resident = false;
+    r->since_sort = 0;
     if ((rc = dalloc(c, r->queue, q.queue_bytes)) || (rc = dalloc(c, r->sortbuf, q.sort_bytes)))
         return rc;
     r->use_queue = q.use_queue;
@@ -283,6 +330,12 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
     r->sb.nl = q.nl_key;
     r->sb.work = q.work;
     WorkState* ws[2] = {&r->sb.a, &r->sb.b};
+    char* aux = b + q.off_aux;
+    auto take_aux = [&](size_t bytes) { char* t = aux; aux += al256(bytes); return t; };
+    double* lpos = (q.work & W_AUXW) ? (double*)take_aux(n * 8 * D) : nullptr;
+    double* lvel = (q.work & W_AUXW) ? (double*)take_aux(n * 8 * D) : nullptr;
+    double* fvs_out = ((q.work & W_AUXW) && !(q.work & W_FVS)) ? (double*)take_aux(n * 8 * D)
+                                                                : nullptr;
     for (int k = 0; k < 2; ++k) {
         char* w = b + q.off_w[k];
         auto take = [&](size_t bytes) { char* t = w; w += al256(bytes); return t; };
@@ -292,11 +345,25 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
         ws[k]->tag = (int*)take(n * 8);
         ws[k]->slot = (int*)take(n * 8);
         ws[k]->vel = (q.work & W_VEL) ? (double*)take(n * 8 * D) : nullptr;
-        ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * 8 * D) : nullptr;
+        ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * 8 * D) : fvs_out;
         ws[k]->layer = (q.work & W_LAYER) ? (int*)take(n * 4) : nullptr;
         ws[k]->diam = (q.work & W_DIAM) ? (double*)take(n * 8) : nullptr;
+        ws[k]->ltri = (q.work & W_AUXW) ? (int*)take(n * 4) : nullptr;
+        ws[k]->lpos = lpos;
+        ws[k]->lvel = lvel;
     }
     r->sort_period = r->prm.sort_period;
+    return CG_OK;
+}
+
+// Working copies -> the caller's arrays (stream-ordered), after which the
+// caller's arrays are the run's state again and the next step gathers them.
+static int write_back(cg_run* r) {
+    if (!r->resident) return CG_OK;
+    cg_ctx* c = r->ctx;
+    launch_sort_scatter(r->st, r->sb, c->stream);
+    r->resident = false;
+    CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
 }
 
@@ -705,6 +772,8 @@ int cg_run_seed(cg_run* r) {
     if (!r) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = write_back(r);
+    if (rc) return rc;
     launch_seed(r->st.tag, r->st.rng, r->st.n, r->prm.seed, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -765,8 +834,9 @@ int cg_run_init(cg_run* r) {
     if (!r) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     CUDA_TRY(c, cudaSetDevice(c->device));
-    int rc = ensure_fields(r);
+    int rc = write_back(r);
     if (rc) return rc;
+    if ((rc = ensure_fields(r))) return rc;
     launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, r->st,
                 r->prm.particle_velocity_init, -1, (uint32_t*)r->errw.p, c->stream);
     CUDA_TRY(c, cudaGetLastError());
@@ -817,10 +887,10 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaEventCreate(&e));
         r->ev.push_back(e);
     }
-    // element-sorted working state: only for calls long enough to pay for the
-    // gather/scatter (a few steps per sort period)
-    const bool sorted = r->sort_period > 0 && nsteps >= r->sort_period;
-    DevState ws = r->st;
+    // element-sorted working state: gathered from the caller's arrays at the
+    // first step after a write-back, re-sorted every sort_period steps
+    // (counted across calls), kept resident between calls
+    const bool sorted = r->sort_period > 0 && r->st.n > 0;
     int launches = 0;   // kernels launched by this call
     for (int s = 0; s < nsteps; ++s) {
         // solver.pyx:440: fields at the step-start time
@@ -829,19 +899,21 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         // particles added since the last step: initialized with this step's
         // fields, then advanced by it (solver.pyx:443-470)
         if (s == 0 && r->pending_init) {
+            if ((rc = write_back(r))) return rc;
             launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, added_view(r),
                         r->prm.particle_velocity_init, -2 - (int)r->iteration,
                         (uint32_t*)r->errw.p, c->stream);
             r->pending_init = false;
             launches += 1;
         }
-        if (sorted && s % r->sort_period == 0) {
-            if (s == 0) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
+        if (sorted && (!r->resident || r->since_sort >= r->sort_period)) {
+            if (!r->resident) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
             else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
+            r->resident = true;
+            r->since_sort = 0;
             launches += 6;   // histogram, 3 scan passes, index scatter, gather
-            ws = sorted_view(r->st, r->sb);
         }
-        const DevState& run_state = sorted ? ws : r->st;
+        const DevState run_state = sorted ? sorted_view(r->st, r->sb) : r->st;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * row;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
@@ -867,10 +939,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
         CUDA_TRY(c, cudaGetLastError());
         launches += r->st.n > 0 ? (r->use_queue ? 2 : 1) : 0;   // step (+ walk)
-        if (sorted && s == nsteps - 1) {
-            launch_sort_scatter(r->st, r->sb, c->stream);
-            launches += 1;
-        }
+        if (sorted) r->since_sort += 1;
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;
@@ -979,6 +1048,10 @@ int cg_run_resize(cg_run* r, const cg_state_desc* s) {
                      !s->last_position || !s->last_velocity || !s->tri || !s->last_tri ||
                      !s->lowerlayer || !s->tag || !s->diameter || !s->rng_state))
         return set_err(c, CG_EINVAL, "incomplete particle state description");
+    if (r->resident)
+        return set_err(c, CG_ESTATE,
+                       "cg_run_resize: the run's newest state is in its working copies; "
+                       "call cg_run_writeback before replacing the particle arrays");
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     const ScratchPlan plan = plan_scratch(c, &r->prm, s->n);
@@ -1021,11 +1094,21 @@ int cg_run_added(cg_run* r, int32_t n_init) {
     if (!r || n_init < 0) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = write_back(r);
+    if (rc) return rc;
     launch_seed_added(r->st.tri, r->st.tag, r->st.rng, r->st.n, r->prm.seed, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     r->pending_init = n_init > 0;
     r->init_n = n_init < r->st.n ? n_init : r->st.n;
     return CG_OK;
+}
+
+int cg_run_writeback(cg_run* r) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    if (!r->resident) return CG_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    return write_back(r);
 }
 
 int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
@@ -1044,19 +1127,32 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
                        "cg_run_step_noalloc: run has %d particles, the allocation-free "
                        "scratch holds at most %d (use cg_run_step)",
                        r->st.n, CG_NOALLOC_MAX_PARTICLES);
+    // section counts and stranding records are per-call device buffers of
+    // cg_run_step; this entry point produces neither, so it refuses runs
+    // that asked for them rather than dropping them
+    if (r->dp.ncsec > 0 || r->strand_on)
+        return set_err(c, CG_EINVAL,
+                       "cg_run_step_noalloc: the run has control sections or stranding output "
+                       "on, which only cg_run_step records");
+    r->last_ms = 0.;
+    r->last_launches = 0;
     if (nsteps == 0) return CG_OK;
     CUDA_TRY(c, cudaSetDevice(c->device));
     NoallocScratch* scratch = nullptr;
     int rc = noalloc_scratch(c, &scratch);
     if (rc) return rc;
+    int launches = r->resident ? 1 : 0;   // the write-back of sorted working copies
+    if ((rc = write_back(r))) return rc;
     if ((rc = ensure_fields(r))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         if ((rc = time_interpolation(r, r->time))) return rc;
+        if (!r->frozen) launches += 1;
         if (s == 0 && r->pending_init) {
             launch_init(r->prm.precision, c->mesh, field_view(r), r->dp, added_view(r),
                         r->prm.particle_velocity_init, -2 - (int)r->iteration,
                         (uint32_t*)r->errw.p, c->stream);
             r->pending_init = false;
+            launches += 1;
         }
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         WalkQueue wq{nullptr, nullptr};
@@ -1081,9 +1177,11 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
                 launch_walk_plain(c->mesh, fv, r->dp, r->st, wq, aux, it, nullptr, errw, c->stream);
         }
         CUDA_TRY(c, cudaGetLastError());
+        launches += r->st.n > 0 ? (wq.e ? 2 : 1) : 0;
         r->time += r->prm.time_step;
         r->iteration += 1;
     }
+    r->last_launches = launches;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
@@ -1146,8 +1244,9 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
     if (r->pending_init)
         return set_err(c, CG_ESTATE, "particles await initialization: step them with cg_run_step");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    int rc = ensure_fields(r);
+    int rc = write_back(r);
     if (rc) return rc;
+    if ((rc = ensure_fields(r))) return rc;
     const int n = r->st.n, D = r->prm.dim;
     // chunk boundaries: `chunk` particles each, or (chunk == 0) a ramp of
     // 1/32, 2/32, then 4/32 of the pool, down to 2/32, 2/32, 1/32 at the end,

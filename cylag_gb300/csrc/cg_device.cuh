@@ -6,6 +6,8 @@
 // rounds exactly as the reference's C does.
 #pragma once
 
+#include <climits>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -160,6 +162,15 @@ constexpr int W_VEL = 1, W_FVS = 2, W_LAYER = 4, W_DIAM = 8;
 // working positions held as float4 {x_hi, y_hi, x_lo, y_lo}, the unevaluated
 // sums x_hi + x_lo (mixed LSM1 2D step over sorted working copies)
 constexpr int W_SPLIT = 16;
+// the step's outputs that no later step reads -- last_position,
+// last_velocity, last_tri and (unless W_FVS carries it) the fluid velocity
+// seen -- are written to working arrays in element order instead of the
+// caller's slots.  A re-sort does not move them: each working last_tri is
+// reset to LAST_UNSET there (or kept at -1, a deletion, whose outputs are
+// zero), and only entries set since are written back.  Every call ends with
+// a step that sets them for each active particle.
+constexpr int W_AUXW = 32;
+constexpr int LAST_UNSET = INT_MIN;
 
 // An FP64 position as a pair of FP32 values hi + lo (|lo| <= ulp(hi)/2):
 // 48 significant bits, so the step's arithmetic on it stays in FP32.

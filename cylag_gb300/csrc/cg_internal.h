@@ -106,7 +106,10 @@ void launch_serve_mixed(int grid, const DevMesh& m, const FieldView& fv, const D
 // Working copies of the per-step state in element order (cg_sort.cu):
 // always position, tri, tag, PCG32 state and the caller slot; velocity,
 // fluid velocity seen, layer and diameter as well when the model reads them
-// every step (nullptr otherwise: reached through slot).
+// (nullptr otherwise: reached through slot).  With W_AUXW the outputs no
+// step reads (last position, last velocity, last element and, unless W_FVS
+// carries it, the fluid velocity seen) have working arrays too; the re-sort
+// does not move them (see W_AUXW).
 struct WorkState {
     double* pos;              // [n][dim]
     int* tri;                 // [n]
@@ -117,6 +120,9 @@ struct WorkState {
     double* fvs;              // [n][dim] or nullptr
     int* layer;               // [n] or nullptr
     double* diam;             // [n] or nullptr
+    double* lpos;             // [n][dim] last position (W_AUXW) or nullptr
+    double* lvel;             // [n][dim] last velocity (W_AUXW) or nullptr
+    int* ltri;                // [n] last element, LAST_UNSET or -1 (W_AUXW) or nullptr
 };
 struct SortBuffers {
     int* count;          // [nkeys] histogram, then scan offsets

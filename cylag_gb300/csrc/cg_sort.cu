@@ -143,12 +143,16 @@ __device__ __forceinline__ void move_rows(const T* __restrict__ src, T* __restri
 
 // dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays.
 // split: working positions are split FP32 pairs (W_SPLIT), made from the
-// caller's FP64 positions here and moved as they are between working copies
+// caller's FP64 positions here and moved as they are between working copies.
+// The outputs kept with W_AUXW are not moved: dst's last element becomes
+// LAST_UNSET, or stays -1 for a particle deleted since the last write-back
+// (its outputs are zero).
 __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src, WorkState dst,
-                                    int n, int dim, bool split) {
+                                    int n, int dim, int work) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&perm[j]);
+    const bool split = (work & W_SPLIT) != 0;
     if (split && src.slot == nullptr) {
         const double2 x = __ldcs(reinterpret_cast<const double2*>(src.pos) + i);
         reinterpret_cast<float4*>(dst.pos)[j] = split_pos(x.x, x.y);
@@ -159,18 +163,20 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
     dst.tag[j] = __ldcs(src.tag + i);
     dst.rng[j] = __ldcs(src.rng + i);
     dst.slot[j] = src.slot ? __ldcs(src.slot + i) : i;
-    if (dst.vel) move_rows(src.vel, dst.vel, i, j, dim);
-    if (dst.fvs) move_rows(src.fvs, dst.fvs, i, j, dim);
-    if (dst.layer) dst.layer[j] = __ldcs(src.layer + i);
-    if (dst.diam) dst.diam[j] = __ldcs(src.diam + i);
+    if (work & W_VEL) move_rows(src.vel, dst.vel, i, j, dim);
+    if (work & W_FVS) move_rows(src.fvs, dst.fvs, i, j, dim);
+    if (work & W_LAYER) dst.layer[j] = __ldcs(src.layer + i);
+    if (work & W_DIAM) dst.diam[j] = __ldcs(src.diam + i);
+    if (work & W_AUXW)
+        dst.ltri[j] = (src.slot != nullptr && __ldcs(src.ltri + i) == -1) ? -1 : LAST_UNSET;
 }
 
-// caller[slot[j]] = work[j]
-__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim, bool split) {
+// caller[slot[j]] = work[j]; the W_AUXW outputs only where a step set them
+__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim, int work) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&w.slot[j]);
-    if (split)
+    if (work & W_SPLIT)
         __stcs(reinterpret_cast<double2*>(user.pos) + i,
                join_pos(reinterpret_cast<const float4*>(w.pos)[j]));
     else
@@ -179,12 +185,24 @@ __global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim
     __stcs(user.tri + i, w.tri[j]);
     __stcs(user.tag + i, w.tag[j]);
     __stcs(user.rng + i, w.rng[j]);
-    if (w.vel)
+    if (work & W_VEL)
         for (int d = 0; d < dim; ++d) __stcs(user.vel + (size_t)i * dim + d, w.vel[(size_t)j * dim + d]);
-    if (w.fvs)
+    if (work & W_FVS)
         for (int d = 0; d < dim; ++d) __stcs(user.fvs + (size_t)i * dim + d, w.fvs[(size_t)j * dim + d]);
-    if (w.layer) __stcs(user.layer + i, w.layer[j]);
-    if (w.diam) __stcs(user.diam + i, w.diam[j]);
+    if (work & W_LAYER) __stcs(user.layer + i, w.layer[j]);
+    if (work & W_DIAM) __stcs(user.diam + i, w.diam[j]);
+    if (work & W_AUXW) {
+        const int lt = w.ltri[j];
+        if (lt == LAST_UNSET) return;
+        const bool del = lt == -1;
+        for (int d = 0; d < dim; ++d) {
+            const size_t u = (size_t)i * dim + d, k = (size_t)j * dim + d;
+            __stcs(user.lpos + u, del ? 0. : w.lpos[k]);
+            __stcs(user.lvel + u, del ? 0. : w.lvel[k]);
+            if (!(work & W_FVS)) __stcs(user.fvs + u, del ? 0. : w.fvs[k]);
+        }
+        __stcs(user.ltri + i, lt);
+    }
 }
 
 int scan_scratch_ints(int nkeys) { return (nkeys + SCAN_TILE - 1) / SCAN_TILE; }
@@ -202,18 +220,21 @@ static void sort_perm(const int* tri, const int* layer, int n, int nt, SortBuffe
     scatter_index_kernel<<<(n + bs - 1) / bs, bs, 0, st>>>(tri, layer, n, nt, b.nl, b.count, b.perm);
 }
 
-// the caller's arrays seen as a working state (only those kept in b.a)
-static WorkState user_view(const DevState& u, const SortBuffers& b) {
+// the caller's arrays seen as a working state
+static WorkState user_view(const DevState& u) {
     WorkState w;
     w.pos = u.pos;
     w.tri = u.tri;
     w.tag = u.tag;
     w.rng = reinterpret_cast<unsigned long long*>(u.rng);
     w.slot = nullptr;
-    w.vel = (b.work & W_VEL) ? u.vel : nullptr;
-    w.fvs = (b.work & W_FVS) ? u.fvs : nullptr;
-    w.layer = (b.work & W_LAYER) ? u.lowerlayer : nullptr;
-    w.diam = (b.work & W_DIAM) ? u.diameter : nullptr;
+    w.vel = u.vel;
+    w.fvs = u.fvs;
+    w.layer = u.lowerlayer;
+    w.diam = u.diameter;
+    w.lpos = u.last_pos;
+    w.lvel = u.last_vel;
+    w.ltri = u.last_tri;
     return w;
 }
 
@@ -221,15 +242,14 @@ void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream
     int n = user.n;
     if (n == 0) return;
     sort_perm(user.tri, (b.work & W_LAYER) ? user.lowerlayer : nullptr, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user, b), b.a, n, b.dim,
-                                                         (b.work & W_SPLIT) != 0);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user), b.a, n, b.dim,
+                                                         b.work);
 }
 
 void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
     if (n == 0) return;
     sort_perm(b.a.tri, b.a.layer, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim,
-                                                         (b.work & W_SPLIT) != 0);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim, b.work);
     WorkState t = b.a;
     b.a = b.b;
     b.b = t;
@@ -238,8 +258,8 @@ void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
 void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_t st) {
     int n = user.n;
     if (n == 0) return;
-    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user, b), n, b.dim,
-                                                          (b.work & W_SPLIT) != 0);
+    scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user), n, b.dim,
+                                                          b.work);
 }
 
 DevState sorted_view(const DevState& user, const SortBuffers& b) {
@@ -249,10 +269,15 @@ DevState sorted_view(const DevState& user, const SortBuffers& b) {
     w.tag = b.a.tag;
     w.rng = reinterpret_cast<uint64_t*>(b.a.rng);
     w.slot = b.a.slot;
-    if (b.a.vel) w.vel = b.a.vel;
-    if (b.a.fvs) w.fvs = b.a.fvs;
-    if (b.a.layer) w.lowerlayer = b.a.layer;
-    if (b.a.diam) w.diameter = b.a.diam;
+    if (b.work & W_VEL) w.vel = b.a.vel;
+    if (b.work & (W_FVS | W_AUXW)) w.fvs = b.a.fvs;
+    if (b.work & W_LAYER) w.lowerlayer = b.a.layer;
+    if (b.work & W_DIAM) w.diameter = b.a.diam;
+    if (b.work & W_AUXW) {
+        w.last_pos = b.a.lpos;
+        w.last_vel = b.a.lvel;
+        w.last_tri = b.a.ltri;
+    }
     w.work = b.work;
     return w;
 }

@@ -569,20 +569,21 @@ struct Particle {
     __device__ void store(DevState& s, int i, int aux, int step_index, const double* lastv) {
         const int D = DIM;
         const int a = aux_index(s, i);   // slot of the per-particle arrays outside the sort
-        const int iv = widx(s, i, a, W_VEL), iu = widx(s, i, a, W_FVS);
+        const int iv = widx(s, i, a, W_VEL), iu = widx(s, i, a, W_FVS | W_AUXW);
         const int il = widx(s, i, a, W_LAYER), id = widx(s, i, a, W_DIAM);
+        const int ix = widx(s, i, a, W_AUXW);
         if (deleted) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.pos[(size_t)i * D + d] = 0.;
                 s.vel[(size_t)iv * D + d] = 0.;
                 s.fvs[(size_t)iu * D + d] = 0.;
-                s.last_pos[(size_t)a * D + d] = 0.;
-                s.last_vel[(size_t)a * D + d] = 0.;
+                s.last_pos[(size_t)ix * D + d] = 0.;
+                s.last_vel[(size_t)ix * D + d] = 0.;
             }
             s.diameter[id] = 0.;
             s.tri[i] = -1;
-            s.last_tri[a] = -1;
+            s.last_tri[ix] = -1;
             s.lowerlayer[il] = 0;
             s.tag[i] = -2 - step_index;
             s.rng[i] = rng.state;
@@ -608,10 +609,10 @@ struct Particle {
         if (aux >= 2) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                s.last_pos[(size_t)a * D + d] = x0[d];
-                s.last_vel[(size_t)a * D + d] = lastv[d];
+                s.last_pos[(size_t)ix * D + d] = x0[d];
+                s.last_vel[(size_t)ix * D + d] = lastv[d];
             }
-            s.last_tri[a] = ltri;
+            s.last_tri[ix] = ltri;
         }
     }
 

@@ -15,7 +15,6 @@
 // position; only the positions themselves differ (FP32 increments).
 #pragma once
 
-#include "cg_stage.cuh"
 #include "cg_step.cuh"
 
 namespace cg {
@@ -278,8 +277,8 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                                                     int* __restrict__ stats,
                                                     uint32_t* __restrict__ err_word,
                                                     const Zig32& z32, const MixedIn& in, int i) {
-    // particle state streams through L2 once per step (evict-first loads or
-    // bulk copies, evict-first stores): the mesh and node records stay in L2
+    // particle state streams through L2 once per step (evict-first loads and
+    // stores): the mesh and node records stay in L2
     const int tri0 = in.tri;
     if (tri0 < 0) return;
     const float4* __restrict__ cur = reinterpret_cast<const float4*>(f.cur);
@@ -292,7 +291,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     rng.inc = ((uint64_t)(uint32_t)in.tag << 1) | 1ULL;
     rng.err = 0;
     double2 lastv = make_double2(0., 0.);
-    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[aux_index(s, i)];
+    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[widx(s, i, aux_index(s, i), W_VEL)];
 
     const float dt = p.dt32;
     const bool euler = EQ || p.time_scheme == 1;
@@ -448,14 +447,15 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
     if (deleted) {
         const int a = aux_index(s, i);
+        const int ix = widx(s, i, a, W_AUXW);
         reinterpret_cast<double2*>(s.pos)[i] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.vel)[a] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.fvs)[a] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.last_pos)[a] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.last_vel)[a] = make_double2(0., 0.);
-        s.diameter[a] = 0.;
+        reinterpret_cast<double2*>(s.vel)[widx(s, i, a, W_VEL)] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_pos)[ix] = make_double2(0., 0.);
+        reinterpret_cast<double2*>(s.last_vel)[ix] = make_double2(0., 0.);
+        s.diameter[widx(s, i, a, W_DIAM)] = 0.;
         s.tri[i] = -1;
-        s.last_tri[a] = -1;
+        s.last_tri[ix] = -1;
         s.lowerlayer[a] = 0;
         s.tag[i] = -2 - step_index;
         s.rng[i] = rng.state;
@@ -472,25 +472,23 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);
     if (aux >= 1) {
         const int a = aux_index(s, i);
-        reinterpret_cast<double2*>(s.vel)[a] = make_double2(up0, up1);
-        reinterpret_cast<double2*>(s.fvs)[a] = make_double2(up0, up1);
+        reinterpret_cast<double2*>(s.vel)[widx(s, i, a, W_VEL)] = make_double2(up0, up1);
+        reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(up0, up1);
         if (aux >= 2) {
             if constexpr (SPLIT) {
                 if (!have64) x0 = join_pos(xs);
             }
-            reinterpret_cast<double2*>(s.last_pos)[a] = x0;
-            reinterpret_cast<double2*>(s.last_vel)[a] = lastv;
-            s.last_tri[a] = ltri;
+            const int ix = widx(s, i, a, W_AUXW);
+            reinterpret_cast<double2*>(s.last_pos)[ix] = x0;
+            reinterpret_cast<double2*>(s.last_vel)[ix] = lastv;
+            s.last_tri[ix] = ltri;
         }
     }
 }
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
-// STAGED: each warp steps 32-particle tiles whose state the bulk-copy engine
-// staged in shared memory one tile ahead (cg_stage.cuh); the tail of fewer
-// than 32 particles is read directly.  The state arrays must be 16-byte
-// aligned (checked on the host).
-template <int MINB, bool SPLIT = false, bool STAGED = false, bool ASYNC = false, bool EQ = false>
+// MINB: resident blocks of 256 per SM the register budget is set for.
+template <int MINB, bool SPLIT = false, bool EQ = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -503,80 +501,10 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
         z32.wn[t] = (float)g_zig.wn[t];
         z32.fn[t] = (float)g_zig.fn[t];
     }
-    if constexpr (!STAGED) {
-        __syncthreads();
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-            step_mixed_particle<SPLIT, EQ>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
+        step_mixed_particle<SPLIT, EQ>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
                                        load_mixed_in(s, i), i);
-    } else if constexpr (ASYNC) {
-        // per-thread cp.async prefetch of the next particle's state
-        __shared__ ThreadSlot slots[2][256];
-        __syncthreads();
-        const int stride = gridDim.x * blockDim.x;
-        int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < s.n) prefetch_slot(slots[0][threadIdx.x], s.pos, s.rng, s.tri, s.tag, i);
-        cp_async_commit();
-        for (int k = 0; i < s.n; i += stride, ++k) {
-            const int nx = i + stride;
-            if (nx < s.n)
-                prefetch_slot(slots[(k + 1) & 1][threadIdx.x], s.pos, s.rng, s.tri, s.tag, nx);
-            cp_async_commit();
-            cp_async_wait<1>();
-            const ThreadSlot& t = slots[k & 1][threadIdx.x];
-            MixedIn in;
-            in.tri = t.tri;
-            in.tag = t.tag;
-            in.rng = t.rng;
-            in.pos = t.pos;
-            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, in,
-                                       i);
-        }
-        cp_async_wait<0>();
-    } else {
-        constexpr int WPB = 256 / 32;
-        __shared__ WarpTile tiles[WPB][2];
-        __shared__ alignas(8) uint64_t bars[WPB][2];
-        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (lane == 0) {
-            mbar_init(&bars[w][0], 1);
-            mbar_init(&bars[w][1], 1);
-            fence_proxy_async_smem();   // the initialized barriers, to the copy engine
-        }
-        __syncthreads();
-        const int nfull = s.n >> 5;
-        const int gw = blockIdx.x * WPB + w, nw = gridDim.x * WPB;
-        if (lane == 0 && gw < nfull)
-            stage_tile(tiles[w][0], &bars[w][0], s.pos, s.rng, s.tri, s.tag, gw);
-        int k = 0;
-        for (int tile = gw; tile < nfull; tile += nw, ++k) {
-            const int st = k & 1;
-            const int next = tile + nw;
-            if (lane == 0 && next < nfull)
-                stage_tile(tiles[w][st ^ 1], &bars[w][st ^ 1], s.pos, s.rng, s.tri, s.tag, next);
-            if (!__all_sync(0xffffffffu, mbar_wait(&bars[w][st], (k >> 1) & 1))) {
-                // copies that do not complete: flag, wait (bounded) for the
-                // other stage's copy in flight, leave
-                if (lane == 0) atomicOr(err_word, ERR_ASYNC_TIMEOUT);
-                if (next < nfull) mbar_wait(&bars[w][st ^ 1], ((k + 1) >> 1) & 1);
-                return;
-            }
-            const WarpTile& t = tiles[w][st];
-            MixedIn in;
-            in.tri = t.tri[lane];
-            in.tag = t.tag[lane];
-            in.rng = t.rng[lane];
-            in.pos = t.pos[lane];
-            step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32, in,
-                                       tile * 32 + lane);
-            __syncwarp();   // the tile is read before lane 0 stages into it again
-        }
-        if (gw == 0) {
-            const int i = (nfull << 5) + lane;
-            if (i < s.n)
-                step_mixed_particle<SPLIT>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
-                                           load_mixed_in(s, i), i);
-        }
-    }
 }
 
 }  // namespace cg

@@ -163,8 +163,29 @@ int cg_run_init(cg_run *run);
  * interpolation of the fields at each step-start time, the fused particle
  * step, time += dt.  bnd_stats_host (optional) receives [nsteps][nopen]
  * open-boundary exit counts (solver.pyx:567-572).  Synchronous: returns
- * after the last step, CG_EDEVICE if the device raised an error flag. */
+ * after the last step, CG_EDEVICE if the device raised an error flag.
+ *
+ * A run with sort_period > 0 steps on working copies of the particle state
+ * in element order: gathered from the caller's arrays at the first step
+ * (and at the first step after a cg_run_writeback), re-sorted every
+ * sort_period steps counted across calls, and kept in the run between
+ * calls.  While they are, the caller's position, tri, tag and rng_state
+ * (and, as the model needs them every step, velocity, fluid_velocity_seen,
+ * lowerlayer and diameter) are stale: call cg_run_writeback before reading
+ * or changing them.  The other arrays are current after every call. */
 int cg_run_step(cg_run *run, int32_t nsteps, int32_t *bnd_stats_host);
+
+/* Writes a sorted run's working copies back to the caller's arrays and
+ * releases them: after this (stream-ordered; cg_ctx_sync to wait) the
+ * caller's arrays hold the whole state, may be read or changed, and the
+ * next step gathers them again.  A no-op when nothing is held.  The
+ * reference keeps its particle arrays in place (no counterpart); the
+ * Python layer calls it before every access to the particle arrays.
+ * cg_run_seed, cg_run_init, cg_run_added, cg_run_step_host and
+ * cg_run_step_noalloc write back first themselves; cg_run_resize and
+ * cg_run_destroy do not (resize refuses with CG_ESTATE while copies are
+ * held; destroy drops them). */
+int cg_run_writeback(cg_run *run);
 
 /* Allocation-free variant of cg_run_step, for callers that cannot call
  * cudaMalloc while they step: code running under a memory pool or arena that
@@ -174,12 +195,17 @@ int cg_run_step(cg_run *run, int32_t nsteps, int32_t *bnd_stats_host);
  * reference.
  *
  * Same step as cg_run_step (same kernels, same results for the same run
- * state) except: no open-boundary statistics, no element re-sort, no kernel
- * timing.  Its scratch (the queue of particles leaving their triangle) is a
- * file-scope device array of CG_NOALLOC_MAX_PARTICLES entries (8 MiB) that
- * every GPU loading the library holds until exit; runs with more particles
- * are rejected with CG_EINVAL.  It calls no cudaMalloc, cudaFree or other
- * allocating routine.  The first call on a device looks up the array's device
+ * state) on the caller's arrays in their own order (a sorted run's working
+ * copies are written back first), except: no open-boundary statistics, no
+ * element re-sort, kernel time reported as 0 (cg_run_last_kernel_ms gives
+ * this call's launch count).  Runs with control sections or stranding
+ * output on are refused with CG_EINVAL: their per-call buffers belong to
+ * cg_run_step.  Its scratch (the queue of particles leaving their triangle)
+ * is a file-scope device array of CG_NOALLOC_MAX_PARTICLES entries (8 MiB)
+ * that every GPU loading the library holds until exit; runs with more
+ * particles are rejected with CG_EINVAL.  It calls no cudaMalloc, cudaFree
+ * or other allocating routine.  The first call on a device (and the first
+ * after that device's context was reset) looks up the array's device
  * address (cudaGetSymbolAddress), so make that first call before any stream
  * capture.  All calls share the one array: calls whose work overlaps on the
  * GPU (two runs stepped concurrently on different streams) race on it.

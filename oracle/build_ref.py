@@ -20,7 +20,8 @@ neither Cython nor the reference sources:
 Importing the result needs ``oracle/_ref`` and ``oracle/ref_stubs`` on
 ``sys.path`` (see ``oracle/refpath.py``).
 
-Usage: ``python oracle/build_ref.py [--src DIR] [--jobs N]``
+Usage: ``python oracle/build_ref.py [--src DIR] [--jobs N]`` (DIR defaults to
+``$CYLAG_REFERENCE_SRC``, else the reference tree's mount point here).
 """
 from __future__ import annotations
 
@@ -94,9 +95,19 @@ def compile_all(jobs: int) -> None:
             pass
 
 
+def default_src() -> Path:
+    """The reference tree: $CYLAG_REFERENCE_SRC, else where this machine
+    mounts it."""
+    return Path(os.environ.get("CYLAG_REFERENCE_SRC", "/root/reference"))
+
+
+def sources_present() -> bool:
+    return (default_src() / "cylag").is_dir()
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=str(default_src()))
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--stage", choices=["all", "generate", "compile"], default="all")
     a = ap.parse_args(argv)

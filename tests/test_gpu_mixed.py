@@ -107,45 +107,6 @@ def test_split_working_positions_follow_fp64_positions():
     assert np.max(np.abs(pa[same] - pb[same])) < 1e-4
 
 
-_STAGED_CHILD = """
-import sys, numpy as np
-sys.path.insert(0, sys.argv[2])
-import cylag_gb300 as cg
-from cylag_gb300 import synth
-from cylag_gb300.mesh import TriangularMesh
-c = synth.keps_drift_channel(npart=30000, nx=101, ny=26, seed=5)
-mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
-fs = cg.EulerianFieldSet(mesh, dim=2, nlayers=1, times=c["times"], elevation=c["elevation"],
-                         velocity_x=c["velocity_x"], velocity_y=c["velocity_y"],
-                         opt_fields=c["opt_fields"], opt_fields_names=c["opt_fields_names"])
-ps = cg.LagrangianParticleSet(c["position"][:30007], dim=2)
-p = dict(c["parameters"], time_step=2.0, final_time=400.0)
-s = cg.Solver(fs, ps, p, precision="mixed", seed=2, sort_period=10)
-s.forward(nsteps=60)
-np.savez(sys.argv[1], pos=ps.position, tri=ps.tri, tag=ps.tag)
-s.close()
-"""
-
-
-@pytest.mark.parametrize("stage", ["2", "3", "4"])
-def test_staged_state_tiles_same_results(tmp_path, stage):
-    """The bulk-copy staged variant of the mixed step (opt-in through
-    CYLAG_MIXED_STAGE; a ragged tail of 7 particles) gives bit-identical
-    results to the default kernel."""
-    import os
-    import subprocess
-    import sys
-    from conftest import ROOT
-    out = {}
-    for v in ("0", stage):
-        f = tmp_path / f"s{v}.npz"
-        subprocess.run([sys.executable, "-c", _STAGED_CHILD, str(f), str(ROOT)], check=True,
-                       env=dict(os.environ, CYLAG_MIXED_STAGE=v), timeout=600)
-        out[v] = np.load(f)
-    for k in ("pos", "tri", "tag"):
-        np.testing.assert_array_equal(out["0"][k], out[stage][k], err_msg=k)
-
-
 @pytest.mark.parametrize("sort_period", [0, 20])
 @pytest.mark.parametrize("name", ["keps_ts1_rm2", "keps_ts2_rm1", "keps_ts3_rm3", "keps_ts4_rm2"])
 def test_mixed_time_schemes_follow_reference(name, sort_period):

@@ -115,3 +115,45 @@ def test_gpu_run_from_telemac_files(tmp_path):
     got = s.bnd_statistics()
     np.testing.assert_array_equal(got[:, [o - 1 for o in order]], want["bnd_stats"])
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sorted_state_kept_across_calls(precision):
+    """An element-sorted run keeps its working copies between forward()
+    calls (re-sorted every sort_period steps counted across calls).  100
+    single-step calls, 100 steps in calls of 7 with the arrays read after
+    every call (each read writes the copies back and the next step gathers
+    them again), and one 100-step call leave the same state bit for bit:
+    positions, elements, tags and PCG32 states."""
+    import cylag_gb300 as cg
+    from cylag_gb300 import synth
+    c = synth.keps_drift_channel(npart=20000, nx=101, ny=26, seed=5)
+    case = {k: c[k] for k in ("x", "y", "triangles", "times", "elevation", "velocity_x",
+                              "velocity_y", "opt_fields", "position")}
+    case["opt_fields_names"] = c["opt_fields_names"]
+    p = dict(c["parameters"], time_step=2.0, final_time=400.0)
+    out = []
+    for mode in ("one", "single", "read7"):
+        f = fields_from_case(case)
+        fs = cg.EulerianFieldSet(mesh_from_case(case), **f)
+        ps = cg.LagrangianParticleSet(case["position"], dim=2)
+        s = cg.Solver(fs, ps, p, precision=precision, seed=3, sort_period=10)
+        if mode == "one":
+            s.forward(nsteps=100)
+        elif mode == "single":
+            for _ in range(100):
+                s.forward()
+        else:
+            done = 0
+            while done < 100:
+                k = min(7, 100 - done)
+                s.forward(nsteps=k)
+                done += k
+                _ = ps.position
+        ps._sync()
+        out.append({k: ps._dev[k].cpu().numpy() for k in ("position", "tri", "tag", "rng_state",
+                                                           "last_position", "velocity")})
+        s.close()
+    for mode, o in zip(("single", "read7"), out[1:]):
+        for k in out[0]:
+            np.testing.assert_array_equal(o[k], out[0][k], err_msg=f"{precision} {mode}: {k}")

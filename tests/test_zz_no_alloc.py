@@ -7,12 +7,15 @@ For them the library has one entry point whose scratch (the queue of
 particles leaving their triangle) is a fixed device array inside the
 library instead of cudaMalloc'd memory.
 
-This test calls it through the C ABI and checks, on two calls in a row,
+These tests call it through the C ABI and check, on two calls in a row,
 that it leaves the particle state exactly where the regular entry point
 (cg_run_step) leaves it: element indices and deletions identical, positions
-and velocities within the tolerance of the parity tests.  It also checks
-that runs larger than the array are refused with a clear error.  Collected
-last (file name) so that a failure here does not hide any other result.
+and velocities within the tolerance of the parity tests -- for the 2D LSM1
+step (walk queue in the fixed array) and for a 3D LSM2 run (walk inline, no
+queue).  They also check that runs larger than the array, and runs with
+control sections or stranding output on (which only cg_run_step records),
+are refused with a clear error that leaves the run usable.  Collected last
+(file name) so that a failure here does not hide any other result.
 """
 import ctypes as C
 
@@ -63,11 +66,78 @@ def test_noalloc_step_matches_cg_run_step(precision):
         sa.forward(nsteps=40)                       # existing entry point
         rc = L.cg_run_step_noalloc(sb._run, 40)     # allocation-free entry point
         _lib.check(sb._ctx, rc)
+        ms, launches = sb.last_kernel_ms()
+        assert ms == 0.0 and launches > 0     # this call's own count, no stale timing
         want = _state(pa)
         assert_state_close(_state(pb), want, rtol=RTOL, what=f"{precision} call {call + 1}")
         np.testing.assert_array_equal(pb.tag, pa.tag)
     sa.close()
     sb.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noalloc_step_matches_cg_run_step_lsm2_3d(precision):
+    """3D LSM2 (direct integrator, k-epsilon velocity diffusion): the path
+    without a walk queue.  The regular run is element-sorted, so its working
+    copies are also written back between the calls."""
+    import cylag_gb300 as cg
+    from cylag_gb300 import _lib, synth
+    from cylag_gb300.mesh import TriangularMesh
+    c = synth.lsm2_loglaw_workload(npart=20_000, nx=41, ny=21, nplanes=6, seed=3)
+    p = dict(c["parameters"], final_time=1e6)
+    runs = []
+    for sort_period in (10, 0):
+        mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+        fs = cg.EulerianFieldSet(mesh, dim=3, nlayers=c["nlayers"], times=c["times"],
+                                 elevation=c["elevation"], velocity_x=c["velocity_x"],
+                                 velocity_y=c["velocity_y"], velocity_z=c["velocity_z"],
+                                 opt_fields=c["opt_fields"],
+                                 opt_fields_names=c["opt_fields_names"])
+        ps = cg.LagrangianParticleSet(c["position"], dim=3, **c["pset"])
+        runs.append((cg.Solver(fs, ps, p, precision=precision, seed=6,
+                               sort_period=sort_period), ps))
+    (sa, pa), (sb, pb) = runs
+    L = _lib.load()
+    for call in range(2):
+        sa.forward(nsteps=25)
+        _lib.check(sb._ctx, L.cg_run_step_noalloc(sb._run, 25))
+        got = dict(_state(pb), lowerlayer=pb.lowerlayer,
+                   fluid_velocity_seen=pb.fluid_velocity_seen)
+        want = dict(_state(pa), lowerlayer=pa.lowerlayer,
+                    fluid_velocity_seen=pa.fluid_velocity_seen)
+        assert_state_close(got, want, rtol=RTOL, what=f"lsm2 3d {precision} call {call + 1}")
+        np.testing.assert_array_equal(pb.tag, pa.tag)
+    sa.close()
+    sb.close()
+
+
+@pytest.mark.parametrize("what", ["sections", "stranding"])
+def test_noalloc_refuses_section_and_stranding_runs(what):
+    """Control-section counts and stranding records are kept in per-call
+    buffers that only cg_run_step fills: the allocation-free entry point
+    refuses such runs (CG_EINVAL, a message naming them) and changes
+    nothing, so cg_run_step still steps the run afterwards."""
+    from cylag_gb300 import _lib
+    case, p = _case(2_000)
+    s, ps = _solver(case, p, "mixed")
+    L = _lib.load()
+    if what == "sections":
+        seg = np.array([[1000.0, 0.0, 1000.0, 1000.0]])
+        _lib.check(s._ctx, L.cg_run_set_sections(s._run, 1, seg.ctypes.data))
+    else:
+        _lib.check(s._ctx, L.cg_run_set_stranding_output(s._run, 1))
+    t0 = C.c_double()
+    L.cg_run_time(s._run, C.byref(t0), None)
+    rc = L.cg_run_step_noalloc(s._run, 3)
+    assert rc == _lib.CG_EINVAL
+    buf = C.create_string_buffer(512)
+    L.cg_last_error(s._ctx, buf, 512)
+    assert b"control sections or stranding" in buf.value
+    t1 = C.c_double()
+    L.cg_run_time(s._run, C.byref(t1), None)
+    assert t1.value == t0.value
+    _lib.check(s._ctx, L.cg_run_step(s._run, 2, None))
+    s.close()
 
 
 def test_noalloc_refuses_runs_beyond_its_scratch():
