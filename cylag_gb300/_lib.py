@@ -98,6 +98,7 @@ SIGNATURES = [
     ("cg_run_step", C.c_int, [P, I32, P]),
     ("cg_run_step_noalloc", C.c_int, [P, I32]),
     ("cg_run_writeback", C.c_int, [P]),
+    ("cg_rng_draws", C.c_int, [P, C.c_uint64, C.c_uint64, I32, I32, C.c_int64, P]),
     ("cg_run_time", C.c_int, [P, C.POINTER(F64), C.POINTER(C.c_int64)]),
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),

@@ -1111,6 +1111,33 @@ int cg_run_writeback(cg_run* r) {
     return write_back(r);
 }
 
+int cg_rng_draws(cg_ctx* c, uint64_t seed, uint64_t stream, int32_t kind, int32_t method,
+                 int64_t n, double* out_host) {
+    if (!c || !out_host || n < 0 || kind < 0 || kind > 4 || method < 1 || method > 3)
+        return set_err(c, CG_EINVAL, "cg_rng_draws: bad arguments");
+    if (n == 0) return CG_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const size_t vals = (size_t)n * (kind == 3 ? 2 : 1);
+    DevBuf buf, err;
+    int rc;
+    if ((rc = dalloc(c, buf, vals * sizeof(double))) || (rc = dalloc(c, err, 256))) {
+        dfree(buf);
+        return rc;
+    }
+    cudaMemsetAsync(err.p, 0, sizeof(uint32_t), c->stream);
+    launch_rng_draws(seed, stream, kind, method, n, (double*)buf.p, (uint32_t*)err.p, c->stream);
+    uint32_t flags = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(out_host, buf.p, vals * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&flags, err.p, sizeof flags, cudaMemcpyDeviceToHost);
+    dfree(buf);
+    dfree(err);
+    if (e != cudaSuccess) return set_err(c, CG_ECUDA, "cg_rng_draws: %s", cudaGetErrorString(e));
+    if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
+    return CG_OK;
+}
+
 int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
     if (!r) return CG_EINVAL;
     if (time) *time = r->time;

@@ -143,6 +143,11 @@ void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_
 // the run's state with the working copies of b.a in place of the caller's
 DevState sorted_view(const DevState& user, const SortBuffers& b);
 
+// random_utils.pyx draws on the device (see rng_draws_kernel); out holds n
+// values (2n for kind 3)
+void launch_rng_draws(uint64_t seed, uint64_t stream, int kind, int method, int64_t n,
+                      double* out, uint32_t* err, cudaStream_t st);
+
 // rng[i] = pcg32_seed(seed, tag[i])
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st);
 // the same for the particles awaiting initialization (tri == -2)

@@ -256,6 +256,39 @@ __global__ void seed_kernel(const int* __restrict__ tag, uint64_t* __restrict__ 
     rng[i] = st;
 }
 
+// random_utils.pyx's public draws from pcg32_seed(seed, stream), in stream
+// order (one thread): 0 uniform, 1 ziggurat normal, 2 polar normal (the
+// first of a pair), 3 pairs of generate_random_pair(method) (2n values),
+// 4 generate_random_single(method).  Plain form (FP64 samplers).
+__global__ void rng_draws_kernel(uint64_t seed, uint64_t stream, int kind, int method, int64_t n,
+                                 double* __restrict__ out, uint32_t* __restrict__ err) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    Rng r;
+    pcg_seed(seed, stream, r.state, r.inc);
+    r.err = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (kind == 0) {
+            out[i] = rng_uniform(r);
+        } else if (kind == 1) {
+            out[i] = rng_ziggurat(r, g_zig);
+        } else if (kind == 2) {
+            double a, b;
+            rng_polar(r, a, b);
+            out[i] = a;
+        } else if (kind == 3) {
+            rng_pair(r, method, g_zig, out[2 * i], out[2 * i + 1]);
+        } else {
+            out[i] = rng_single(r, method, g_zig);
+        }
+    }
+    if (r.err) atomicOr(err, r.err);
+}
+
+void launch_rng_draws(uint64_t seed, uint64_t stream, int kind, int method, int64_t n,
+                      double* out, uint32_t* err, cudaStream_t st) {
+    rng_draws_kernel<<<1, 32, 0, st>>>(seed, stream, kind, method, n, out, err);
+}
+
 void launch_seed(const int* tag, uint64_t* rng, int n, uint64_t seed, cudaStream_t st) {
     int bs = 256;
     int nb = (n + bs - 1) / bs;

@@ -213,6 +213,15 @@ int cg_run_writeback(cg_run *run);
 #define CG_NOALLOC_MAX_PARTICLES 262144
 int cg_run_step_noalloc(cg_run *run, int32_t nsteps);
 
+/* The device samplers the step draws from, run in stream order from
+ * pcg32_seed(seed, stream) (random_utils.pyx:30-37): kind 0 random_uniform
+ * (55-67), 1 the ziggurat normal (154-194), 2 the polar normal (72-108),
+ * 3 generate_random_pair(method) (202-233; 2n values), 4
+ * generate_random_single(method) (235-263).  FP64 (plain-form) samplers;
+ * n values copied to out_host.  Synchronous. */
+int cg_rng_draws(cg_ctx *ctx, uint64_t seed, uint64_t stream, int32_t kind, int32_t method,
+                 int64_t n, double *out_host);
+
 /* Current simulated time and iteration (cylag/core/simutime.pyx:77-84). */
 int cg_run_time(const cg_run *run, double *time, int64_t *iteration);
 

@@ -157,3 +157,37 @@ def test_sorted_state_kept_across_calls(precision):
     for mode, o in zip(("single", "read7"), out[1:]):
         for k in out[0]:
             np.testing.assert_array_equal(o[k], out[0][k], err_msg=f"{precision} {mode}: {k}")
+
+
+def test_device_samplers_match_reference_streams():
+    """The device's PCG32 and its uniform, ziggurat and polar samplers
+    (cg_rng_draws) against the streams the compiled reference drew from
+    pcg32_seed(seed, stream): uniform draws and method-1 pairs bit-exact
+    (integer arithmetic and exact FP64 scaling); ziggurat and polar draws
+    within 1e-14 relative (exp and log of CUDA's library against the host's;
+    an acceptance test decided the other way would desynchronize the stream
+    and fail by far more)."""
+    import ctypes as C
+    from conftest import GOLDEN
+    from cylag_gb300 import _lib
+    L = _lib.load()
+    ctx = C.c_void_p()
+    _lib.check(None, L.cg_ctx_create(0, 0, C.byref(ctx)))
+    z = np.load(GOLDEN / "rng.npz")
+
+    def draws(seed, stream, kind, n, method=2):
+        out = np.zeros(n * (2 if kind == 3 else 1))
+        _lib.check(ctx, L.cg_rng_draws(ctx, seed, stream, kind, method, n, out.ctypes.data))
+        return out
+
+    def close(a, b, what):
+        err = np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+        assert err <= 1e-14, f"{what}: max rel err {err:.3e}"
+
+    for j, (seed, stream) in enumerate(z["pairs"].tolist()):
+        np.testing.assert_array_equal(draws(seed, stream, 0, 512), z[f"uniform_{j}"])
+        close(draws(seed, stream, 1, 512), z[f"zig_{j}"], f"ziggurat {j}")
+        close(draws(seed, stream, 2, 256), z[f"polar_{j}"], f"polar {j}")
+        close(draws(seed, stream, 3, 128, method=3), z[f"pair3_{j}"], f"pair3 {j}")
+        np.testing.assert_array_equal(draws(seed, stream, 3, 128, method=1), z[f"pair1_{j}"])
+    L.cg_ctx_destroy(ctx)
