@@ -68,6 +68,13 @@ def parse():
     ap.add_argument("--serve-duration", type=float, default=60.0, help="arrival window, s (serve)")
     ap.add_argument("--serve-chunk", type=int, default=32, help="steps queued per loop (serve)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle-error", action="store_true",
+                    help="skip the mixed form's error against the FP64 oracle subsample")
+    ap.add_argument("--legs", type=int, default=1,
+                    help="also measure the LSM2 3D, LSM3 3D and serving legs (default line only)")
+    ap.add_argument("--leg-steps", type=int, default=20, help="timed steps of each 3D leg")
+    ap.add_argument("--leg-serve-duration", type=float, default=10.0,
+                    help="arrival window of the serving leg, s")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=0,
                     help="particles per copy/step chunk of the end-to-end steps (0: about n/8)")
@@ -150,19 +157,21 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
-def make_workload(args, rank=0):
+def make_workload(args, rank=0, workload=None):
     """The workload's case dict (mesh, fields, particles, parameters); rank r
     > 0 gets its own particles (same count) from its own seed."""
     from cylag_gb300 import synth
-    kw = {k: v for k, v in (("npart", args.npart), ("nx", args.nx), ("ny", args.ny)) if v}
-    if args.workload == "lsm1_2d":
+    workload = workload or args.workload
+    kw = {k: v for k, v in (("npart", args.npart), ("nx", args.nx), ("ny", args.ny)) if v} \
+        if workload == args.workload else {}
+    if workload == "lsm1_2d":
         # field records A, B, A, ... every 600 s covering warm-up, timed and
         # end-to-end steps at dt = 0.5 s (0 / 600 / 1200 s up to 1197 timed
         # steps, the default case)
         horizon = max(1200.0, 0.5 * (args.warmup + 2 * args.steps))
         c = synth.keps_drift_channel(seed=0, horizon=horizon, **kw)
         c.update(dim=2, nlayers=1, pset={})
-    elif args.workload == "lsm2_3d":
+    elif workload == "lsm2_3d":
         c = synth.lsm2_loglaw_workload(seed=0, **kw)
     else:
         c = synth.lsm3_taylor_green_workload(seed=0, **kw)
@@ -195,7 +204,10 @@ def bytes_per_particle_step(workload, precision):
 # DRAM bytes per particle-step of one step's kernels (step + walk), from ncu
 # captures of the same kernels at 4e6 particles (element-sorted; traffic
 # grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 58.9, ("lsm1_2d", "fp64"): 147.0}
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 59.2, ("lsm1_2d", "fp64"): 147.0}
+NCU_TRAFFIC_SOURCE = {
+    k: "ncu dram bytes (read+write) of the element-sorted step and walk kernels at 4e6 "
+       "particles, scaled to the launch" for k in NCU_TRAFFIC_B_PER_PARTICLE_STEP}
 
 
 def field_set_of(c):
@@ -301,19 +313,22 @@ def run_reference_arm(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
+def measure(args, c, params, precision, rank, world, local, dist, do_e2e, steps=None,
+            sort_period=None):
     """Warm-up, then K timed steps (CUDA events on the library's stream),
     then optionally K end-to-end steps through the C ABI with host buffers."""
     import torch
     import cylag_gb300 as cg
     from cylag_gb300 import _lib
+    steps = args.steps if steps is None else steps
+    sort_period = args.sort_period if sort_period is None else sort_period
     mesh, fs = field_set_of(c)
     ps = cg.LagrangianParticleSet(c["position"], dim=c["dim"], **c.get("pset", {}))
     if "diameter" in c:
         ps.diameter = c["diameter"]
     log(f"creating solver ({precision})")
     solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local,
-                       sort_period=args.sort_period)
+                       sort_period=sort_period)
     L = solver.L
     # all library work on a torch-owned stream (torch manages its lifetime)
     stream = torch.cuda.Stream(device=local)
@@ -332,7 +347,7 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
     ev1 = torch.cuda.Event(enable_timing=True)
     log("timed region")
     ev0.record(stream)
-    solver.forward(nsteps=args.steps)
+    solver.forward(nsteps=steps)
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -343,14 +358,15 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
         ms = allreduce_max(ms, dist)
     log(f"{precision}: timed {ms:.3f} ms, kernel {kern_ms:.4f} ms/launch")
     res = {"precision": precision, "ms": ms, "kernel_ms": kern_ms, "launches": launches,
-           "value": world * n * args.steps / (ms / 1e3), "clocks": clk, "n": n,
+           "value": world * n * steps / (ms / 1e3), "clocks": clk, "n": n,
            "position": ps.position, "velocity": ps.velocity, "inactive": ps.inactive,
-           "nt": int(mesh.nt)}
+           "nt": int(mesh.nt), "steps": steps}
     if do_e2e:
         # end to end: the particle state lives in pinned host memory; every
         # step, one C-ABI call copies it in, steps and copies it back
         # (cg_run_step_host: chunked, copies overlapping the step)
         log("end-to-end region")
+        ps._sync()
         d = ps._dev
         keys = ["position", "tri", "tag", "rng_state"]
         if c["dim"] == 3:
@@ -373,7 +389,7 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
         e1 = torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             rc = L.cg_run_step_host(solver._run, 1, C.byref(arr), C.byref(arr), args.e2e_chunk,
                                     None)
             _lib.check(solver._ctx, rc)
@@ -385,7 +401,7 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
         if dist:
             from cylag_gb300.shard import allreduce_max
             ems = allreduce_max(ems, dist)
-        res["e2e"] = {"value": world * n * args.steps / (ems / 1e3), "unit": UNIT,
+        res["e2e"] = {"value": world * n * steps / (ems / 1e3), "unit": UNIT,
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "wall_s": wall}
     torch.cuda.synchronize()
@@ -393,6 +409,71 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e):
     del ps, solver
     torch.cuda.empty_cache()
     return res
+
+
+def oracle_subsample_error(c, params, res, nsteps, every, threads):
+    """The mixed form's error against the FP64 oracle: the oracle advances
+    every `every`-th particle (tags = their indices, so their PCG32 streams
+    are the GPU's) by the same steps; ensemble mean and variance of the
+    displacement (and of the velocity for LSM2/LSM3) compared on that
+    subsample."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from cylag_gb300.mesh import TriangularMesh
+    from cylag_gb300.stats import displacement_report
+    n = len(c["position"])
+    idx = np.arange(0, n, every)
+    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+    diam = c["diameter"][idx] if "diameter" in c else None
+    o = oracle.OracleSolver(mesh, fields_dict(c), params, c["position"][idx], pset=c.get("pset"),
+                            seed=0, tags=idx, nthreads=threads, diameter=diam)
+    o.solve(nsteps)
+    act = (res["inactive"][idx] == 0) & (o.inactive == 0)
+    rep = displacement_report(c["position"][idx], res["position"][idx], o.pos, act)
+    out = {"steps": nsteps, "particles": int(act.sum()),
+           "rms_displacement_diff_m": rep["rms_displacement_diff"],
+           "var_rel_err": max(rep["var_rel_err"]), "mean_rel_err": max(rep["mean_rel_err"])}
+    if params["model"] >= 2:
+        va, vb = res["velocity"][idx][act], o.vel[act]
+        out["velocity_var_rel_err"] = float(
+            np.max(np.abs(va.var(0) - vb.var(0)) / np.maximum(vb.var(0), 1e-300)))
+    return out
+
+
+MODEL_DESC = {"lsm1_2d": "LSM1 Euler, k-eps drift",
+              "lsm2_3d": "LSM2 direct integrator, k-eps velocity diffusion",
+              "lsm3_3d": "LSM3 direct integrator, constant K, polydisperse settling"}
+
+
+def workload_line(args, workload, c, params, res, main_form, peak, peak_kind, world):
+    """The bench line's fields of one workload: throughput, roofline of its
+    step kernels, the plain form beside the mixed one."""
+    r = res[main_form]
+    n = r["n"]
+    bpp = bytes_per_particle_step(workload, main_form)
+    achieved = bpp * n / (r["kernel_ms"] / 1e3) / 1e9
+    traffic = NCU_TRAFFIC_B_PER_PARTICLE_STEP.get((workload, main_form))
+    line = {
+        "value": r["value"], "ms_per_step": r["ms"] / r["steps"], "steps": r["steps"],
+        "config": {"workload": WORKLOADS[workload], "particles_per_gpu": n,
+                   "triangles": r["nt"], "layers": c["nlayers"], "precision": main_form,
+                   "dt": params["time_step"], "l2": "state larger than L2 (no flush)",
+                   "model": MODEL_DESC[workload], "sort_period": args.sort_period},
+        "gpu_launches": int(r["launches"]),   # every kernel of the timed cg_run_step call
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "traffic": float(traffic * n) if traffic else None,
+                     "traffic_source": NCU_TRAFFIC_SOURCE.get((workload, main_form)),
+                     "peak_kind": peak_kind, "kernel_ms": r["kernel_ms"],
+                     "bytes_per_particle_step": bpp},
+        "clocks": r["clocks"],
+    }
+    if "fp64" in res and main_form != "fp64":
+        q = res["fp64"]
+        line["plain_fp64"] = {"value": q["value"], "kernel_ms": q["kernel_ms"],
+                              "ms_per_step": q["ms"] / q["steps"], "clocks": q["clocks"]}
+        line["mixed_over_plain"] = r["value"] / q["value"]
+    return line
 
 
 def run_gpu_arm(args):
@@ -415,63 +496,58 @@ def run_gpu_arm(args):
     for prec in forms:
         res[prec] = measure(args, c, params, prec, rank, world, local, dist,
                             do_e2e=(not args.no_e2e and prec == forms[0]))
-    if rank != 0:
-        return
-    main_form = forms[0]
-    r = res[main_form]
-    n = r["n"]
-    bpp = bytes_per_particle_step(args.workload, main_form)
+    threads = os.cpu_count() or 1
     peak, peak_kind = peaks()
-    achieved = bpp * n / (r["kernel_ms"] / 1e3) / 1e9
-    traffic = NCU_TRAFFIC_B_PER_PARTICLE_STEP.get((args.workload, main_form))
-    model_desc = {"lsm1_2d": "LSM1 Euler, k-eps drift",
-                  "lsm2_3d": "LSM2 direct integrator, k-eps velocity diffusion",
-                  "lsm3_3d": "LSM3 direct integrator, constant K, polydisperse settling"}
-    line = {
-        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if main_form == "fp64" else "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "particles_per_gpu": n,
-                   "triangles": r["nt"], "layers": c["nlayers"], "precision": main_form,
-                   "dt": params["time_step"], "l2": "state larger than L2 (no flush)",
-                   "model": model_desc[args.workload],
-                   "sort_period": args.sort_period if c["dim"] == 2 else 0},
-        "gpu_launches": int(r["launches"]),   # every kernel of the timed cg_run_step call
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     "traffic": float(traffic * n) if traffic else None,
-                     "traffic_source": "ncu dram bytes (read+write) of the step and walk "
-                                       "kernels at 4e6 particles, scaled to the launch",
-                     "peak_kind": peak_kind, "kernel_ms": r["kernel_ms"],
-                     "bytes_per_particle_step": bpp},
-        "clocks": r["clocks"],
-    }
-    if "e2e" in r:
-        line["e2e"] = r["e2e"]
-    if "fp64" in res and main_form != "fp64":
-        from cylag_gb300.stats import displacement_report
-        q = res["fp64"]
-        act = (r["inactive"] == 0) & (q["inactive"] == 0)
-        rep = displacement_report(c["position"], r["position"], q["position"], act)
-        line["plain_fp64"] = {"value": q["value"], "kernel_ms": q["kernel_ms"],
-                              "ms_per_step": q["ms"] / args.steps, "clocks": q["clocks"]}
-        line["mixed_over_plain"] = r["value"] / q["value"]
-        line["mixed_error_vs_fp64"] = {
-            "steps": args.warmup + args.steps, "rms_displacement_diff_m": rep["rms_displacement_diff"],
-            "var_rel_err": max(rep["var_rel_err"]), "mean_rel_err": max(rep["mean_rel_err"])}
-        if params["model"] >= 2:
-            va, vb = r["velocity"][act], q["velocity"][act]
-            line["mixed_error_vs_fp64"]["velocity_var_rel_err"] = float(
-                np.max(np.abs(va.var(0) - vb.var(0)) / np.maximum(vb.var(0), 1e-300)))
-    if not args.no_cpu_baseline:
-        log("cpu baseline")
-        threads = os.cpu_count() or 1
-        nsample = int(os.environ.get("CYLAG_CPU_SAMPLE", "200000"))
-        rate, dt = cpu_rate(c, params, nsample, 4, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{nsample} particles x 4 steps of the workload"}
-    print(json.dumps(line), flush=True)
+    main_form = forms[0]
+    line = None
+    if rank == 0:
+        wl = workload_line(args, args.workload, c, params, res, main_form, peak, peak_kind,
+                           world)
+        line = {"metric": METRIC, "value": wl["value"], "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if main_form == "fp64" else "f32+f64", "data": "synthetic"}
+        line.update({k: v for k, v in wl.items() if k not in ("value", "ms_per_step", "steps")})
+        if "e2e" in res[main_form]:
+            line["e2e"] = res[main_form]["e2e"]
+        if main_form == "mixed" and not args.no_oracle_error:
+            log("mixed form vs the FP64 oracle")
+            line["mixed_error_vs_oracle"] = oracle_subsample_error(
+                c, params, res["mixed"], args.warmup + args.steps,
+                max(1, len(c["position"]) // 50_000), threads)
+        if not args.no_cpu_baseline:
+            log("cpu baseline")
+            nsample = int(os.environ.get("CYLAG_CPU_SAMPLE", "200000"))
+            rate, dt = cpu_rate(c, params, nsample, 4, threads)
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": f"{nsample} particles x 4 steps of the workload"}
+    del res
+    # the other configurations of the metric, as legs of the same line: the
+    # 3D LSM2 and LSM3 workloads at their full sizes, and the serving mix on
+    # a shortened arrival window (p50/p99 latency); each in its own process,
+    # so that host memory is released between workloads
+    if args.legs and args.workload == "lsm1_2d" and world == 1 and rank == 0:
+        legs = {}
+        for wl_name, extra in (("lsm2_3d", ["--steps", str(args.leg_steps), "--no-e2e"]),
+                               ("lsm3_3d", ["--steps", str(args.leg_steps), "--no-e2e"]),
+                               ("serve", ["--serve-duration", str(args.leg_serve_duration),
+                                          "--precision", "mixed"])):
+            log(f"leg {wl_name}")
+            cmd = [sys.executable, str(ROOT / "bench.py"), "--workload", wl_name,
+                   "--warmup", str(args.warmup), "--legs", "0", "--no-cpu-baseline",
+                   "--sort-period", str(args.sort_period)] + extra
+            r = subprocess.run(cmd, stdout=subprocess.PIPE, text=True)
+            out = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not out:
+                legs[wl_name] = {"error": f"exit {r.returncode}"}
+                continue
+            d = json.loads(out[-1])
+            legs[wl_name] = {k: v for k, v in d.items()
+                             if k not in ("metric", "unit", "n_gpus", "higher_is_better",
+                                          "scaling", "vs_baseline", "data", "warmup")}
+        line["legs"] = legs
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     log("done")
 
 
@@ -492,10 +568,42 @@ def serve_cpu_rate(fs_case, threads, nsample=100_000, nsteps=4):
     return 2.0 / (1.0 / rates[0] + 1.0 / rates[1])
 
 
+def serve_once(fs, reqs, prec, local, chunk):
+    """Plays the requests in real time through one serving pool; per-request
+    latency (arrival -> result on the host), throughput over the wall time."""
+    import torch
+    from cylag_gb300.serve import DispersionServer, poisson_mix
+    work = sum(len(r.position) * r.horizon for r in reqs)
+    npart = sum(len(r.position) for r in reqs)
+    # pool: every particle of the mix fits (120 GB admission budget)
+    srv = DispersionServer(fs, precision=prec, capacity=max(npart, 1 << 20) + 32 * len(reqs),
+                           max_runs=len(reqs) + 8, device=local, hbm_budget=120 * 10**9)
+    warm = poisson_mix(rate=100.0, duration=0.05, seed=99, nmax=1e4, hmax=200)
+    srv.serve(warm, realtime=False)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    log(f"{prec}: serving")
+    t0 = time.perf_counter()
+    res = srv.serve(reqs, realtime=True, chunk=chunk)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r.latency for r in res])
+    queue = np.array([r.admitted - r.arrival for r in res])
+    out = {"value": work / wall, "wall_s": wall, "p50_s": float(np.percentile(lat, 50)),
+           "p99_s": float(np.percentile(lat, 99)), "max_s": float(lat.max()),
+           "admission_wait_p99_s": float(np.percentile(queue, 99)),
+           "steps": int(st["steps_issued"]), "clocks": clk, "completed": len(res)}
+    log(f"{prec}: {wall:.1f} s, p50 {out['p50_s']:.2f} s, p99 {out['p99_s']:.2f} s")
+    return out
+
+
 def run_serve(args):
     import torch
     from cylag_gb300 import synth
-    from cylag_gb300.serve import DispersionServer, poisson_mix
+    from cylag_gb300.serve import poisson_mix
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
     c = synth.couette_channel(npart=10)
@@ -506,30 +614,7 @@ def run_serve(args):
     npart = sum(len(r.position) for r in reqs)
     log(f"serving mix: {len(reqs)} requests, {npart:.3e} particles, {work:.3e} particle-steps")
     forms = [args.precision] if args.precision != "both" else ["mixed", "fp64"]
-    out = {}
-    for prec in forms:
-        # pool: every particle of the mix fits (120 GB admission budget)
-        srv = DispersionServer(fs, precision=prec, capacity=max(npart, 1 << 20) + 32 * len(reqs),
-                               max_runs=len(reqs) + 8, device=local, hbm_budget=120 * 10**9)
-        warm = poisson_mix(rate=100.0, duration=0.05, seed=99, nmax=1e4, hmax=200)
-        srv.serve(warm, realtime=False)
-        torch.cuda.synchronize()
-        clocks = ClockSampler(local)
-        clocks.start()
-        log(f"{prec}: serving")
-        t0 = time.perf_counter()
-        res = srv.serve(reqs, realtime=True, chunk=args.serve_chunk)
-        wall = time.perf_counter() - t0
-        clk = clocks.stop()
-        st = srv.stats()
-        srv.close()
-        lat = np.array([r.latency for r in res])
-        queue = np.array([r.admitted - r.arrival for r in res])
-        out[prec] = {"value": work / wall, "wall_s": wall, "p50_s": float(np.percentile(lat, 50)),
-                     "p99_s": float(np.percentile(lat, 99)), "max_s": float(lat.max()),
-                     "admission_wait_p99_s": float(np.percentile(queue, 99)),
-                     "steps": int(st["steps_issued"]), "clocks": clk, "completed": len(res)}
-        log(f"{prec}: {wall:.1f} s, p50 {out[prec]['p50_s']:.2f} s, p99 {out[prec]['p99_s']:.2f} s")
+    out = {prec: serve_once(fs, reqs, prec, local, args.serve_chunk) for prec in forms}
     if rank != 0:
         return
     m = out[forms[0]]

@@ -48,7 +48,7 @@ class FieldsDesc(C.Structure):
     _fields_ = [("dim", I32), ("nlayers", I32), ("npoints", I32), ("ntimes", I32),
                 ("times", P), ("elevation", P), ("velocity_x", P), ("velocity_y", P),
                 ("velocity_z", P), ("turbulent_energy", P), ("dissipation", P),
-                ("bottom", P)]
+                ("bottom", P), ("friction_model", I32), ("friction_coefficient", F64)]
 
 
 class Params(C.Structure):
@@ -73,7 +73,8 @@ class Params(C.Structure):
 class StateDesc(C.Structure):
     _fields_ = [("n", I32), ("position", P), ("velocity", P), ("fluid_velocity_seen", P),
                 ("last_position", P), ("last_velocity", P), ("tri", P), ("last_tri", P),
-                ("lowerlayer", P), ("tag", P), ("diameter", P), ("rng_state", P)]
+                ("lowerlayer", P), ("tag", P), ("diameter", P), ("rng_state", P),
+                ("depth", P)]
 
 
 class HostArrays(C.Structure):
@@ -103,9 +104,9 @@ SIGNATURES = [
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),
     ("cg_snapshot_txt", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_int64,
-                                  C.c_int32, P, P, P, P, P, P]),
+                                  C.c_int32, P, P, P, P, P, P, P]),
     ("cg_snapshot_vtk", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_int64,
-                                  C.c_int32, P, P, P, P, P, P]),
+                                  C.c_int32, P, P, P, P, P, P, P]),
     ("cg_run_step_host", C.c_int, [P, I32, C.POINTER(HostArrays), C.POINTER(HostArrays), I32, P]),
     ("cg_run_set_stranding_output", C.c_int, [P, C.c_int32]),
     ("cg_run_stranded", C.c_int, [P, P, C.POINTER(C.c_int32)]),

@@ -404,12 +404,9 @@ class LagrangianParticleSet:
         self.buoyancy_velocity_value = buoyancy_velocity
         self.additional_velocity = False
         self.additional_force = False
-        self.compute_depth = compute_depth
+        self.compute_depth = bool(compute_depth)
         if compute_depth and dim != 3:
             raise ValueError("compute_depth can only be True for 3D pset")
-        if compute_depth:
-            raise NotImplementedError("compute_depth is not built in the GPU step")
-        self.depth = None   # as the reference without compute_depth
         self.max_stranded = max_stranded if max_stranded is not None else self.npart
         self.stranded_count = 0
         self.stranded_positions = np.zeros((self.max_stranded, 3))
@@ -449,11 +446,73 @@ class LagrangianParticleSet:
         h["lowerlayer"] = np.zeros(n, dtype=np.int32)
         h["tag"] = np.arange(n, dtype=np.int32)
         h["diameter"] = np.full(n, float(particle_diameter))
+        if self.compute_depth:
+            # depth below the free surface (lagrangian_particle_set.pyx:212-219),
+            # set by the solver at initialization and after every step
+            h["depth"] = np.zeros(n)
         self.maxtag = n - 1
+        # new tags are maxtag + tag_stride, + 2 tag_stride, ...: 1 as in the
+        # reference; the rank count for a shard of a split set, so that the
+        # ranks' new tags (and so their PCG32 streams) never coincide
+        self.tag_stride = 1
         self._added = False     # entries set to tri = -2 since the run's last step
         self._host = h
         self._dev = None
         self._ctx = None
+
+    # ---- one rank's share of a set split across ranks -------------------------
+    def parallel_split(self, rank, world):
+        """Keeps this rank's share of the set, as the reference's parallel
+        solver splits it (solver_parallel.pyx:126-149 for the counts,
+        lagrangian_particle_set.pyx:449-520 for the arrays): the active
+        particles [offset, offset + count) with offset = rank * (na // world)
+        and the remainder to the last rank, in a pool of max(1, n // world)
+        entries (the remainder of the pool to the last rank), padded with
+        inactive entries.  Kept particles keep their tags, so their PCG32
+        streams are those of the unsplit run.  Unlike the reference, whose
+        ranks share one generator, the streams here follow the tags, so new
+        tags must not coincide across ranks: rank r draws them from
+        maxtag + r + 1, maxtag + r + 1 + world, ... (tag_stride = world),
+        starting with its padding entries.  Call before the Solver attaches."""
+        if self._dev is not None:
+            raise RuntimeError("parallel_split must come before the Solver attaches")
+        rank, world = int(rank), int(world)
+        if not 0 <= rank < world:
+            raise ValueError(f"rank {rank} outside [0, {world})")
+        n = self.npart
+        active = np.flatnonzero(self._host["tri"] != -1)
+        na = len(active)
+        npart0 = [max(1, n // world)] * world
+        npart0[-1] += n % world
+        npartp = [na // world] * world
+        npartp[-1] += na % world
+        offset, count = rank * npartp[0], npartp[rank]
+        new_n = max(npart0[rank], count)
+        pad = new_n - count
+        keep = active[offset:offset + count]
+        h = self._host
+        out = {}
+        for k, v in h.items():
+            fill = {"tri": -1, "last_tri": -1}.get(k, 0)
+            a = np.full((new_n,) + v.shape[1:], fill, dtype=v.dtype)
+            a[:count] = v[keep]
+            out[k] = a
+        out["tri"][:count] = -2             # awaiting initialization
+        out["last_tri"][:] = -1
+        out["lowerlayer"][:] = 0
+        out["last_position"][:count] = out["position"][:count]
+        out["last_velocity"][:count] = out["velocity"][:count]
+        base = self.maxtag
+        self.tag_stride = world
+        self.maxtag = base + rank + 1 - world
+        out["tag"][count:] = (self.maxtag + world * np.arange(1, pad + 1, dtype=np.int64)
+                              ).astype(np.int32)
+        self.maxtag += pad * world
+        self._host = out
+        self.npart = new_n
+        self.max_stranded = max(self.max_stranded, new_n)
+        self.stranded_positions = np.zeros((self.max_stranded, 3))
+        return self
 
     # ---- device attachment -----------------------------------------------------
     def _attach(self, ctx, device):
@@ -471,7 +530,8 @@ class LagrangianParticleSet:
         p = lambda k: d[k].data_ptr()
         return _lib.StateDesc(self.npart, p("position"), p("velocity"), p("fluid_velocity_seen"),
                               p("last_position"), p("last_velocity"), p("tri"), p("last_tri"),
-                              p("lowerlayer"), p("tag"), p("diameter"), p("rng_state"))
+                              p("lowerlayer"), p("tag"), p("diameter"), p("rng_state"),
+                              p("depth") if "depth" in d else None)
 
     def _sync(self):
         """Makes the device arrays the whole particle state and waits for
@@ -494,7 +554,8 @@ class LagrangianParticleSet:
     def _set(self, key, value):
         value = np.ascontiguousarray(value, dtype=np.float64 if key in
                                      ("position", "velocity", "fluid_velocity_seen",
-                                      "last_position", "last_velocity", "diameter") else np.int32)
+                                      "last_position", "last_velocity", "diameter",
+                                      "depth") else np.int32)
         if self._dev is None:
             self._host[key][...] = value
         else:
@@ -511,7 +572,7 @@ class LagrangianParticleSet:
         neg = (tag < 0).nonzero().flatten()
         if neg.numel() == 0:
             return
-        new, self.maxtag = retag(tag.cpu().numpy(), self.maxtag)
+        new, self.maxtag = retag(tag.cpu().numpy(), self.maxtag, self.tag_stride)
         torch = _torch()
         tag.copy_(torch.from_numpy(new).to(tag.device))
         torch.cuda.synchronize()
@@ -527,6 +588,12 @@ class LagrangianParticleSet:
     last_tri = property(lambda s: s._get("last_tri"))
     lowerlayer = property(lambda s: s._get("lowerlayer"))
     diameter = property(lambda s: s._get("diameter"), lambda s, v: s._set("diameter", v))
+
+    @property
+    def depth(self):
+        """Depth below the free surface of each particle (compute_depth sets
+        only; None otherwise, as the reference)."""
+        return self._get("depth") if self.compute_depth else None
 
     @property
     def volume(self):
@@ -589,7 +656,8 @@ class LagrangianParticleSet:
 
     # ---- particles added during the run ---------------------------------------
     _PAD = {"position": 0., "velocity": 0., "fluid_velocity_seen": 0., "last_position": 0.,
-            "last_velocity": 0., "tri": -1, "last_tri": 0, "lowerlayer": 0, "diameter": 0.}
+            "last_velocity": 0., "tri": -1, "last_tri": 0, "lowerlayer": 0, "diameter": 0.,
+            "depth": 0.}
 
     def _increase_pool_size(self, size):
         """lagrangian_particle_set.pyx:522-582: grows every array by
@@ -597,7 +665,8 @@ class LagrangianParticleSet:
         zero state) tagged maxtag+1, maxtag+2, ...; an attached run is
         pointed at the new arrays."""
         add = max(int(self.min_pool_size_update), int(size))
-        newtags = np.arange(self.maxtag + 1, self.maxtag + 1 + add, dtype=np.int32)
+        newtags = (self.maxtag + self.tag_stride *
+                   np.arange(1, add + 1, dtype=np.int64)).astype(np.int32)
         if self._dev is None:
             for k, v in self._host.items():
                 if k == "tag":
@@ -618,7 +687,7 @@ class LagrangianParticleSet:
                                      device=v.device)
                 self._dev[k] = torch.cat([v, pad], dim=0)
             torch.cuda.synchronize(v.device)
-        self.maxtag += add
+        self.maxtag += add * self.tag_stride
         self.npart += add
         solver = getattr(self, "_solver", None)
         if solver is not None and self._dev is not None:
@@ -743,9 +812,14 @@ class LagrangianParticleSet:
         d = self._get("diameter")
         d[idx] = 0.
         self._set("diameter", d)
+        if self.compute_depth:
+            d = self._get("depth")
+            d[idx] = 0.
+            self._set("depth", d)
         t = self._get("tag")
-        t[idx] = self.maxtag + 1 + np.arange(len(idx), dtype=np.int32)
-        self.maxtag += len(idx)
+        t[idx] = (self.maxtag + self.tag_stride *
+                  np.arange(1, len(idx) + 1, dtype=np.int64)).astype(np.int32)
+        self.maxtag += len(idx) * self.tag_stride
         self._set("tag", t)
 
 
@@ -766,20 +840,21 @@ def c_params(P, dim, density=1000., drag_model=1, drag_coef=0.44, added_mass=Fal
         added_mass_coef, buoyancy_model, buoyancy_value, precision, int(seed), int(sort_period))
 
 
-def retag(tag, maxtag):
+def retag(tag, maxtag, stride=1):
     """Deleted particles carry a negative marker (-1: deleted while being
     initialized, -2-it: deleted during iteration it); give them maxtag+1,
     maxtag+2, ... in deletion order then index order, as delete_single does
-    (lagrangian_particle_set.pyx:786-788).  Returns (tags, new maxtag)."""
+    (lagrangian_particle_set.pyx:786-788); with stride s (a shard of a split
+    set), maxtag+s, maxtag+2s, ...  Returns (tags, new maxtag)."""
     tag = np.array(tag, dtype=np.int32, copy=True)
     idx = np.nonzero(tag < 0)[0]
     if len(idx) == 0:
         return tag, maxtag
     order = np.lexsort((idx, -tag[idx]))
     new = np.empty(len(idx), dtype=np.int32)
-    new[order] = maxtag + 1 + np.arange(len(idx), dtype=np.int32)
+    new[order] = (maxtag + stride * np.arange(1, len(idx) + 1, dtype=np.int64)).astype(np.int32)
     tag[idx] = new
-    return tag, maxtag + len(idx)
+    return tag, maxtag + stride * len(idx)
 
 
 def upload_mesh_fields(L, ctx, field_set):
@@ -800,7 +875,8 @@ def upload_mesh_fields(L, ctx, field_set):
     fd = _lib.FieldsDesc(fs.dim, fs.nlayers, fs.npoints, fs.ntimes, ptr(fs.times),
                          ptr(fs.elevation), ptr(fs.velocity_x), ptr(fs.velocity_y),
                          ptr(fs.velocity_z), ptr(fs._opt.get("turbulent_energy")),
-                         ptr(fs._opt.get("dissipation")), ptr(fs._opt.get("bottom")))
+                         ptr(fs._opt.get("dissipation")), ptr(fs._opt.get("bottom")),
+                         int(fs.friction_model), float(fs.friction_coefficient))
     _lib.check(ctx, L.cg_fields_upload(ctx, C.byref(fd)))
     return keep
 
@@ -812,12 +888,16 @@ class Solver:
     ('fp64' plain form or 'mixed'), ``seed`` (PCG32 seed of every particle
     stream), ``device`` (CUDA ordinal), ``hbm_budget`` (bytes, 0 = none),
     ``sort_period`` (steps between re-sorts of the particles by element, 0 =
-    never; results do not depend on it).
+    never; results do not depend on it), ``shard`` ((rank, world): this
+    process steps rank's share of the particle set, split as the
+    reference's parallel solver splits it (LagrangianParticleSet.
+    parallel_split); its exit counts are this rank's, to be summed over
+    ranks, e.g. with cylag_gb300.shard.allreduce_sum).
     """
 
     def __init__(self, field_set, particle_set, parameters={}, sources=None,
                  control_sections=None, precision="fp64", seed=0, device=0, hbm_budget=0,
-                 sort_period=25):
+                 sort_period=25, shard=None):
         self.parameters = Parameters(parameters)
         self.parameters.check_values()
         P = self.parameters
@@ -830,11 +910,24 @@ class Solver:
         self.particle_set = particle_set
         self.field_set = field_set
         fs, ps = field_set, particle_set
+        # one rank of a particle set split across ranks (solver_parallel.pyx:113-179)
+        self.shard = None if shard is None else (int(shard[0]), int(shard[1]))
+        if self.shard is not None and self.shard[1] > 1:
+            ps.parallel_split(*self.shard)
+        # solver.pyx:122-132: 3D particles on 2D fields (pseudo-3D) need the
+        # free surface and the BOTTOM field
         if fs.dim != ps.dim:
             if fs.dim == 2 and ps.dim == 3:
-                raise NotImplementedError("pseudo-3D (2D fields, 3D particles) is not built in the GPU step")
-            raise ValueError(f"EulerianFieldSet dimension ({fs.dim}) does not match "
-                             f"LagrangianParticleSet set dimension ({ps.dim})")
+                if fs.fid_zs == -1 or fs.fid_zb == -1:
+                    raise ValueError(
+                        "2D EulerianFieldSet with 3D LagrangianParticleSet : EulerianFieldSet "
+                        "should contain free surface and bottom fields")
+                if P.model != 1:
+                    raise NotImplementedError(
+                        "pseudo-3D (2D fields, 3D particles) is built for LSM1 (model 1)")
+            else:
+                raise ValueError(f"EulerianFieldSet dimension ({fs.dim}) does not match "
+                                 f"LagrangianParticleSet set dimension ({ps.dim})")
         if P.frozen_eulerian_fields != 1 and P.final_time > fs.times[-1]:
             raise ValueError("final_time > EulerianFieldSet maximum time")
         fs.frozen_hydro = bool(P.frozen_eulerian_fields)

@@ -153,9 +153,20 @@ int check_params(cg_ctx* c, const cg_params* p) {
         return set_err(c, CG_EINVAL, "unknown precision %d", p->precision);
     if (p->model < 1 || p->model > 3)
         return set_err(c, CG_EINVAL, "model %d is not built in this library (1, 2, 3)", p->model);
-    if (p->dim != c->fdim)
-        return set_err(c, CG_EINVAL, "particle dim %d != field dim %d (pseudo-3D not built)",
-                       p->dim, c->fdim);
+    // solver.pyx:122-132; 3D particles on 2D fields (pseudo-3D) for LSM1
+    if (p->dim != c->fdim) {
+        if (!(c->fdim == 2 && p->dim == 3))
+            return set_err(c, CG_EINVAL,
+                           "EulerianFieldSet dimension (%d) does not match LagrangianParticleSet "
+                           "set dimension (%d)", c->fdim, p->dim);
+        if (!c->has_bottom)
+            return set_err(c, CG_EINVAL,
+                           "2D EulerianFieldSet with 3D LagrangianParticleSet : EulerianFieldSet "
+                           "should contain free surface and bottom fields");
+        if (p->model != 1)
+            return set_err(c, CG_EINVAL,
+                           "pseudo-3D (2D fields, 3D particles) is built for LSM1 only");
+    }
     // parameters.pyx:208-279
     if (p->model == 1 && (p->time_scheme < 1 || p->time_scheme > 4))
         return set_err(c, CG_EINVAL, "LSM1 time_scheme must be 1..4");
@@ -217,6 +228,8 @@ void make_dev_params(const cg_ctx* c, const cg_params* p, DevParams& d) {
     d.edge_opt = p->lsm3_edge_opt;
     d.tl_h = p->tl_horizontal;
     d.tl_v = p->tl_vertical;
+    d.friction_model = c->friction_model;
+    d.friction_coef = c->friction_coef;
     // lagrangian_particle_set.pyx:361-375
     {
         double rhop = p->particle_density, rho0 = p->water_density;
@@ -268,8 +281,9 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     const size_t n = (size_t)(n32 > 0 ? n32 : 0);
     q.n = n;
     q.dim = p->dim;
-    // deferred 2D walk: LSM1 (its queue entry carries no velocities)
-    q.use_queue = c->fdim == 2 && n > 0 && p->model == 1;
+    // deferred 2D walk: LSM1 2D particles (its queue entry carries no
+    // velocities and no elevation)
+    q.use_queue = p->dim == 2 && n > 0 && p->model == 1;
     q.queue_bytes = q.use_queue ? 256 + n * sizeof(WalkEntry) : 0;
     // element sort: keys tri * layers + layer (+1 for inactive) within 4096
     // scan tiles of 4096; the optional working arrays are those the model
@@ -649,6 +663,11 @@ int cg_fields_upload(cg_ctx* c, const cg_fields_desc* d) {
     c->nlayers = d->nlayers;
     c->npoints = d->npoints;
     c->has_keps = d->turbulent_energy && d->dissipation;
+    c->has_bottom = d->bottom != nullptr;
+    if (d->friction_model < 0 || d->friction_model > 3)
+        return set_err(c, CG_EINVAL, "Invalid friction model %d", d->friction_model);
+    c->friction_model = d->friction_model;
+    c->friction_coef = d->friction_coefficient;
     c->have_fields = true;
     return CG_OK;
 }
@@ -687,7 +706,9 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
         return set_err(c, CG_EINVAL, "final_time > EulerianFieldSet maximum time");
     CUDA_TRY(c, cudaSetDevice(c->device));
 
-    size_t rec_bytes = record_bytes(c->fdim, p->precision) * c->frames.nnodes;
+    // the record layout follows the particles' dimension (3D particles on 2D
+    // fields read the 3D layout with one layer, the bed in its ZB slot)
+    size_t rec_bytes = record_bytes(p->dim, p->precision) * c->frames.nnodes;
     // LSM2/LSM3 with k-epsilon diffusion read k and eps themselves
     bool need_turb = p->model >= 2 && (p->diffusion_model == 2 || p->diffusion_model == 3);
     size_t turb_bytes = need_turb ? 2 * c->frames.nnodes * (p->precision ? 4 : 8) : 0;
@@ -732,6 +753,7 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     st.tag = s->tag;
     st.diameter = s->diameter;
     st.rng = s->rng_state;
+    st.depth = (s->depth && r->prm.dim == 3) ? s->depth : nullptr;
 
     // simutime.pyx:46-75
     r->time = p->initial_time;
@@ -794,7 +816,7 @@ static int time_interpolation(cg_run* r, double time) {
     if (r->frozen) {
         if (!r->fields_ready) {
             launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
-                     c->stream);
+                     r->prm.dim, c->stream);
             CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes,
                                         cudaMemcpyDeviceToDevice, c->stream));
             r->fields_ready = true;
@@ -811,7 +833,7 @@ static int time_interpolation(cg_run* r, double time) {
         return set_err(c, CG_EINVAL, "Time interpolation failed: duplicate times at record %d", rec);
     double tf = (time - c->times[rec + 1]) / dt;
     launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
-                 c->stream);
+                 r->prm.dim, c->stream);
     r->fields_ready = true;
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -824,7 +846,7 @@ static int ensure_fields(cg_run* r) {
     // EulerianFieldSet._init_tmp (743-776): both temps hold record 0, then
     // Solver.__init__ interpolates at initial_time (solver.pyx:190-191).
     launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
-                     c->stream);
+                     r->prm.dim, c->stream);
     CUDA_TRY(c, cudaMemcpyAsync(r->prev.p, r->cur.p, r->cur.bytes, cudaMemcpyDeviceToDevice,
                                 c->stream));
     return time_interpolation(r, r->prm.initial_time);
@@ -943,6 +965,12 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;
+    }
+    if (r->st.depth) {
+        // solver.pyx:526-538 after the call's last step
+        launch_depth(r->prm.precision, c->mesh, field_view(r),
+                     r->resident ? sorted_view(r->st, r->sb) : r->st, c->stream);
+        launches += 1;
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     double tot = 0.;
@@ -1087,6 +1115,7 @@ int cg_run_resize(cg_run* r, const cg_state_desc* s) {
     st.tag = s->tag;
     st.diameter = s->diameter;
     st.rng = s->rng_state;
+    st.depth = (s->depth && r->prm.dim == 3) ? s->depth : nullptr;
     return alloc_strand(c, r);
 }
 
@@ -1207,6 +1236,10 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
         launches += r->st.n > 0 ? (wq.e ? 2 : 1) : 0;
         r->time += r->prm.time_step;
         r->iteration += 1;
+    }
+    if (r->st.depth) {
+        launch_depth(r->prm.precision, c->mesh, field_view(r), r->st, c->stream);
+        launches += 1;
     }
     r->last_launches = launches;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1360,6 +1393,11 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
         }
         r->time += r->prm.time_step;
         r->iteration += 1;
+    }
+    if (r->st.depth) {
+        // after every chunk's last step (the device state of the whole pool)
+        for (int j = 0; j < nch; ++j) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, ev_comp[j], 0));
+        launch_depth(r->prm.precision, c->mesh, field_view(r), r->st, c->stream);
     }
     CUDA_TRY(c, cudaStreamSynchronize(r->d2h));
     CUDA_TRY(c, cudaStreamSynchronize(r->h2d));

@@ -127,7 +127,21 @@ struct DevParams {
     int strand_cap;
     int* strand_count;
     StrandRec* strand_rec;
+    // the field set's friction law (pseudo-3D log-law correction,
+    // eulerian_field_set.pyx:1957-1993)
+    int friction_model;
+    double friction_coef;
 };
+
+// x**y (x > 0) as the compiled reference evaluates it: Cython gives
+// double ** double a complex result, computed by the C library's complex
+// power exp(y * log x) through the complex logarithm, whose real part is
+// log1p((x-1)(x+1))/2 for 0.5 <= x < 2 and log(x) elsewhere.
+template <typename R>
+__device__ __forceinline__ R cpow_re(R x, R y) {
+    R L = (x >= R(0.5) && x < R(2.)) ? log1p((x - R(1.)) * (x + R(1.))) / R(2.) : log(x);
+    return exp(y * L);
+}
 
 __device__ __forceinline__ void record_strand(const DevParams& p, int step, int index, double x,
                                               double y, double z) {
@@ -149,6 +163,7 @@ struct DevState {
     int* __restrict__ tag;
     double* __restrict__ diameter;
     uint64_t* __restrict__ rng;
+    double* __restrict__ depth;   // depth below the free surface (compute_depth) or nullptr
     // sorted runs: pos/tri/tag/rng are working copies in sorted order and
     // slot[i] is the caller's index of working particle i, where the
     // remaining arrays live, except those flagged in `work` (W_*), which are
@@ -709,7 +724,9 @@ __device__ __forceinline__ P1 p1_at(const DevMesh& m, int k, double x, double y)
 // node record accessors --------------------------------------------------------
 template <int DIM> struct Slots;
 template <> struct Slots<2> { static constexpr int NF = 4, UX = 0, UY = 1, K = 2, ZS = 3, UZ = -1; };
-template <> struct Slots<3> { static constexpr int NF = 8, ZS = 0, UX = 1, UY = 2, UZ = 3, K = 4; };
+// 3D records also carry the bed elevation (BOTTOM) for 3D particles on 2D
+// fields (pseudo-3D), whose records use this layout with one layer
+template <> struct Slots<3> { static constexpr int NF = 8, ZS = 0, UX = 1, UY = 2, UZ = 3, K = 4, ZB = 5; };
 
 template <int DIM, typename FT>
 __device__ __forceinline__ double nodev(const FT* __restrict__ f, int node, int slot) {

@@ -38,6 +38,9 @@ struct cg_ctx {
     std::vector<double> times;
     int fdim = 2, nlayers = 1, npoints = 0;
     bool has_keps = false;
+    bool has_bottom = false;
+    int friction_model = 1;
+    double friction_coef = 40.;
 };
 
 inline int set_err(cg_ctx* c, int code, const char* fmt, ...) {

@@ -38,9 +38,15 @@ struct FieldView {
 
 // Time interpolation + nodal diffusivity into the packed per-node record
 // (eulerian_field_set.pyx:866-938 and 1995-1997); turb != nullptr also
-// receives {k, eps} per node.  frozen: copy record 0.
+// receives {k, eps} per node.  frozen: copy record 0.  rdim: the record
+// layout (the particles' dimension: 3 for 3D particles on 2D fields)
 void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac_keps,
-                  void* cur, void* turb, int precision, cudaStream_t st);
+                  void* cur, void* turb, int precision, int rdim, cudaStream_t st);
+
+// depth below the free surface of every active particle of a 3D run with a
+// depth array (solver.pyx:526-538)
+void launch_depth(int precision, const DevMesh& m, const FieldView& fv, const DevState& s,
+                  cudaStream_t st);
 
 // One fused step over every particle of a run (plain FP64 form).
 // wq.e == nullptr: walk inline; else queue leavers and run launch_walk after.

@@ -27,7 +27,7 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
     }
     DevFields<float> f = fv.as<float>();
     WalkQueue none{nullptr, nullptr};
-    if (fv.dim == 2) {
+    if (p.pdim == 2) {
         // persistent grid: one wave of resident blocks.  The Euler scheme with
         // a walk queue (EQ) has no out-of-line calls and runs 4 blocks of 256
         // per SM (64 registers); the other forms 3 (80).  Split positions on

@@ -41,7 +41,7 @@ __global__ void blend_kernel(DevFrames fr, int rec, double tf, int frozen, doubl
     r[S::K] = (FT)K;
     if (DIM == 3) {
         r[Slots<3>::UZ] = (FT)val(RF_UZ);
-        r[5] = (FT)0;
+        r[Slots<3>::ZB] = (FT)val(RF_ZB);   // BOTTOM (2D fields: pseudo-3D runs)
         r[6] = (FT)0;
         r[7] = (FT)0;
     }
@@ -78,7 +78,7 @@ __global__ void blend32_kernel(DevFrames fr, int rec, float tf, int frozen, floa
     r[S::K] = fac * kt * kt / fmaxf(ep, 1e-16f);   // eulerian_field_set.pyx:1995-1997
     if (DIM == 3) {
         r[Slots<3>::UZ] = val(RF_UZ);
-        r[5] = 0.f;
+        r[Slots<3>::ZB] = val(RF_ZB);
         r[6] = 0.f;
         r[7] = 0.f;
     }
@@ -89,23 +89,23 @@ __global__ void blend32_kernel(DevFrames fr, int rec, float tf, int frozen, floa
 }
 
 void launch_blend(const DevFrames& fr, int rec, double tf, bool frozen, double fac, void* cur,
-                  void* turb, int precision, cudaStream_t st) {
+                  void* turb, int precision, int rdim, cudaStream_t st) {
     int bs = 256;
     int64_t nb = (fr.nnodes + bs - 1) / bs;
     if (precision == 0) {
         double *c = (double*)cur, *t = (double*)turb;
-        if (fr.dim == 2) blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
+        if (rdim == 2) blend_kernel<2, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
         else blend_kernel<3, double><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
     } else if (fr.frames32) {
         float *c = (float*)cur, *t = (float*)turb;
-        if (fr.dim == 2)
+        if (rdim == 2)
             blend32_kernel<2><<<nb, bs, 0, st>>>(fr, rec, (float)tf, frozen, (float)fac, c, t);
         else
             blend32_kernel<3><<<nb, bs, 0, st>>>(fr, rec, (float)tf, frozen, (float)fac, c, t);
     } else {
         // FP64 interpolation, rounded once to the FP32 record
         float *c = (float*)cur, *t = (float*)turb;
-        if (fr.dim == 2) blend_kernel<2, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
+        if (rdim == 2) blend_kernel<2, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
         else blend_kernel<3, float><<<nb, bs, 0, st>>>(fr, rec, tf, frozen, fac, c, t);
     }
 }
@@ -121,7 +121,7 @@ void launch_step_plain(const DevMesh& m, const FieldView& fv, const DevParams& p
         return;
     }
     DevFields<double> f = fv.as<double>();
-    if (fv.dim == 2) {
+    if (p.pdim == 2) {
         launch_lsm1_kernel<2, double>(m, f, p, s, wq, aux, step_index, stats, err, st);
     } else {
         WalkQueue none{nullptr, nullptr};
@@ -174,6 +174,7 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
             s.last_vel[(size_t)i * D + d] = 0.;
         }
         s.diameter[i] = 0.;
+        if (s.depth) s.depth[i] = 0.;
         s.tri[i] = -1;
         s.last_tri[i] = -1;
         s.lowerlayer[i] = 0;
@@ -183,17 +184,28 @@ __global__ void init_kernel(DevMesh m, DevFields<FT> f, DevParams p, DevState s,
     int ll = 0;
     if (DIM == 3) {
         double zs = q.zs_at(k, f.nlayers - 1, q.x[0], q.x[1]);
-        double zb = q.zs_at(k, 0, q.x[0], q.x[1]);
+        double zb = q.zb_at(k, q.x[0], q.x[1]);
         ll = lower_layer_index(f.nlayers, zs, zb, q.x[2]);
         if (q.x[2] < zb) q.x[2] = zb + EPSILON;
         if (q.x[2] > zs) q.x[2] = zs - EPSILON;
         s.pos[(size_t)i * D + 2] = q.x[2];
         s.lowerlayer[i] = ll;
+        if (s.depth) s.depth[i] = zs - q.x[2];   // solver.pyx:325-332
     }
     s.tri[i] = k;
     if (vinit == 1) {
         double ux, uy, uz;
-        q.velocity(k, ll, q.x[0], q.x[1], DIM == 3 ? q.x[2] : 0., ux, uy, uz);
+        if (DIM == 3 && f.dim == 2) {
+            // 2D fields: the depth-averaged velocity, no pseudo-3D
+            // correction; the vertical components keep their values
+            // (solver.pyx:334-340, 366-372)
+            P1 q1 = p1_at(m, k, q.x[0], q.x[1]);
+            ux = p1_eval<DIM>(f.cur, 0, q1, Slots<3>::UX);
+            uy = p1_eval<DIM>(f.cur, 0, q1, Slots<3>::UY);
+            uz = s.vel[(size_t)i * D + 2];
+        } else {
+            q.velocity(k, ll, q.x[0], q.x[1], DIM == 3 ? q.x[2] : 0., ux, uy, uz);
+        }
         double u[3] = {ux, uy, uz}, w[3] = {ux, uy, uz};
         if (p.model >= 2) {
             // stationary fluctuations from the particle's own stream
@@ -235,13 +247,36 @@ void launch_init(int precision, const DevMesh& m, const FieldView& fv, const Dev
     if (nb == 0) return;
     if (precision != 0) {
         DevFields<float> f = fv.as<float>();
-        if (fv.dim == 2) init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
+        if (p.pdim == 2) init_kernel<2, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
         else init_kernel<3, float><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
         return;
     }
     DevFields<double> f = fv.as<double>();
-    if (fv.dim == 2) init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
+    if (p.pdim == 2) init_kernel<2, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
     else init_kernel<3, double><<<nb, bs, 0, st>>>(m, f, p, s, vinit, del_mark, err);
+}
+
+// solver.pyx:526-538: depth below the free surface of every active 3D
+// particle, from its end-of-step position and element and the step's
+// fields (a sorted run's working copies, written to the caller's slots)
+template <typename FT>
+__global__ void depth_kernel(DevMesh m, DevFields<FT> f, DevState s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    const int k = s.tri[i];
+    if (k < 0) return;
+    const double px = s.pos[(size_t)i * 3], py = s.pos[(size_t)i * 3 + 1];
+    const P1 q = p1_at(m, k, px, py);
+    const double zs = p1_eval<3>(f.cur, (f.nlayers - 1) * f.npoints, q, Slots<3>::ZS);
+    s.depth[aux_index(s, i)] = zs - s.pos[(size_t)i * 3 + 2];
+}
+
+void launch_depth(int precision, const DevMesh& m, const FieldView& fv, const DevState& s,
+                  cudaStream_t st) {
+    const int bs = 256, nb = (s.n + bs - 1) / bs;
+    if (nb == 0 || s.depth == nullptr) return;
+    if (precision != 0) depth_kernel<float><<<nb, bs, 0, st>>>(m, fv.as<float>(), s);
+    else depth_kernel<double><<<nb, bs, 0, st>>>(m, fv.as<double>(), s);
 }
 
 // ---------------------------------------------------------------------------

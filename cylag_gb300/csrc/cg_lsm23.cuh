@@ -20,15 +20,6 @@ namespace cg {
 template <typename FT> struct ArithOf { using type = double; };
 template <> struct ArithOf<float> { using type = float; };
 
-// x**y (x > 0) as the compiled reference evaluates it: Cython gives
-// double ** double a complex result, computed by the C library's complex
-// power exp(y * log x) through the complex logarithm, whose real part is
-// log1p((x-1)(x+1))/2 for 0.5 <= x < 2 and log(x) elsewhere.
-template <typename R>
-__device__ __forceinline__ R cpow_re(R x, R y) {
-    R L = (x >= R(0.5) && x < R(2.)) ? log1p((x - R(1.)) * (x + R(1.))) / R(2.) : log(x);
-    return exp(y * L);
-}
 
 // lagrangian_particle_set.pyx:790-832.  The Almedeij powers overflow FP32
 // at small Re: that law is evaluated in FP64 in both forms.

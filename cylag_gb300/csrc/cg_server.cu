@@ -240,7 +240,7 @@ int cg_server_create(cg_ctx* c, int32_t precision, int64_t capacity, int32_t max
     CUDA_TRY(c, cudaMemsetAsync(s->err_buf.p, 0, (size_t)max_runs * 4, c->stream));
     // frozen field records (record 0) and, with k-epsilon fields, {k, eps}
     launch_blend(c->frames, 0, 1.0, true, CMU / schmidt_number, s->rec_buf.p, s->turb_buf.p,
-                 precision, c->stream);
+                 precision, 2, c->stream);
     CUDA_TRY(c, cudaGetLastError());
     CUDA_TRY(c, cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking));
     for (int k = 0; k < 2; ++k) {

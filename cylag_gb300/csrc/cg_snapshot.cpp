@@ -88,6 +88,7 @@ struct Snap {
     const double* vel;
     const double* fvs;
     const double* diam;
+    const double* depth;
 };
 
 // chunk boundaries over [0, n) and the active indices of each
@@ -131,11 +132,12 @@ extern "C" {
 
 int cg_snapshot_txt(const char* path, int32_t dim, int32_t model, double time, int64_t iteration,
                     int32_t n, const int32_t* tri, const int32_t* tag, const double* pos,
-                    const double* vel, const double* fvs, const double* diameter) {
+                    const double* vel, const double* fvs, const double* diameter,
+                    const double* depth) {
     if (!path || (dim != 2 && dim != 3) || n < 0 || (n > 0 && (!tri || !tag || !pos || !vel)) ||
         (model >= 2 && n > 0 && !fvs))
         return CG_EINVAL;
-    Snap s{dim, model, n, tri, tag, pos, vel, fvs, diameter};
+    Snap s{dim, model, n, tri, tag, pos, vel, fvs, diameter, depth};
     std::string head;
     put_fmt(head, "Time = %.8f, ", time);
     put_int(head, "Iter = %16lld, ", (long long)iteration);
@@ -163,6 +165,7 @@ int cg_snapshot_txt(const char* path, int32_t dim, int32_t model, double time, i
                 else o += "0, ";
             }
             if (s.diam) put_fmt(o, "%.8e, ", s.diam[j]);
+            if (s.depth) put_fmt(o, "%.8e, ", s.depth[j]);
             o += '\n';
         }
     });
@@ -171,11 +174,12 @@ int cg_snapshot_txt(const char* path, int32_t dim, int32_t model, double time, i
 
 int cg_snapshot_vtk(const char* path, int32_t dim, int32_t model, double time, int64_t iteration,
                     int32_t n, const int32_t* tri, const int32_t* tag, const double* pos,
-                    const double* vel, const double* fvs, const double* diameter) {
+                    const double* vel, const double* fvs, const double* diameter,
+                    const double* depth) {
     if (!path || (dim != 2 && dim != 3) || n < 0 || (n > 0 && (!tri || !tag || !pos || !vel)) ||
         (model >= 2 && n > 0 && !fvs))
         return CG_EINVAL;
-    Snap s{dim, model, n, tri, tag, pos, vel, fvs, diameter};
+    Snap s{dim, model, n, tri, tag, pos, vel, fvs, diameter, depth};
     const int na = count_active(s);
     // one pass per section, each section formatted in parallel
     auto section = [&](auto&& line) {
@@ -239,6 +243,13 @@ int cg_snapshot_vtk(const char* path, int32_t dim, int32_t model, double time, i
     if (model >= 2) {
         out += "VECTORS fluid_velocity_seen FLOAT\n";
         out += section([&](int j, std::string& o) { vec3(s.fvs, j, o); });
+    }
+    if (s.depth) {
+        out += "SCALARS depth FLOAT\nLOOKUP_TABLE default\n";
+        out += section([&](int j, std::string& o) {
+            put_repr(o, s.depth[j]);
+            o += '\n';
+        });
     }
     return write_all(path, "wb", out);
 }

@@ -56,6 +56,17 @@ struct Particle {
             ux = p1_eval<DIM>(f.cur, 0, q, S::UX);
             uy = p1_eval<DIM>(f.cur, 0, q, S::UY);
             uz = 0.;
+        } else if (f.dim == 2) {
+            // 3D particle on 2D fields: depth-averaged velocity with the
+            // pseudo-3D corrections (update_state_lsm1.pyx:144-163)
+            ux = p1_eval<DIM>(f.cur, 0, q, S::UX);
+            uy = p1_eval<DIM>(f.cur, 0, q, S::UY);
+            uz = 0.;
+            double w, hor;
+            pseudo_3d_corrections(q, pz, ux, uy, w, hor);
+            uz += w;
+            ux *= hor;
+            uy *= hor;
         } else {
             if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ux = uy = uz = 0.; return; }
             int jl = l * f.npoints, ju = (l + 1) * f.npoints;
@@ -72,14 +83,60 @@ struct Particle {
         }
     }
 
-    // eulerian_field_set.pyx:1117-1182 (3D fields)
+    // eulerian_field_set.pyx:1957-1993: friction coefficient of the depth h
+    __device__ double friction_calc(double h) {
+        const double fc = p.friction_coef;
+        if (p.friction_model == 0) return 2. * GRAV / (fc * fc);   // Chezy
+        if (p.friction_model == 1)                                  // Strickler
+            return 2. * GRAV / (fc * fc) / cpow_re(fmax(EPSILON, h), 1. / 3.);
+        if (p.friction_model == 2)                                  // Manning
+            return 2. * GRAV * (fc * fc) / cpow_re(fmax(EPSILON, h), 1. / 3.);
+        double aux = h * 11.036 / fc;                               // Nikuradse
+        if (!(aux > 1.001)) aux = 1.001;
+        const double r = log(aux) / KAPPA;
+        return 2. / (r * r);
+    }
+
+    // eulerian_field_set.pyx:1887-1955 (with 1581-1642 for dzs/dt): the
+    // vertical velocity w that keeps the relative elevation of a particle
+    // advected by the log-law velocity, and the log-law factor of the
+    // depth-averaged velocity at height pz (3D particle, 2D fields)
+    __device__ void pseudo_3d_corrections(const P1& q, double pz, double ux, double uy,
+                                          double& w, double& hor) {
+        using S = Slots<3>;
+        const double zs = p1_eval<DIM>(f.cur, 0, q, S::ZS);
+        const double zb = p1_eval<DIM>(f.cur, 0, q, S::ZB);
+        const double h = fmax(EPSILON, zs - zb);
+        const double sigma = fmin(1., fmax(0., (pz - zb) / h));
+        const double Cf = friction_calc(h);
+        const double z0 = fmax(EPSILON, h * exp(-(1. + KAPPA / sqrt(Cf / 2.))));
+        hor = (pz - zb <= z0) ? 0.0 : log((pz - zb) / z0) / (log(h / z0) - 1.);
+        const double uc = ux * hor, vc = uy * hor;
+        const double dzsdx = p1_gx<DIM>(f.cur, 0, q, S::ZS), dzsdy = p1_gy<DIM>(f.cur, 0, q, S::ZS);
+        const double dzbdx = p1_gx<DIM>(f.cur, 0, q, S::ZB), dzbdy = p1_gy<DIM>(f.cur, 0, q, S::ZB);
+        // frozen fields or the first interpolation: no previous surface
+        double dzsdt = 0.;
+        if (f.prev_valid) dzsdt = (zs - p1_eval<DIM>(f.prev, 0, q, S::ZS)) / p.dt;
+        w = (1. - sigma) * (uc * dzbdx + vc * dzbdy) + sigma * (dzsdt + uc * dzsdx + vc * dzsdy);
+    }
+
+    // eulerian_field_set.pyx:1117-1182; 2D fields (pseudo-3D): the bed is
+    // the BOTTOM field and the point is in layer 0 unless outside the column
     __device__ int z_localize(int k, double px, double py, double pz) {
         if (k == -1) return PART_LOC_O;
         P1 q = p1_at(m, k, px, py);
         int nl = f.nlayers;
-        double zbp = p1_eval<DIM>(f.cur, 0, q, Slots<DIM>::ZS);
-        double zsp = p1_eval<DIM>(f.cur, (nl - 1) * f.npoints, q, Slots<DIM>::ZS);
-        int l = lower_layer_index(nl, zsp, zbp, pz);
+        double zbp, zsp;
+        int l;
+        if (DIM == 3 && f.dim == 2) {
+            zbp = p1_eval<DIM>(f.cur, 0, q, Slots<3>::ZB);
+            zsp = p1_eval<DIM>(f.cur, 0, q, Slots<DIM>::ZS);
+            l = 0;
+        } else {
+            zbp = p1_eval<DIM>(f.cur, 0, q, Slots<DIM>::ZS);
+            zsp = p1_eval<DIM>(f.cur, (nl - 1) * f.npoints, q, Slots<DIM>::ZS);
+            l = lower_layer_index(nl, zsp, zbp, pz);
+        }
         if (pz < zbp) l = PART_LOC_B;
         else if (pz > zsp) l = PART_LOC_A;
         return l;
@@ -91,11 +148,21 @@ struct Particle {
         return p1_eval<DIM>(f.cur, l * f.npoints, q, Slots<DIM>::ZS);
     }
 
+    // bed elevation: the bottom layer's elevation, or on 2D fields the
+    // BOTTOM field (solver.pyx:284-297)
+    __device__ double zb_at(int k, double px, double py) {
+        if (DIM == 3 && f.dim == 2) {
+            P1 q = p1_at(m, k, px, py);
+            return p1_eval<DIM>(f.cur, 0, q, Slots<3>::ZB);
+        }
+        return zs_at(k, 0, px, py);
+    }
+
     // eulerian_field_set.pyx:1644-1763
     __device__ void diffusivity_q(const P1& q, int l, double pz, double& K, double& dKdx,
                                   double& dKdy, double& dKdz) {
         using S = Slots<DIM>;
-        if (DIM == 2) {
+        if (DIM == 2 || f.dim == 2) {
             double kn0 = nodev<DIM>(f.cur, q.i0, S::K), kn1 = nodev<DIM>(f.cur, q.i1, S::K),
                    kn2 = nodev<DIM>(f.cur, q.i2, S::K);
             double Kp = kn0 * q.f0 + kn1 * q.f1 + kn2 * q.f2;
@@ -582,6 +649,7 @@ struct Particle {
                 s.last_vel[(size_t)ix * D + d] = 0.;
             }
             s.diameter[id] = 0.;
+            if (s.depth) s.depth[a] = 0.;
             s.tri[i] = -1;
             s.last_tri[ix] = -1;
             s.lowerlayer[il] = 0;
@@ -704,7 +772,7 @@ struct Particle {
             for (int side = 0; side < 2; ++side) {
                 int want = side == 0 ? PART_LOC_B : PART_LOC_A;
                 if (!(ll == want && tri != PART_LOC_O)) continue;
-                double zbp = zs_at(tri, 0, x[0], x[1]);
+                double zbp = zb_at(tri, x[0], x[1]);
                 double zsp = zs_at(tri, f.nlayers - 1, x[0], x[1]);
                 double hp = fmax(0., zsp - zbp);
                 if (side == 0) {

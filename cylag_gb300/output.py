@@ -45,12 +45,13 @@ def _ptr(a):
 def write_snapshot(arrays, dim, model, time, iteration, outputdir, file_name, fmt):
     """write_particles.pyx:52-91 on host copies of the particle arrays
     (``arrays``: tri, tag, position, velocity, fluid_velocity_seen,
-    diameter or None)."""
+    diameter or None, and optionally depth or None)."""
     L = _lib.load()
-    tri, tag, pos, vel, fvs, diam = arrays
+    tri, tag, pos, vel, fvs, diam = arrays[:6]
+    depth = arrays[6] if len(arrays) > 6 else None
     n = len(tri)
     args = (int(dim), int(model), float(time), int(iteration), n, _ptr(tri), _ptr(tag),
-            _ptr(pos), _ptr(vel), _ptr(fvs), _ptr(diam))
+            _ptr(pos), _ptr(vel), _ptr(fvs), _ptr(diam), _ptr(depth))
     if fmt in ("vtk", "all"):
         path = os.path.join(outputdir, f"{file_name}_{iteration}.vtk").encode()
         if L.cg_snapshot_vtk(path, *args) != 0:
@@ -74,7 +75,8 @@ class SnapshotWriter:
         c = np.ascontiguousarray
         arrays = (c(pset.tri), c(pset.tag), c(pset.position), c(pset.velocity),
                   c(pset.fluid_velocity_seen) if self.model >= 2 else None,
-                  None if pset.diameter_distribution == "monodisperse" else c(pset.diameter))
+                  None if pset.diameter_distribution == "monodisperse" else c(pset.diameter),
+                  c(pset.depth) if pset.compute_depth else None)
         p = self.p
         self._pending.append(self._ex.submit(write_snapshot, arrays, pset.dim, self.model, time,
                                              iteration, p.output_rep, p.output_file_name,

@@ -74,7 +74,12 @@ typedef struct {
     const double *velocity_x, *velocity_y, *velocity_z; /* ids 1-3 */
     const double *turbulent_energy;  /* 'TURBULENT ENERG.' */
     const double *dissipation;       /* 'DISSIPATION' */
-    const double *bottom;            /* 'BOTTOM' */
+    const double *bottom;            /* 'BOTTOM' (required for 3D particles on 2D fields) */
+    /* friction law of the pseudo-3D log-law profile (EulerianFieldSet's
+     * friction_model 0 Chezy, 1 Strickler, 2 Manning, 3 Nikuradse, and
+     * friction_coefficient; eulerian_field_set.pyx:125-138, 1957-1993) */
+    int32_t friction_model;
+    double friction_coefficient;
 } cg_fields_desc;
 
 /* Parameters (cylag/cylag_dico.py:9-51, cylag/core/parameters.pyx:116-195)
@@ -113,6 +118,10 @@ typedef struct {
     int32_t *tri, *last_tri, *lowerlayer, *tag;          /* [n] */
     double *diameter;                                    /* [n] */
     uint64_t *rng_state;                                 /* [n] PCG32 state */
+    double *depth;   /* [n] depth below the free surface, set at initialization and
+                        after every call for active particles, zeroed at deletion
+                        (LagrangianParticleSet.compute_depth, solver.pyx:325-332,
+                        526-538; 3D particles), or NULL */
 } cg_state_desc;
 
 /* ---- context ---------------------------------------------------------- */
@@ -284,18 +293,20 @@ int cg_run_stranded(const cg_run *run, double *xyz, int32_t *count);
 /* parameters['output_file'] every output_printout_period iterations
  * (write_particles.pyx:52-91).  Host arrays of the whole pool (n entries;
  * an entry is written when tri != -1, i.e. active); fvs is read when
- * model >= 2, diameter (may be NULL) adds the polydisperse column.
+ * model >= 2, diameter (may be NULL) adds the polydisperse column, depth
+ * (may be NULL) the compute_depth column (writer_txt.pyx:177-178,
+ * writer_vtk.pyx:277-283).
  * cg_snapshot_txt appends one block to <path> (writer_txt.pyx:25-180);
  * cg_snapshot_vtk writes <path> (writer_vtk.pyx:25-304).  Byte-identical to
  * the reference's files; formatted on all host threads.  No device work. */
 int cg_snapshot_txt(const char *path, int32_t dim, int32_t model, double time,
                     int64_t iteration, int32_t n, const int32_t *tri, const int32_t *tag,
                     const double *pos, const double *vel, const double *fvs,
-                    const double *diameter);
+                    const double *diameter, const double *depth);
 int cg_snapshot_vtk(const char *path, int32_t dim, int32_t model, double time,
                     int64_t iteration, int32_t n, const int32_t *tri, const int32_t *tag,
                     const double *pos, const double *vel, const double *fvs,
-                    const double *diameter);
+                    const double *diameter, const double *depth);
 
 /* ---- particles added during a run -------------------------------------- */
 /* Points the run at a new (larger) particle state after the caller grew

@@ -518,6 +518,7 @@ static void delete_single(cgo_particles *s, int pdim, int i) {
         s->last_pos[i * pdim + d] = 0.;
         s->last_vel[i * pdim + d] = 0.;
     }
+    if (s->depth) s->depth[i] = 0.;
     s->tri[i] = -1;
     s->lowerlayer[i] = 0;
     s->last_tri[i] = -1;
@@ -550,12 +551,68 @@ typedef struct {
 #define LPOS(c, d) ((c)->s->last_pos[(c)->i * (c)->pd + (d)])
 #define LVEL(c, d) ((c)->s->last_vel[(c)->i * (c)->pd + (d)])
 
+static double cpow_re(double x, double y);
+
+/* eulerian_field_set.pyx:1957-1993: friction coefficient of the depth h */
+static double friction_calc(const cgo_params *p, double h) {
+    double fc = p->friction_coef;
+    switch (p->friction_model) {
+    case 0: return 2. * GRAV / (fc * fc);                                     /* Chezy */
+    case 1: return 2. * GRAV / (fc * fc) / cpow_re(fmax(EPSILON, h), 1. / 3.);  /* Strickler */
+    case 2: return 2. * GRAV * (fc * fc) / cpow_re(fmax(EPSILON, h), 1. / 3.);  /* Manning */
+    default: {                                                                /* Nikuradse */
+        double aux = h * 11.036 / fc;
+        if (!(aux > 1.001)) aux = 1.001;
+        double q = log(aux) / KAPPA;
+        return 2. / (q * q);
+    }
+    }
+}
+
+/* eulerian_field_set.pyx:1887-1955: vertical velocity w and horizontal
+ * log-law factor of a 3D particle on 2D fields (pseudo-3D) */
+static void pseudo_3d_corrections(ctx_t *c, int k, double x, double y, double z, double dt,
+                                  double ux, double uy, double *w, double *hor) {
+    const cgo_mesh *m = c->m;
+    const cgo_fields *f = c->f;
+    p1_t p = p1_factors(m, k, x, y);
+    const double *gx = m->gradx + 3 * k, *gy = m->grady + 3 * k;
+    double zs = p1_eval(f->zs, 0, &p);
+    double zb = p1_eval(f->zb, 0, &p);
+    double h = fmax(EPSILON, zs - zb);
+    double sigma = fmin(1., fmax(0., (z - zb) / h));
+    double Cf = friction_calc(c->p, h);
+    double z0 = fmax(EPSILON, h * exp(-(1. + KAPPA / sqrt(Cf / 2.))));
+    double hh = (z - zb <= z0) ? 0.0 : log((z - zb) / z0) / (log(h / z0) - 1.);
+    double uc = ux * hh, vc = uy * hh;
+    double dzsdx = f->zs[p.i0] * gx[0] + f->zs[p.i1] * gx[1] + f->zs[p.i2] * gx[2];
+    double dzsdy = f->zs[p.i0] * gy[0] + f->zs[p.i1] * gy[1] + f->zs[p.i2] * gy[2];
+    double dzbdx = f->zb[p.i0] * gx[0] + f->zb[p.i1] * gx[1] + f->zb[p.i2] * gx[2];
+    double dzbdy = f->zb[p.i0] * gy[0] + f->zb[p.i1] * gy[1] + f->zb[p.i2] * gy[2];
+    /* eulerian_field_set.pyx:1581-1642 */
+    double dzsdt = 0.;
+    if (!(f->frozen == 1 || !f->prev_valid)) {
+        double z0p = p1_eval(f->z0, 0, &p);
+        dzsdt = (zs - z0p) / dt;
+    }
+    *w = (1. - sigma) * (uc * dzbdx + vc * dzbdy) + sigma * (dzsdt + uc * dzsdx + vc * dzsdy);
+    *hor = hh;
+}
+
 /* mean velocity at (k, ll, x, y, z), update_state_lsm1.pyx:144-163 */
 static void lsm1_velocity(ctx_t *c, int k, int ll, double x, double y, double z,
                           double *ux, double *uy, double *uz) {
     if (c->f->dim == 2) {
         interp_velocity_2d(c->m, c->f, k, x, y, ux, uy);
         *uz = 0.;
+        if (c->pd == 3) {
+            /* pseudo-3D corrections (update_state_lsm1.pyx:156-162) */
+            double w, hor;
+            pseudo_3d_corrections(c, k, x, y, z, c->p->dt, *ux, *uy, &w, &hor);
+            *uz += w;
+            *ux *= hor;
+            *uy *= hor;
+        }
     } else {
         if (interp_velocity_3d(c->m, c->f, k, ll, x, y, z, ux, uy, uz)) c->err = 1;
     }
@@ -1941,6 +1998,8 @@ static void init_particle(ctx_t *c) {
         s->lowerlayer[i] = cgo_lower_layer_index(c->f->nlayers, zs, zb, POS(c, 2));
         if (POS(c, 2) < zb) POS(c, 2) = zb + EPSILON;
         if (POS(c, 2) > zs) POS(c, 2) = zs - EPSILON;
+        /* solver.pyx:325-332 */
+        if (p->compute_depth && s->depth) s->depth[i] = zs - POS(c, 2);
     }
     if (s->inactive[i] == 0 && p->particle_velocity_init == 1) {
         double ux, uy, uz;
@@ -2034,6 +2093,12 @@ int cgo_step_range(const cgo_mesh *m, const cgo_fields *f, const cgo_params *p,
                 if (s->tri[i] == PART_LOC_O) delete_single(s, c.pd, i);
                 if (s->lowerlayer[i] == PART_LOC_B) delete_single(s, c.pd, i);
                 if (s->lowerlayer[i] == PART_LOC_A) delete_single(s, c.pd, i);
+            }
+            /* solver.pyx:526-538: depth below the free surface */
+            if (p->compute_depth && s->depth && s->inactive[i] == 0 && c.pd == 3) {
+                int k = s->tri[i];
+                double zs = interp_field_2d(m, f, f->zs, k, f->nlayers - 1, POS(&c, 0), POS(&c, 1));
+                s->depth[i] = zs - POS(&c, 2);
             }
             /* control sections, solver.pyx:542-549 (zeroed arrays when the
              * step deleted the particle) */

@@ -73,6 +73,11 @@ typedef struct {
     int added_mass; double added_mass_coef;
     int buoy_model; double buoy_value;
     double a0c, a1c, a2c, a3c;
+    /* field-set friction law of the pseudo-3D log-law correction
+     * (eulerian_field_set.pyx:125-138, 1957-1993) */
+    int friction_model; double friction_coef;
+    /* LagrangianParticleSet.compute_depth (solver.pyx:526-538) */
+    int compute_depth;
 } cgo_params;
 
 typedef struct {
@@ -82,6 +87,7 @@ typedef struct {
     int32_t *tri, *last_tri, *lowerlayer, *inactive, *tag;
     double *diameter, *volume;
     uint64_t *rng_state, *rng_inc;      /* per-particle PCG32 */
+    double *depth;                      /* [n] or NULL (compute_depth) */
 } cgo_particles;
 
 /* ---- RNG (cylag/lsm/random_utils.pyx) ---- */

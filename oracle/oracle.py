@@ -81,7 +81,8 @@ class Params(C.Structure):
                 ("added_mass", C.c_int), ("added_mass_coef", C.c_double),
                 ("buoy_model", C.c_int), ("buoy_value", C.c_double),
                 ("a0c", C.c_double), ("a1c", C.c_double), ("a2c", C.c_double),
-                ("a3c", C.c_double)]
+                ("a3c", C.c_double), ("friction_model", C.c_int),
+                ("friction_coef", C.c_double), ("compute_depth", C.c_int)]
 
 
 class Particles(C.Structure):
@@ -91,7 +92,8 @@ class Particles(C.Structure):
                 ("tri", C.c_void_p), ("last_tri", C.c_void_p),
                 ("lowerlayer", C.c_void_p), ("inactive", C.c_void_p),
                 ("tag", C.c_void_p), ("diameter", C.c_void_p), ("volume", C.c_void_p),
-                ("rng_state", C.c_void_p), ("rng_inc", C.c_void_p)]
+                ("rng_state", C.c_void_p), ("rng_inc", C.c_void_p),
+                ("depth", C.c_void_p)]
 
 
 def lib():
@@ -179,7 +181,7 @@ class OracleSolver:
     def __init__(self, mesh, fields, params, position, pset=None, seed=0,
                  tags=None, nthreads=1, diameter=None, sources=None, initial_pool_size=None,
                  min_pool_size_update=1000, field_set=None, control_sections=None,
-                 max_stranded=None):
+                 max_stranded=None, friction_model=1, friction_coefficient=40.):
         from cylag_gb300.parameters import Parameters
         L = lib()
         self.L = L
@@ -259,6 +261,9 @@ class OracleSolver:
         self.diameter = (np.full(n, dp) if diameter is None
                          else np.asarray(diameter, dtype=np.float64).copy())
         self.volume = np.pi * (self.diameter ** 3) / 6.
+        # lagrangian_particle_set.pyx:212-219
+        self.compute_depth = bool(pset.get("compute_depth", False))
+        self.depth = np.zeros(n) if self.compute_depth else None
         self.rng_state, self.rng_inc = seed_streams(seed, self.tag)
         self._bind()
         # ---- params ----------------------------------------------------------
@@ -282,7 +287,8 @@ class OracleSolver:
             pd, rho0, rhop, pset.get("drag_coefficient_model", 1),
             pset.get("drag_coefficient", 0.44), am, Ca,
             pset.get("buoyancy_velocity_model", 0), pset.get("buoyancy_velocity", 0.0),
-            a0c, a1c, a2c, a3c)
+            a0c, a1c, a2c, a3c, int(friction_model), float(friction_coefficient),
+            int(self.compute_depth))
         self.time = P.initial_time
         self.dt = P.time_step
         self.time_step = P.time_step
@@ -314,7 +320,8 @@ class OracleSolver:
                             _p(self.fvs), _p(self.last_pos), _p(self.last_vel), _p(self.tri),
                             _p(self.last_tri), _p(self.lowerlayer), _p(self.inactive),
                             _p(self.tag), _p(self.diameter), _p(self.volume),
-                            _p(self.rng_state), _p(self.rng_inc))
+                            _p(self.rng_state), _p(self.rng_inc),
+                            _p(self.depth) if self.depth is not None else None)
 
     # ---- particles added during the run (lagrangian_particle_set.pyx) ------------
     def _increase_pool_size(self, size):
@@ -334,6 +341,8 @@ class OracleSolver:
         self.last_tri = cat(self.last_tri, z(add, dt=np.int32))
         self.rng_state = cat(self.rng_state, z(add, dt=self.rng_state.dtype))
         self.rng_inc = cat(self.rng_inc, z(add, dt=self.rng_inc.dtype))
+        if self.depth is not None:
+            self.depth = cat(self.depth, z(add))
         self.n += add
         self._bind()
 

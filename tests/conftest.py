@@ -98,7 +98,10 @@ def mesh_from_case(case):
 
 
 def fields_from_case(case):
-    return dict(dim=case.get("dim", 2), nlayers=case.get("nlayers", 1), times=case["times"],
+    """The field-set arguments of a fixture case (``fdim``: the field set's
+    dimension when it differs from the particles', pseudo-3D)."""
+    return dict(dim=case.get("fdim", case.get("dim", 2)), nlayers=case.get("nlayers", 1),
+                times=case["times"],
                 elevation=case["elevation"], velocity_x=case["velocity_x"],
                 velocity_y=case["velocity_y"], velocity_z=case.get("velocity_z"),
                 opt_fields=case.get("opt_fields"), opt_fields_names=case.get("opt_fields_names"))
@@ -109,7 +112,9 @@ def run_oracle(case, meta, nthreads=1, nsteps=None, seed=None):
     o = oracle.OracleSolver(mesh_from_case(case), fields_from_case(case), meta["params"],
                             case["position"], pset=meta.get("pset"),
                             seed=meta["seed"] if seed is None else seed, nthreads=nthreads,
-                            control_sections=[np.array(q) for q in meta.get("sections") or []])
+                            control_sections=[np.array(q) for q in meta.get("sections") or []],
+                            friction_model=case.get("friction_model", 1),
+                            friction_coefficient=case.get("friction_coefficient", 40.))
     o.solve(meta["nsteps"] if nsteps is None else nsteps)
     return o
 
@@ -120,7 +125,7 @@ def assert_state_close(got, want, rtol=RTOL, exact=False, what=""):
         if k in want and k in got:
             np.testing.assert_array_equal(np.asarray(got[k]), want[k], err_msg=f"{what}: {k}")
     active = np.asarray(want["inactive"]) == 0
-    for k in ("position", "velocity", "fluid_velocity_seen", "last_position"):
+    for k in ("position", "velocity", "fluid_velocity_seen", "last_position", "depth"):
         if k not in want or k not in got:
             continue
         g, w = np.asarray(got[k])[active], np.asarray(want[k])[active]

@@ -115,16 +115,21 @@ def run_reference(case, params, nsteps, seed=0, pset_kw=None, sections=None):
     mesh = cy.TriangularMesh(case["x"], case["y"], case["triangles"],
                              boundary_points=case.get("boundary_points"),
                              nopen=case.get("nopen", 0))
+    fdim = case.get("fdim", dim)
     fset = cy.EulerianFieldSet(
-        mesh, dim=dim, nlayers=case.get("nlayers", 1), times=case["times"],
+        mesh, dim=fdim, nlayers=case.get("nlayers", 1), times=case["times"],
         elevation=case["elevation"], velocity_x=case["velocity_x"], velocity_y=case["velocity_y"],
         velocity_z=case.get("velocity_z"), opt_fields=case.get("opt_fields"),
-        opt_fields_names=case.get("opt_fields_names"))
+        opt_fields_names=case.get("opt_fields_names"),
+        friction_model=case.get("friction_model", 1),
+        friction_coefficient=case.get("friction_coefficient", 40.))
     tmp = tempfile.mkdtemp(prefix="cylag_golden_")
     params = dict(params)
     params["output_rep"] = tmp
     keys = ("position", "velocity", "fluid_velocity_seen", "last_position", "last_velocity")
     res = {k: [] for k in keys + ("tri", "last_tri", "lowerlayer", "inactive")}
+    if pset_kw.get("compute_depth"):
+        res["depth"] = []
     nopen = case.get("nopen", 0)
     stats = np.zeros((nsteps, max(1, nopen)), dtype=np.int64)
     ncsec = len(sections or [])
@@ -152,6 +157,8 @@ def run_reference(case, params, nsteps, seed=0, pset_kw=None, sections=None):
         res["last_tri"].append(ps.last_tri[0])
         res["lowerlayer"].append(ps.lowerlayer[0])
         res["inactive"].append(ps.inactive[0])
+        if "depth" in res:
+            res["depth"].append(np.asarray(ps.depth)[0])
         if params.get("bnd_statistics"):
             stats += np.asarray(s._bnd_stats_data)[:nsteps]
     out = {k: np.array(v) for k, v in res.items()}
@@ -549,8 +556,85 @@ def section_fixtures():
     save_traj("loglaw3d_lsm2", c3, p3, 60, seed=8, sections=sec3, prefix="sec")
 
 
+def _p3d_channel(npart=48, unsteady=False, keps=False, seed=21):
+    """Pseudo-3D case: 2D fields (free surface, depth-averaged current,
+    BOTTOM) on a 400 m x 100 m walled channel (41x11 vertices, random
+    diagonals), 3D particles.  The bed slopes down along x and across the
+    channel, the free surface carries a standing wave; unsteady: records 0,
+    200, 400 s with the wave rising and the current strengthening (dzs/dt
+    and the Eulerian fields change between steps).  keps: nodal k and eps
+    (K = 0.02 + 0.03 (1 + sin(2 pi x / 200)) / 2) for the k-epsilon
+    diffusion models."""
+    x, y, tri = synth.channel_mesh(400.0, 100.0, 41, 11, seed=seed)
+    zb = -4.0 - 2.0 * (x / 400.0) - 0.5 * (y / 100.0)
+    times = np.array([0.0, 200.0, 400.0]) if unsteady else np.zeros(1)
+    amp = [1.0, 1.4, 1.8] if unsteady else [1.0]
+    zs = np.stack([0.3 * a * np.sin(2 * np.pi * x / 400.0) for a in amp])
+    u = np.stack([(0.25 + 0.05 * a) + 0.05 * np.cos(2 * np.pi * y / 100.0) for a in amp])
+    v = np.stack([0.04 * a * np.sin(2 * np.pi * x / 200.0) for a in amp])
+    names = ["BOTTOM"]
+    opt = [np.stack([zb] * len(times))]
+    if keps:
+        K = 0.02 + 0.03 * 0.5 * (1.0 + np.sin(2 * np.pi * x / 200.0))
+        k, eps = synth.keps_from_K(K)
+        names += ["TURBULENT ENERG.", "DISSIPATION"]
+        opt += [np.stack([k] * len(times)), np.stack([eps] * len(times))]
+    rng = np.random.default_rng(seed + 1)
+    px = rng.uniform(20.0, 380.0, npart)
+    py = rng.uniform(2.0, 98.0, npart)
+    zbp = -4.0 - 2.0 * (px / 400.0) - 0.5 * (py / 100.0)
+    zsp = 0.3 * np.sin(2 * np.pi * px / 400.0)
+    pz = zbp + (zsp - zbp) * rng.uniform(0.02, 0.98, npart)
+    return dict(x=x, y=y, triangles=tri, dim=3, fdim=2, nlayers=1, times=times,
+                elevation=zs, velocity_x=u, velocity_y=v, opt_fields=np.stack(opt),
+                opt_fields_names=names, position=np.stack([px, py, pz], 1))
+
+
+def p3d_fixtures():
+    """Pseudo-3D LSM1 (2D fields, 3D particles; the log-law horizontal
+    factor and the vertical velocity of eulerian_field_set.pyx:1887-1955
+    inside every time scheme) and compute_depth (solver.pyx:526-538)."""
+    base = dict(model=1, frozen_eulerian_fields=True, time_step=5.0, final_time=1000.0)
+    c = _p3d_channel()
+    # advection only, every time scheme and the four friction laws
+    for ts, fm, fc in ((1, 1, 40.), (2, 0, 60.), (3, 2, 0.025), (4, 3, 0.05)):
+        cc = dict(c, friction_model=fm, friction_coefficient=fc)
+        save_traj(f"p3d_ts{ts}_fm{fm}", cc, dict(base, diffusion_model=0, time_scheme=ts), 80,
+                  pset_kw=dict(compute_depth=True))
+    # constant diffusion, settling, bed and surface reflection, walls
+    save_traj("p3d_rk2_diff_settling", c,
+              dict(base, diffusion_model=1, time_scheme=2, horizontal_diffusivity=0.05,
+                   vertical_diffusivity=5e-3, rebound_damping_coef=0.2), 80, seed=2,
+              pset_kw=dict(particle_density=2650., particle_diameter=2e-4,
+                           buoyancy_velocity_model=1, compute_depth=True))
+    # unsteady fields (dzs/dt, time interpolation), k-epsilon diffusion
+    cu = _p3d_channel(unsteady=True, keps=True)
+    for dm, ts in ((2, 1), (3, 4)):
+        save_traj(f"p3d_unsteady_keps{dm}_ts{ts}", cu,
+                  dict(model=1, frozen_eulerian_fields=False, time_step=4.0, final_time=400.0,
+                       diffusion_model=dm, time_scheme=ts, vertical_diffusivity=1e-3), 90,
+                  seed=5, pset_kw=dict(compute_depth=True))
+    # compute_depth on 3D sigma-layer fields: LSM1 k-eps, LSM2 DI, LSM3 DI
+    c3 = _loglaw3d(npart=40)
+    save_traj("depth_3d_lsm1", c3, dict(model=1, diffusion_model=3, time_scheme=1,
+                                        frozen_eulerian_fields=True, time_step=1.0,
+                                        final_time=60.0, vertical_diffusivity=1e-3), 60,
+              pset_kw=dict(compute_depth=True))
+    save_traj("depth_3d_lsm2", c3, dict(model=2, time_scheme=5, diffusion_model=3,
+                                        diffusion_lsm2_option=2, frozen_eulerian_fields=True,
+                                        time_step=1.0, final_time=60.0), 60, seed=4,
+              pset_kw=dict(compute_depth=True, particle_density=1000., particle_diameter=1e-4))
+    save_traj("depth_3d_lsm3", c3, dict(model=3, time_scheme=5, diffusion_model=1,
+                                        horizontal_diffusivity=0.01, vertical_diffusivity=1e-3,
+                                        frozen_eulerian_fields=True, time_step=1.0,
+                                        final_time=60.0), 60, seed=6,
+              pset_kw=dict(compute_depth=True, particle_density=2650.,
+                           particle_diameter=1e-4))
+
+
 GROUPS = {"rng": rng_fixture, "mesh": mesh_fixture, "lsm1": traj_fixtures,
-          "lsm23": lsm23_fixtures, "sources": source_fixtures, "sections": section_fixtures}
+          "lsm23": lsm23_fixtures, "sources": source_fixtures, "sections": section_fixtures,
+          "p3d": p3d_fixtures}
 
 if __name__ == "__main__":
     for g in (sys.argv[1:] or list(GROUPS)):

@@ -20,8 +20,10 @@ def gpu_run(case, meta, nsteps=None, batch=None, precision="fp64", seed=None):
     fs = cg.EulerianFieldSet(mesh, dim=f["dim"], nlayers=f["nlayers"], times=f["times"],
                              elevation=f["elevation"], velocity_x=f["velocity_x"],
                              velocity_y=f["velocity_y"], velocity_z=f["velocity_z"],
-                             opt_fields=f["opt_fields"], opt_fields_names=f["opt_fields_names"])
-    ps = cg.LagrangianParticleSet(case["position"], dim=f["dim"], **meta.get("pset", {}))
+                             opt_fields=f["opt_fields"], opt_fields_names=f["opt_fields_names"],
+                             friction_model=case.get("friction_model", 1),
+                             friction_coefficient=case.get("friction_coefficient", 40.))
+    ps = cg.LagrangianParticleSet(case["position"], dim=case.get("dim", 2), **meta.get("pset", {}))
     s = cg.Solver(fs, ps, meta["params"], precision=precision,
                   seed=meta["seed"] if seed is None else seed)
     n = meta["nsteps"] if nsteps is None else nsteps
@@ -37,9 +39,12 @@ def gpu_run(case, meta, nsteps=None, batch=None, precision="fp64", seed=None):
 
 
 def state(ps):
-    return dict(position=ps.position, velocity=ps.velocity,
-                fluid_velocity_seen=ps.fluid_velocity_seen, tri=ps.tri,
-                inactive=ps.inactive, lowerlayer=ps.lowerlayer, last_position=ps.last_position)
+    out = dict(position=ps.position, velocity=ps.velocity,
+               fluid_velocity_seen=ps.fluid_velocity_seen, tri=ps.tri,
+               inactive=ps.inactive, lowerlayer=ps.lowerlayer, last_position=ps.last_position)
+    if ps.compute_depth:
+        out["depth"] = ps.depth
+    return out
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -52,7 +57,8 @@ def test_gpu_matches_reference_golden(name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["couette", "keps_ts2_rm1", "open", "3d_keps"])
+@pytest.mark.parametrize("name", ["couette", "keps_ts2_rm1", "open", "3d_keps",
+                                  "p3d_unsteady_keps3_ts4", "depth_3d_lsm2"])
 def test_gpu_matches_oracle_stepwise(name):
     """Single-step calls (every public array refreshed each step) equal one
     batched call, and both equal the oracle run on this machine."""
@@ -60,6 +66,8 @@ def test_gpu_matches_oracle_stepwise(name):
     o = run_oracle(case, meta)
     want = dict(position=o.pos, velocity=o.vel, fluid_velocity_seen=o.fvs, tri=o.tri,
                 inactive=o.inactive, lowerlayer=o.lowerlayer, last_position=o.last_pos)
+    if o.depth is not None:
+        want["depth"] = o.depth
     s1, p1 = gpu_run(case, meta, batch=7)
     assert_state_close(state(p1), want, rtol=RTOL, what=name + " batch=7")
     np.testing.assert_array_equal(p1.tag, o.tag)

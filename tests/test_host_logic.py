@@ -256,14 +256,22 @@ def test_particle_set_delete_like_the_reference():
 
 def test_particle_set_depth_like_the_reference():
     """compute_depth: the reference refuses it for 2D sets (ValueError) and
-    leaves depth None without it; the 3D depth output is not built here."""
+    leaves depth None without it; a 3D set starts with zero depths
+    (lagrangian_particle_set.pyx:212-219), grows them with the pool and
+    zeroes a deleted particle's."""
     import cylag_gb300 as cg
     ps = cg.LagrangianParticleSet(np.zeros((3, 2)) + 1.0, dim=2)
     assert ps.depth is None
     with pytest.raises(ValueError):
         cg.LagrangianParticleSet(np.zeros((3, 2)) + 1.0, dim=2, compute_depth=True)
-    with pytest.raises(NotImplementedError):
-        cg.LagrangianParticleSet(np.zeros((3, 3)) + 1.0, dim=3, compute_depth=True)
+    ps3 = cg.LagrangianParticleSet(np.zeros((3, 3)) + 1.0, dim=3, compute_depth=True,
+                                   min_pool_size_update=4)
+    np.testing.assert_array_equal(ps3.depth, np.zeros(3))
+    ps3._host["depth"][:] = [1.0, 2.0, 3.0]
+    ps3.delete([1])
+    np.testing.assert_array_equal(ps3.depth, [1.0, 0.0, 3.0])
+    ps3.add(np.array([[5.0, 5.0, -1.0], [6.0, 6.0, -1.0]]))
+    assert ps3.depth.shape == (7,) and ps3.depth[3:].tolist() == [0.0] * 4
 
 
 # ---------------------------------------------------------------------------

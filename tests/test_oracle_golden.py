@@ -83,6 +83,8 @@ def test_oracle_trajectories_match_reference(oracle_lib, name):
     o = run_oracle(case, meta)
     got = dict(position=o.pos, velocity=o.vel, fluid_velocity_seen=o.fvs, tri=o.tri,
                inactive=o.inactive, lowerlayer=o.lowerlayer, last_position=o.last_pos)
+    if o.depth is not None:
+        got["depth"] = o.depth
     assert_state_close(got, want, exact=X86, what=name)
     if meta["params"].get("bnd_statistics"):
         np.testing.assert_array_equal(np.stack(o.bnd_stats), want["bnd_stats"])

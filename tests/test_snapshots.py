@@ -30,8 +30,10 @@ def _arrays(dim, n, seed):
     return pos, vel, fvs, inactive, tag
 
 
-@pytest.mark.parametrize("dim,model", [(2, 1), (2, 2), (3, 1), (3, 3)])
-def test_snapshot_files_match_reference_writers(tmp_path, dim, model):
+@pytest.mark.parametrize("dim,model,depth", [(2, 1, False), (2, 2, False), (3, 1, False),
+                                             (3, 3, False), (3, 1, True), (3, 2, True)])
+def test_snapshot_files_match_reference_writers(tmp_path, dim, model, depth):
+    """... with the compute_depth column (3D) in both formats."""
     cy = _ref()
     import importlib
     WT = importlib.import_module("cylag.io.writer_txt")
@@ -40,7 +42,12 @@ def test_snapshot_files_match_reference_writers(tmp_path, dim, model):
     n = 50000 if dim == 2 else 30000   # above the parallel-format threshold
     pos, vel, fvs, inactive, tag = _arrays(dim, n, dim * 10 + model)
     ps = cy.LagrangianParticleSet(pos.copy(), velocity=vel.copy(), fluid_velocity_seen=fvs.copy(),
-                                  dim=dim)
+                                  dim=dim, compute_depth=depth)
+    dep = None
+    if depth:
+        dep = np.random.default_rng(5).uniform(-1.0, 30.0, n)
+        dep[: len(AWKWARD)] = AWKWARD
+        np.asarray(ps.depth)[:] = dep
     np.asarray(ps.inactive)[:] = inactive
     np.asarray(ps.tag)[:] = tag
     ps.npart_active = int((inactive == 0).sum())
@@ -53,8 +60,8 @@ def test_snapshot_files_match_reference_writers(tmp_path, dim, model):
     wt(ps, t, it, 1, -1, str(ref), "particles", model)
     wv(ps, t, it, 1, -1, str(ref), "particles", model)
     tri = np.where(inactive == 0, 0, -1).astype(np.int32)
-    output.write_snapshot((tri, tag, pos, vel, fvs if model >= 2 else None, None), dim, model,
-                          t, it, str(ours), "particles", "all")
+    output.write_snapshot((tri, tag, pos, vel, fvs if model >= 2 else None, None, dep), dim,
+                          model, t, it, str(ours), "particles", "all")
     for name in ("particles.txt", f"particles_{it}.vtk"):
         a, b = (ref / name).read_bytes(), (ours / name).read_bytes()
         assert a == b, (name, _first_diff(a, b))
