@@ -17,8 +17,10 @@ flush is needed between steps.
                   [--workload lsm1_2d|lsm2_3d|lsm3_3d]
   python bench.py --impl reference ...   # the CPU implementation, host cores
 
-Prints one JSON line (rank 0).  Under torchrun each rank advances its own
-1e7-particle shard (weak scaling, no data-path collective).
+Prints one JSON line (rank 0).  Under torchrun the particle set holds
+N x 1e7 particles and each rank advances its share, split as the reference's
+parallel solver splits particles (weak scaling, no data-path collective; the
+timed region is the max over ranks).
 """
 from __future__ import annotations
 
@@ -157,13 +159,19 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
-def make_workload(args, rank=0, workload=None):
-    """The workload's case dict (mesh, fields, particles, parameters); rank r
-    > 0 gets its own particles (same count) from its own seed."""
+def make_workload(args, world=1, workload=None):
+    """The workload's case dict (mesh, fields, particles, parameters).  With
+    several ranks the particle set holds world x the per-GPU count; each
+    rank's Solver steps its share (Solver(shard=(rank, world)), the
+    reference's parallel split)."""
     from cylag_gb300 import synth
     workload = workload or args.workload
     kw = {k: v for k, v in (("npart", args.npart), ("nx", args.nx), ("ny", args.ny)) if v} \
         if workload == args.workload else {}
+    if world > 1:
+        per = kw.get("npart") or {"lsm1_2d": 10_000_000, "lsm2_3d": 4_000_000,
+                                  "lsm3_3d": 10_000_000}[workload]
+        kw["npart"] = per * world
     if workload == "lsm1_2d":
         # field records A, B, A, ... every 600 s covering warm-up, timed and
         # end-to-end steps at dt = 0.5 s (0 / 600 / 1200 s up to 1197 timed
@@ -175,16 +183,11 @@ def make_workload(args, rank=0, workload=None):
         c = synth.lsm2_loglaw_workload(seed=0, **kw)
     else:
         c = synth.lsm3_taylor_green_workload(seed=0, **kw)
-    if rank:
-        rng = np.random.default_rng(1000 + rank)
-        c["position"] = c["position"][rng.permutation(len(c["position"]))]
-        c["position"][:, :2] += rng.uniform(-1.0, 1.0, (len(c["position"]), 2))
-        lo, hi = c["x"].min() + 1.0, c["x"].max() - 1.0
-        c["position"][:, 0] = np.clip(c["position"][:, 0], lo, hi)
-        lo, hi = c["y"].min() + 1.0, c["y"].max() - 1.0
-        c["position"][:, 1] = np.clip(c["position"][:, 1], lo, hi)
-    c["parameters"]["final_time"] = 1e9 if c["parameters"].get("frozen_eulerian_fields") \
-        else c["parameters"]["final_time"]
+    if c["parameters"].get("frozen_eulerian_fields"):
+        # frozen fields: a horizon covering warm-up, timed and end-to-end steps
+        dt = c["parameters"]["time_step"]
+        c["parameters"]["final_time"] = dt * (args.warmup + 2 * max(args.steps, args.leg_steps)
+                                              + 10)
     return c
 
 
@@ -327,8 +330,8 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e, steps=
     if "diameter" in c:
         ps.diameter = c["diameter"]
     log(f"creating solver ({precision})")
-    solver = cg.Solver(fs, ps, params, precision=precision, seed=rank, device=local,
-                       sort_period=sort_period)
+    solver = cg.Solver(fs, ps, params, precision=precision, seed=0, device=local,
+                       sort_period=sort_period, shard=(rank, world) if world > 1 else None)
     L = solver.L
     # all library work on a torch-owned stream (torch manages its lifetime)
     stream = torch.cuda.Stream(device=local)
@@ -389,10 +392,12 @@ def measure(args, c, params, precision, rank, world, local, dist, do_e2e, steps=
         e1 = torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record(stream)
-        for _ in range(steps):
-            rc = L.cg_run_step_host(solver._run, 1, C.byref(arr), C.byref(arr), args.e2e_chunk,
-                                    None)
-            _lib.check(solver._ctx, rc)
+        # one call of K steps: every step copies its whole state in from the
+        # pinned host arrays and its results back out, chunk by chunk, and the
+        # copy pipeline runs on from one step to the next
+        rc = L.cg_run_step_host(solver._run, steps, C.byref(arr), C.byref(arr), args.e2e_chunk,
+                                None)
+        _lib.check(solver._ctx, rc)
         e1.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -485,7 +490,7 @@ def run_gpu_arm(args):
         dist.init_process_group("gloo")
     torch.cuda.set_device(local)
     log("building workload")
-    c = make_workload(args, rank)
+    c = make_workload(args, world)
     params = dict(c["parameters"])
     total_steps = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
     if not params.get("frozen_eulerian_fields") and \
@@ -510,7 +515,7 @@ def run_gpu_arm(args):
         line.update({k: v for k, v in wl.items() if k not in ("value", "ms_per_step", "steps")})
         if "e2e" in res[main_form]:
             line["e2e"] = res[main_form]["e2e"]
-        if main_form == "mixed" and not args.no_oracle_error:
+        if main_form == "mixed" and not args.no_oracle_error and world == 1:
             log("mixed form vs the FP64 oracle")
             line["mixed_error_vs_oracle"] = oracle_subsample_error(
                 c, params, res["mixed"], args.warmup + args.steps,

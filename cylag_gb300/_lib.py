@@ -2,14 +2,19 @@
 
 The library is loaded from ``cylag_gb300/_native``; if it is missing the
 import fails loudly -- there is no CPU fallback for the particle step.
+With CYLAG_DEBUG_BOUNDS=1 in the environment the bounds-checked build
+(``libcylag_gpu_debug.so``, built on first use) is loaded instead.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 from pathlib import Path
 
-_NATIVE = Path(__file__).resolve().parent / "_native" / "libcylag_gpu.so"
+_DEBUG_BOUNDS = os.environ.get("CYLAG_DEBUG_BOUNDS") == "1"
+_NATIVE = Path(__file__).resolve().parent / "_native" / (
+    "libcylag_gpu_debug.so" if _DEBUG_BOUNDS else "libcylag_gpu.so")
 _lock = threading.Lock()
 _lib = None
 
@@ -24,6 +29,8 @@ CG_ERR_INTERP_OUTSIDE = 1
 CG_ERR_DEGENERATE_LAYER = 2
 CG_ERR_RNG_LIMIT = 4
 CG_ERR_UNSUPPORTED = 8
+CG_ERR_NONFINITE = 16
+CG_ERR_BOUNDS = 32
 
 CG_PRECISION_FP64 = 0
 CG_PRECISION_MIXED = 1
@@ -135,6 +142,9 @@ def load():
     global _lib
     with _lock:
         if _lib is None:
+            if _DEBUG_BOUNDS:
+                from .build import build
+                build(debug_bounds=True)
             if not _NATIVE.exists():
                 raise ImportError(
                     f"{_NATIVE} is missing: build it with `python -m cylag_gb300.build` "

@@ -3,7 +3,13 @@ machinery, no cmake).  Translation units compile in parallel; the plain-form
 kernels use -fmad=false so that FP64 arithmetic rounds exactly like the
 reference's C.
 
-Usage: ``python -m cylag_gb300.build [--force]``
+A second library, ``libcylag_gpu_debug.so``, is the same code built with
+-DCG_DEBUG_BOUNDS: every gather index read from the mesh tables or the
+particle state is range-checked in the kernels (an out-of-range index sets
+CG_ERR_BOUNDS and is redirected in bounds; nothing traps).  The Python layer
+loads it instead of the normal library when CYLAG_DEBUG_BOUNDS=1.
+
+Usage: ``python -m cylag_gb300.build [--force] [--debug-bounds]``
 """
 from __future__ import annotations
 
@@ -18,6 +24,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_native"
 LIB = OUT_DIR / "libcylag_gpu.so"
+LIB_DEBUG = OUT_DIR / "libcylag_gpu_debug.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -56,17 +63,20 @@ def _sources_newest() -> float:
     return max(f.stat().st_mtime for f in files)
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= _sources_newest():
-        return LIB
+def build(force: bool = False, verbose: bool = False, debug_bounds: bool = False) -> Path:
+    lib = LIB_DEBUG if debug_bounds else LIB
+    if not force and lib.exists() and lib.stat().st_mtime >= _sources_newest():
+        return lib
     OUT_DIR.mkdir(exist_ok=True)
     objs = []
     exe = nvcc()
+    flags = ["-DCG_DEBUG_BOUNDS"] if debug_bounds else []
+    suffix = "_debug.o" if debug_bounds else ".o"
 
     def one(item):
         src, extra = item
-        obj = OUT_DIR / (Path(src).stem + ".o")
-        cmd = [exe, *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+        obj = OUT_DIR / (Path(src).stem + suffix)
+        cmd = [exe, *ARCH, *COMMON, *flags, *extra, "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -76,15 +86,15 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 1)) as ex:
         objs = list(ex.map(one, UNITS.items()))
-    tmp = LIB.with_suffix(f".so.{os.getpid()}")
+    tmp = lib.with_suffix(f".so.{os.getpid()}")
     cmd = [exe, *ARCH, "-shared", *map(str, objs), "-o", str(tmp), "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
-    print(LIB)
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                debug_bounds="--debug-bounds" in sys.argv))

@@ -79,10 +79,18 @@ class SimuTime:
         self.time_step = time_step
         self.final_time = final_time
         self.nt = int((final_time - initial_time) / time_step)
-        self.times = np.linspace(initial_time, final_time, self.nt + 1)
+        self._times = None
         self.iteration = 0
         self.is_finished = False
         self.print_progress = print_progress
+
+    @property
+    def times(self):
+        """The nt + 1 step times, np.linspace(initial_time, final_time,
+        nt + 1), built on first access (a long horizon makes it large)."""
+        if self._times is None:
+            self._times = np.linspace(self.initial_time, self.final_time, self.nt + 1)
+        return self._times
 
     def increment(self):
         self.time += self.time_step

@@ -370,6 +370,21 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
     return CG_OK;
 }
 
+// The bounds-checked build's error word (ERR_BOUNDS), read and cleared; 0 in
+// normal builds, which never set it (call after synchronizing the stream).
+static uint32_t take_bounds_error(cg_ctx* c) {
+#ifdef CG_DEBUG_BOUNDS
+    uint32_t b = 0;
+    if (c->mesh.dbg && cudaMemcpy(&b, c->mesh.dbg, sizeof b, cudaMemcpyDeviceToHost) == cudaSuccess &&
+        b)
+        cudaMemset(c->mesh.dbg, 0, sizeof b);
+    return b;
+#else
+    (void)c;
+    return 0;
+#endif
+}
+
 // Working copies -> the caller's arrays (stream-ordered), after which the
 // caller's arrays are the run's state again and the next step gathers them.
 static int write_back(cg_run* r) {
@@ -567,6 +582,14 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
                             d->edgetri_map[2 * j + 1]);
         lab[j] = d->edges_labels[j];
     }
+    // error word of the bounds-checked build (ERR_BOUNDS)
+    c->mesh_bufs.emplace_back();
+    {
+        int rc0 = dalloc(c, c->mesh_bufs.back(), 256);
+        if (rc0) return rc0;
+        CUDA_TRY(c, cudaMemset(c->mesh_bufs.back().p, 0, 256));
+    }
+    uint32_t* dbg_word = (uint32_t*)c->mesh_bufs.back().p;
     std::vector<int> gstart(d->grid_start, d->grid_start + ncell + 1);
     std::vector<int> gtris(d->grid_tris, d->grid_tris + ngt);
     DevMesh m{};
@@ -591,6 +614,7 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
     m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64; m.t64s = p_t64s; m.nbr = p_nbr;
     m.gstart = p_gs; m.gtris = p_gt;
+    m.dbg = dbg_word;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;
     m.ginv = d->grid_inv_cell;
@@ -996,6 +1020,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     }
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    flags |= take_bounds_error(c);
     if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
     return CG_OK;
 }
@@ -1245,6 +1270,7 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    flags |= take_bounds_error(c);
     if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
     return CG_OK;
 }
@@ -1417,6 +1443,7 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
     if ((rc = collect_stranded(r))) return rc;
     uint32_t flags = 0;
     CUDA_TRY(c, cudaMemcpy(&flags, r->errw.p, sizeof flags, cudaMemcpyDeviceToHost));
+    flags |= take_bounds_error(c);
     if (flags) return set_err(c, CG_EDEVICE, "device error flags 0x%x", flags);
     return CG_OK;
 }

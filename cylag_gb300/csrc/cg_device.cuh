@@ -43,6 +43,7 @@ constexpr uint32_t ERR_DEGENERATE_LAYER = 2;
 constexpr uint32_t ERR_RNG_LIMIT = 4;
 constexpr uint32_t ERR_UNSUPPORTED = 8;
 constexpr uint32_t ERR_NONFINITE = 16;   // LSM2/LSM3 coefficients the reference rejects
+constexpr uint32_t ERR_BOUNDS = 32;      // bounds-checked builds: a gather index out of range
 
 // ---------------------------------------------------------------------------
 // device views
@@ -74,7 +75,27 @@ struct DevMesh {
     int gnx, gny;
     const int* __restrict__ gstart;     // [gnx*gny+1]
     const int* __restrict__ gtris;
+    // bounds-checked builds (CG_DEBUG_BOUNDS): error word for out-of-range
+    // gather indices (ERR_BOUNDS); unused otherwise
+    uint32_t* dbg;
 };
+
+// Every index read from the mesh tables or the particle state goes through
+// CG_IDX(m, i, n) before it addresses an array of n entries.  Normal builds:
+// the index as it is.  Bounds-checked builds (-DCG_DEBUG_BOUNDS, selected by
+// CYLAG_DEBUG_BOUNDS=1 at load time): an index outside [0, n) sets
+// ERR_BOUNDS in m.dbg and is replaced by 0, so the access stays in bounds
+// and the run reports the error instead of faulting.
+#ifdef CG_DEBUG_BOUNDS
+__device__ __forceinline__ long long cg_checked_index(uint32_t* dbg, long long i, long long n) {
+    if ((unsigned long long)i < (unsigned long long)n) return i;
+    if (dbg) atomicOr(dbg, ERR_BOUNDS);
+    return 0;
+}
+#define CG_IDX(m, i, n) cg_checked_index((m).dbg, (long long)(i), (long long)(n))
+#else
+#define CG_IDX(m, i, n) (i)
+#endif
 
 // Time-interpolated node fields for one step, packed per node.
 // 2D: 4 values {ux, uy, K, zs};  3D: 8 values {zs, ux, uy, uz, K, -, -, -}
@@ -524,7 +545,7 @@ __device__ __forceinline__ bool rot_ok(double x, double y, double2 v, double2 eo
 
 // utils.pyx:363-385 with xylocalizer.pyx:126-167
 __device__ __forceinline__ bool in_tri(const DevMesh& m, int k, double x, double y) {
-    const double2* g = m.geo + 6 * (size_t)k;
+    const double2* g = m.geo + 6 * (size_t)CG_IDX(m, k, m.nt);
     double2 a = __ldg(&g[0]), b = __ldg(&g[1]), c = __ldg(&g[2]);
     double2 dab = __ldg(&g[3]), dbc = __ldg(&g[4]), dca = __ldg(&g[5]);
     return rot_ok(x, y, a, dab, dca) && rot_ok(x, y, b, dbc, dab) && rot_ok(x, y, c, dca, dbc);
@@ -592,6 +613,7 @@ __device__ inline int grid_locate(const DevMesh& m, double x, double y) {
     int cx = fx > (double)(m.gnx - 1) ? m.gnx - 1 : (int)fx;
     int cy = fy > (double)(m.gny - 1) ? m.gny - 1 : (int)fy;
     int c = cy * m.gnx + cx;
+    c = (int)CG_IDX(m, c, (long long)m.gnx * m.gny);
     int b = __ldg(&m.gstart[c]), e = __ldg(&m.gstart[c + 1]);
     for (int j = b; j < e; ++j) {
         int k = __ldg(&m.gtris[j]);
@@ -610,6 +632,7 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
         // (numpy wraparound) but compares with -1
         int row = k < 0 ? k + m.nt : k;
         if (row < 0) break;
+        row = (int)CG_IDX(m, row, m.nt);
         int4 ta = __ldg(&m.tv[2 * row]);
         int4 tb = __ldg(&m.tv[2 * row + 1]);
         int ed[3] = {ta.w, tb.x, tb.y};
@@ -618,8 +641,8 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
         for (int i = 0; i < 3; ++i) {
             int j = ed[i];
             if (j == intersected_edge) continue;
-            int4 e = __ldg(&m.edge[j]);
-            double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+            int4 e = __ldg(&m.edge[CG_IDX(m, j, m.ne)]);
+            double2 a = __ldg(&m.xy[CG_IDX(m, e.x, m.nv)]), b = __ldg(&m.xy[CG_IDX(m, e.y, m.nv)]);
             if (intersec2d(p0x, p0y, x, y, a.x, a.y, b.x, b.y)) {
                 intersects = true;
                 int kn = (e.z == k) ? e.w : e.z;
@@ -707,6 +730,7 @@ struct P1 {
 // eulerian_field_set.pyx:1043-1052 (factors) + the vertex ids
 __device__ __forceinline__ P1 p1_at(const DevMesh& m, int k, double x, double y) {
     P1 p;
+    k = (int)CG_IDX(m, k, m.nt);
     int4 t = __ldg(&m.tv[2 * k]);
     p.i0 = t.x; p.i1 = t.y; p.i2 = t.z;
     double2 b0 = __ldg(&m.basis[5 * k]), b1 = __ldg(&m.basis[5 * k + 1]),
@@ -776,6 +800,7 @@ __device__ __forceinline__ int tri32s_nbr(const Tri32S& t, int j) {
 
 __device__ __forceinline__ Tri32S load_tri32s(const DevMesh& m, int k) {
     Tri32S t;
+    k = (int)CG_IDX(m, k, m.nt);
     const float4* r = reinterpret_cast<const float4*>(m.t64s + 4 * (size_t)k);
     t.tv = __ldg(&m.t64s[4 * (size_t)k]);
     t.as = __ldg(&r[1]);
@@ -794,6 +819,7 @@ __device__ __forceinline__ float2 split_offset(const Tri32S& t, float4 p) {
 
 __device__ __forceinline__ Tri32 load_tri32(const DevMesh& m, int k) {
     Tri32 t;
+    k = (int)CG_IDX(m, k, m.nt);
     const int4* r = m.t64 + 4 * (size_t)k;
     t.tv = __ldg(&r[0]);
     int4 a = __ldg(&r[1]);
@@ -887,8 +913,8 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
         for (int i = 0; i < 3; ++i) {
             int j = tri32_edge(tk, i);
             if (j == intersected_edge) continue;
-            int4 e = __ldg(&m.edge[j]);
-            double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+            int4 e = __ldg(&m.edge[CG_IDX(m, j, m.ne)]);
+            double2 a = __ldg(&m.xy[CG_IDX(m, e.x, m.nv)]), b = __ldg(&m.xy[CG_IDX(m, e.y, m.nv)]);
             float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
             float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
             if (intersec2d_filtered(p1, fa, fb, p0x, p0y, x, y, a, b)) {

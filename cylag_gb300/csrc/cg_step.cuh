@@ -69,7 +69,8 @@ struct Particle {
             uy *= hor;
         } else {
             if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ux = uy = uz = 0.; return; }
-            int jl = l * f.npoints, ju = (l + 1) * f.npoints;
+            l = (int)CG_IDX(m, l, f.nlayers - 1);
+        int jl = l * f.npoints, ju = (l + 1) * f.npoints;
             double zlp = p1_eval<DIM>(f.cur, jl, q, S::ZS);
             double zup = p1_eval<DIM>(f.cur, ju, q, S::ZS);
             double dz = zlp - zup;
@@ -173,6 +174,7 @@ struct Particle {
             return;
         }
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; K = dKdx = dKdy = dKdz = 0.; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         double Kl = p1_eval<DIM>(f.cur, jl, q, S::K);
         double gxl = p1_gx<DIM>(f.cur, jl, q, S::K);
@@ -223,6 +225,7 @@ struct Particle {
             return;
         }
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; kt = ep = 0.; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         double zlp = p1_eval<DIM>(f.cur, jl, q, Slots<DIM>::ZS);
         double zup = p1_eval<DIM>(f.cur, ju, q, Slots<DIM>::ZS);
@@ -296,6 +299,7 @@ struct Particle {
         }
         using S = Slots<3>;
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ax = ay = az = 0.; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         double e0 = nodev<DIM>(f.cur, jl + q.i0, S::ZS), e1 = nodev<DIM>(f.cur, jl + q.i1, S::ZS),
                e2 = nodev<DIM>(f.cur, jl + q.i2, S::ZS);
@@ -362,6 +366,7 @@ struct Particle {
             return;
         }
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ux = uy = uz = 0.f; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         float zlp = ev(f.cur, jl, q, S::ZS), zup = ev(f.cur, ju, q, S::ZS);
         float dz = zlp - zup;
@@ -385,6 +390,7 @@ struct Particle {
             return;
         }
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; kt = ep = 0.f; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         float zlp = ev(f.cur, jl, q, Slots<DIM>::ZS), zup = ev(f.cur, ju, q, Slots<DIM>::ZS);
         float dz = zlp - zup;
@@ -432,6 +438,7 @@ struct Particle {
         }
         using S = Slots<3>;
         if (l == PART_LOC_B || l == PART_LOC_A) { err |= ERR_INTERP_OUTSIDE; ax = ay = az = 0.f; return; }
+        l = (int)CG_IDX(m, l, f.nlayers - 1);
         int jl = l * f.npoints, ju = (l + 1) * f.npoints;
         float e0 = nf(f.cur, jl + q.i0, S::ZS), e1 = nf(f.cur, jl + q.i1, S::ZS), e2 = nf(f.cur, jl + q.i2, S::ZS);
         float h0 = nf(f.cur, ju + q.i0, S::ZS), h1 = nf(f.cur, ju + q.i1, S::ZS), h2 = nf(f.cur, ju + q.i2, S::ZS);
@@ -723,14 +730,14 @@ struct Particle {
         double damp = p.damp;
         bool strand_condition = false;
         if (bnd_j != -1) {
-            int lab = __ldg(&m.elabel[bnd_j]);
+            int lab = __ldg(&m.elabel[CG_IDX(m, bnd_j, m.ne)]);
             if (lab == BND_WALL_REF && p.strand > 0.) strand_condition = rng_uniform(rng) < p.strand;
             if (strand_condition) record_strand(p, pstep, pidx, x[0], x[1], DIM == 3 ? x[2] : 0.);
             if (lab == BND_WALL_REF && !strand_condition) {
                 int bnd_jj = bnd_j;
                 for (int rc = 0; tri == PART_LOC_O && rc < p.max_rebounds; ++rc) {
-                    int4 e = __ldg(&m.edge[bnd_jj]);
-                    double2 a = __ldg(&m.xy[e.x]), b = __ldg(&m.xy[e.y]);
+                    int4 e = __ldg(&m.edge[CG_IDX(m, bnd_jj, m.ne)]);
+                    double2 a = __ldg(&m.xy[CG_IDX(m, e.x, m.nv)]), b = __ldg(&m.xy[CG_IDX(m, e.y, m.nv)]);
                     // intersections.pyx:27-62
                     double coef = 1. - damp / 2.;
                     double nx = a.y - b.y, ny = b.x - a.x;
@@ -748,7 +755,7 @@ struct Particle {
                     else
                         xy_localize(m, ltri, x0[0], x0[1], px, py, tri, bnd_jj);
                     if (tri == PART_LOC_O && bnd_jj != -1) {
-                        int lj = __ldg(&m.elabel[bnd_jj]);
+                        int lj = __ldg(&m.elabel[CG_IDX(m, bnd_jj, m.ne)]);
                         if (lj >= BND_OPEN_REF) {
                             count_open(stats, lj);
                             deleted = true;
@@ -993,7 +1000,7 @@ __global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<F
     load_zig(zt);
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
         WalkEntry w = wq.e[j];
-        int i = w.i;
+        int i = (int)CG_IDX(m, w.i, s.n);
         Particle<2, FT> q(m, f, p, zt);
         int tri0 = s.tri[i];
         double2 x0 = (s.work & W_SPLIT) ? join_pos(reinterpret_cast<const float4*>(s.pos)[i])

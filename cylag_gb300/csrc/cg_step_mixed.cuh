@@ -52,7 +52,7 @@ __device__ __forceinline__ int one_hop(const DevMesh& m, int tri0, const Bary& b
         else if (n1 && p0 && p2) j = 1;
         else if (n2 && p0 && p1) j = 2;
         else return -1;
-        int4 nb = __ldg(&m.nbr[k]);
+        int4 nb = __ldg(&m.nbr[CG_IDX(m, k, m.nt)]);
         int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
         if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
         Tri32 tn = load_tri32(m, kn);

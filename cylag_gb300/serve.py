@@ -41,6 +41,7 @@ class Request:
     seed: int = 0
     pset: dict = field(default_factory=dict)
     arrival: float = 0.0          # seconds after the start of serve()
+    deadline: float | None = None  # seconds from admission to result, or none
 
 
 @dataclass
@@ -55,6 +56,7 @@ class Result:
     arrival: float = 0.0
     admitted: float = 0.0
     finished: float = 0.0
+    error: str | None = None      # set when the run was cancelled (no state)
 
     @property
     def latency(self):
@@ -150,6 +152,24 @@ class DispersionServer:
         _lib.check(self._ctx, self.L.cg_server_release(self._srv, run_id))
         self.runs.pop(run_id)
 
+    def expire(self, now):
+        """The watchdog: cancels every run whose request has a deadline that
+        passed (``now`` - admission > deadline) before its last step was
+        queued, and returns an error result for each (no particle state)."""
+        out = []
+        for run_id, (req, t_adm) in list(self.runs.items()):
+            if req.deadline is None or now - t_adm <= req.deadline:
+                continue
+            if self.steps_left(run_id) == 0:
+                continue   # finished: its result is collected as usual
+            self.cancel(run_id)
+            e = np.zeros((0, 2))
+            ei = np.zeros(0, np.int32)
+            out.append(Result(req.rid, e, e, e, ei, ei, ei, req.arrival, t_adm, now,
+                              error=f"deadline of {req.deadline:g} s exceeded after "
+                                    f"{now - t_adm:.3f} s"))
+        return out
+
     def stats(self):
         ar, ap, lf, si, ms = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_double()
         _lib.check(self._ctx, self.L.cg_server_stats(self._srv, C.byref(ar), C.byref(ap),
@@ -158,16 +178,19 @@ class DispersionServer:
                     largest_free_range=lf.value, steps_issued=si.value, last_step_ms=ms.value)
 
     # ---- a schedule of arrivals ---------------------------------------------------
-    def serve(self, requests, realtime=True, chunk=32, log=None):
+    def serve(self, requests, realtime=True, chunk=32, log=None, clock=None):
         """Plays the requests (sorted by arrival) and returns their results in
         completion order.  Each loop admits what has arrived and fits (in
         arrival order), queues up to ``chunk`` steps (fewer when a run
         completes earlier), then reads back the runs finished by the previous
-        queue, which overlaps the copies with the steps on the GPU."""
+        queue, which overlaps the copies with the steps on the GPU, and
+        cancels the runs whose deadline passed (``expire``).  ``clock``:
+        seconds since the start (default: the wall clock)."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         t0 = time.perf_counter()
-        now = (lambda: time.perf_counter() - t0) if realtime else (lambda: float("inf"))
-        clock = (lambda: time.perf_counter() - t0)
+        if clock is None:
+            clock = (lambda: time.perf_counter() - t0)
+        now = clock if realtime else (lambda: float("inf"))
         pending = deque()
         results = []
         i = 0
@@ -185,6 +208,7 @@ class DispersionServer:
                     self.step(min(chunk, min(todo)))
                 # runs finished by earlier queues: their copies overlap these steps
                 results.extend(self.collect(done, clock))
+                results.extend(self.expire(clock()))
             elif pending:
                 # nothing runs, so nothing will free room for it
                 raise RuntimeError(f"request {pending[0].rid} does not fit in an empty pool")

@@ -39,6 +39,10 @@ extern "C" {
                                      ValueError (update_state_lsm2.pyx:1283,
                                      update_state_lsm3.pyx:98-104,
                                      init_lsm2_fluctuations.pyx:68-77) */
+#define CG_ERR_BOUNDS 32          /* bounds-checked library build only: a gather
+                                     index read from the mesh tables or the
+                                     particle state was out of range (the
+                                     access was redirected, not made) */
 
 #define CG_PRECISION_FP64 0       /* plain form: FP64 end to end */
 #define CG_PRECISION_MIXED 1      /* FP32 fields/updates, FP64 position + localization */

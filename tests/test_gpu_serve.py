@@ -147,3 +147,24 @@ def test_serve_schedule_runs_every_request():
         alone = _alone(fs, "mixed", req)
         assert_state_close(_state(by[req.rid]), _state(alone), rtol=0.0, exact=True,
                            what=f"schedule request {req.rid}")
+
+
+def test_watchdog_cancels_a_run_past_its_deadline_and_leaves_the_others():
+    """On the device pool: a request with a zero deadline is cancelled by
+    the watchdog at the first loop after its admission (an error result, no
+    state); the other runs of the mix give exactly their results alone."""
+    import dataclasses
+    from cylag_gb300.serve import DispersionServer
+    fs = _channel()
+    reqs = _requests()[:4]
+    reqs[1] = dataclasses.replace(reqs[1], deadline=0.0)
+    srv = DispersionServer(fs, precision="mixed", capacity=1 << 15, max_runs=16)
+    res = {r.rid: r for r in srv.serve(reqs, realtime=False, chunk=8)}
+    srv.close()
+    assert sorted(res) == [0, 1, 2, 3]
+    assert res[1].error and len(res[1].position) == 0
+    for k in (0, 2, 3):
+        assert res[k].error is None
+        want = _alone(fs, "mixed", reqs[k])
+        np.testing.assert_array_equal(res[k].position, want.position)
+        np.testing.assert_array_equal(res[k].tri, want.tri)

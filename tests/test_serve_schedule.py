@@ -99,3 +99,43 @@ def test_schedule_refuses_a_request_larger_than_the_pool():
     reqs = _requests([10, 5000], [3, 3])
     with pytest.raises(RuntimeError, match="does not fit in an empty pool"):
         PoolModel(capacity=1000).serve(reqs, realtime=False)
+
+
+class ClockedPool(PoolModel):
+    """The pool model with a fake clock that each queued step advances by
+    `dt` seconds, and cancellation that frees the run's particles."""
+
+    def __init__(self, capacity, dt):
+        super().__init__(capacity)
+        self.t = 0.0
+        self.dt = dt
+        self.cancelled = []
+
+    def step(self, nsteps=1):
+        super().step(nsteps)
+        self.t += self.dt * nsteps
+
+    def cancel(self, run_id):
+        req, _ = self.runs.pop(run_id)
+        del self.left[run_id]
+        self.used -= len(req.position)
+        self.cancelled.append(req.rid)
+
+
+def test_watchdog_cancels_runs_past_their_deadline():
+    """A run whose deadline passes before its last step is queued is
+    cancelled (its pool range freed) and returned as an error result; runs
+    that finish in time, or have no deadline, complete as usual; a request
+    waiting for room is admitted once the cancelled run frees it."""
+    reqs = _requests([300, 300, 600], [400, 20, 30])
+    reqs[0].deadline = 5.0      # 400 steps at 0.1 s: cannot finish in 5 s
+    reqs[1].deadline = 5.0      # 20 steps: finishes in 2 s
+    pool = ClockedPool(capacity=700, dt=0.1)
+    res = pool.serve(reqs, realtime=False, chunk=8, clock=lambda: pool.t)
+    by = {r.rid: r for r in res}
+    assert sorted(by) == [0, 1, 2]
+    assert pool.cancelled == [0]
+    assert by[0].error and "deadline" in by[0].error and len(by[0].position) == 0
+    assert 5.0 < by[0].finished - by[0].admitted <= 5.0 + 8 * 0.1 + 1e-9
+    assert by[1].error is None and by[2].error is None
+    assert pool.admitted == [0, 1, 2] and pool.used == 0
