@@ -49,7 +49,7 @@ WORKLOADS = {
 }
 
 
-def parse():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=0,
                     help="particles per copy/step chunk of the end-to-end steps (0: about n/8)")
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     if args.steps is None:
         args.steps = 1000 if args.workload == "lsm1_2d" else 100
     return args
@@ -259,6 +259,61 @@ def cpu_rate(c, params, nsample, nsteps, threads):
     return nsample * nsteps / dt, dt
 
 
+def _reference_worker(job):
+    """One host process of the reference's parallel decomposition
+    (solver_parallel.pyx:113-179 without MPI): the unmodified compiled
+    reference's Solver over a contiguous slice of the sample, set up
+    untimed, W warm-up steps, then K timed forward() calls.  Returns the
+    seconds of the timed steps."""
+    import tempfile
+    workload, argv, lo, hi, warmup, steps = job
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refpath
+    cy = refpath.use_reference()
+    ns = parse_args(argv)
+    c = make_workload(ns, workload=workload)
+    params = dict(c["parameters"], listing=False,
+                  output_rep=tempfile.mkdtemp(prefix="cylag_ref_"))
+    mesh = cy.TriangularMesh(c["x"], c["y"], c["triangles"])
+    f = fields_dict(c)
+    fset = cy.EulerianFieldSet(mesh, dim=f["dim"], nlayers=f["nlayers"], times=f["times"],
+                               elevation=f["elevation"], velocity_x=f["velocity_x"],
+                               velocity_y=f["velocity_y"], velocity_z=f["velocity_z"],
+                               opt_fields=f["opt_fields"],
+                               opt_fields_names=f["opt_fields_names"])
+    ps = cy.LagrangianParticleSet(np.ascontiguousarray(c["position"][lo:hi]), dim=c["dim"],
+                                  **c.get("pset", {}))
+    if "diameter" in c:
+        np.asarray(ps.diameter)[:] = c["diameter"][lo:hi]
+        np.asarray(ps.volume)[:] = np.pi * c["diameter"][lo:hi] ** 3 / 6.
+    cy.random_utils.pcg32_seed(0, lo)
+    s = cy.Solver(fset, ps, params)
+    for _ in range(warmup):
+        s.forward(s.simutime.time_step)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.forward(s.simutime.time_step)
+    return time.perf_counter() - t0
+
+
+def reference_rate(args, nsample, steps, warmup, procs):
+    """particle-steps/s of the compiled reference on `procs` host processes
+    over the first `nsample` particles of the workload (the slowest process
+    sets the time), or None when the reference is not built here."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refpath
+    if not refpath.available():
+        return None
+    import multiprocessing as mp
+    from cylag_gb300.shard import split
+    argv = [a for a in sys.argv[1:] if a not in ("--impl", "reference", "gb300")]
+    jobs = [(args.workload, argv, a, a + n, warmup, steps) for a, n in split(nsample, procs)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        secs = pool.map(_reference_worker, jobs)
+    return nsample * steps / max(secs), max(secs)
+
+
 def run_reference_arm(args):
     rank, world, local = dist_info()
     if rank != 0:
@@ -278,36 +333,49 @@ def run_reference_arm(args):
                              "sample": "100,000 LSM1 + 100,000 LSM2 particles x 4 steps"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
-    c = make_workload(args)
-    params = dict(c["parameters"])
-    nsample = int(os.environ.get("CYLAG_REF_SAMPLE", "200000"))
-    # one solver over the sample (mesh and solver set up once, untimed); W
-    # warm-up steps, then each timed step advances the sample by one step
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-    from cylag_gb300.mesh import TriangularMesh
-    mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
-    diam = c["diameter"][:nsample] if "diameter" in c else None
-    o = oracle.OracleSolver(mesh, fields_dict(c), params, c["position"][:nsample],
-                            pset=c.get("pset"), nthreads=threads, diameter=diam)
-    for _ in range(args.warmup):
-        o.forward()
-    t_all = 0.
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        o.forward()
-        t_all += time.perf_counter() - t0
-    value = float(nsample * args.steps / t_all)
+    # the compiled reference (its own Solver, one process per host core),
+    # else the C restatement on all host threads
+    nall = len(make_workload(args)["position"])
+    nref = min(nall, int(os.environ.get("CYLAG_REF_SAMPLE", str(25000 * threads))))
+    procs = max(1, min(threads, nref))
+    got = reference_rate(args, nref, args.steps, args.warmup, procs)
+    if got is not None:
+        value, secs = got
+        kind, nsample, ms = "reference", nref, 1e3 * secs / args.steps
+        sample = (f"{nref} particles of the workload in {procs} processes, each the compiled "
+                  f"reference's Solver over a contiguous slice, one forward() per timed step")
+    else:
+        c = make_workload(args)
+        params = dict(c["parameters"])
+        nsample = int(os.environ.get("CYLAG_REF_SAMPLE", "200000"))
+        # one solver over the sample (mesh and solver set up once, untimed); W
+        # warm-up steps, then each timed step advances the sample by one step
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        from cylag_gb300.mesh import TriangularMesh
+        mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+        diam = c["diameter"][:nsample] if "diameter" in c else None
+        o = oracle.OracleSolver(mesh, fields_dict(c), params, c["position"][:nsample],
+                                pset=c.get("pset"), nthreads=threads, diameter=diam)
+        for _ in range(args.warmup):
+            o.forward()
+        t_all = 0.
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            o.forward()
+            t_all += time.perf_counter() - t0
+        value = float(nsample * args.steps / t_all)
+        kind, ms = "port", 1e3 * t_all / args.steps
+        sample = f"{nsample} particles of the workload advanced one step per timed step"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * t_all / args.steps, "higher_is_better": True,
+        "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "sample_particles": nsample,
                    "note": "each step advances a bounded sample of the particles on all host cores"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{nsample} particles of the workload advanced one step per "
-                                   "timed step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -524,8 +592,18 @@ def run_gpu_arm(args):
             log("cpu baseline")
             nsample = int(os.environ.get("CYLAG_CPU_SAMPLE", "200000"))
             rate, dt = cpu_rate(c, params, nsample, 4, threads)
-            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": f"{nsample} particles x 4 steps of the workload"}
+            port = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                    "sample": f"{nsample} particles x 4 steps of the workload"}
+            nref = min(len(c["position"]), 25000 * threads)
+            got = reference_rate(args, nref, 8, 2, threads) if world == 1 else None
+            if got is not None:
+                line["cpu_baseline"] = {
+                    "value": got[0], "unit": UNIT, "cores": threads, "kind": "reference",
+                    "sample": f"{nref} particles x 8 steps of the workload in {threads} "
+                              "processes, each the compiled reference's Solver over a slice"}
+                line["cpu_port"] = port
+            else:
+                line["cpu_baseline"] = port
     del res
     # the other configurations of the metric, as legs of the same line: the
     # 3D LSM2 and LSM3 workloads at their full sizes, and the serving mix on
@@ -666,7 +744,7 @@ def run_serve(args):
 
 
 def main():
-    args = parse()
+    args = parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
     elif args.workload == "serve":

@@ -105,6 +105,11 @@ def sources_present() -> bool:
     return (default_src() / "cylag").is_dir()
 
 
+def generated_present() -> bool:
+    """The generated C (stage 1's output) is here: stage 2 can run."""
+    return any((GEN / "cylag").rglob("*.c")) if (GEN / "cylag").is_dir() else False
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--src", default=str(default_src()))
