@@ -622,6 +622,21 @@ __device__ inline int grid_locate(const DevMesh& m, double x, double y) {
     return -1;
 }
 
+// The three edge records of a triangle and their end points, issued
+// together: a hop of the walk then waits for two dependent loads instead of
+// two per edge tested.  Every id is a valid edge of the mesh (the intersected
+// edge too, loaded and not tested).
+__device__ __forceinline__ void walk_gather(const DevMesh& m, const int* ed, int4* er,
+                                            double2* va, double2* vb) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) er[i] = __ldg(&m.edge[CG_IDX(m, ed[i], m.ne)]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        va[i] = __ldg(&m.xy[CG_IDX(m, er[i].x, m.nv)]);
+        vb[i] = __ldg(&m.xy[CG_IDX(m, er[i].y, m.nv)]);
+    }
+}
+
 // xylocalizer.pyx:338-435
 __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y, double x,
                                  double y, int& new_k, int& bnd) {
@@ -636,13 +651,18 @@ __device__ inline void path_walk(const DevMesh& m, int k, double p0x, double p0y
         int4 ta = __ldg(&m.tv[2 * row]);
         int4 tb = __ldg(&m.tv[2 * row + 1]);
         int ed[3] = {ta.w, tb.x, tb.y};
+        // the three edges and their end points are loaded together (two
+        // dependent levels per hop), then tested in the reference's order
+        int4 er[3];
+        double2 va[3], vb[3];
+        walk_gather(m, ed, er, va, vb);
         bool intersects = false;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             int j = ed[i];
             if (j == intersected_edge) continue;
-            int4 e = __ldg(&m.edge[CG_IDX(m, j, m.ne)]);
-            double2 a = __ldg(&m.xy[CG_IDX(m, e.x, m.nv)]), b = __ldg(&m.xy[CG_IDX(m, e.y, m.nv)]);
+            const int4 e = er[i];
+            const double2 a = va[i], b = vb[i];
             if (intersec2d(p0x, p0y, x, y, a.x, a.y, b.x, b.y)) {
                 intersects = true;
                 int kn = (e.z == k) ? e.w : e.z;
@@ -908,13 +928,17 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
     const float2 p1 = make_float2((float)(x - p0x), (float)(y - p0y));
     Tri32 tk = load_tri32(m, k);
     for (int niter = 0; niter <= NITER_MAX; ++niter) {
+        const int ed[3] = {tri32_edge(tk, 0), tri32_edge(tk, 1), tri32_edge(tk, 2)};
+        int4 er[3];
+        double2 va[3], vb[3];
+        walk_gather(m, ed, er, va, vb);
         bool intersects = false;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            int j = tri32_edge(tk, i);
+            int j = ed[i];
             if (j == intersected_edge) continue;
-            int4 e = __ldg(&m.edge[CG_IDX(m, j, m.ne)]);
-            double2 a = __ldg(&m.xy[CG_IDX(m, e.x, m.nv)]), b = __ldg(&m.xy[CG_IDX(m, e.y, m.nv)]);
+            const int4 e = er[i];
+            const double2 a = va[i], b = vb[i];
             float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
             float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
             if (intersec2d_filtered(p1, fa, fb, p0x, p0y, x, y, a, b)) {
