@@ -195,22 +195,31 @@ def bytes_per_particle_step(workload, precision):
     """Algorithmic (compulsory) DRAM bytes per particle-step of the fused
     step, per particle: the state it must read and write.
     LSM1 2D: position r+w 32, tri r+w 8, PCG32 state r+w 16, tag r 4.
-    LSM2 3D: position r+w 48, velocity r+w 48, tri r+w 8, layer r+w 8,
-             PCG32 r+w 16, tag r 4, diameter r 8.
-    LSM3 3D: the LSM2 set + fluid velocity seen r+w 48."""
+    LSM2 3D: position r+w 48, velocity r+w 48 (FP64) or 24 (the mixed form's
+             FP32 working copies), tri r+w 8, layer r+w 8, PCG32 r+w 16,
+             tag r 4, diameter r 8.
+    LSM3 3D: the LSM2 set + fluid velocity seen r+w 48 (FP64) or 24."""
     if workload == "lsm1_2d":
         return 32 + 8 + 16 + 4
-    b = 48 + 48 + 8 + 8 + 16 + 4 + 8
-    return b + 48 if workload == "lsm3_3d" else b
+    v = 24 if precision == "mixed" else 48
+    b = 48 + v + 8 + 8 + 16 + 4 + 8
+    return b + v if workload == "lsm3_3d" else b
 
 
-# DRAM bytes per particle-step of one step's kernels (step + walk), from ncu
-# captures of the same kernels at 4e6 particles (element-sorted; traffic
+# DRAM bytes per particle-step of one step's kernels, from ncu captures of
+# the same kernels on smaller particle counts (element-sorted; the traffic
 # grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 59.2, ("lsm1_2d", "fp64"): 147.0}
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 59.2, ("lsm1_2d", "fp64"): 147.0,
+                                   ("lsm2_3d", "mixed"): 155.2, ("lsm3_3d", "mixed"): 136.6}
 NCU_TRAFFIC_SOURCE = {
-    k: "ncu dram bytes (read+write) of the element-sorted step and walk kernels at 4e6 "
-       "particles, scaled to the launch" for k in NCU_TRAFFIC_B_PER_PARTICLE_STEP}
+    ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step and walk "
+                          "kernels at 4e6 particles, scaled to the launch",
+    ("lsm1_2d", "fp64"): "ncu dram bytes (read+write) of the element-sorted step and walk "
+                         "kernels at 4e6 particles, scaled to the launch",
+    ("lsm2_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel at "
+                          "2e6 particles, scaled to the launch",
+    ("lsm3_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel at "
+                          "2e6 particles, scaled to the launch"}
 
 
 def field_set_of(c):

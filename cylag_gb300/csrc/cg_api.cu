@@ -246,7 +246,14 @@ void make_dev_params(const cg_ctx* c, const cg_params* p, DevParams& d) {
             d.a3c = aux;
         }
     }
-
+    d.a0c32 = (float)d.a0c;
+    d.a1c32 = (float)d.a1c;
+    d.a2c32 = (float)d.a2c;
+    d.nux32 = (float)d.nux;
+    d.nuz32 = (float)d.nuz;
+    d.tl_h32 = (float)d.tl_h;
+    d.tl_v32 = (float)d.tl_v;
+    d.drag_coef32 = (float)d.drag_coef;
 }
 
 // ---------------------------------------------------------------------------
@@ -302,10 +309,13 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     if (p->dim == 3) q.work |= W_LAYER | W_DIAM;
     // mixed LSM1 2D: working positions as split FP32 pairs (same 16 bytes)
     if (p->precision == CG_PRECISION_MIXED && p->dim == 2 && p->model == 1) q.work |= W_SPLIT;
+    // mixed LSM2/LSM3: FP32 working velocities (and fluid velocities seen)
+    if (p->precision == CG_PRECISION_MIXED && p->model >= 2) q.work |= W_V32;
     const size_t D = (size_t)p->dim;
+    const size_t vb = (q.work & W_V32) ? 4 : 8;
     const size_t work_bytes = al256(n * 8 * D) + 4 * al256(n * 8) +
-                              ((q.work & W_VEL) ? al256(n * 8 * D) : 0) +
-                              ((q.work & W_FVS) ? al256(n * 8 * D) : 0) +
+                              ((q.work & W_VEL) ? al256(n * vb * D) : 0) +
+                              ((q.work & W_FVS) ? al256(n * vb * D) : 0) +
                               ((q.work & W_LAYER) ? al256(n * 4) : 0) +
                               ((q.work & W_DIAM) ? al256(n * 8) : 0) +
                               ((q.work & W_AUXW) ? al256(n * 4) : 0);
@@ -358,8 +368,9 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
         ws[k]->tri = (int*)take(n * 8);
         ws[k]->tag = (int*)take(n * 8);
         ws[k]->slot = (int*)take(n * 8);
-        ws[k]->vel = (q.work & W_VEL) ? (double*)take(n * 8 * D) : nullptr;
-        ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * 8 * D) : fvs_out;
+        const size_t vb = (q.work & W_V32) ? 4 : 8;
+        ws[k]->vel = (q.work & W_VEL) ? (double*)take(n * vb * D) : nullptr;
+        ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * vb * D) : fvs_out;
         ws[k]->layer = (q.work & W_LAYER) ? (int*)take(n * 4) : nullptr;
         ws[k]->diam = (q.work & W_DIAM) ? (double*)take(n * 8) : nullptr;
         ws[k]->ltri = (q.work & W_AUXW) ? (int*)take(n * 4) : nullptr;
@@ -575,6 +586,42 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
         t64s[4 * k + 3].z = nbr[k].y;
         t64s[4 * k + 3].w = nbr[k].z;
     }
+    // walk records (DevMesh::wrec, WalkRec): vertices, FP32 gradients, edge
+    // ids, the two elements of each edge and its end points' local indices
+    std::vector<int4> wrec(8 * (size_t)nt, make_int4(0, 0, 0, 0));
+    for (int k = 0; k < nt; ++k) {
+        const int32_t* t = d->triangles + 3 * k;
+        const int32_t* e = d->triedge_map + 3 * k;
+        int4* w = &wrec[8 * (size_t)k];
+        for (int v = 0; v < 3; ++v) {
+            const double xv = d->x[t[v]], yv = d->y[t[v]];
+            long long bx, by;
+            memcpy(&bx, &xv, 8);
+            memcpy(&by, &yv, 8);
+            w[v] = make_int4((int)(bx & 0xffffffffLL), (int)(bx >> 32), (int)(by & 0xffffffffLL),
+                             (int)(by >> 32));
+        }
+        memcpy(&w[3], &g32[2 * k], 16);
+        const float4 g1 = g32[2 * k + 1];
+        memcpy(&w[4].x, &g1.x, 4);
+        memcpy(&w[4].y, &g1.y, 4);
+        int ez[3], ew[3], order = 0;
+        for (int i = 0; i < 3; ++i) {
+            const int j = e[i];
+            ez[i] = d->edgetri_map[2 * j];
+            ew[i] = d->edgetri_map[2 * j + 1];
+            int la = 0, lb = 0;
+            for (int v = 0; v < 3; ++v) {
+                if (t[v] == d->edges[2 * j]) la = v;
+                if (t[v] == d->edges[2 * j + 1]) lb = v;
+            }
+            order |= (la << (4 * i)) | (lb << (4 * i + 2));
+        }
+        w[4].z = e[0];
+        w[4].w = e[1];
+        w[5] = make_int4(e[2], ez[0], ew[0], ez[1]);
+        w[6] = make_int4(ew[1], ez[2], ew[2], order);
+    }
     std::vector<int4> edge(ne);
     std::vector<int> lab(ne);
     for (int j = 0; j < ne; ++j) {
@@ -597,7 +644,7 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     int rc;
     const double2 *p_xy, *p_basis, *p_geo;
     const float4* p_g32;
-    const int4 *p_tv, *p_edge, *p_t64, *p_t64s, *p_nbr;
+    const int4 *p_tv, *p_edge, *p_t64, *p_t64s, *p_nbr, *p_wrec;
     const int *p_lab, *p_gs, *p_gt;
     if ((rc = upload(c, xy, p_xy))) return rc;
     if ((rc = upload(c, tv, p_tv))) return rc;
@@ -608,12 +655,13 @@ int cg_mesh_upload(cg_ctx* c, const cg_mesh_desc* d) {
     if ((rc = upload(c, t64s, p_t64s))) return rc;
     if ((rc = upload(c, edge, p_edge))) return rc;
     if ((rc = upload(c, nbr, p_nbr))) return rc;
+    if ((rc = upload(c, wrec, p_wrec))) return rc;
     if ((rc = upload(c, lab, p_lab))) return rc;
     if ((rc = upload(c, gstart, p_gs))) return rc;
     if ((rc = upload(c, gtris, p_gt))) return rc;
     m.xy = p_xy; m.tv = p_tv; m.basis = p_basis; m.edge = p_edge; m.elabel = p_lab;
     m.geo = p_geo; m.g32 = p_g32; m.t64 = p_t64; m.t64s = p_t64s; m.nbr = p_nbr;
-    m.gstart = p_gs; m.gtris = p_gt;
+    m.gstart = p_gs; m.gtris = p_gt; m.wrec = p_wrec;
     m.dbg = dbg_word;
     m.gx0 = d->grid_x0;
     m.gy0 = d->grid_y0;
@@ -1038,12 +1086,12 @@ int cg_run_set_sections(cg_run* r, int32_t ncsec, const double* segments) {
     r->csec_counts.clear();
     r->csec_steps = 0;
     if (ncsec == 0) return CG_OK;
-    int rc = dalloc(c, r->csec, (size_t)ncsec * sizeof(double4));
+    int rc = dalloc(c, r->csec, (size_t)ncsec * sizeof(SectionSeg));
     if (rc) return rc;
-    CUDA_TRY(c, cudaMemcpy(r->csec.p, segments, (size_t)ncsec * sizeof(double4),
+    CUDA_TRY(c, cudaMemcpy(r->csec.p, segments, (size_t)ncsec * sizeof(SectionSeg),
                            cudaMemcpyHostToDevice));
     r->dp.ncsec = ncsec;
-    r->dp.csec = (const double4*)r->csec.p;
+    r->dp.csec = (const SectionSeg*)r->csec.p;
     return CG_OK;
 }
 

@@ -71,6 +71,10 @@ struct DevMesh {
     // (-1: boundary edge)
     const int4* __restrict__ nbr;
     const int* __restrict__ elabel;     // [ne]
+    // [8*nt] walk record per element (WalkRec): what one hop of the mixed
+    // form's path walk reads, in one 128-byte line instead of the element
+    // row, three edge records and six vertices
+    const int4* __restrict__ wrec;
     double gx0, gy0, ginv;
     int gnx, gny;
     const int* __restrict__ gstart;     // [gnx*gny+1]
@@ -123,6 +127,11 @@ struct StrandRec {
     double x, y, z;
 };
 
+// a control section's segment {x0, y0, x1, y1}
+struct SectionSeg {
+    double x0, y0, x1, y1;
+};
+
 struct DevParams {
     int model, time_scheme, rng_method, diffmod;
     int bc_on, bc_type, max_rebounds, bnd_statistics, nopen;
@@ -143,7 +152,7 @@ struct DevParams {
     // control sections: one segment {x0, y0, x1, y1} each; their per-step
     // counts follow the nopen exit counts in a step's statistics row
     int ncsec;
-    const double4* csec;
+    const SectionSeg* csec;
     // stranding output: records of this call's stranded particles
     int strand_cap;
     int* strand_count;
@@ -152,7 +161,17 @@ struct DevParams {
     // eulerian_field_set.pyx:1957-1993)
     int friction_model;
     double friction_coef;
+    // FP32 copies of the LSM2/LSM3 coefficients for the mixed form
+    float a0c32, a1c32, a2c32, nux32, nuz32, tl_h32, tl_v32, drag_coef32;
 };
+
+// a parameter in the arithmetic R: its FP64 value, or (R = float) its FP32
+// copy, which equals R(v) without a conversion per particle
+template <typename R>
+__device__ __forceinline__ R par(double v, float v32) {
+    if constexpr (sizeof(R) == sizeof(float)) return v32;
+    else return v;
+}
 
 // x**y (x > 0) as the compiled reference evaluates it: Cython gives
 // double ** double a complex result, computed by the C library's complex
@@ -207,6 +226,30 @@ constexpr int W_SPLIT = 16;
 // a step that sets them for each active particle.
 constexpr int W_AUXW = 32;
 constexpr int LAST_UNSET = INT_MIN;
+// mixed LSM2/LSM3: the working velocities (W_VEL) and, with W_FVS, the
+// working fluid velocities seen are FP32 -- the values the mixed step
+// computes in FP32 and rounds every velocity it stores to
+constexpr int W_V32 = 64;
+
+// component k of the particle velocity / fluid velocity seen of a state
+// whose working copies may be FP32 (W_V32); the caller's arrays are FP64
+__device__ __forceinline__ double vel_ld(const DevState& s, size_t k) {
+    return (s.work & W_V32) ? (double)reinterpret_cast<const float*>(s.vel)[k] : s.vel[k];
+}
+__device__ __forceinline__ void vel_st(const DevState& s, size_t k, double v) {
+    if (s.work & W_V32) reinterpret_cast<float*>(s.vel)[k] = (float)v;
+    else s.vel[k] = v;
+}
+__device__ __forceinline__ bool fvs_is32(const DevState& s) {
+    return (s.work & (W_V32 | W_FVS)) == (W_V32 | W_FVS);
+}
+__device__ __forceinline__ double fvs_ld(const DevState& s, size_t k) {
+    return fvs_is32(s) ? (double)reinterpret_cast<const float*>(s.fvs)[k] : s.fvs[k];
+}
+__device__ __forceinline__ void fvs_st(const DevState& s, size_t k, double v) {
+    if (fvs_is32(s)) reinterpret_cast<float*>(s.fvs)[k] = (float)v;
+    else s.fvs[k] = v;
+}
 
 // An FP64 position as a pair of FP32 values hi + lo (|lo| <= ulp(hi)/2):
 // 48 significant bits, so the step's arithmetic on it stays in FP32.
@@ -254,7 +297,7 @@ struct WalkEntry {
     double xn, yn;       // end-of-step position (before localization)
     uint64_t rng;        // PCG32 state after the step's draws
     int i;               // particle index
-    int pad;
+    int tri0;            // element at the step's start
 };
 
 struct WalkQueue {
@@ -596,8 +639,8 @@ __device__ __forceinline__ void count_sections(const DevParams& p, int* stats, d
     if (p.ncsec == 0 || stats == nullptr) return;
     int* row = stats + (p.nopen > 0 ? p.nopen : 1);
     for (int c = 0; c < p.ncsec; ++c) {
-        const double4 g = p.csec[c];
-        if (intersec2d(x0, y0, x1, y1, g.x, g.y, g.z, g.w)) atomicAdd(&row[c], 1);
+        const SectionSeg g = p.csec[c];
+        if (intersec2d(x0, y0, x1, y1, g.x0, g.y0, g.x1, g.y1)) atomicAdd(&row[c], 1);
     }
 }
 
@@ -620,6 +663,68 @@ __device__ inline int grid_locate(const DevMesh& m, double x, double y) {
         if (in_tri(m, k, x, y)) return k;
     }
     return -1;
+}
+
+// The walk record of element k (DevMesh::wrec, 8 x 16 bytes): vertices a,
+// b, c (FP64, the element's vertex order), its FP32 P1 gradients as in
+// Tri32, the ids of its three edges in the element's edge order, the two
+// elements of each edge as the edge table holds them, and each edge's end
+// points as local vertex indices (2 bits each: first end, second end).
+struct WalkRec {
+    double2 a, b, c;
+    float4 g0, g1;    // {gx0, gx1, gx2, gy0}, {gy1, gy2, -, -}
+    int e0, e1, e2;
+    int z0, w0, z1, w1, z2, w2;
+    int order;
+};
+
+__device__ __forceinline__ double2 bits_double2(int4 w) {
+    return make_double2(__hiloint2double(w.y, w.x), __hiloint2double(w.w, w.z));
+}
+
+__device__ __forceinline__ WalkRec load_walkrec(const DevMesh& m, int k) {
+    const int4* r = m.wrec + 8 * (size_t)CG_IDX(m, k, m.nt);
+    const int4 w0 = __ldg(&r[0]), w1 = __ldg(&r[1]), w2 = __ldg(&r[2]), w3 = __ldg(&r[3]);
+    const int4 w4 = __ldg(&r[4]), w5 = __ldg(&r[5]), w6 = __ldg(&r[6]);
+    WalkRec t;
+    t.a = bits_double2(w0);
+    t.b = bits_double2(w1);
+    t.c = bits_double2(w2);
+    t.g0 = make_float4(__int_as_float(w3.x), __int_as_float(w3.y), __int_as_float(w3.z),
+                       __int_as_float(w3.w));
+    t.g1 = make_float4(__int_as_float(w4.x), __int_as_float(w4.y), 0.f, 0.f);
+    t.e0 = w4.z; t.e1 = w4.w; t.e2 = w5.x;
+    t.z0 = w5.y; t.w0 = w5.z; t.z1 = w5.w;
+    t.w1 = w6.x; t.z2 = w6.y; t.w2 = w6.z;
+    t.order = w6.w;
+    return t;
+}
+
+__device__ __forceinline__ double2 rec_vertex(const WalkRec& t, int l) {
+    return l == 0 ? t.a : (l == 1 ? t.b : t.c);
+}
+
+// edge slot i of the record: id, end points (the edge table's order) and
+// the element across it from k (the edge table's test, so that k == -1
+// behaves as in the reference)
+__device__ __forceinline__ void rec_edge(const WalkRec& t, int i, int k, int& j, double2& ea,
+                                         double2& eb, int& kn) {
+    const int ez = i == 0 ? t.z0 : (i == 1 ? t.z1 : t.z2);
+    const int ew = i == 0 ? t.w0 : (i == 1 ? t.w1 : t.w2);
+    j = i == 0 ? t.e0 : (i == 1 ? t.e1 : t.e2);
+    ea = rec_vertex(t, (t.order >> (4 * i)) & 3);
+    eb = rec_vertex(t, (t.order >> (4 * i + 2)) & 3);
+    kn = ez == k ? ew : ez;
+}
+
+// in_tri from the record: the same vertices and edge vectors (b - a, c - b,
+// a - c, formed with the host's FP64 subtractions) as DevMesh::geo
+__device__ __forceinline__ bool in_tri_rec(const WalkRec& t, double x, double y) {
+    const double2 dab = make_double2(__dsub_rn(t.b.x, t.a.x), __dsub_rn(t.b.y, t.a.y));
+    const double2 dbc = make_double2(__dsub_rn(t.c.x, t.b.x), __dsub_rn(t.c.y, t.b.y));
+    const double2 dca = make_double2(__dsub_rn(t.a.x, t.c.x), __dsub_rn(t.a.y, t.c.y));
+    return rot_ok(x, y, t.a, dab, dca) && rot_ok(x, y, t.b, dbc, dab) &&
+           rot_ok(x, y, t.c, dca, dbc);
 }
 
 // The three edge records of a triangle and their end points, issued
@@ -917,6 +1022,14 @@ __device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, i
     return in_tri_decide(m, bary32(t, x, y), k, x, y);
 }
 
+// the same from a walk record (its vertex a and gradients are Tri32's)
+__device__ __forceinline__ bool in_tri_mixed_rec(const WalkRec& t, double x, double y) {
+    const Bary b = bary32_off(t, (float)(x - t.a.x), (float)(y - t.a.y));
+    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return true;
+    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return false;
+    return in_tri_rec(t, x, y);
+}
+
 // xylocalizer.pyx:338-435 with FP32-filtered predicates: the in-element
 // tests through in_tri_mixed, the segment/edge tests through
 // intersec2d_filtered, both falling back to FP64 where the FP32 value is
@@ -924,43 +1037,92 @@ __device__ __forceinline__ bool in_tri_mixed(const DevMesh& m, const Tri32& t, i
 // boundary edge, as path_walk.
 __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, double p0y, double x,
                                        double y, int& new_k, int& bnd) {
+    new_k = -1;
+    bnd = -1;
     int intersected_edge = -1;
     const float2 p1 = make_float2((float)(x - p0x), (float)(y - p0y));
-    Tri32 tk = load_tri32(m, k);
+    WalkRec t = load_walkrec(m, k);
     for (int niter = 0; niter <= NITER_MAX; ++niter) {
-        const int ed[3] = {tri32_edge(tk, 0), tri32_edge(tk, 1), tri32_edge(tk, 2)};
-        int4 er[3];
-        double2 va[3], vb[3];
-        walk_gather(m, ed, er, va, vb);
         bool intersects = false;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            int j = ed[i];
+            int j, kn;
+            double2 a, b;
+            rec_edge(t, i, k, j, a, b, kn);
             if (j == intersected_edge) continue;
-            const int4 e = er[i];
-            const double2 a = va[i], b = vb[i];
-            float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
-            float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
+            const float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
+            const float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
             if (intersec2d_filtered(p1, fa, fb, p0x, p0y, x, y, a, b)) {
                 intersects = true;
-                int kn = (e.z == k) ? e.w : e.z;
-                if (kn == -1) { new_k = -1; bnd = j; return; }
-                Tri32 tn = load_tri32(m, kn);
-                if (in_tri_mixed(m, tn, kn, x, y)) { new_k = kn; bnd = -1; return; }
+                if (kn == -1) { bnd = j; return; }
+                const WalkRec tn = load_walkrec(m, kn);
+                if (in_tri_mixed_rec(tn, x, y)) { new_k = kn; return; }
                 k = kn;
-                tk = tn;
+                t = tn;
                 intersected_edge = j;
                 break;
             }
         }
         if (!intersects) {
-            new_k = in_tri_mixed(m, tk, k, x, y) ? k : -1;
-            bnd = -1;
+            if (in_tri_mixed_rec(t, x, y)) new_k = k;
             return;
         }
     }
-    new_k = -1;
-    bnd = -1;
+}
+
+// in-element decision from FP32 barycentrics: 1 certainly inside, 0
+// certainly outside, -1 within the rounding band (exact test needed)
+__device__ __forceinline__ int decide32(const Bary& b) {
+    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return 1;
+    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return 0;
+    return -1;
+}
+
+// index of the one edge (opposite vertex j) that the point is certainly
+// beyond while certainly inside the other two; -1 otherwise
+__device__ __forceinline__ int single_exit(const Bary& b) {
+    const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
+    const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
+    if (n0 && p1 && p2) return 0;
+    if (n1 && p0 && p2) return 1;
+    if (n2 && p0 && p1) return 2;
+    return -1;
+}
+
+// One-hop exit.  When the start point is certainly inside the start
+// triangle and the end point certainly beyond exactly one of its edges (the
+// other two barycentric coordinates certainly positive at both points), the
+// segment crosses that edge alone, in its interior: the first edge the
+// reference's path walk finds (xylocalizer.pyx:375-415).  The walk's next
+// test, the point in the neighbour across it, is made here, and so are up
+// to two further crossings of the same kind (see hop_walk_split).  Returns
+// the triangle holding the end point, else -1 (the full walk decides).
+__device__ __forceinline__ int one_hop(const DevMesh& m, int tri0, const Bary& bs, const Bary& be,
+                                       double xn, double yn) {
+    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
+    int k = tri0;
+    Bary b = be;
+    // further crossings as hop_walk_split argues (up to three in all)
+#pragma unroll 1
+    for (int h = 0; h < 3; ++h) {
+        const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
+        const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
+        int j;
+        if (n0 && p1 && p2) j = 0;
+        else if (n1 && p0 && p2) j = 1;
+        else if (n2 && p0 && p1) j = 2;
+        else return -1;
+        int4 nb = __ldg(&m.nbr[CG_IDX(m, k, m.nt)]);
+        int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
+        if (kn < 0) return -1;   // boundary edge: the full walk finds it
+        Tri32 tn = load_tri32(m, kn);
+        b = bary32(tn, xn, yn);
+        if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return kn;
+        if (!(b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2))   // rounding band
+            return in_tri(m, kn, xn, yn) ? kn : -1;
+        k = kn;
+    }
+    return -1;
 }
 
 // xy_localize (xylocalizer.pyx:27-124, method 3) with the FP32-filtered
@@ -975,7 +1137,11 @@ __device__ inline void xy_localize_filtered(const DevMesh& m, int k, double p0x,
     }
     bnd = -1;
     const Tri32 t = load_tri32(m, k);
-    if (in_tri_mixed(m, t, k, x, y)) { new_k = k; return; }
+    const Bary be = bary32(t, x, y);
+    if (in_tri_decide(m, be, k, x, y)) { new_k = k; return; }
+    // certain single-edge crossings in FP32 (one_hop), the full walk else
+    new_k = one_hop(m, k, bary32(t, p0x, p0y), be, x, y);
+    if (new_k >= 0) return;
     path_walk_mixed(m, k, p0x, p0y, x, y, new_k, bnd);
     if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
 }

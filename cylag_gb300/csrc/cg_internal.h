@@ -122,8 +122,8 @@ struct WorkState {
     int* tag;                 // [n]
     unsigned long long* rng;  // [n]
     int* slot;                // [n] caller index of each working particle
-    double* vel;              // [n][dim] or nullptr
-    double* fvs;              // [n][dim] or nullptr
+    double* vel;              // [n][dim] or nullptr (float rows under W_V32)
+    double* fvs;              // [n][dim] or nullptr (float rows under W_V32 with W_FVS)
     int* layer;               // [n] or nullptr
     double* diam;             // [n] or nullptr
     double* lpos;             // [n][dim] last position (W_AUXW) or nullptr

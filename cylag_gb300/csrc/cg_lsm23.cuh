@@ -35,7 +35,7 @@ __device__ __forceinline__ double drag_almedeij(double Re) {
 template <typename R>
 __device__ __forceinline__ R drag_coefficient(const DevParams& p, R U, R dp) {
     R Re = fmax(R(EPSILON), U * dp / R(NU0));
-    if (p.drag_model == 0) return R(p.drag_coef);
+    if (p.drag_model == 0) return par<R>(p.drag_coef, p.drag_coef32);
     if (p.drag_model == 1) {
         if (Re <= R(1000.)) return (R(24.) / Re) * (R(1.) + R(0.15) * cpow_re(Re, R(0.687)));
         return R(0.44);
@@ -56,7 +56,7 @@ __device__ __forceinline__ double lsm2_a1(const DevParams& p, int dim, double dp
     R unorm = dim == 2 ? sqrt(x * x + y * y) : sqrt(x * x + y * y + z * z);
     unorm = fmax(R(EPSILON_LSM2), unorm);
     R Cd = drag_coefficient<R>(p, unorm, d);
-    return double(R(p.a1c) * (R(1.5) / d) * Cd * unorm);
+    return double(par<R>(p.a1c, p.a1c32) * (R(1.5) / d) * Cd * unorm);
 }
 
 template <typename FT>
@@ -65,15 +65,24 @@ __host__ __device__ constexpr bool is_mixed() { return std::is_same<FT, float>::
 // mean velocity (and, when asked, acceleration) at (k, l, px, py, pz) in the
 // arithmetic V: FP64 interpolation in the plain form, FP32 from the FP32
 // records and barycentrics in the mixed form
+// mixed: mean velocity (and acceleration) from the P1 factors P in FP32
+template <int DIM, typename FT>
+__device__ __forceinline__ void mean_fields32(Particle<DIM, FT>& q,
+                                              const typename Particle<DIM, FT>::P1f& P, int l,
+                                              float pz, bool want_acc, float& ux, float& uy,
+                                              float& uz, float& ax, float& ay, float& az) {
+    ax = ay = az = 0.f;
+    q.velocity32(P, l, pz, ux, uy, uz);
+    if (want_acc) q.accel32(P, l, pz, ux, uy, uz, ax, ay, az);
+}
+
 template <typename V, int DIM, typename FT>
 __device__ __forceinline__ void mean_fields(Particle<DIM, FT>& q, int k, int l, double px,
                                             double py, double pz, bool want_acc, V& ux, V& uy,
                                             V& uz, V& ax, V& ay, V& az) {
     if constexpr (is_mixed<FT>()) {
-        auto P = q.p1f_at(k, px, py);
-        float u, v, w, a = 0.f, b = 0.f, c = 0.f;
-        q.velocity32(P, l, (float)pz, u, v, w);
-        if (want_acc) q.accel32(P, l, (float)pz, u, v, w, a, b, c);
+        float u, v, w, a, b, c;
+        mean_fields32(q, q.p1f_at(k, px, py), l, (float)pz, want_acc, u, v, w, a, b, c);
         ux = V(u); uy = V(v); uz = V(w);
         ax = V(a); ay = V(b); az = V(c);
     } else {
@@ -238,13 +247,18 @@ __device__ __forceinline__ int rk_lsm2(Particle<DIM, FT>& q, double dp) {
 
 // T_L and eps at the particle from the FP32 records (mixed form)
 template <int DIM, typename FT>
-__device__ __forceinline__ float keps_tml32(Particle<DIM, FT>& q, int k, int l, double px,
-                                            double py, double pz, float& ep) {
-    auto P = q.p1f_at(k, px, py);
+__device__ __forceinline__ float keps_tml32p(Particle<DIM, FT>& q,
+                                             const typename Particle<DIM, FT>::P1f& P, int l,
+                                             float pz, float& ep) {
     float kt;
-    q.turb32(P, l, (float)pz, kt, ep);
+    q.turb32(P, l, pz, kt, ep);
     ep = fmaxf(ep, (float)EPSILON);
     return (kt / ep) / (0.5f + 0.75f * (float)C0KOLM);
+}
+template <int DIM, typename FT>
+__device__ __forceinline__ float keps_tml32(Particle<DIM, FT>& q, int k, int l, double px,
+                                            double py, double pz, float& ep) {
+    return keps_tml32p(q, q.p1f_at(k, px, py), l, (float)pz, ep);
 }
 
 // B_k^2 terms of the k-epsilon LSM2 diffusion: T_L and (kt, eps) at the
@@ -356,8 +370,7 @@ __device__ __forceinline__ bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>
 // di_ode_lsm2, 1232-1238).  Mixed form: coefficients, means and increments
 // in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
-__device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, double nux, double nuz,
-                        int nuopt) {
+__device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int diffmod, int nuopt) {
     using R = typename ArithOf<FT>::type;
     const DevParams& p = q.p;
     const double dt = p.dt;
@@ -376,9 +389,9 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
     } else {
         R sx = ux - R(up0[0]), sy = uy - R(up0[1]), sz = DIM == 3 ? uz - R(up0[2]) : R(0.);
         R unorm = fmax(R(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
-        a1 = R(p.a1c) * (R(1.5) / R(dp)) * drag_coefficient<R>(p, unorm, R(dp)) * unorm;
+        a1 = par<R>(p.a1c, p.a1c32) * (R(1.5) / R(dp)) * drag_coefficient<R>(p, unorm, R(dp)) * unorm;
     }
-    const R rdt = R(dt);
+    const R rdt = par<R>(dt, p.dt32);
     Lsm2Coef<R> c;
     if (!lsm2_direct_coefficients<R>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return; }
     R um_beta = -expm1(-a1 * rdt);
@@ -390,13 +403,13 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
         } else {
             tml = keps_tml32(q, q.tri, q.ll, xp0[0], xp0[1], z0, ep);
         }
-        const R rnuz = R(nuz);
+        const R rnuz = par<R>(p.nuz, p.nuz32);
         b2[0] = a1 * a1 * R(C0KOLM) * ep * (tml * tml);
         b2[1] = b2[0];
         if (diffmod == 2) b2[2] = nuopt == 2 ? rnuz * rnuz : R(2.) * rnuz * a1 * a1;
         else b2[2] = b2[0];
     } else if (diffmod != 0) {
-        const R rnux = R(nux), rnuz = R(nuz);
+        const R rnux = par<R>(p.nux, p.nux32), rnuz = par<R>(p.nuz, p.nuz32);
         if (nuopt == 2) {
             b2[0] = rnux * rnux;
             b2[1] = b2[0];
@@ -412,11 +425,12 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         const R u_k = mu[d];
-        const R Fp = d == 2 ? R(p.a2c) * acc[2] - R(GRAV) * R(p.a0c) : R(p.a2c) * acc[d];
+        const R a2c = par<R>(p.a2c, p.a2c32);
+        const R Fp = d == 2 ? a2c * acc[2] - R(GRAV) * par<R>(p.a0c, p.a0c32) : a2c * acc[d];
         const R v0 = R(up0[d]);
         q.us[d] = double(mu[d]);
         R Gp = R(0.), Gx = R(0.);
-        const bool noise = !(b2[d] == R(0.) || dt == 0.);
+        const bool noise = !(b2[d] == R(0.) || rdt == R(0.));
         if (noise) {
             R var_gp = b2[d] * c.q_uu, cov = b2[d] * c.q_xu, var_gx = b2[d] * c.q_xx;
             R L_pp = sqrt(fmax(R(0.), var_gp));
@@ -455,7 +469,7 @@ __device__ __forceinline__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
         else if constexpr (SCHEME == 2) bnd_j = rk_lsm2<2>(q, dp);
         else if constexpr (SCHEME == 3) bnd_j = rk_lsm2<3>(q, dp);
         else if constexpr (SCHEME == 4) bnd_j = rk_lsm2<4>(q, dp);
-        else di_lsm2(q, dp, 0, 0., 0., 2);
+        else di_lsm2(q, dp, 0, 2);
         if (diffmod != 0) {
             // K and its gradient at the start point only for the k-epsilon models
             P1 q0{};
@@ -465,7 +479,7 @@ __device__ __forceinline__ int update_lsm2(Particle<DIM, FT>& q, double dp) {
     } else if constexpr (SCHEME == 1) {
         euler_maruyama_lsm2_u(q, dp);
     } else if constexpr (SCHEME == 5) {
-        di_lsm2(q, dp, diffmod, p.nux, p.nuz, nuopt);
+        di_lsm2(q, dp, diffmod, nuopt);
     } else {
         q.err |= ERR_UNSUPPORTED;
         return -1;
@@ -839,7 +853,7 @@ __device__ __forceinline__ void lsm3_cholesky_clipped(const R* q, R* lower) {
 template <typename R>
 __device__ __forceinline__ R lsm3_a1(const DevParams& p, R dp, R unorm) {
     R Cd = drag_coefficient(p, unorm, dp);
-    return R(p.a1c) * (R(1.5) / dp) * unorm * Cd;
+    return par<R>(p.a1c, p.a1c32) * (R(1.5) / dp) * unorm * Cd;
 }
 
 template <int DIM>
@@ -935,26 +949,27 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
         unorm = fmax(R(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
     }
     const R a1 = lsm3_a1<R>(p, R(dp), unorm);
-    const R a2 = p.added_mass ? R(p.a2c) : R(0.);
-    R tl_h = R(p.tl_h), tl_v = R(p.tl_v), sigma_h, sigma_v = R(0.);
+    const R a2 = p.added_mass ? par<R>(p.a2c, p.a2c32) : R(0.);
+    R tl_h = par<R>(p.tl_h, p.tl_h32), tl_v = par<R>(p.tl_v, p.tl_v32), sigma_h, sigma_v = R(0.);
     if (diffmod == 2 || diffmod == 3) {
         tl_h = fmax(R(EPSILON_LSM3), tml_ke);
         sigma_h = sqrt(R(C0KOLM) * ep);
     } else {
-        sigma_h = sqrt(R(2.) * R(p.nux)) / tl_h;
+        sigma_h = sqrt(R(2.) * par<R>(p.nux, p.nux32)) / tl_h;
     }
     if (DIM == 3) {
         if (diffmod == 3) {
             tl_v = tl_h;
             sigma_v = sigma_h;
         } else {
-            sigma_v = sqrt(R(2.) * R(p.nuz)) / tl_v;
+            sigma_v = sqrt(R(2.) * par<R>(p.nuz, p.nuz32)) / tl_v;
         }
     }
     const R mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
     Lsm3Coef<R> c;
     R lower[9];
-    if (!lsm3_coefficients<R>(a1, a2, tl_h, R(dt), edge_opt, c)) { q.err |= ERR_NONFINITE; return; }
+    const R rdt = par<R>(dt, p.dt32);
+    if (!lsm3_coefficients<R>(a1, a2, tl_h, rdt, edge_opt, c)) { q.err |= ERR_NONFINITE; return; }
     bool factored = false;
     R sigma_s = sigma_h;
 #pragma unroll
@@ -964,7 +979,7 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
             tl_k = tl_v;
             sigma_s = sigma_v;
             if (tl_v != tl_h) {
-                if (!lsm3_coefficients<R>(a1, a2, tl_v, R(dt), edge_opt, c)) {
+                if (!lsm3_coefficients<R>(a1, a2, tl_v, rdt, edge_opt, c)) {
                     q.err |= ERR_NONFINITE;
                     return;
                 }
@@ -972,7 +987,7 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
             }
         }
         const R u_k = mean_flow[d], acc = mean_acc[d];
-        const R Fp = d == 2 ? -R(GRAV) * R(p.a0c) : R(0.);
+        const R Fp = d == 2 ? -R(GRAV) * par<R>(p.a0c, p.a0c32) : R(0.);
         const R s0 = R(us0[d]);
         const R ur0 = exact ? R(up0[d] - a2 * us0[d]) : R(up0[d]) - a2 * s0;
         R us_mean = (s0 * c.phi[0] + u_k * c.flow[0] + acc * tl_k * c.flow[0]);

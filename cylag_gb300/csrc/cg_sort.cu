@@ -141,6 +141,33 @@ __device__ __forceinline__ void move_rows(const T* __restrict__ src, T* __restri
     for (int d = 0; d < dim; ++d) dst[(size_t)to * dim + d] = __ldcs(src + (size_t)from * dim + d);
 }
 
+// velocity rows: FP64 in the caller's arrays, FP32 in working copies under
+// W_V32 (converted on the way in from the caller's arrays)
+__device__ __forceinline__ void move_vel_rows(const double* __restrict__ src,
+                                              double* __restrict__ dst, int from, int to,
+                                              int dim, bool v32, bool from_caller) {
+    if (!v32) {
+        move_rows(src, dst, from, to, dim);
+        return;
+    }
+    float* d32 = reinterpret_cast<float*>(dst);
+    if (from_caller) {
+        for (int d = 0; d < dim; ++d)
+            d32[(size_t)to * dim + d] = (float)__ldcs(src + (size_t)from * dim + d);
+    } else {
+        move_rows(reinterpret_cast<const float*>(src), d32, from, to, dim);
+    }
+}
+
+// working velocity row j -> the caller's FP64 row i
+__device__ __forceinline__ void put_vel_rows(const double* __restrict__ w, double* __restrict__ user,
+                                             int j, int i, int dim, bool v32) {
+    for (int d = 0; d < dim; ++d) {
+        const size_t k = (size_t)j * dim + d;
+        __stcs(user + (size_t)i * dim + d, v32 ? (double)reinterpret_cast<const float*>(w)[k] : w[k]);
+    }
+}
+
 // dst[j] = src[perm[j]]; src.slot == nullptr: the source is the caller's arrays.
 // split: working positions are split FP32 pairs (W_SPLIT), made from the
 // caller's FP64 positions here and moved as they are between working copies.
@@ -163,8 +190,9 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
     dst.tag[j] = __ldcs(src.tag + i);
     dst.rng[j] = __ldcs(src.rng + i);
     dst.slot[j] = src.slot ? __ldcs(src.slot + i) : i;
-    if (work & W_VEL) move_rows(src.vel, dst.vel, i, j, dim);
-    if (work & W_FVS) move_rows(src.fvs, dst.fvs, i, j, dim);
+    const bool v32 = (work & W_V32) != 0, from_caller = src.slot == nullptr;
+    if (work & W_VEL) move_vel_rows(src.vel, dst.vel, i, j, dim, v32, from_caller);
+    if (work & W_FVS) move_vel_rows(src.fvs, dst.fvs, i, j, dim, v32, from_caller);
     if (work & W_LAYER) dst.layer[j] = __ldcs(src.layer + i);
     if (work & W_DIAM) dst.diam[j] = __ldcs(src.diam + i);
     if (work & W_AUXW)
@@ -185,10 +213,9 @@ __global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim
     __stcs(user.tri + i, w.tri[j]);
     __stcs(user.tag + i, w.tag[j]);
     __stcs(user.rng + i, w.rng[j]);
-    if (work & W_VEL)
-        for (int d = 0; d < dim; ++d) __stcs(user.vel + (size_t)i * dim + d, w.vel[(size_t)j * dim + d]);
-    if (work & W_FVS)
-        for (int d = 0; d < dim; ++d) __stcs(user.fvs + (size_t)i * dim + d, w.fvs[(size_t)j * dim + d]);
+    const bool v32 = (work & W_V32) != 0;
+    if (work & W_VEL) put_vel_rows(w.vel, user.vel, j, i, dim, v32);
+    if (work & W_FVS) put_vel_rows(w.fvs, user.fvs, j, i, dim, v32);
     if (work & W_LAYER) __stcs(user.layer + i, w.layer[j]);
     if (work & W_DIAM) __stcs(user.diam + i, w.diam[j]);
     if (work & W_AUXW) {

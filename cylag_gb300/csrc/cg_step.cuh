@@ -341,7 +341,9 @@ struct Particle {
     };
     __device__ P1f p1f_at(int k, double px, double py) const {
         Tri32 t = load_tri32(m, k);
-        Bary b = bary32(t, px, py);
+        return p1f_of(t, bary32(t, px, py));
+    }
+    __device__ P1f p1f_of(const Tri32& t, const Bary& b) const {
         P1f r;
         r.i0 = t.tv.x; r.i1 = t.tv.y; r.i2 = t.tv.z;
         r.f0 = b.l0; r.f1 = b.l1; r.f2 = b.l2;
@@ -469,11 +471,12 @@ struct Particle {
     // (eulerian_field_set.pyx:1117-1182)
     __device__ int z_localize32(int k, double px, double py, double pz) {
         if (k == -1) return PART_LOC_O;
-        P1f q = p1f_at(k, px, py);
+        return z_localize32_q(p1f_at(k, px, py), (float)pz);
+    }
+    __device__ int z_localize32_q(const P1f& q, float z) {
         int nl = f.nlayers;
         float zbp = ev(f.cur, 0, q, Slots<DIM>::ZS);
         float zsp = ev(f.cur, (nl - 1) * f.npoints, q, Slots<DIM>::ZS);
-        float z = (float)pz;
         int l = 0;
         if (nl > 1) {
             float hl = (zsp - zbp) / (float)(nl - 1);
@@ -640,18 +643,23 @@ struct Particle {
     // end of the step (solver.pyx:505-524): state write-back; deletion per
     // lagrangian_particle_set.pyx:766-788, the tag recording the iteration
     // for the host-side retag (maxtag+1, ... in iteration then index order)
-    __device__ void store(DevState& s, int i, int aux, int step_index, const double* lastv) {
+    // last_velocity (aux >= 2) is the velocity the state held at the step's
+    // start, read here before the new one overwrites it
+    __device__ void store(DevState& s, int i, int aux, int step_index) {
         const int D = DIM;
         const int a = aux_index(s, i);   // slot of the per-particle arrays outside the sort
         const int iv = widx(s, i, a, W_VEL), iu = widx(s, i, a, W_FVS | W_AUXW);
         const int il = widx(s, i, a, W_LAYER), id = widx(s, i, a, W_DIAM);
         const int ix = widx(s, i, a, W_AUXW);
+        // the mixed LSM2/LSM3 form keeps its velocities as FP32 values,
+        // whether the state is FP32 working copies or the caller's arrays
+        const bool v32 = std::is_same<FT, float>::value && p.model >= 2;
         if (deleted) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.pos[(size_t)i * D + d] = 0.;
-                s.vel[(size_t)iv * D + d] = 0.;
-                s.fvs[(size_t)iu * D + d] = 0.;
+                vel_st(s, (size_t)iv * D + d, 0.);
+                fvs_st(s, (size_t)iu * D + d, 0.);
                 s.last_pos[(size_t)ix * D + d] = 0.;
                 s.last_vel[(size_t)ix * D + d] = 0.;
             }
@@ -673,13 +681,23 @@ struct Particle {
         s.tri[i] = tri;
         if (DIM == 3) s.lowerlayer[il] = ll;
         s.rng[i] = rng.state;
+        double lastv[3] = {0., 0., 0.};
+        if (aux >= 2) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const double v = vel_ld(s, (size_t)iv * D + d);
+                lastv[d] = v32 ? (double)(float)v : v;
+            }
+        }
         if (p.model >= 2 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.vel[(size_t)iv * D + d] = up[d];
+            for (int d = 0; d < D; ++d)
+                vel_st(s, (size_t)iv * D + d, v32 ? (double)(float)up[d] : up[d]);
         }
         if (p.model == 3 || aux >= 1) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s.fvs[(size_t)iu * D + d] = us[d];
+            for (int d = 0; d < D; ++d)
+                fvs_st(s, (size_t)iu * D + d, v32 ? (double)(float)us[d] : us[d]);
         }
         if (aux >= 2) {
 #pragma unroll
@@ -849,15 +867,21 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
         q.x0[d] = q.x[d];
     }
     const double sx = q.x[0], sy = q.x[1];   // last_position of the step
-    bool need_vel = (MODEL >= 2) || aux >= 2;
-    if (need_vel) {
+    // mixed LSM2/LSM3: velocities as FP32 values (see Particle::store)
+    constexpr bool v32 = std::is_same<FT, float>::value && MODEL >= 2;
+    if (MODEL >= 2) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.up[d] = s.vel[(size_t)widx(s, i, ai, W_VEL) * D + d];
+        for (int d = 0; d < D; ++d) {
+            const double v = vel_ld(s, (size_t)widx(s, i, ai, W_VEL) * D + d);
+            q.up[d] = v32 ? (double)(float)v : v;
+        }
     }
-    double lastv[3] = {q.up[0], q.up[1], DIM == 3 ? q.up[2] : 0.};
     if (MODEL == 3) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) q.us[d] = s.fvs[(size_t)widx(s, i, ai, W_FVS) * D + d];
+        for (int d = 0; d < D; ++d) {
+            const double v = fvs_ld(s, (size_t)widx(s, i, ai, W_FVS) * D + d);
+            q.us[d] = v32 ? (double)(float)v : v;
+        }
     }
     q.rng.state = s.rng[i];
     q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
@@ -878,7 +902,7 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
         w.yn = q.x[1];
         w.rng = q.rng.state;
         w.i = i;
-        w.pad = 0;
+        w.tri0 = q.tri0;
         wq.e[slot] = w;
         return;
     }
@@ -891,7 +915,7 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
     }
     e = q.err | q.rng.err;
     if (e) atomicOr(err_word, e);
-    q.store(s, i, aux, step_index, lastv);
+    q.store(s, i, aux, step_index);
     if (p.ncsec) {
         const bool del = q.deleted;
         count_sections(p, stats, del ? 0. : sx, del ? 0. : sy, del ? 0. : q.x[0],
@@ -909,8 +933,18 @@ __device__ __forceinline__ void step_particle(const DevMesh& m, const DevFields<
 // instantiation per combination, so that each kernel holds one integrator
 // inlined (no particle state in local memory) and the LSM1 kernels keep
 // their register budget.
+// Resident blocks of 256 per SM that a step kernel's register budget is set
+// for: two for the mixed LSM2/LSM3 kernels (at most 128 registers; at one
+// block per SM their dependent loads stall with nothing to hide them), one
+// otherwise.
+template <typename FT, int MODEL>
+constexpr int step_min_blocks() {
+    return (MODEL >= 2 && std::is_same<FT, float>::value) ? 2 : 1;
+}
+
 template <int DIM, typename FT, int MODEL = 1, int SCHEME = 0>
-__global__ void __launch_bounds__(256) step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
+__global__ void __launch_bounds__(256, step_min_blocks<FT, MODEL>())
+    step_kernel(DevMesh m, DevFields<FT> f, DevParams p,
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
@@ -1002,7 +1036,7 @@ __global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<F
         WalkEntry w = wq.e[j];
         int i = (int)CG_IDX(m, w.i, s.n);
         Particle<2, FT> q(m, f, p, zt);
-        int tri0 = s.tri[i];
+        const int tri0 = w.tri0;   // s.tri[i], carried in the entry: the first record load need not wait for it
         double2 x0 = (s.work & W_SPLIT) ? join_pos(reinterpret_cast<const float4*>(s.pos)[i])
                                         : reinterpret_cast<const double2*>(s.pos)[i];
         q.tri0 = tri0;
@@ -1015,12 +1049,6 @@ __global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<F
         q.rng.state = w.rng;
         q.rng.inc = ((uint64_t)(uint32_t)s.tag[i] << 1) | 1ULL;
         q.rng.err = 0;
-        double lastv[3] = {0., 0., 0.};
-        if (aux >= 2) {
-            double2 v = reinterpret_cast<const double2*>(s.vel)[widx(s, i, aux_index(s, i), W_VEL)];
-            lastv[0] = v.x;
-            lastv[1] = v.y;
-        }
         if (aux >= 1 || p.model >= 2) {
             // LSM1: up = us = U(x0) (update_state_lsm1.pyx:144-163)
             double ux, uy, uz;
@@ -1039,7 +1067,7 @@ __global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<F
         else if (q.tri == PART_LOC_O) q.deleted = true;
         uint32_t e = q.err | q.rng.err;
         if (e) atomicOr(err_word, e);
-        q.store(s, i, aux, step_index, lastv);
+        q.store(s, i, aux, step_index);
         if (p.ncsec) {
             const bool del = q.deleted;
             count_sections(p, stats, del ? 0. : x0.x, del ? 0. : x0.y, del ? 0. : q.x[0],

@@ -29,42 +29,6 @@ __device__ __forceinline__ void xy_localize_mixed(const DevMesh& m, const Tri32&
     if (new_k == -1 && bnd == -1) new_k = grid_locate(m, x, y);
 }
 
-// One-hop exit.  When the start point is certainly inside the start
-// triangle and the end point certainly beyond exactly one of its edges (the
-// other two barycentric coordinates certainly positive at both points), the
-// segment crosses that edge alone, in its interior: the first edge the
-// reference's path walk finds (xylocalizer.pyx:375-415).  The walk's next
-// test, the point in the neighbour across it, is made here, and so are up
-// to two further crossings of the same kind (see hop_walk_split).  Returns
-// the triangle holding the end point, else -1 (the walk kernel decides).
-__device__ __forceinline__ int one_hop(const DevMesh& m, int tri0, const Bary& bs, const Bary& be,
-                                       double xn, double yn) {
-    if (!(bs.l0 > bs.e0 && bs.l1 > bs.e1 && bs.l2 > bs.e2)) return -1;
-    int k = tri0;
-    Bary b = be;
-    // further crossings as hop_walk_split argues (up to three in all)
-#pragma unroll 1
-    for (int h = 0; h < 3; ++h) {
-        const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
-        const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
-        int j;
-        if (n0 && p1 && p2) j = 0;
-        else if (n1 && p0 && p2) j = 1;
-        else if (n2 && p0 && p1) j = 2;
-        else return -1;
-        int4 nb = __ldg(&m.nbr[CG_IDX(m, k, m.nt)]);
-        int kn = j == 0 ? nb.x : (j == 1 ? nb.y : nb.z);
-        if (kn < 0) return -1;   // boundary edge: the walk kernel applies the conditions
-        Tri32 tn = load_tri32(m, kn);
-        b = bary32(tn, xn, yn);
-        if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return kn;
-        if (!(b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2))   // rounding band
-            return in_tri(m, kn, xn, yn) ? kn : -1;
-        k = kn;
-    }
-    return -1;
-}
-
 // FP32 P1 interpolation of the packed node record {ux, uy, K, zs}
 struct Node4 {
     float4 n0, n1, n2;
@@ -175,25 +139,6 @@ static __device__ __noinline__ BcOut bc_mixed(const DevMesh& m, const DevFields<
     o.tri = q.tri;
     o.deleted = q.deleted;
     return o;
-}
-
-// in-element decision from FP32 barycentrics: 1 certainly inside, 0
-// certainly outside, -1 within the rounding band (exact test needed)
-__device__ __forceinline__ int decide32(const Bary& b) {
-    if (b.l0 > b.e0 && b.l1 > b.e1 && b.l2 > b.e2) return 1;
-    if (b.l0 < -b.e0 || b.l1 < -b.e1 || b.l2 < -b.e2) return 0;
-    return -1;
-}
-
-// index of the one edge (opposite vertex j) that the point is certainly
-// beyond while certainly inside the other two; -1 otherwise
-__device__ __forceinline__ int single_exit(const Bary& b) {
-    const bool n0 = b.l0 < -b.e0, n1 = b.l1 < -b.e1, n2 = b.l2 < -b.e2;
-    const bool p0 = b.l0 > b.e0, p1 = b.l1 > b.e1, p2 = b.l2 > b.e2;
-    if (n0 && p1 && p2) return 0;
-    if (n1 && p0 && p2) return 1;
-    if (n2 && p0 && p1) return 2;
-    return -1;
 }
 
 // The walk's first hops for a split end position, decided in FP32 where the
@@ -417,7 +362,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                 w.yn = yn;
                 w.rng = rng.state;
                 w.i = i;
-                w.pad = 0;
+                w.tri0 = tri0;
                 wq.e[slot] = w;
                 return;
             }
