@@ -33,8 +33,10 @@ __device__ __noinline__ void serve_particle(const DevMesh& m, const DevFields<FT
     step_particle<2, FT, MODEL, SCHEME>(m, f, p, pool, none, aux, k, nullptr, err, zt, i, z32);
 }
 
+// the mixed form is bounded to two resident blocks of 256 per SM (128
+// registers), as the step kernels of the mixed LSM2/LSM3 runs it steps
 template <typename FT, bool MIXED>
-__global__ void __launch_bounds__(256) serve_step_kernel(DevMesh m, DevFields<FT> f, DevState pool,
+__global__ void __launch_bounds__(256, MIXED ? 2 : 1) serve_step_kernel(DevMesh m, DevFields<FT> f, DevState pool,
                                                          const ServeRun* __restrict__ runs,
                                                          const int2* __restrict__ active,
                                                          const int* __restrict__ nactive,
