@@ -209,7 +209,7 @@ def bytes_per_particle_step(workload, precision):
 # DRAM bytes per particle-step of one step's kernels, from ncu captures of
 # the same kernels on smaller particle counts (element-sorted; the traffic
 # grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 59.2, ("lsm1_2d", "fp64"): 147.0,
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 57.8, ("lsm1_2d", "fp64"): 147.0,
                                    ("lsm2_3d", "mixed"): 155.2, ("lsm3_3d", "mixed"): 136.6}
 NCU_TRAFFIC_SOURCE = {
     ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step and walk "
