@@ -219,6 +219,61 @@ class EulerianFieldSet:
                                 None, friction_model=friction_model,
                                 friction_coefficient=friction_coefficient)
 
+    @staticmethod
+    def from_hdf5(fset_file="cylag_fset_file.h5", mesh_file="cylag_mesh_file.h5",
+                  optional_fields=None, init_trifinder=True, friction_model=1,
+                  friction_coefficient=40.):
+        """eulerian_field_set.pyx:486-566 from a CyLag field-set file and mesh
+        file (written by the reference's ``save_hdf5`` or by this one; read by
+        ``cylag_gb300.hdf5``).  The optional fields are named from the file
+        unless ``optional_fields`` names them.  ``init_trifinder`` is accepted
+        and unused: the grid locator replaces matplotlib's trifinder."""
+        from . import hdf5
+        mesh = TriangularMesh.from_hdf5(file_name=mesh_file)
+        f = hdf5.read(fset_file)
+        first = lambda k: int(np.asarray(f[k]).reshape(-1)[0])
+        dim, nplan, nopt = first("dim"), first("nplan"), first("nopt")
+        opt = None
+        if nopt != 0:
+            if optional_fields is None:
+                if "opt_fields_names" in f:
+                    optional_fields = [n.decode("utf-8") if isinstance(n, bytes) else str(n)
+                                       for n in f["opt_fields_names"]]
+                else:
+                    optional_fields = [f"opt_field_{i}" for i in range(nopt)]
+            opt = f["opt_fields"]
+        else:
+            optional_fields = None
+        if dim == 2:
+            return EulerianFieldSet(mesh, 2, 1, f["times"], f["elevation"], f["velocity_x"],
+                                    f["velocity_y"], None, opt, optional_fields, None,
+                                    friction_model=friction_model,
+                                    friction_coefficient=friction_coefficient)
+        if dim == 3:
+            return EulerianFieldSet(mesh, 3, nplan, f["times"], f["elevation"], f["velocity_x"],
+                                    f["velocity_y"], f["velocity_z"], opt, optional_fields, None,
+                                    friction_model=friction_model,
+                                    friction_coefficient=friction_coefficient)
+        raise ValueError(f"{fset_file}: dim {dim} is neither 2 nor 3")
+
+    def save_hdf5(self, fset_file="cylag_fset_file.h5", mesh_file="cylag_mesh_file.h5"):
+        """eulerian_field_set.pyx:568-604: the mesh file, then the field-set
+        file with the same datasets (the optional fields' names as
+        variable-length UTF-8 strings)."""
+        from . import hdf5
+        self.triangular_mesh.save_mesh_hdf5(mesh_file)
+        d = {"dim": np.array([self.dim], dtype=np.int64),
+             "nplan": np.array([self.nlayers], dtype=np.int64),
+             "times": np.asarray(self.times), "elevation": np.asarray(self.elevation),
+             "velocity_x": np.asarray(self.velocity_x), "velocity_y": np.asarray(self.velocity_y),
+             "nopt": np.array([self.nopt], dtype=np.int64)}
+        if self.dim == 3:
+            d["velocity_z"] = np.asarray(self.velocity_z)
+        if self.nopt != 0:
+            d["opt_fields"] = np.asarray(self.opt_fields)
+            d["opt_fields_names"] = [str(n) for n in self.opt_fields_names]
+        hdf5.write(fset_file, d)
+
     def _get_field_from_id(self, field_id):
         """eulerian_field_set.pyx:673-720: 0 elevation, 1-3 velocity, 4+ the
         optional fields in the given order ([ntimes, npoints*nlayers])."""

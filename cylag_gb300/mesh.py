@@ -84,8 +84,48 @@ class TriangularMesh:
             self.gradx = np.ascontiguousarray(gradx, dtype=np.float64)
             self.grady = np.ascontiguousarray(grady, dtype=np.float64)
             self.det = np.ascontiguousarray(det, dtype=np.float64)
-        self.triangle_centroids = triangle_centroids
+        if triangle_centroids is None:
+            # triangular_mesh.pyx:605-628 (the KD-tree's points; the bucket
+            # grid replaces the tree, the centroids are kept for the files)
+            t = self.triangles
+            triangle_centroids = np.stack(
+                [(self.x[t[:, 0]] + self.x[t[:, 1]] + self.x[t[:, 2]]) / 3.0,
+                 (self.y[t[:, 0]] + self.y[t[:, 1]] + self.y[t[:, 2]]) / 3.0], axis=1)
+        self.triangle_centroids = np.ascontiguousarray(triangle_centroids, dtype=np.float64)
         self._grid = None
+
+    # -- HDF5 files (triangular_mesh.pyx:204-290) ------------------------------
+    _HDF5_ARRAYS = ("x", "y", "triangles", "edges", "vertex_adjacency", "edgetri_map",
+                    "triedge_map", "boundary_points", "boundary_edges", "vertex_labels",
+                    "edges_labels", "signed_area", "gradx", "grady", "det",
+                    "triangle_centroids")
+
+    @staticmethod
+    def from_hdf5(file_name="cylag_mesh_file.h5"):
+        """triangular_mesh.pyx:204-246: every array from a CyLag mesh file
+        (written by the reference's ``save_mesh_hdf5`` or by this one), so the
+        mesh keeps the file's edge numbering; read by ``cylag_gb300.hdf5``."""
+        from . import hdf5
+        f = hdf5.read(file_name)
+        missing = [k for k in TriangularMesh._HDF5_ARRAYS + ("nopen",) if k not in f]
+        if missing:
+            raise KeyError(f"{file_name}: not a CyLag mesh file (no {', '.join(missing)})")
+        return TriangularMesh(
+            f["x"], f["y"], f["triangles"], f["edges"], f["vertex_adjacency"],
+            f.get("triangle_adjacency"), f.get("triangle_neighbors"), f["edgetri_map"],
+            f["triedge_map"], f["boundary_points"], f["boundary_edges"], f["vertex_labels"],
+            f["edges_labels"], f["signed_area"], f["gradx"], f["grady"], f["det"],
+            f["triangle_centroids"], int(np.asarray(f["nopen"]).reshape(-1)[0]))
+
+    def save_mesh_hdf5(self, file_name="cylag_mesh_file.h5"):
+        """triangular_mesh.pyx:248-286: the same datasets, names and dtypes."""
+        from . import hdf5
+        d = {k: np.asarray(getattr(self, k)) for k in self._HDF5_ARRAYS}
+        for k in ("triangle_adjacency", "triangle_neighbors"):
+            if getattr(self, k, None) is not None:
+                d[k] = np.asarray(getattr(self, k))
+        d["nopen"] = np.array([self.nopen], dtype=np.int64)
+        hdf5.write(file_name, d)
 
     # -- edges (triangular_mesh.pyx:288-309) --------------------------------
     @staticmethod

@@ -125,6 +125,25 @@ def test_gpu_run_from_telemac_files(tmp_path):
     s.close()
 
 
+def test_gpu_run_from_hdf5_files(tmp_path):
+    """The open-channel fixture's field set saved as CyLag HDF5 mesh and
+    field-set files (save_hdf5) and read back (from_hdf5): the reference's
+    trajectories and exit counts.  The reloaded mesh is a second
+    TriangularMesh built from the file's arrays, not the one that wrote it."""
+    import cylag_gb300 as cg
+    case, meta, want = load_golden("open")
+    fs0 = cg.EulerianFieldSet(mesh_from_case(case), **fields_from_case(case))
+    fs0.save_hdf5(str(tmp_path / "f.h5"), str(tmp_path / "m.h5"))
+    fs = cg.EulerianFieldSet.from_hdf5(str(tmp_path / "f.h5"), str(tmp_path / "m.h5"))
+    assert fs.triangular_mesh is not fs0.triangular_mesh and fs.triangular_mesh.nopen == 2
+    ps = cg.LagrangianParticleSet(case["position"], dim=2, **meta.get("pset", {}))
+    s = cg.Solver(fs, ps, meta["params"], seed=meta["seed"])
+    s.forward(nsteps=meta["nsteps"])
+    assert_state_close(state(ps), want, rtol=RTOL, what="from hdf5")
+    np.testing.assert_array_equal(s.bnd_statistics(), want["bnd_stats"])
+    s.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_sorted_state_kept_across_calls(precision):
     """An element-sorted run keeps its working copies between forward()
