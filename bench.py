@@ -79,7 +79,8 @@ def parse_args(argv=None):
                     help="arrival window of the serving leg, s")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-chunk", type=int, default=0,
-                    help="particles per copy/step chunk of the end-to-end steps (0: about n/8)")
+                    help="particles per copy/step chunk of the end-to-end steps (0: the library's "
+                         "default, four chunks)")
     args = ap.parse_args(argv)
     if args.steps is None:
         args.steps = 1000 if args.workload == "lsm1_2d" else 100

@@ -64,8 +64,20 @@ void launch_walk_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     DevFields<float> f = fv.as<float>();
-    walk_kernel<float, true><<<nsm * WALK_BLOCKS_PER_SM, WALK_BLOCK, 0, st>>>(
-        m, f, p, s, wq, aux, step_index, stats, err);
+    // programmatic dependent launch: the walk grid is set up while the step
+    // kernel's last blocks run (they signal it at their start); its blocks
+    // wait for the step grid to finish before reading the queue
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nsm * WALK_BLOCKS_PER_SM);
+    cfg.blockDim = dim3(WALK_BLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, walk_kernel<float, true>, m, f, p, s, wq, aux, step_index, stats, err);
 }
 
 }  // namespace cg

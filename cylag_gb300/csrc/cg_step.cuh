@@ -1026,6 +1026,10 @@ __global__ void __launch_bounds__(WALK_BLOCK) walk_kernel(DevMesh m, DevFields<F
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
+    // launched as a programmatic dependent of the step kernel (mixed form):
+    // wait until that grid has finished and its writes are visible (a no-op
+    // for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int count = *wq.count;
     // blocks beyond the queue leave before loading the tables (the grid is
     // sized for any count; most steps queue few particles)

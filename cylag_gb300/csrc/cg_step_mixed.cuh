@@ -284,7 +284,14 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     if (p.diffmod != 0) {
         float diffx, driftx = 0.f, drifty = 0.f;
         if (p.diffmod == 2 || p.diffmod == 3) {
-            const float4 g0 = SPLIT ? t0s.g0 : t0.g0, g1 = SPLIT ? t0s.g1 : t0.g1;
+            float4 g0, g1;
+            if constexpr (SPLIT) {
+                g0 = t0s.g0;
+                g1 = t0s.g1;
+            } else {
+                g0 = t0.g0;
+                g1 = t0.g1;
+            }
             float K = b0.l0 * n0.n0.z + b0.l1 * n0.n1.z + b0.l2 * n0.n2.z;
             float dKdx = n0.n0.z * g0.x + n0.n1.z * g0.y + n0.n2.z * g0.z;
             float dKdy = n0.n0.z * g0.w + n0.n1.z * g1.x + n0.n2.z * g1.y;
@@ -440,6 +447,9 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
                                                                 int step_index,
                                                                 int* __restrict__ stats,
                                                                 uint32_t* __restrict__ err_word) {
+    // every block of this one-wave grid is resident: let the walk kernel
+    // that follows be set up now (it waits for this grid's completion)
+    asm volatile("griddepcontrol.launch_dependents;");
     __shared__ Zig32 z32;
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
         z32.kn[t] = g_zig.kn[t];

@@ -261,9 +261,9 @@ typedef struct {
  * drop-in for a caller whose arrays are the reference's host arrays: every
  * step copies the `in` arrays into the run's device arrays, steps, and copies
  * the device arrays back into the `out` arrays, chunk by chunk (`chunk`
- * particles; 0 = a ramp of 1/32 .. 4/32 of the pool), so that the copies of one chunk overlap the
- * step of another (a host->device stream, the run's stream, a device->host
- * stream).  Same results as copying in, cg_run_step(run, 1), copying out, per
+ * particles; 0 = four equal chunks on 256-particle boundaries from 2^20
+ * particles up), so that the copies of one chunk overlap the step of another
+ * (a host->device stream, the run's stream, a device->host stream).  Same results as copying in, cg_run_step(run, 1), copying out, per
  * step.  Refused (CG_ESTATE) while added particles await initialization. */
 int cg_run_step_host(cg_run *run, int32_t nsteps, const cg_host_arrays *in,
                      const cg_host_arrays *out, int32_t chunk, int32_t *bnd_stats);
