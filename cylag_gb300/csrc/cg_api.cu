@@ -39,11 +39,16 @@ struct cg_run {
     DevBuf turb;          // {k, eps} per node (LSM2/LSM3 k-epsilon runs)
     DevBuf stats;
     int stats_rows = 0;
+    int qpar = 0;   // which of the walk queue's two counters the next step uses
     int stats_cols = 0;
     DevBuf csec;                     // control-section segments {x0, y0, x1, y1}
     std::vector<int32_t> csec_counts;  // [nsteps, ncsec] of the last cg_run_step
     int csec_steps = 0;
     cudaStream_t h2d = nullptr, d2h = nullptr;   // cg_run_step_host copy streams
+    // cg_run_step of a run with a walk queue: the next step's field blend on
+    // its own stream, during this step (step_started -> blend -> blended)
+    cudaStream_t bstream = nullptr;
+    cudaEvent_t step_started = nullptr, blended = nullptr;
     std::vector<cudaEvent_t> hev;                // ... and its per-chunk events
     DevBuf strand;                   // stranding output: count (first 256 B) + n records
     bool strand_on = false;
@@ -394,6 +399,41 @@ static uint32_t take_bounds_error(cg_ctx* c) {
     (void)c;
     return 0;
 #endif
+}
+
+// The walk queue of the next step (or chunk): a run's steps alternate
+// between two counters, so that no step needs a separate reset.  The one a
+// step uses is zero when it starts (the call zeroed it, or the previous step
+// kernel did); the step kernel zeroes the other, whose walk has finished.
+static WalkQueue next_queue(cg_run* r, int* counters, WalkEntry* entries) {
+    WalkQueue wq{nullptr, nullptr, nullptr};
+    if (!r->use_queue) return wq;
+    wq.count = counters + r->qpar;
+    wq.e = entries;
+    wq.reset = counters + (1 - r->qpar);
+    r->qpar ^= 1;
+    return wq;
+}
+
+// a call's first step: its counter zeroed, whatever ran on the array before
+static int start_queue(cg_run* r, int* counters) {
+    if (!r->use_queue) return CG_OK;
+    CUDA_TRY(r->ctx, cudaMemsetAsync(counters + r->qpar, 0, sizeof(int), r->ctx->stream));
+    return CG_OK;
+}
+
+// The per-step statistics rows of a call: grown to at least 1024 rows and by
+// doubling, so that a call longer than the last one does not reallocate
+// (cudaFree and cudaMalloc synchronize the device) inside a timed loop.
+static int ensure_stats(cg_run* r, int nsteps, int row) {
+    if (r->stats_rows >= nsteps && r->stats_cols == row) return CG_OK;
+    const int rows = std::max(nsteps, std::max(2 * r->stats_rows, 1024));
+    dfree(r->stats);
+    int rc = dalloc(r->ctx, r->stats, (size_t)rows * row * sizeof(int));
+    if (rc) return rc;
+    r->stats_rows = rows;
+    r->stats_cols = row;
+    return CG_OK;
 }
 
 // Working copies -> the caller's arrays (stream-ordered), after which the
@@ -857,6 +897,9 @@ int cg_run_destroy(cg_run* r) {
     for (auto e : r->hev) cudaEventDestroy(e);
     if (r->h2d) cudaStreamDestroy(r->h2d);
     if (r->d2h) cudaStreamDestroy(r->d2h);
+    if (r->bstream) cudaStreamDestroy(r->bstream);
+    if (r->step_started) cudaEventDestroy(r->step_started);
+    if (r->blended) cudaEventDestroy(r->blended);
     c->used -= r->bytes;
     delete r;
     return CG_OK;
@@ -883,8 +926,9 @@ static FieldView field_view(const cg_run* r) {
 
 // eulerian_field_set.pyx:866-938: saves the previous temps (pointer swap)
 // and interpolates at `time` into the current ones.
-static int time_interpolation(cg_run* r, double time) {
+static int time_interpolation(cg_run* r, double time, cudaStream_t st = nullptr) {
     cg_ctx* c = r->ctx;
+    if (!st) st = c->stream;
     if (r->frozen) {
         if (!r->fields_ready) {
             launch_blend(c->frames, 0, 1.0, true, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
@@ -905,7 +949,7 @@ static int time_interpolation(cg_run* r, double time) {
         return set_err(c, CG_EINVAL, "Time interpolation failed: duplicate times at record %d", rec);
     double tf = (time - c->times[rec + 1]) / dt;
     launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
-                 r->prm.dim, c->stream);
+                 r->prm.dim, st);
     r->fields_ready = true;
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -967,28 +1011,44 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     // sections' counts
     const int nopen = c->nopen > 0 ? c->nopen : 1;
     const int row = nopen + r->dp.ncsec;
-    if (r->stats_rows < nsteps || r->stats_cols != row) {
-        dfree(r->stats);
-        if ((rc = dalloc(c, r->stats, (size_t)nsteps * row * sizeof(int)))) return rc;
-        r->stats_rows = nsteps;
-        r->stats_cols = row;
-    }
+    if ((rc = ensure_stats(r, nsteps, row))) return rc;
     CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * row * sizeof(int), c->stream));
     if (r->strand_on) CUDA_TRY(c, cudaMemsetAsync(r->strand.p, 0, sizeof(int), c->stream));
-    int nev = 2 * nsteps;
-    while ((int)r->ev.size() < nev) {
-        cudaEvent_t e;
-        CUDA_TRY(c, cudaEventCreate(&e));
-        r->ev.push_back(e);
+    // two timing events per step, created ahead by doubling (as the rows)
+    const int nev = 2 * nsteps;
+    if ((int)r->ev.size() < nev) {
+        const int want = std::max(nev, std::max(2 * (int)r->ev.size(), 512));
+        while ((int)r->ev.size() < want) {
+            cudaEvent_t e;
+            CUDA_TRY(c, cudaEventCreate(&e));
+            r->ev.push_back(e);
+        }
     }
     // element-sorted working state: gathered from the caller's arrays at the
     // first step after a write-back, re-sorted every sort_period steps
     // (counted across calls), kept resident between calls
     const bool sorted = r->sort_period > 0 && r->st.n > 0;
+    if ((rc = start_queue(r, (int*)r->queue.p))) return rc;
     int launches = 0;   // kernels launched by this call
+    // LSM1 2D runs (a walk queue; neither kernel reads the previous record):
+    // step s + 1's blend writes the record that step s - 1 used, so it runs
+    // on its own stream from the start of step s, overlapping the step's
+    // tail and its walk
+    const bool pre_blend = r->use_queue && !r->frozen && nsteps > 1;
+    if (pre_blend && !r->bstream) {
+        CUDA_TRY(c, cudaStreamCreateWithFlags(&r->bstream, cudaStreamNonBlocking));
+        CUDA_TRY(c, cudaEventCreateWithFlags(&r->step_started, cudaEventDisableTiming));
+        CUDA_TRY(c, cudaEventCreateWithFlags(&r->blended, cudaEventDisableTiming));
+    }
+    bool blended = false;   // this step's fields were blended during the last one
     for (int s = 0; s < nsteps; ++s) {
         // solver.pyx:440: fields at the step-start time
-        if ((rc = time_interpolation(r, r->time))) return rc;
+        if (blended) {
+            CUDA_TRY(c, cudaStreamWaitEvent(c->stream, r->blended, 0));
+            blended = false;
+        } else if ((rc = time_interpolation(r, r->time))) {
+            return rc;
+        }
         if (!r->frozen) launches += 1;   // field blend
         // particles added since the last step: initialized with this step's
         // fields, then advanced by it (solver.pyx:443-470)
@@ -1011,15 +1071,20 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * row;
         CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
-        WalkQueue wq{nullptr, nullptr};
-        if (r->use_queue) {
-            wq.count = (int*)r->queue.p;
-            wq.e = (WalkEntry*)((char*)r->queue.p + 256);
-            CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
-        }
+        const WalkQueue wq = next_queue(r, (int*)r->queue.p,
+                                        (WalkEntry*)((char*)r->queue.p + 256));
         const FieldView fv = field_view(r);
         uint32_t* errw = (uint32_t*)r->errw.p;
         const int it = (int)r->iteration;
+        if (pre_blend && s + 1 < nsteps) {
+            // the next step's fields (the records swap in time_interpolation;
+            // this step keeps the view taken above)
+            CUDA_TRY(c, cudaEventRecord(r->step_started, c->stream));
+            CUDA_TRY(c, cudaStreamWaitEvent(r->bstream, r->step_started, 0));
+            if ((rc = time_interpolation(r, r->time + r->prm.time_step, r->bstream))) return rc;
+            CUDA_TRY(c, cudaEventRecord(r->blended, r->bstream));
+            blended = true;
+        }
         if (r->prm.precision == CG_PRECISION_MIXED)
             launch_step_mixed(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         else
@@ -1273,6 +1338,7 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
     int launches = r->resident ? 1 : 0;   // the write-back of sorted working copies
     if ((rc = write_back(r))) return rc;
     if ((rc = ensure_fields(r))) return rc;
+    if ((rc = start_queue(r, scratch->count))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         if ((rc = time_interpolation(r, r->time))) return rc;
         if (!r->frozen) launches += 1;
@@ -1284,14 +1350,7 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
             launches += 1;
         }
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
-        WalkQueue wq{nullptr, nullptr};
-        if (r->use_queue) {
-            // the array keeps the previous call's contents: the counter must
-            // start at zero every step
-            wq.count = scratch->count;
-            wq.e = scratch->entries;
-            CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
-        }
+        const WalkQueue wq = next_queue(r, scratch->count, scratch->entries);
         const FieldView fv = field_view(r);
         uint32_t* errw = (uint32_t*)r->errw.p;
         const int it = (int)r->iteration;
@@ -1416,12 +1475,7 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
     cudaEvent_t ev_start = r->hev[3 * nch];
     const int nopen = c->nopen > 0 ? c->nopen : 1;
     const int row = nopen + r->dp.ncsec;
-    if (r->stats_rows < nsteps || r->stats_cols != row) {
-        dfree(r->stats);
-        if ((rc = dalloc(c, r->stats, (size_t)nsteps * row * sizeof(int)))) return rc;
-        r->stats_rows = nsteps;
-        r->stats_cols = row;
-    }
+    if ((rc = ensure_stats(r, nsteps, row))) return rc;
     CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * row * sizeof(int), c->stream));
     if (r->strand_on) CUDA_TRY(c, cudaMemsetAsync(r->strand.p, 0, sizeof(int), c->stream));
     // the copy streams start after what is queued on the run's stream
@@ -1429,6 +1483,7 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
     CUDA_TRY(c, cudaStreamWaitEvent(r->h2d, ev_start, 0));
     CUDA_TRY(c, cudaStreamWaitEvent(r->d2h, ev_start, 0));
     uint32_t* errw = (uint32_t*)r->errw.p;
+    if ((rc = start_queue(r, (int*)r->queue.p))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         if ((rc = time_interpolation(r, r->time))) return rc;
         const int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
@@ -1445,12 +1500,8 @@ int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
             // step
             CUDA_TRY(c, cudaStreamWaitEvent(c->stream, ev_in[j], 0));
             const DevState v = slice_state(r->st, a, m, D);
-            WalkQueue wq{nullptr, nullptr};
-            if (r->use_queue) {
-                wq.count = (int*)r->queue.p;
-                wq.e = (WalkEntry*)((char*)r->queue.p + 256);
-                CUDA_TRY(c, cudaMemsetAsync(wq.count, 0, sizeof(int), c->stream));
-            }
+            const WalkQueue wq = next_queue(r, (int*)r->queue.p,
+                                            (WalkEntry*)((char*)r->queue.p + 256));
             if (r->prm.precision == CG_PRECISION_MIXED) {
                 launch_step_mixed(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);
                 if (wq.e) launch_walk_mixed(c->mesh, fv, r->dp, v, wq, aux, it, stats, errw, c->stream);

@@ -301,9 +301,18 @@ struct WalkEntry {
 };
 
 struct WalkQueue {
-    int* count;          // entries this step (reset before the step)
+    int* count;          // entries this step (zero when the step starts)
     WalkEntry* e;        // capacity: one entry per particle
+    // a run's steps alternate between two counters: the step kernel zeroes
+    // the other one here for the next step (nullptr: nothing to zero)
+    int* reset;
 };
+
+// block 0 of a step kernel that fills the walk queue: the next step's
+// counter (the previous step's, whose walk has finished) back to zero
+__device__ __forceinline__ void reset_next_queue(const WalkQueue& wq) {
+    if (wq.reset != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *wq.reset = 0;
+}
 
 // warp-aggregated slot reservation
 __device__ __forceinline__ int queue_slot(const WalkQueue& q) {

@@ -948,6 +948,7 @@ __global__ void __launch_bounds__(256, step_min_blocks<FT, MODEL>())
                                                    DevState s, WalkQueue wq, int aux,
                                                    int step_index, int* __restrict__ stats,
                                                    uint32_t* __restrict__ err_word) {
+    reset_next_queue(wq);
     __shared__ ZigTables zt;
     // the mixed LSM2/LSM3 direct integrators draw from FP32 tables
     constexpr bool z32_on = std::is_same<FT, float>::value && MODEL >= 2;

@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     // every block of this one-wave grid is resident: let the walk kernel
     // that follows be set up now (it waits for this grid's completion)
     asm volatile("griddepcontrol.launch_dependents;");
+    reset_next_queue(wq);
     __shared__ Zig32 z32;
     for (int t = threadIdx.x; t < 128; t += blockDim.x) {
         z32.kn[t] = g_zig.kn[t];
