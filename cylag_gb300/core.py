@@ -1210,6 +1210,12 @@ class Solver:
         self.L.cg_run_last_kernel_ms(self._run, C.byref(ms), C.byref(n))
         return ms.value, n.value
 
+    def last_kernel_split_ms(self):
+        """Mean ms per step of the last call: (step kernel, walk kernel)."""
+        a, b = C.c_double(), C.c_double()
+        self.L.cg_run_last_kernel_split_ms(self._run, C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def close(self):
         if getattr(self, "_snapshots", None) is not None:
             self._snapshots.close()

@@ -71,6 +71,7 @@ struct cg_run {
     std::vector<cudaEvent_t> ev;
     int last_launches = 0;
     double last_ms = 0.;
+    double last_step_ms = 0., last_walk_ms = 0.;   // the step kernel alone, the walk alone
 };
 
 template <typename T>
@@ -288,7 +289,7 @@ struct ScratchPlan {
 
 static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32) {
+static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32, bool depth) {
     ScratchPlan q;
     const size_t n = (size_t)(n32 > 0 ? n32 : 0);
     q.n = n;
@@ -316,6 +317,13 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     if (p->precision == CG_PRECISION_MIXED && p->dim == 2 && p->model == 1) q.work |= W_SPLIT;
     // mixed LSM2/LSM3: FP32 working velocities (and fluid velocities seen)
     if (p->precision == CG_PRECISION_MIXED && p->model >= 2) q.work |= W_V32;
+    // ... and, for the 3D direct integrators without compute_depth, FP32-pair
+    // working positions (step_split3_kernel): LSM3, and LSM2 with its
+    // velocity diffusion (the integrator that moves the position itself)
+    if (p->precision == CG_PRECISION_MIXED && p->dim == 3 && p->time_scheme == 5 && !depth &&
+        (p->model == 3 ||
+         (p->model == 2 && p->diffusion_model != 0 && p->diffusion_lsm2_option >= 2)))
+        q.work |= W_SPLIT3;
     const size_t D = (size_t)p->dim;
     const size_t vb = (q.work & W_V32) ? 4 : 8;
     const size_t work_bytes = al256(n * 8 * D) + 4 * al256(n * 8) +
@@ -825,7 +833,7 @@ int cg_run_create(cg_ctx* c, const cg_params* p, const cg_state_desc* s, cg_run*
     bool need_turb = p->model >= 2 && (p->diffusion_model == 2 || p->diffusion_model == 3);
     size_t turb_bytes = need_turb ? 2 * c->frames.nnodes * (p->precision ? 4 : 8) : 0;
     uint64_t state_bytes = state_bytes_of(s->n, p->dim);
-    const ScratchPlan plan = plan_scratch(c, p, s->n);
+    const ScratchPlan plan = plan_scratch(c, p, s->n, s->depth != nullptr);
     uint64_t need = state_bytes + 2 * rec_bytes + turb_bytes + 64 + plan.queue_bytes + plan.sort_bytes;
     if (c->budget && c->used + need > c->budget)
         return set_err(c, CG_ENOMEM_BUDGET, "run needs %llu bytes, %llu of %llu in use",
@@ -1014,8 +1022,9 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
     if ((rc = ensure_stats(r, nsteps, row))) return rc;
     CUDA_TRY(c, cudaMemsetAsync(r->stats.p, 0, (size_t)nsteps * row * sizeof(int), c->stream));
     if (r->strand_on) CUDA_TRY(c, cudaMemsetAsync(r->strand.p, 0, sizeof(int), c->stream));
-    // two timing events per step, created ahead by doubling (as the rows)
-    const int nev = 2 * nsteps;
+    // three timing events per step (before the step kernel, between it and
+    // the walk, after the walk), created ahead by doubling (as the rows)
+    const int nev = 3 * nsteps;
     if ((int)r->ev.size() < nev) {
         const int want = std::max(nev, std::max(2 * (int)r->ev.size(), 512));
         while ((int)r->ev.size() < want) {
@@ -1070,7 +1079,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         const DevState run_state = sorted ? sorted_view(r->st, r->sb) : r->st;
         int aux = (s == nsteps - 1) ? 2 : (s == nsteps - 2 ? 1 : 0);
         int* stats = (int*)r->stats.p + (size_t)s * row;
-        CUDA_TRY(c, cudaEventRecord(r->ev[2 * s], c->stream));
+        CUDA_TRY(c, cudaEventRecord(r->ev[3 * s], c->stream));
         const WalkQueue wq = next_queue(r, (int*)r->queue.p,
                                         (WalkEntry*)((char*)r->queue.p + 256));
         const FieldView fv = field_view(r);
@@ -1089,13 +1098,14 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             launch_step_mixed(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         else
             launch_step_plain(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
+        CUDA_TRY(c, cudaEventRecord(r->ev[3 * s + 1], c->stream));
         if (r->use_queue) {
             if (r->prm.precision == CG_PRECISION_MIXED)
                 launch_walk_mixed(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
             else
                 launch_walk_plain(c->mesh, fv, r->dp, run_state, wq, aux, it, stats, errw, c->stream);
         }
-        CUDA_TRY(c, cudaEventRecord(r->ev[2 * s + 1], c->stream));
+        CUDA_TRY(c, cudaEventRecord(r->ev[3 * s + 2], c->stream));
         CUDA_TRY(c, cudaGetLastError());
         launches += r->st.n > 0 ? (r->use_queue ? 2 : 1) : 0;   // step (+ walk)
         if (sorted) r->since_sort += 1;
@@ -1110,13 +1120,17 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         launches += 1;
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    double tot = 0.;
+    double tot = 0., tstep = 0.;
     for (int s = 0; s < nsteps; ++s) {
-        float ms = 0.f;
-        CUDA_TRY(c, cudaEventElapsedTime(&ms, r->ev[2 * s], r->ev[2 * s + 1]));
+        float ms = 0.f, ms1 = 0.f;
+        CUDA_TRY(c, cudaEventElapsedTime(&ms, r->ev[3 * s], r->ev[3 * s + 2]));
+        CUDA_TRY(c, cudaEventElapsedTime(&ms1, r->ev[3 * s], r->ev[3 * s + 1]));
         tot += ms;
+        tstep += ms1;
     }
     r->last_ms = tot / nsteps;
+    r->last_step_ms = tstep / nsteps;
+    r->last_walk_ms = (tot - tstep) / nsteps;
     r->last_launches = launches;
     if (bnd_stats_host && c->nopen > 0)
         CUDA_TRY(c, cudaMemcpy2D(bnd_stats_host, (size_t)c->nopen * sizeof(int), r->stats.p,
@@ -1220,7 +1234,7 @@ int cg_run_resize(cg_run* r, const cg_state_desc* s) {
                        "call cg_run_writeback before replacing the particle arrays");
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    const ScratchPlan plan = plan_scratch(c, &r->prm, s->n);
+    const ScratchPlan plan = plan_scratch(c, &r->prm, s->n, s->depth != nullptr);
     const uint64_t old_state = state_bytes_of(r->st.n, r->prm.dim);
     const uint64_t new_state = state_bytes_of(s->n, r->prm.dim);
     const uint64_t old_bytes = r->bytes;
@@ -1328,7 +1342,7 @@ int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
         return set_err(c, CG_EINVAL,
                        "cg_run_step_noalloc: the run has control sections or stranding output "
                        "on, which only cg_run_step records");
-    r->last_ms = 0.;
+    r->last_ms = r->last_step_ms = r->last_walk_ms = 0.;
     r->last_launches = 0;
     if (nsteps == 0) return CG_OK;
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1561,6 +1575,13 @@ int cg_run_last_kernel_ms(const cg_run* r, double* ms, int32_t* launches) {
     if (!r) return CG_EINVAL;
     if (ms) *ms = r->last_ms;
     if (launches) *launches = r->last_launches;
+    return CG_OK;
+}
+
+int cg_run_last_kernel_split_ms(const cg_run* r, double* step_ms, double* walk_ms) {
+    if (!r) return CG_EINVAL;
+    if (step_ms) *step_ms = r->last_step_ms;
+    if (walk_ms) *walk_ms = r->last_walk_ms;
     return CG_OK;
 }
 

@@ -230,6 +230,10 @@ constexpr int LAST_UNSET = INT_MIN;
 // working fluid velocities seen are FP32 -- the values the mixed step
 // computes in FP32 and rounds every velocity it stores to
 constexpr int W_V32 = 64;
+// mixed LSM2/LSM3 3D direct integrators: working positions as an FP32 pair
+// hi + lo per coordinate, {x_hi, x_lo, y_hi, y_lo, z_hi, z_lo} in the
+// 24-byte row of the FP64 position
+constexpr int W_SPLIT3 = 128;
 
 // component k of the particle velocity / fluid velocity seen of a state
 // whose working copies may be FP32 (W_V32); the caller's arrays are FP64
@@ -257,6 +261,13 @@ __device__ __forceinline__ float4 split_pos(double x, double y) {
     const float hx = (float)x, hy = (float)y;
     return make_float4(hx, hy, (float)(x - (double)hx), (float)(y - (double)hy));
 }
+
+// one coordinate as an FP32 pair hi + lo (|lo| <= ulp(hi)/2), and back
+__device__ __forceinline__ float2 split1(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double join1(float2 p) { return (double)p.x + (double)p.y; }
 
 // the FP64 value of a split position (rounded to nearest double)
 __device__ __forceinline__ double2 join_pos(float4 p) {

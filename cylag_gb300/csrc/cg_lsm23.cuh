@@ -366,6 +366,72 @@ __device__ __forceinline__ bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>
     return true;
 }
 
+// The mixed form's LSM2 direct integrator on FP32 state
+// (update_state_lsm2.pyx:1329-1542): from the start point's P1 factors P0
+// and height z0 (in q.ll), the particle velocity up (updated), the fluid
+// velocity seen us (set) and the displacement dx.  False, with ERR_NONFINITE
+// in q.err and nothing set, when the coefficients are not finite.
+template <int DIM, typename FT>
+__device__ __forceinline__ bool di_lsm2_32(Particle<DIM, FT>& q,
+                                           const typename Particle<DIM, FT>::P1f& P0, float z0,
+                                           float dp, int diffmod, int nuopt, float* up, float* us,
+                                           float* dx) {
+    const DevParams& p = q.p;
+    float ux, uy, uz, ax, ay, az;
+    mean_fields32(q, P0, q.ll, z0, p.added_mass, ux, uy, uz, ax, ay, az);
+    const float sx = ux - up[0], sy = uy - up[1], sz = DIM == 3 ? uz - up[2] : 0.f;
+    const float unorm = fmax(float(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
+    const float a1 = p.a1c32 * (1.5f / dp) * drag_coefficient<float>(p, unorm, dp) * unorm;
+    const float rdt = p.dt32;
+    Lsm2Coef<float> c;
+    if (!lsm2_direct_coefficients<float>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return false; }
+    const float um_beta = -expm1(-a1 * rdt);
+    float b2[3] = {0.f, 0.f, 0.f};
+    if (diffmod == 2 || diffmod == 3) {
+        float ep;
+        const float tml = keps_tml32p(q, P0, q.ll, z0, ep);
+        const float rnuz = p.nuz32;
+        b2[0] = a1 * a1 * float(C0KOLM) * ep * (tml * tml);
+        b2[1] = b2[0];
+        if (diffmod == 2) b2[2] = nuopt == 2 ? rnuz * rnuz : 2.f * rnuz * a1 * a1;
+        else b2[2] = b2[0];
+    } else if (diffmod != 0) {
+        const float rnux = p.nux32, rnuz = p.nuz32;
+        if (nuopt == 2) {
+            b2[0] = rnux * rnux;
+            b2[1] = b2[0];
+            b2[2] = rnuz * rnuz;
+        } else if (nuopt == 3) {
+            b2[0] = 2.f * rnux * a1 * a1;
+            b2[1] = b2[0];
+            b2[2] = 2.f * rnuz * a1 * a1;
+        }
+    }
+    const float mu[3] = {ux, uy, uz};
+    const float acc[3] = {ax, ay, az};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const float u_k = mu[d];
+        const float Fp = d == 2 ? p.a2c32 * acc[2] - float(GRAV) * p.a0c32 : p.a2c32 * acc[d];
+        const float v0 = up[d];
+        us[d] = u_k;
+        float Gp = 0.f, Gx = 0.f;
+        if (!(b2[d] == 0.f || rdt == 0.f)) {
+            const float var_gp = b2[d] * c.q_uu, cov = b2[d] * c.q_xu, var_gx = b2[d] * c.q_xx;
+            const float L_pp = sqrt(fmax(0.f, var_gp));
+            const float L_xp = L_pp > 0.f ? cov / L_pp : 0.f;
+            const float L_xx = sqrt(fmax(0.f, var_gx - L_xp * L_xp));
+            float xix, xiy;
+            pair32_ol(q.rng, p.rng_method, *q.z32, xix, xiy);   // FP32 draws
+            Gp = L_pp * xix;
+            Gx = L_xp * xix + L_xx * xiy;
+        }
+        up[d] = v0 * c.beta + u_k * um_beta + Fp * c.D1 + Gp;
+        dx[d] = v0 * c.D1 + u_k * c.D2 + Fp * c.force_x + Gx;
+    }
+    return true;
+}
+
 // update_state_lsm2.pyx:1329-1542 (diffmod 0, nux = nuz = 0, nuopt 2:
 // di_ode_lsm2, 1232-1238).  Mixed form: coefficients, means and increments
 // in FP32, one FP64 add per position coordinate.
@@ -381,16 +447,25 @@ __device__ __forceinline__ void di_lsm2(Particle<DIM, FT>& q, double dp, int dif
         up0[d] = q.up[d];
     }
     double z0 = DIM == 3 ? xp0[2] : 0.;
+    if constexpr (!std::is_same<R, double>::value) {
+        // mixed: the FP32 integrator, one FP64 add per position coordinate
+        float up[3] = {0.f, 0.f, 0.f}, us[3], dx[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) up[d] = float(up0[d]);
+        if (!di_lsm2_32(q, q.p1f_at(q.tri, xp0[0], xp0[1]), float(z0), float(dp), diffmod, nuopt,
+                        up, us, dx))
+            return;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            q.us[d] = double(us[d]);
+            q.up[d] = double(up[d]);
+            q.x[d] = xp0[d] + double(dx[d]);
+        }
+        return;
+    }
     R ux, uy, uz, ax, ay, az;
     mean_fields<R>(q, q.tri, q.ll, xp0[0], xp0[1], z0, p.added_mass, ux, uy, uz, ax, ay, az);
-    R a1;
-    if constexpr (std::is_same<R, double>::value) {
-        a1 = lsm2_a1<R>(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.);
-    } else {
-        R sx = ux - R(up0[0]), sy = uy - R(up0[1]), sz = DIM == 3 ? uz - R(up0[2]) : R(0.);
-        R unorm = fmax(R(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
-        a1 = par<R>(p.a1c, p.a1c32) * (R(1.5) / R(dp)) * drag_coefficient<R>(p, unorm, R(dp)) * unorm;
-    }
+    R a1 = lsm2_a1<R>(p, DIM, dp, ux - up0[0], uy - up0[1], DIM == 3 ? uz - up0[2] : 0.);
     const R rdt = par<R>(dt, p.dt32);
     Lsm2Coef<R> c;
     if (!lsm2_direct_coefficients<R>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return; }
@@ -916,6 +991,105 @@ __device__ __forceinline__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double
     }
 }
 
+// The mixed form's LSM3 direct integrator on FP32 state
+// (update_state_lsm3.pyx:822-996): from the start point's P1 factors P0 and
+// height z0 (in q.ll), the particle velocity up and fluid velocity seen us
+// (both updated) and the displacement dx.  False, with ERR_NONFINITE in
+// q.err and nothing set, when a coefficient or factor is not finite.
+template <int DIM, typename FT>
+__device__ __forceinline__ bool di_lsm3_32(Particle<DIM, FT>& q,
+                                           const typename Particle<DIM, FT>::P1f& P0, float z0,
+                                           float dp, float* up, float* us, float* dx) {
+    const DevParams& p = q.p;
+    const int diffmod = p.diffmod, edge_opt = p.edge_opt;
+    float ux, uy, uz, ax, ay, az, ep = 0.f, tml_ke = 0.f;
+    mean_fields32(q, P0, q.ll, z0, true, ux, uy, uz, ax, ay, az);
+    if (diffmod == 2 || diffmod == 3) tml_ke = keps_tml32p(q, P0, q.ll, z0, ep);
+    const float sx = us[0] - up[0], sy = us[1] - up[1], sz = DIM == 3 ? us[2] - up[2] : 0.f;
+    const float unorm = fmax(float(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
+    const float a1 = lsm3_a1<float>(p, dp, unorm);
+    const float a2 = p.added_mass ? p.a2c32 : 0.f;
+    float tl_h = p.tl_h32, tl_v = p.tl_v32, sigma_h, sigma_v = 0.f;
+    if (diffmod == 2 || diffmod == 3) {
+        tl_h = fmax(float(EPSILON_LSM3), tml_ke);
+        sigma_h = sqrt(float(C0KOLM) * ep);
+    } else {
+        sigma_h = sqrt(2.f * p.nux32) / tl_h;
+    }
+    if (DIM == 3) {
+        if (diffmod == 3) {
+            tl_v = tl_h;
+            sigma_v = sigma_h;
+        } else {
+            sigma_v = sqrt(2.f * p.nuz32) / tl_v;
+        }
+    }
+    const float mean_flow[3] = {ux, uy, uz}, mean_acc[3] = {ax, ay, az};
+    Lsm3Coef<float> c;
+    float lower[9];
+    const float rdt = p.dt32;
+    if (!lsm3_coefficients<float>(a1, a2, tl_h, rdt, edge_opt, c)) {
+        q.err |= ERR_NONFINITE;
+        return false;
+    }
+    float nus[3], nup[3], ndx[3];
+    bool factored = false;
+    float sigma_s = sigma_h;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        float tl_k = tl_h;
+        if (d == 2) {
+            tl_k = tl_v;
+            sigma_s = sigma_v;
+            if (tl_v != tl_h) {
+                if (!lsm3_coefficients<float>(a1, a2, tl_v, rdt, edge_opt, c)) {
+                    q.err |= ERR_NONFINITE;
+                    return false;
+                }
+                factored = false;
+            }
+        }
+        const float u_k = mean_flow[d], acc = mean_acc[d];
+        const float Fp = d == 2 ? -float(GRAV) * p.a0c32 : 0.f;
+        const float s0 = us[d];
+        const float ur0 = up[d] - a2 * s0;
+        float us_mean = (s0 * c.phi[0] + u_k * c.flow[0] + acc * tl_k * c.flow[0]);
+        float ur_mean = (ur0 * c.phi[4] + s0 * c.phi[3] + u_k * c.flow[1] +
+                         acc * tl_k * c.flow[1] + Fp * c.force[1]);
+        // the position's mean without x0 (added by the caller)
+        float xp_mean = (ur0 * c.force[1] + s0 * c.phi[6] + u_k * c.flow[2] +
+                         acc * tl_k * c.flow[2] + Fp * c.force[2]);
+        if (sigma_s > 0.f && c.q[0] > 0.f) {
+            if (!factored) {
+                if (edge_opt == 2) {
+                    lsm3_cholesky_clipped<float>(c.q, lower);
+                } else if (!lsm3_cholesky<float>(c.q, lower)) {
+                    q.err |= ERR_NONFINITE;
+                    return false;
+                }
+                factored = true;
+            }
+            float xix, xiy = 0.f, xiz = 0.f;   // FP32 draws
+            if (lower[4] > 0.f) pair32_ol(q.rng, p.rng_method, *q.z32, xix, xiy);
+            else xix = single32_ol(q.rng, p.rng_method, *q.z32);
+            if (lower[8] > 0.f) xiz = single32_ol(q.rng, p.rng_method, *q.z32);
+            us_mean += sigma_s * lower[0] * xix;
+            ur_mean += sigma_s * (lower[3] * xix + lower[4] * xiy);
+            xp_mean += sigma_s * (lower[6] * xix + lower[7] * xiy + lower[8] * xiz);
+        }
+        nus[d] = us_mean;
+        nup[d] = ur_mean + a2 * us_mean;
+        ndx[d] = xp_mean;
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        us[d] = nus[d];
+        up[d] = nup[d];
+        dx[d] = ndx[d];
+    }
+    return true;
+}
+
 // update_state_lsm3.pyx:822-996.  Mixed form: coefficients, Cholesky factor,
 // means and increments in FP32, one FP64 add per position coordinate.
 template <int DIM, typename FT>
@@ -934,6 +1108,24 @@ __device__ __forceinline__ void di_lsm3(Particle<DIM, FT>& q, double dp) {
         us0[d] = q.us[d];
     }
     double z0 = DIM == 3 ? xp0[2] : 0.;
+    if constexpr (!exact) {
+        // mixed: the FP32 integrator, one FP64 add per position coordinate
+        float up[3] = {0.f, 0.f, 0.f}, us[3] = {0.f, 0.f, 0.f}, dx[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            up[d] = float(up0[d]);
+            us[d] = float(us0[d]);
+        }
+        if (!di_lsm3_32(q, q.p1f_at(q.tri, xp0[0], xp0[1]), float(z0), float(dp), up, us, dx))
+            return;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            q.us[d] = double(us[d]);
+            q.up[d] = double(up[d]);
+            q.x[d] = xp0[d] + double(dx[d]);
+        }
+        return;
+    }
     R ux, uy, uz, ax, ay, az, ep = R(0.), tml_ke = R(0.);
     mean_fields<R>(q, q.tri, q.ll, xp0[0], xp0[1], z0, true, ux, uy, uz, ax, ay, az);
     if (diffmod == 2 || diffmod == 3) {

@@ -183,6 +183,10 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
     if (split && src.slot == nullptr) {
         const double2 x = __ldcs(reinterpret_cast<const double2*>(src.pos) + i);
         reinterpret_cast<float4*>(dst.pos)[j] = split_pos(x.x, x.y);
+    } else if ((work & W_SPLIT3) && src.slot == nullptr) {
+        for (int d = 0; d < dim; ++d)
+            reinterpret_cast<float2*>(dst.pos)[(size_t)j * dim + d] =
+                split1(__ldcs(src.pos + (size_t)i * dim + d));
     } else {
         move_rows(src.pos, dst.pos, i, j, dim);
     }
@@ -207,6 +211,10 @@ __global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim
     if (work & W_SPLIT)
         __stcs(reinterpret_cast<double2*>(user.pos) + i,
                join_pos(reinterpret_cast<const float4*>(w.pos)[j]));
+    else if (work & W_SPLIT3)
+        for (int d = 0; d < dim; ++d)
+            __stcs(user.pos + (size_t)i * dim + d,
+                   join1(reinterpret_cast<const float2*>(w.pos)[(size_t)j * dim + d]));
     else
         for (int d = 0; d < dim; ++d)
             __stcs(user.pos + (size_t)i * dim + d, w.pos[(size_t)j * dim + d]);

@@ -343,7 +343,8 @@ struct Particle {
         Tri32 t = load_tri32(m, k);
         return p1f_of(t, bary32(t, px, py));
     }
-    __device__ P1f p1f_of(const Tri32& t, const Bary& b) const {
+    template <typename T>   // Tri32 or Tri32S (the same vertex ids and gradients)
+    __device__ P1f p1f_of(const T& t, const Bary& b) const {
         P1f r;
         r.i0 = t.tv.x; r.i1 = t.tv.y; r.i2 = t.tv.z;
         r.f0 = b.l0; r.f1 = b.l1; r.f2 = b.l2;

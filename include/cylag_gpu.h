@@ -387,6 +387,11 @@ int cg_server_stats(cg_server *srv, int32_t *active_runs, int64_t *active_partic
  * (step, walk, field time interpolation, element sort). */
 int cg_run_last_kernel_ms(const cg_run *run, double *ms, int32_t *launches);
 
+/* The same time split: the step kernel alone and the walk kernel alone
+ * (0 for runs without a walk), mean ms per step over the last cg_run_step
+ * call. */
+int cg_run_last_kernel_split_ms(const cg_run *run, double *step_ms, double *walk_ms);
+
 #ifdef __cplusplus
 }
 #endif

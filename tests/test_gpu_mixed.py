@@ -107,6 +107,55 @@ def test_split_working_positions_follow_fp64_positions():
     assert np.max(np.abs(pa[same] - pb[same])) < 1e-4
 
 
+@pytest.mark.parametrize("model", [2, 3])
+def test_split3_working_positions_follow_fp64_positions(model):
+    """Mixed LSM2/LSM3 3D direct integrators over sorted working copies keep
+    positions as FP32 pairs hi + lo per coordinate and FP32 velocities;
+    without the sort (sort_period=0) the same run keeps FP64 positions.  Same
+    streams: element and layer indices agree for all but a handful of
+    particles, positions to 1e-5 m and velocities to 1e-4 of their spread
+    after 60 steps for all but 1% of them.  Those are particles whose bed
+    reflection the two FP32 layer tests (FP32 heights against FP32 bed
+    elevations, about 1e-6 m apart between the two position forms) decide
+    differently near the bed; they move apart by a few velocity-steps, under
+    0.05 m here."""
+    import cylag_gb300 as cg
+    from cylag_gb300 import synth
+    from cylag_gb300.mesh import TriangularMesh
+    if model == 2:
+        c = synth.lsm2_loglaw_workload(npart=30_000, nx=41, ny=21, nplanes=6, seed=3)
+    else:
+        c = synth.lsm3_taylor_green_workload(npart=30_000, nx=41, ny=21, nplanes=6, seed=3)
+    p = dict(c["parameters"], final_time=1e6)
+    out = {}
+    for sp in (0, 10):
+        mesh = TriangularMesh(c["x"], c["y"], c["triangles"])
+        fs = cg.EulerianFieldSet(mesh, dim=3, nlayers=c["nlayers"], times=c["times"],
+                                 elevation=c["elevation"], velocity_x=c["velocity_x"],
+                                 velocity_y=c["velocity_y"], velocity_z=c["velocity_z"],
+                                 opt_fields=c.get("opt_fields"),
+                                 opt_fields_names=c.get("opt_fields_names"))
+        ps = cg.LagrangianParticleSet(c["position"], dim=3, **c.get("pset", {}))
+        if "diameter" in c:
+            ps.diameter = c["diameter"]
+        s = cg.Solver(fs, ps, p, precision="mixed", seed=3, sort_period=sp)
+        s.forward(nsteps=60)
+        out[sp] = (ps.position, ps.tri, ps.lowerlayer, ps.inactive, ps.velocity)
+        s.close()
+    (pa, ta, la, ia, va), (pb, tb, lb, ib, vb) = out[0], out[10]
+    both = (ia == 0) & (ib == 0)
+    assert both.sum() > 0.5 * len(ia)
+    assert (ia != ib).sum() <= max(5, int(1e-3 * len(ia)))
+    same = both & (ta == tb) & (la == lb)
+    assert (~same & both).sum() <= max(5, int(1e-3 * both.sum()))
+    few = max(5, int(1e-2 * same.sum()))
+    dpos = np.max(np.abs(pa[same] - pb[same]), axis=1)
+    assert (dpos > 1e-5).sum() <= few and dpos.max() < 0.05, np.sort(dpos)[-10:]
+    spread = np.std(va[both], axis=0)
+    dvel = np.max(np.abs(va[same] - vb[same]) / spread, axis=1)
+    assert (dvel > 1e-4).sum() <= few, np.sort(dvel)[-10:]
+
+
 @pytest.mark.parametrize("sort_period", [0, 20])
 @pytest.mark.parametrize("name", ["keps_ts1_rm2", "keps_ts2_rm1", "keps_ts3_rm3", "keps_ts4_rm2"])
 def test_mixed_time_schemes_follow_reference(name, sort_period):
