@@ -111,6 +111,8 @@ SIGNATURES = [
     ("cg_run_errors", C.c_int, [P, C.POINTER(C.c_uint32)]),
     ("cg_run_last_kernel_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(I32)]),
     ("cg_run_last_kernel_split_ms", C.c_int, [P, C.POINTER(F64), C.POINTER(F64)]),
+    ("cg_run_clock", C.c_int, [P, C.POINTER(F64), C.POINTER(F64), C.POINTER(C.c_int64)]),
+    ("cg_run_resume", C.c_int, [P, F64, F64, C.c_int64]),
     ("cg_snapshot_txt", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_int64,
                                   C.c_int32, P, P, P, P, P, P, P]),
     ("cg_snapshot_vtk", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_int64,

@@ -1210,6 +1210,51 @@ class Solver:
         self.L.cg_run_last_kernel_ms(self._run, C.byref(ms), C.byref(n))
         return ms.value, n.value
 
+    # ---- checkpoint / resume -------------------------------------------------
+    _CHECKPOINT_ARRAYS = ("position", "velocity", "fluid_velocity_seen", "last_position",
+                          "last_velocity", "tri", "last_tri", "lowerlayer", "tag", "diameter",
+                          "rng_state", "depth")
+
+    def save_checkpoint(self, file_name):
+        """Writes the particle state (every device array, the PCG32 states
+        included) and the clock to an .npz file; ``load_checkpoint`` on a
+        Solver over the same field set and parameters resumes it bit for
+        bit (the reference has no checkpoint: its snapshots lack the random
+        streams)."""
+        ps = self.particle_set
+        ps._sync()
+        t, ft, it = C.c_double(), C.c_double(), C.c_int64()
+        _lib.check(self._ctx, self.L.cg_run_clock(self._run, C.byref(t), C.byref(ft),
+                                                 C.byref(it)))
+        arrays = {k: ps._dev[k].cpu().numpy() for k in self._CHECKPOINT_ARRAYS if k in ps._dev}
+        np.savez(file_name, npart=ps.npart, maxtag=ps.maxtag, tag_stride=ps.tag_stride,
+                 run_time=t.value, fields_time=ft.value, iteration=it.value,
+                 simutime=np.array([self.simutime.time, self.simutime.iteration], dtype=np.float64),
+                 **arrays)
+
+    def load_checkpoint(self, file_name):
+        """Restores a ``save_checkpoint`` file into this Solver's particle set
+        (the same pool size) and clock; the next forward() continues the
+        checkpointed run."""
+        ps = self.particle_set
+        f = np.load(file_name)
+        if int(f["npart"]) != ps.npart:
+            raise ValueError(f"checkpoint of {int(f['npart'])} particles, particle set of "
+                             f"{ps.npart}")
+        ps._sync()
+        torch = _torch()
+        for k in self._CHECKPOINT_ARRAYS:
+            if k in ps._dev and k in f.files:
+                ps._dev[k].copy_(torch.from_numpy(np.ascontiguousarray(f[k])))
+        torch.cuda.synchronize()
+        ps.maxtag = int(f["maxtag"])
+        ps.tag_stride = int(f["tag_stride"])
+        self.simutime.time = float(f["simutime"][0])
+        self.simutime.iteration = int(f["simutime"][1])
+        _lib.check(self._ctx, self.L.cg_run_resume(self._run, float(f["run_time"]),
+                                                   float(f["fields_time"]),
+                                                   int(f["iteration"])))
+
     def last_kernel_split_ms(self):
         """Mean ms per step of the last call: (step kernel, walk kernel)."""
         a, b = C.c_double(), C.c_double()

@@ -32,6 +32,7 @@ struct cg_run {
     int64_t nt = 0;
     bool frozen = false;
     int record = 0;
+    double fields_time = NAN;   // the time the current field record was blended at
     bool interp_done = false;
     bool prev_valid = false;
     bool fields_ready = false;
@@ -448,6 +449,7 @@ static int ensure_stats(cg_run* r, int nsteps, int row) {
 // caller's arrays are the run's state again and the next step gathers them.
 static int write_back(cg_run* r) {
     if (!r->resident) return CG_OK;
+    NvtxRange nvtx("write back");
     cg_ctx* c = r->ctx;
     launch_sort_scatter(r->st, r->sb, c->stream);
     r->resident = false;
@@ -958,6 +960,7 @@ static int time_interpolation(cg_run* r, double time, cudaStream_t st = nullptr)
     double tf = (time - c->times[rec + 1]) / dt;
     launch_blend(c->frames, rec, tf, false, keps_fac(r), r->cur.p, r->turb.p, r->prm.precision,
                  r->prm.dim, st);
+    r->fields_time = time;
     r->fields_ready = true;
     CUDA_TRY(c, cudaGetLastError());
     return CG_OK;
@@ -1009,6 +1012,7 @@ static int collect_stranded(cg_run* r) {
 }
 
 int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
+    NvtxRange nvtx_call("cg_run_step");
     if (!r || nsteps < 0) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     if (nsteps == 0) return CG_OK;
@@ -1070,6 +1074,7 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
             launches += 1;
         }
         if (sorted && (!r->resident || r->since_sort >= r->sort_period)) {
+            NvtxRange nvtx_sort("element sort");
             if (!r->resident) launch_sort_gather(r->st, c->mesh.nt, r->sb, c->stream);
             else launch_sort_resort(r->st.n, c->mesh.nt, r->sb, c->stream);
             r->resident = true;
@@ -1328,6 +1333,7 @@ int cg_run_time(const cg_run* r, double* time, int64_t* iteration) {
 
 // Allocation-free variant of cg_run_step: see include/cylag_gpu.h.
 int cg_run_step_noalloc(cg_run* r, int32_t nsteps) {
+    NvtxRange nvtx_call("cg_run_step_noalloc");
     if (!r || nsteps < 0) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     if (r->st.n > CG_NOALLOC_MAX_PARTICLES)
@@ -1445,6 +1451,7 @@ static cudaError_t copy_chunk(const cg_run* r, const cg_host_arrays* h, bool to_
 
 int cg_run_step_host(cg_run* r, int32_t nsteps, const cg_host_arrays* in,
                      const cg_host_arrays* out, int32_t chunk, int32_t* bnd_stats_host) {
+    NvtxRange nvtx_call("cg_run_step_host");
     if (!r || nsteps < 0 || !in || !out || chunk < 0) return CG_EINVAL;
     cg_ctx* c = r->ctx;
     if (nsteps == 0) return CG_OK;
@@ -1582,6 +1589,36 @@ int cg_run_last_kernel_split_ms(const cg_run* r, double* step_ms, double* walk_m
     if (!r) return CG_EINVAL;
     if (step_ms) *step_ms = r->last_step_ms;
     if (walk_ms) *walk_ms = r->last_walk_ms;
+    return CG_OK;
+}
+
+int cg_run_clock(const cg_run* r, double* time, double* fields_time, int64_t* iteration) {
+    if (!r) return CG_EINVAL;
+    if (time) *time = r->time;
+    if (fields_time) *fields_time = r->frozen ? NAN : r->fields_time;
+    if (iteration) *iteration = r->iteration;
+    return CG_OK;
+}
+
+int cg_run_resume(cg_run* r, double time, double fields_time, int64_t iteration) {
+    if (!r) return CG_EINVAL;
+    cg_ctx* c = r->ctx;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (r->pending_init)
+        return set_err(c, CG_ESTATE, "particles await initialization: resume a stepped run");
+    int rc = write_back(r);
+    if (rc) return rc;
+    if ((rc = ensure_fields(r))) return rc;
+    r->time = time;
+    r->iteration = iteration;
+    if (!r->frozen && std::isfinite(fields_time)) {
+        // the current record as the checkpointed run held it (blended at
+        // its last step's time): the first resumed step's previous record,
+        // as in the uninterrupted run
+        r->record = 0;
+        if ((rc = time_interpolation(r, fields_time))) return rc;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return CG_OK;
 }
 

@@ -3,11 +3,23 @@
 #pragma once
 
 #include <cstdint>
+
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 
 #include "cg_device.cuh"
 
 namespace cg {
+
+// An NVTX range for the scope (shown by Nsight tools, free otherwise):
+// the library's host phases -- a step call, the element sort, admissions
+// and steps of the serving pool -- appear on the timeline by name.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Raw node fields on the device, planar: frames[t][f][node] for the raw
 // field ids below (absent fields are not stored; raw_slot[f] == -1).

@@ -302,6 +302,7 @@ int cg_server_destroy(cg_server* s) {
 int cg_server_admit(cg_server* s, const cg_params* prm, int32_t n, const double* position,
                     double particle_diameter, const double* diameter, int32_t horizon,
                     int32_t* run_id) {
+    NvtxRange nvtx("cg_server_admit");
     if (!s || !prm || !position || !run_id || n <= 0 || horizon <= 0) return CG_EINVAL;
     cg_ctx* c = s->ctx;
     *run_id = -1;
@@ -390,6 +391,7 @@ int cg_server_admit(cg_server* s, const cg_params* prm, int32_t n, const double*
 }
 
 int cg_server_step(cg_server* s, int32_t nsteps) {
+    NvtxRange nvtx("cg_server_step");
     if (!s || nsteps < 0) return CG_EINVAL;
     cg_ctx* c = s->ctx;
     if (nsteps == 0) return CG_OK;

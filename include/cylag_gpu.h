@@ -392,6 +392,23 @@ int cg_run_last_kernel_ms(const cg_run *run, double *ms, int32_t *launches);
  * call. */
 int cg_run_last_kernel_split_ms(const cg_run *run, double *step_ms, double *walk_ms);
 
+/* ---- checkpoint / resume ------------------------------------------------ */
+/* The run's clock: simulated time, the time its current field record was
+ * blended at (NaN for frozen fields or before the first step) and the
+ * iteration count.  A checkpoint stores them with the particle state
+ * (every array of cg_state_desc, the PCG32 states included). */
+int cg_run_clock(const cg_run *run, double *time, double *fields_time, int64_t *iteration);
+
+/* Resume a checkpoint in a run over the same mesh, fields and parameters,
+ * whose state arrays now hold the checkpoint's particle state (write the
+ * arrays after cg_run_writeback): the clock is set and the current field
+ * record re-blended at fields_time, so that the following steps are bit for
+ * bit those of the uninterrupted run (the plain form; the mixed form's
+ * FP32-pair working positions round-trip through the FP64 arrays exactly
+ * except at rounding ties).  CG_ESTATE while added particles await
+ * initialization. */
+int cg_run_resume(cg_run *run, double time, double fields_time, int64_t iteration);
+
 #ifdef __cplusplus
 }
 #endif
