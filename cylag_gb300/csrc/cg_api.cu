@@ -283,7 +283,7 @@ static DevState added_view(const cg_run* r) {
 struct ScratchPlan {
     bool use_queue = false, use_sort = false;
     size_t queue_bytes = 0, sort_bytes = 0;
-    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0}, off_aux = 0;
+    size_t off_sums = 0, off_perm = 0, off_w[2] = {0, 0}, off_aux = 0, off_v2 = 0;
     int nkeys = 0, nl_key = 1, work = 0, dim = 2;
     size_t n = 0;
 };
@@ -316,6 +316,11 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
     if (p->dim == 3) q.work |= W_LAYER | W_DIAM;
     // mixed LSM1 2D: working positions as split FP32 pairs (same 16 bytes)
     if (p->precision == CG_PRECISION_MIXED && p->dim == 2 && p->model == 1) q.work |= W_SPLIT;
+    // 2D LSM1: two working velocity arrays (the last velocity without
+    // copies); its velocity is the fluid velocity seen (in 3D the settling
+    // velocity is added to the velocity alone).  Every W_SPLIT run has them
+    // (the split step kernels are compiled for it).
+    if (p->model == 1 && p->dim == 2) q.work |= W_VEL2;
     // mixed LSM2/LSM3: FP32 working velocities (and fluid velocities seen)
     if (p->precision == CG_PRECISION_MIXED && p->model >= 2) q.work |= W_V32;
     // ... and, for the 3D direct integrators without compute_depth, FP32-pair
@@ -334,15 +339,19 @@ static ScratchPlan plan_scratch(const cg_ctx* c, const cg_params* p, int32_t n32
                               ((q.work & W_DIAM) ? al256(n * 8) : 0) +
                               ((q.work & W_AUXW) ? al256(n * 4) : 0);
     // the outputs the re-sort does not move: one set shared by both copies
+    // (no fluid-velocity-seen array for W_VEL2 runs: it is the velocity)
     const size_t aux_bytes = (q.work & W_AUXW)
-        ? 2 * al256(n * 8 * D) + ((q.work & W_FVS) ? 0 : al256(n * 8 * D)) : 0;
+        ? 2 * al256(n * 8 * D) + ((q.work & (W_FVS | W_VEL2)) ? 0 : al256(n * 8 * D)) : 0;
     if (q.use_sort) {
         q.off_sums = al256((size_t)q.nkeys * 4);
         q.off_perm = al256(q.off_sums + (size_t)scan_scratch_ints(q.nkeys) * 4);
         q.off_w[0] = al256(q.off_perm + n * 4);
         q.off_w[1] = q.off_w[0] + work_bytes;
         q.off_aux = q.off_w[1] + work_bytes;
-        q.sort_bytes = q.off_aux + aux_bytes;
+        // W_VEL2: the two copies' second velocity arrays after the rest (the
+        // copies' other arrays keep the offsets they have without them)
+        q.off_v2 = q.off_aux + aux_bytes;
+        q.sort_bytes = q.off_v2 + ((q.work & W_VEL2) ? 2 * al256(n * 8 * D) : 0);
     }
     return q;
 }
@@ -367,13 +376,14 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
     r->sb.dim = q.dim;
     r->sb.nl = q.nl_key;
     r->sb.work = q.work;
+    r->sb.vpar = 0;
     WorkState* ws[2] = {&r->sb.a, &r->sb.b};
     char* aux = b + q.off_aux;
     auto take_aux = [&](size_t bytes) { char* t = aux; aux += al256(bytes); return t; };
     double* lpos = (q.work & W_AUXW) ? (double*)take_aux(n * 8 * D) : nullptr;
     double* lvel = (q.work & W_AUXW) ? (double*)take_aux(n * 8 * D) : nullptr;
-    double* fvs_out = ((q.work & W_AUXW) && !(q.work & W_FVS)) ? (double*)take_aux(n * 8 * D)
-                                                                : nullptr;
+    double* fvs_out = ((q.work & W_AUXW) && !(q.work & (W_FVS | W_VEL2)))
+                          ? (double*)take_aux(n * 8 * D) : nullptr;
     for (int k = 0; k < 2; ++k) {
         char* w = b + q.off_w[k];
         auto take = [&](size_t bytes) { char* t = w; w += al256(bytes); return t; };
@@ -384,6 +394,8 @@ static int take_scratch(cg_ctx* c, cg_run* r, const ScratchPlan& q) {
         ws[k]->slot = (int*)take(n * 8);
         const size_t vb = (q.work & W_V32) ? 4 : 8;
         ws[k]->vel = (q.work & W_VEL) ? (double*)take(n * vb * D) : nullptr;
+        ws[k]->vel2 = (q.work & W_VEL2) ? (double*)(b + q.off_v2 + k * al256(n * 8 * D))
+                                        : nullptr;
         ws[k]->fvs = (q.work & W_FVS) ? (double*)take(n * vb * D) : fvs_out;
         ws[k]->layer = (q.work & W_LAYER) ? (int*)take(n * 4) : nullptr;
         ws[k]->diam = (q.work & W_DIAM) ? (double*)take(n * 8) : nullptr;
@@ -1114,6 +1126,8 @@ int cg_run_step(cg_run* r, int32_t nsteps, int32_t* bnd_stats_host) {
         CUDA_TRY(c, cudaGetLastError());
         launches += r->st.n > 0 ? (r->use_queue ? 2 : 1) : 0;   // step (+ walk)
         if (sorted) r->since_sort += 1;
+        // W_VEL2: this step's velocity array is now the newest
+        if (sorted && (r->sb.work & W_VEL2) && aux >= 1) r->sb.vpar ^= 1;
         // simutime.pyx:77-84
         r->time += r->prm.time_step;
         r->iteration += 1;

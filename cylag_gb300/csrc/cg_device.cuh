@@ -234,6 +234,14 @@ constexpr int W_V32 = 64;
 // hi + lo per coordinate, {x_hi, x_lo, y_hi, y_lo, z_hi, z_lo} in the
 // 24-byte row of the FP64 position
 constexpr int W_SPLIT3 = 128;
+// LSM1 runs (the velocity is an output, U(x0), equal to the fluid velocity
+// seen): two working velocity arrays that the steps writing the velocity
+// alternate between, so that the other one holds the last velocity.  A
+// step writes its velocity into DevState::vel only; the write-back gives
+// velocity and fluid velocity seen from the newest array, last_velocity
+// from the other (no per-particle copies of the last velocity, no second
+// write of the same velocity).
+constexpr int W_VEL2 = 256;
 
 // component k of the particle velocity / fluid velocity seen of a state
 // whose working copies may be FP32 (W_V32); the caller's arrays are FP64

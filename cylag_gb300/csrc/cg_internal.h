@@ -135,6 +135,7 @@ struct WorkState {
     unsigned long long* rng;  // [n]
     int* slot;                // [n] caller index of each working particle
     double* vel;              // [n][dim] or nullptr (float rows under W_V32)
+    double* vel2;             // [n][dim] the second velocity array (W_VEL2) or nullptr
     double* fvs;              // [n][dim] or nullptr (float rows under W_V32 with W_FVS)
     int* layer;               // [n] or nullptr
     double* diam;             // [n] or nullptr
@@ -150,6 +151,7 @@ struct SortBuffers {
     int dim;             // 2 or 3
     int nl;              // layers per column (1 in 2D): key = tri * nl + layer
     int work;            // W_* flags of the optional arrays
+    int vpar;            // W_VEL2: the array holding the newest velocity (0: vel, 1: vel2)
 };
 int scan_scratch_ints(int nkeys);
 // caller arrays -> b.a in element order

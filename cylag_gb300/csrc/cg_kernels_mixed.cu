@@ -31,23 +31,29 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         // persistent grid: one wave of resident blocks.  The Euler scheme with
         // a walk queue (EQ) has no out-of-line calls and runs 4 blocks of 256
         // per SM (64 registers); the other forms 3 (80).  Split positions on
-        // the element-sorted working copies (W_SPLIT).
+        // the element-sorted working copies (W_SPLIT), which always come with
+        // two velocity arrays (W_VEL2: TWO); the steps without per-call
+        // outputs (aux 0) write no velocity, so they run the one-array form.
         static const int w3 = wave(step_mixed2d_kernel<3>, bs),
-                         w3s = wave(step_mixed2d_kernel<3, true>, bs),
+                         w3s = wave(step_mixed2d_kernel<3, true, false, true>, bs),
                          w4e = wave(step_mixed2d_kernel<4, false, true>, bs),
-                         w4se = wave(step_mixed2d_kernel<4, true, true>, bs);
+                         w4se = wave(step_mixed2d_kernel<4, true, true>, bs),
+                         w4s2 = wave(step_mixed2d_kernel<4, true, true, true>, bs);
         auto grid = [nb](int w) { return nb < w ? nb : w; };
         const bool eq = p.time_scheme == 1 && wq.e != nullptr;
         const bool split = (s.work & W_SPLIT) != 0;
-        if (split && eq)
+        if (split && eq && aux == 0)
             step_mixed2d_kernel<4, true, true><<<grid(w4se), bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                         step_index, stats, err);
+        else if (split && eq)
+            step_mixed2d_kernel<4, true, true, true><<<grid(w4s2), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
         else if (eq)
             step_mixed2d_kernel<4, false, true><<<grid(w4e), bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                          step_index, stats, err);
         else if (split)
-            step_mixed2d_kernel<3, true><<<grid(w3s), bs, 0, st>>>(m, f, p, s, wq, aux,
-                                                                  step_index, stats, err);
+            step_mixed2d_kernel<3, true, false, true><<<grid(w3s), bs, 0, st>>>(
+                m, f, p, s, wq, aux, step_index, stats, err);
         else
             step_mixed2d_kernel<3><<<grid(w3), bs, 0, st>>>(m, f, p, s, wq, aux, step_index,
                                                            stats, err);

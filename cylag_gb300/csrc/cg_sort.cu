@@ -174,8 +174,11 @@ __device__ __forceinline__ void put_vel_rows(const double* __restrict__ w, doubl
 // The outputs kept with W_AUXW are not moved: dst's last element becomes
 // LAST_UNSET, or stays -1 for a particle deleted since the last write-back
 // (its outputs are zero).
+// W_VEL2 re-sorts move the newest velocity array alone (vpar): the other one
+// is the next velocity-writing step's target, and every call ends with such
+// a step (the last one, after any re-sort of the call), before any read.
 __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src, WorkState dst,
-                                    int n, int dim, int work) {
+                                    int n, int dim, int work, int vpar) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&perm[j]);
@@ -195,7 +198,12 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
     dst.rng[j] = __ldcs(src.rng + i);
     dst.slot[j] = src.slot ? __ldcs(src.slot + i) : i;
     const bool v32 = (work & W_V32) != 0, from_caller = src.slot == nullptr;
-    if (work & W_VEL) move_vel_rows(src.vel, dst.vel, i, j, dim, v32, from_caller);
+    if ((work & W_VEL2) && !from_caller) {
+        if (vpar) move_rows(src.vel2, dst.vel2, i, j, dim);
+        else move_rows(src.vel, dst.vel, i, j, dim);
+    } else if (work & W_VEL) {
+        move_vel_rows(src.vel, dst.vel, i, j, dim, v32, from_caller);
+    }
     if (work & W_FVS) move_vel_rows(src.fvs, dst.fvs, i, j, dim, v32, from_caller);
     if (work & W_LAYER) dst.layer[j] = __ldcs(src.layer + i);
     if (work & W_DIAM) dst.diam[j] = __ldcs(src.diam + i);
@@ -204,7 +212,8 @@ __global__ void gather_state_kernel(const int* __restrict__ perm, WorkState src,
 }
 
 // caller[slot[j]] = work[j]; the W_AUXW outputs only where a step set them
-__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim, int work) {
+__global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim, int work,
+                                     int vpar) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = __ldg(&w.slot[j]);
@@ -222,7 +231,16 @@ __global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim
     __stcs(user.tag + i, w.tag[j]);
     __stcs(user.rng + i, w.rng[j]);
     const bool v32 = (work & W_V32) != 0;
-    if (work & W_VEL) put_vel_rows(w.vel, user.vel, j, i, dim, v32);
+    // W_VEL2: the newest velocity and the one before it
+    const double* vnew = ((work & W_VEL2) && vpar) ? w.vel2 : w.vel;
+    const double* vold = ((work & W_VEL2) && vpar) ? w.vel : w.vel2;
+    if ((work & W_VEL2) && w.tri[j] == -1) {
+        // inactive: zero velocity (the arrays are written only by the steps
+        // that output the velocity)
+        for (int d = 0; d < dim; ++d) __stcs(user.vel + (size_t)i * dim + d, 0.);
+    } else if (work & W_VEL) {
+        put_vel_rows(vnew, user.vel, j, i, dim, v32);
+    }
     if (work & W_FVS) put_vel_rows(w.fvs, user.fvs, j, i, dim, v32);
     if (work & W_LAYER) __stcs(user.layer + i, w.layer[j]);
     if (work & W_DIAM) __stcs(user.diam + i, w.diam[j]);
@@ -230,11 +248,12 @@ __global__ void scatter_state_kernel(WorkState w, WorkState user, int n, int dim
         const int lt = w.ltri[j];
         if (lt == LAST_UNSET) return;
         const bool del = lt == -1;
+        const bool two = (work & W_VEL2) != 0;
         for (int d = 0; d < dim; ++d) {
             const size_t u = (size_t)i * dim + d, k = (size_t)j * dim + d;
             __stcs(user.lpos + u, del ? 0. : w.lpos[k]);
-            __stcs(user.lvel + u, del ? 0. : w.lvel[k]);
-            if (!(work & W_FVS)) __stcs(user.fvs + u, del ? 0. : w.fvs[k]);
+            __stcs(user.lvel + u, del ? 0. : (two ? vold[k] : w.lvel[k]));
+            if (!(work & W_FVS)) __stcs(user.fvs + u, del ? 0. : (two ? vnew[k] : w.fvs[k]));
         }
         __stcs(user.ltri + i, lt);
     }
@@ -264,6 +283,7 @@ static WorkState user_view(const DevState& u) {
     w.rng = reinterpret_cast<unsigned long long*>(u.rng);
     w.slot = nullptr;
     w.vel = u.vel;
+    w.vel2 = nullptr;
     w.fvs = u.fvs;
     w.layer = u.lowerlayer;
     w.diam = u.diameter;
@@ -274,17 +294,19 @@ static WorkState user_view(const DevState& u) {
 }
 
 void launch_sort_gather(const DevState& user, int nt, SortBuffers& b, cudaStream_t st) {
+    b.vpar = 0;   // the caller's velocity lands in vel
     int n = user.n;
     if (n == 0) return;
     sort_perm(user.tri, (b.work & W_LAYER) ? user.lowerlayer : nullptr, n, nt, b, st);
     gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, user_view(user), b.a, n, b.dim,
-                                                         b.work);
+                                                         b.work, 0);
 }
 
 void launch_sort_resort(int n, int nt, SortBuffers& b, cudaStream_t st) {
     if (n == 0) return;
     sort_perm(b.a.tri, b.a.layer, n, nt, b, st);
-    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim, b.work);
+    gather_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.perm, b.a, b.b, n, b.dim, b.work,
+                                                         b.vpar);
     WorkState t = b.a;
     b.a = b.b;
     b.b = t;
@@ -294,7 +316,7 @@ void launch_sort_scatter(const DevState& user, const SortBuffers& b, cudaStream_
     int n = user.n;
     if (n == 0) return;
     scatter_state_kernel<<<(n + 255) / 256, 256, 0, st>>>(b.a, user_view(user), n, b.dim,
-                                                          b.work);
+                                                          b.work, b.vpar);
 }
 
 DevState sorted_view(const DevState& user, const SortBuffers& b) {
@@ -304,7 +326,9 @@ DevState sorted_view(const DevState& user, const SortBuffers& b) {
     w.tag = b.a.tag;
     w.rng = reinterpret_cast<uint64_t*>(b.a.rng);
     w.slot = b.a.slot;
-    if (b.work & W_VEL) w.vel = b.a.vel;
+    // W_VEL2: a step that writes the velocity writes the older array (the
+    // run then flips vpar); no kernel reads it
+    if (b.work & W_VEL) w.vel = ((b.work & W_VEL2) && !b.vpar) ? b.a.vel2 : b.a.vel;
     if (b.work & (W_FVS | W_AUXW)) w.fvs = b.a.fvs;
     if (b.work & W_LAYER) w.lowerlayer = b.a.layer;
     if (b.work & W_DIAM) w.diameter = b.a.diam;

@@ -655,14 +655,17 @@ struct Particle {
         // the mixed LSM2/LSM3 form keeps its velocities as FP32 values,
         // whether the state is FP32 working copies or the caller's arrays
         const bool v32 = std::is_same<FT, float>::value && p.model >= 2;
+        const bool two = (s.work & W_VEL2) != 0;   // (the write-back gives fvs, last_velocity)
         if (deleted) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.pos[(size_t)i * D + d] = 0.;
                 vel_st(s, (size_t)iv * D + d, 0.);
-                fvs_st(s, (size_t)iu * D + d, 0.);
                 s.last_pos[(size_t)ix * D + d] = 0.;
-                s.last_vel[(size_t)ix * D + d] = 0.;
+                if (!two) {
+                    fvs_st(s, (size_t)iu * D + d, 0.);
+                    s.last_vel[(size_t)ix * D + d] = 0.;
+                }
             }
             s.diameter[id] = 0.;
             if (s.depth) s.depth[a] = 0.;
@@ -683,7 +686,7 @@ struct Particle {
         if (DIM == 3) s.lowerlayer[il] = ll;
         s.rng[i] = rng.state;
         double lastv[3] = {0., 0., 0.};
-        if (aux >= 2) {
+        if (aux >= 2 && !two) {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const double v = vel_ld(s, (size_t)iv * D + d);
@@ -695,7 +698,7 @@ struct Particle {
             for (int d = 0; d < D; ++d)
                 vel_st(s, (size_t)iv * D + d, v32 ? (double)(float)up[d] : up[d]);
         }
-        if (p.model == 3 || aux >= 1) {
+        if ((p.model == 3 || aux >= 1) && !two) {
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 fvs_st(s, (size_t)iu * D + d, v32 ? (double)(float)us[d] : us[d]);
@@ -704,7 +707,7 @@ struct Particle {
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 s.last_pos[(size_t)ix * D + d] = x0[d];
-                s.last_vel[(size_t)ix * D + d] = lastv[d];
+                if (!two) s.last_vel[(size_t)ix * D + d] = lastv[d];
             }
             s.last_tri[ix] = ltri;
         }

@@ -215,7 +215,10 @@ __device__ __forceinline__ double2 double2_from_bits(float4 r) {
 // EQ: the Euler scheme with a walk queue (the caller guarantees both): every
 // particle that does not end in a triangle reached here goes to the queue,
 // so this form has no out-of-line calls and no deletions.
-template <bool SPLIT, bool EQ = false>
+// TWO: the working copies have two velocity arrays (W_VEL2); a step writes
+// its velocity alone and the write-back gives the fluid velocity seen and the
+// last velocity.  Only the steps with per-call outputs (aux >= 1) differ.
+template <bool SPLIT, bool EQ = false, bool TWO = false>
 __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
                                                     const DevParams& p, DevState& s,
                                                     const WalkQueue& wq, int aux, int step_index,
@@ -236,7 +239,8 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     rng.inc = ((uint64_t)(uint32_t)in.tag << 1) | 1ULL;
     rng.err = 0;
     double2 lastv = make_double2(0., 0.);
-    if (aux >= 2) lastv = reinterpret_cast<const double2*>(s.vel)[widx(s, i, aux_index(s, i), W_VEL)];
+    if (aux >= 2 && !TWO)
+        lastv = reinterpret_cast<const double2*>(s.vel)[widx(s, i, aux_index(s, i), W_VEL)];
 
     const float dt = p.dt32;
     const bool euler = EQ || p.time_scheme == 1;
@@ -402,9 +406,11 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         const int ix = widx(s, i, a, W_AUXW);
         reinterpret_cast<double2*>(s.pos)[i] = make_double2(0., 0.);
         reinterpret_cast<double2*>(s.vel)[widx(s, i, a, W_VEL)] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(0., 0.);
         reinterpret_cast<double2*>(s.last_pos)[ix] = make_double2(0., 0.);
-        reinterpret_cast<double2*>(s.last_vel)[ix] = make_double2(0., 0.);
+        if (!TWO) {   // (TWO: the write-back zeroes them)
+            reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(0., 0.);
+            reinterpret_cast<double2*>(s.last_vel)[ix] = make_double2(0., 0.);
+        }
         s.diameter[widx(s, i, a, W_DIAM)] = 0.;
         s.tri[i] = -1;
         s.last_tri[ix] = -1;
@@ -424,15 +430,18 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     __stcs(reinterpret_cast<unsigned long long*>(s.rng) + i, (unsigned long long)rng.state);
     if (aux >= 1) {
         const int a = aux_index(s, i);
+        // TWO: the velocity alone (it is the fluid velocity seen; the other
+        // array holds the last velocity)
         reinterpret_cast<double2*>(s.vel)[widx(s, i, a, W_VEL)] = make_double2(up0, up1);
-        reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(up0, up1);
+        if (!TWO)
+            reinterpret_cast<double2*>(s.fvs)[widx(s, i, a, W_FVS | W_AUXW)] = make_double2(up0, up1);
         if (aux >= 2) {
             if constexpr (SPLIT) {
                 if (!have64) x0 = join_pos(xs);
             }
             const int ix = widx(s, i, a, W_AUXW);
             reinterpret_cast<double2*>(s.last_pos)[ix] = x0;
-            reinterpret_cast<double2*>(s.last_vel)[ix] = lastv;
+            if (!TWO) reinterpret_cast<double2*>(s.last_vel)[ix] = lastv;
             s.last_tri[ix] = ltri;
         }
     }
@@ -440,7 +449,7 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
 // MINB: resident blocks of 256 per SM the register budget is set for.
-template <int MINB, bool SPLIT = false, bool EQ = false>
+template <int MINB, bool SPLIT = false, bool EQ = false, bool TWO = false>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -459,8 +468,8 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     }
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_mixed_particle<SPLIT, EQ>(m, f, p, s, wq, aux, step_index, stats, err_word, z32,
-                                       load_mixed_in(s, i), i);
+        step_mixed_particle<SPLIT, EQ, TWO>(m, f, p, s, wq, aux, step_index, stats, err_word,
+                                            z32, load_mixed_in(s, i), i);
 }
 
 }  // namespace cg

@@ -151,7 +151,9 @@ def test_sorted_state_kept_across_calls(precision):
     single-step calls, 100 steps in calls of 7 with the arrays read after
     every call (each read writes the copies back and the next step gathers
     them again), and one 100-step call leave the same state bit for bit:
-    positions, elements, tags and PCG32 states."""
+    positions, elements, tags, PCG32 states and the per-call outputs (the
+    velocity, fluid velocity seen and last velocity come from two working
+    velocity arrays that the re-sorts move only in part)."""
     import cylag_gb300 as cg
     from cylag_gb300 import synth
     c = synth.keps_drift_channel(npart=20000, nx=101, ny=26, seed=5)
@@ -179,7 +181,9 @@ def test_sorted_state_kept_across_calls(precision):
                 _ = ps.position
         ps._sync()
         out.append({k: ps._dev[k].cpu().numpy() for k in ("position", "tri", "tag", "rng_state",
-                                                           "last_position", "velocity")})
+                                                           "last_position", "velocity",
+                                                           "fluid_velocity_seen", "last_velocity",
+                                                           "last_tri")})
         s.close()
     for mode, o in zip(("single", "read7"), out[1:]):
         for k in out[0]:
