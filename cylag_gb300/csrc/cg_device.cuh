@@ -452,8 +452,10 @@ struct Zig32 {
 };
 
 // random_utils.pyx:55-67 in FP32
+// (explicitly rounded operations here and below: every compiled form of a
+// step draws the same values)
 __device__ __forceinline__ float uniform32(Rng& r) {
-    return (float)pcg_next(r) * 2.3283064365386963e-10f;
+    return __fmul_rn((float)pcg_next(r), 2.3283064365386963e-10f);
 }
 
 // random_utils.pyx:154-194 in FP32 (same stream consumption as the FP64
@@ -463,18 +465,21 @@ __device__ inline float zig32(Rng& r, const Zig32& z) {
         int32_t hz = (int32_t)pcg_next(r);
         uint32_t iz = (uint32_t)hz & 127u;
         uint32_t ahz = hz < 0 ? 0u - (uint32_t)hz : (uint32_t)hz;
-        if (ahz < z.kn[iz]) return (float)hz * z.wn[iz];
+        if (ahz < z.kn[iz]) return __fmul_rn((float)hz, z.wn[iz]);
         if (iz == 0) {
             for (int t2 = 0; t2 < RNG_MAX_TRIES; ++t2) {
-                float x = -__logf(uniform32(r)) * 0.2904764f;
+                float x = __fmul_rn(-__logf(uniform32(r)), 0.2904764f);
                 float y = -__logf(uniform32(r));
-                if (y + y >= x * x) return hz > 0 ? 3.442619855899f + x : -3.442619855899f - x;
+                if (__fadd_rn(y, y) >= __fmul_rn(x, x))
+                    return hz > 0 ? __fadd_rn(3.442619855899f, x) : __fsub_rn(-3.442619855899f, x);
             }
             r.err |= ERR_RNG_LIMIT;
             return 0.f;
         }
-        float x = (float)hz * z.wn[iz];
-        if (z.fn[iz] + uniform32(r) * (z.fn[iz - 1] - z.fn[iz]) < __expf(-0.5f * x * x)) return x;
+        float x = __fmul_rn((float)hz, z.wn[iz]);
+        if (__fmaf_rn(uniform32(r), __fsub_rn(z.fn[iz - 1], z.fn[iz]), z.fn[iz]) <
+            __expf(__fmul_rn(__fmul_rn(-0.5f, x), x)))
+            return x;
     }
     r.err |= ERR_RNG_LIMIT;
     return 0.f;
@@ -484,21 +489,21 @@ __device__ inline void polar32(Rng& r, float& a, float& b) {
     float x1 = 0.f, x2 = 0.f, w = 2.f;
     int tries = 0;
     while ((w >= 1.f || w == 0.f) && tries < RNG_MAX_TRIES) {
-        x1 = 2.f * uniform32(r) - 1.f;
-        x2 = 2.f * uniform32(r) - 1.f;
-        w = x1 * x1 + x2 * x2;
+        x1 = __fmaf_rn(2.f, uniform32(r), -1.f);
+        x2 = __fmaf_rn(2.f, uniform32(r), -1.f);
+        w = __fmaf_rn(x2, x2, __fmul_rn(x1, x1));
         ++tries;
     }
     if (tries == RNG_MAX_TRIES) { r.err |= ERR_RNG_LIMIT; a = b = 0.f; return; }
-    w = sqrtf((-2.f * __logf(w)) / w);
-    a = x1 * w;
-    b = x2 * w;
+    w = sqrtf(__fdiv_rn(__fmul_rn(-2.f, __logf(w)), w));
+    a = __fmul_rn(x1, w);
+    b = __fmul_rn(x2, w);
 }
 
 __device__ inline void pair32(Rng& r, int method, const Zig32& z, float& a, float& b) {
     if (method == 1) {
-        a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
-        b = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+        a = __fmul_rn(__fsub_rn(uniform32(r), 0.5f), (float)TWO_SQRT3);
+        b = __fmul_rn(__fsub_rn(uniform32(r), 0.5f), (float)TWO_SQRT3);
     } else if (method == 2) {
         a = zig32(r, z);
         b = zig32(r, z);
@@ -539,7 +544,7 @@ static __device__ __noinline__ DrawOut<float> draws32_ol(uint64_t st, uint64_t i
     if (two) {
         pair32(r, method, z, o.a, o.b);
     } else if (method == 1) {
-        o.a = (uniform32(r) - 0.5f) * (float)TWO_SQRT3;
+        o.a = __fmul_rn(__fsub_rn(uniform32(r), 0.5f), (float)TWO_SQRT3);
     } else if (method == 2) {
         o.a = zig32(r, z);
     } else {

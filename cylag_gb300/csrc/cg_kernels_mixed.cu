@@ -7,19 +7,38 @@
 
 namespace cg {
 
+// blocks of one wave of resident blocks of `kernel` (persistent grid)
+template <typename K>
+static int wave_of(K kernel, int bs) {
+    int dev = 0, nsm = 152, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs, 0);
+    return nsm * (per < 1 ? 1 : per);
+}
+
+// the split Euler step compiled for one configuration (diffusion class DC,
+// random number method RM), for the steps without per-call outputs
+template <int DC, int RM>
+static void launch_split_conf(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
+                              const DevState& s, const WalkQueue& wq, int step_index, int* stats,
+                              uint32_t* err, int nb, int bs, cudaStream_t st) {
+    static const int w = wave_of(step_mixed2d_kernel<4, true, true, false, DC, RM>, bs);
+    step_mixed2d_kernel<4, true, true, false, DC, RM><<<nb < w ? nb : w, bs, 0, st>>>(
+        m, f, p, s, wq, 0, step_index, stats, err);
+}
+
+using SplitConfLaunch = void (*)(const DevMesh&, const DevFields<float>&, const DevParams&,
+                                 const DevState&, const WalkQueue&, int, int*, uint32_t*, int,
+                                 int, cudaStream_t);
+
 void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
                        int* stats, uint32_t* err, cudaStream_t st) {
     int bs = 256;
     int nb = (s.n + bs - 1) / bs;
     if (nb == 0) return;
-    auto wave = [](auto kernel, int bs_) {
-        int dev = 0, nsm = 152, per = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, bs_, 0);
-        return nsm * (per < 1 ? 1 : per);
-    };
+    auto wave = [](auto kernel, int bs_) { return wave_of(kernel, bs_); };
     if (p.model != 1) {
         // LSM2 / LSM3: FP32 node records and Langevin coefficients, inline walk
         launch_lsm23_mixed(m, fv, p, s, aux, step_index, stats, err, st);
@@ -42,7 +61,18 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         auto grid = [nb](int w) { return nb < w ? nb : w; };
         const bool eq = p.time_scheme == 1 && wq.e != nullptr;
         const bool split = (s.work & W_SPLIT) != 0;
-        if (split && eq && aux == 0)
+        // the configuration forms: diffusion off / constant / k-epsilon x
+        // random number methods 1-3, steps without per-call outputs and
+        // without control sections
+        static const SplitConfLaunch conf[3][3] = {
+            {launch_split_conf<0, 1>, launch_split_conf<0, 2>, launch_split_conf<0, 3>},
+            {launch_split_conf<1, 1>, launch_split_conf<1, 2>, launch_split_conf<1, 3>},
+            {launch_split_conf<2, 1>, launch_split_conf<2, 2>, launch_split_conf<2, 3>}};
+        const int dc = p.diffmod == 0 ? 0 : (p.diffmod == 1 ? 1 : 2);
+        if (split && eq && aux == 0 && p.ncsec == 0 && p.rng_method >= 1 && p.rng_method <= 3 &&
+            p.diffmod >= 0 && p.diffmod <= 3)
+            conf[dc][p.rng_method - 1](m, f, p, s, wq, step_index, stats, err, nb, bs, st);
+        else if (split && eq && aux == 0)
             step_mixed2d_kernel<4, true, true><<<grid(w4se), bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                         step_index, stats, err);
         else if (split && eq)

@@ -43,9 +43,14 @@ __device__ __forceinline__ Node4 load_nodes(const float4* __restrict__ f, const 
     return r;
 }
 
+// The FP32 arithmetic that reaches the particle state (here, the Euler
+// increment and the samplers) is written with explicitly rounded operations
+// (__fmul_rn, __fmaf_rn, ...), so that every compiled form of the step
+// (per-call outputs or not, configuration forms) rounds the same way and a
+// run's results do not depend on how its steps are split into calls.
 __device__ __forceinline__ void vel32(const Node4& n, const Bary& b, float& ux, float& uy) {
-    ux = b.l0 * n.n0.x + b.l1 * n.n1.x + b.l2 * n.n2.x;
-    uy = b.l0 * n.n0.y + b.l1 * n.n1.y + b.l2 * n.n2.y;
+    ux = __fmaf_rn(b.l2, n.n2.x, __fmaf_rn(b.l1, n.n1.x, __fmul_rn(b.l0, n.n0.x)));
+    uy = __fmaf_rn(b.l2, n.n2.y, __fmaf_rn(b.l1, n.n1.y, __fmul_rn(b.l0, n.n0.y)));
 }
 
 // Runge-Kutta stages of update_state_lsm1.pyx:179-656 in the mixed form:
@@ -218,7 +223,11 @@ __device__ __forceinline__ double2 double2_from_bits(float4 r) {
 // TWO: the working copies have two velocity arrays (W_VEL2); a step writes
 // its velocity alone and the write-back gives the fluid velocity seen and the
 // last velocity.  Only the steps with per-call outputs (aux >= 1) differ.
-template <bool SPLIT, bool EQ = false, bool TWO = false>
+// DC >= 0: a form compiled for one run configuration, for the steps without
+// per-call outputs (aux 0) and without control sections: DC the diffusion
+// class (0 none, 1 constant diffusivity, 2 k-epsilon: diffusion_model 2 or
+// 3), RM the random number method.  -1: read from the parameters.
+template <bool SPLIT, bool EQ = false, bool TWO = false, int DC = -1, int RM = -1>
 __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
                                                     const DevParams& p, DevState& s,
                                                     const WalkQueue& wq, int aux, int step_index,
@@ -274,8 +283,8 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     // the position once
     float dx = 0.f, dy = 0.f;
     if (euler) {
-        dx = ux * dt;
-        dy = uy * dt;
+        dx = __fmul_rn(ux, dt);
+        dy = __fmul_rn(uy, dt);
     } else if constexpr (!EQ) {
         const RkOut r = rk_mixed(m, cur, p, tri0, x0.x, x0.y, ux, uy);
         xn = r.xn;
@@ -285,9 +294,14 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
     }
 
     // diffusion (update_state_lsm1.pyx:658-726), K at the start point
-    if (p.diffmod != 0) {
+    constexpr bool CONF = DC >= 0;
+    const bool diff_on = CONF ? DC != 0 : p.diffmod != 0;
+    const bool diff_k = CONF ? DC == 2 : (p.diffmod == 2 || p.diffmod == 3);
+    const int rng_method = RM > 0 ? RM : p.rng_method;
+    const int ncsec = CONF ? 0 : p.ncsec;
+    if (diff_on) {
         float diffx, driftx = 0.f, drifty = 0.f;
-        if (p.diffmod == 2 || p.diffmod == 3) {
+        if (diff_k) {
             float4 g0, g1;
             if constexpr (SPLIT) {
                 g0 = t0s.g0;
@@ -296,24 +310,24 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
                 g0 = t0.g0;
                 g1 = t0.g1;
             }
-            float K = b0.l0 * n0.n0.z + b0.l1 * n0.n1.z + b0.l2 * n0.n2.z;
-            float dKdx = n0.n0.z * g0.x + n0.n1.z * g0.y + n0.n2.z * g0.z;
-            float dKdy = n0.n0.z * g0.w + n0.n1.z * g1.x + n0.n2.z * g1.y;
+            float K = __fmaf_rn(b0.l2, n0.n2.z, __fmaf_rn(b0.l1, n0.n1.z, __fmul_rn(b0.l0, n0.n0.z)));
+            float dKdx = __fmaf_rn(n0.n2.z, g0.z, __fmaf_rn(n0.n1.z, g0.y, __fmul_rn(n0.n0.z, g0.x)));
+            float dKdy = __fmaf_rn(n0.n2.z, g1.y, __fmaf_rn(n0.n1.z, g1.x, __fmul_rn(n0.n0.z, g0.w)));
             K = fmaxf(0.f, K);
-            diffx = sqrtf(2.f * K) * p.sqrtdt32;
-            driftx = dKdx * dt;
-            drifty = dKdy * dt;
+            diffx = __fmul_rn(sqrtf(__fmul_rn(2.f, K)), p.sqrtdt32);
+            driftx = __fmul_rn(dKdx, dt);
+            drifty = __fmul_rn(dKdy, dt);
         } else {
             diffx = p.diffx32;
         }
         float xix = 0.f, xiy = 0.f;
-        if (diffx != 0.f) pair32(rng, p.rng_method, z32, xix, xiy);
+        if (diffx != 0.f) pair32(rng, rng_method, z32, xix, xiy);
         if (euler) {
-            dx += driftx + diffx * xix;
-            dy += drifty + diffx * xiy;
+            dx = __fadd_rn(dx, __fmaf_rn(diffx, xix, driftx));
+            dy = __fadd_rn(dy, __fmaf_rn(diffx, xiy, drifty));
         } else {
-            xn += (double)(driftx + diffx * xix);
-            yn += (double)(drifty + diffx * xiy);
+            xn += (double)__fmaf_rn(diffx, xix, driftx);
+            yn += (double)__fmaf_rn(diffx, xiy, drifty);
         }
     }
     float4 xe = xs;   // SPLIT: the end position
@@ -417,10 +431,10 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
         s.lowerlayer[a] = 0;
         s.tag[i] = -2 - step_index;
         s.rng[i] = rng.state;
-        if (p.ncsec) count_sections(p, stats, 0., 0., 0., 0.);
+        if (ncsec) count_sections(p, stats, 0., 0., 0., 0.);
         return;
     }
-    if (p.ncsec) {
+    if (ncsec) {
         need64();
         count_sections(p, stats, x0.x, x0.y, xn, yn);
     }
@@ -449,7 +463,9 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
 // MINB: resident blocks of 256 per SM the register budget is set for.
-template <int MINB, bool SPLIT = false, bool EQ = false, bool TWO = false>
+// DC, RM: the form compiled for one run configuration (step_mixed_particle).
+template <int MINB, bool SPLIT = false, bool EQ = false, bool TWO = false, int DC = -1,
+          int RM = -1>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
                                                                 DevParams p, DevState s,
                                                                 WalkQueue wq, int aux,
@@ -468,8 +484,9 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     }
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_mixed_particle<SPLIT, EQ, TWO>(m, f, p, s, wq, aux, step_index, stats, err_word,
-                                            z32, load_mixed_in(s, i), i);
+        step_mixed_particle<SPLIT, EQ, TWO, DC, RM>(m, f, p, s, wq, DC >= 0 ? 0 : aux,
+                                                    step_index, stats, err_word, z32,
+                                                    load_mixed_in(s, i), i);
 }
 
 }  // namespace cg

@@ -43,6 +43,30 @@ def test_mixed_vs_fp64_oracle_keps():
     s.close()
 
 
+@pytest.mark.parametrize("diffusion_model", [0, 1, 2])
+@pytest.mark.parametrize("rng_method", [1, 2, 3])
+def test_mixed_configuration_forms_vs_fp64_oracle(diffusion_model, rng_method):
+    """The element-sorted Euler steps without per-call outputs run a kernel
+    compiled for the run's diffusion (none, constant, k-epsilon) and random
+    number method; each of the nine against the FP64 oracle, 60 steps of
+    20,000 particles in one call: ensemble variance and mean within the
+    mixed form's tolerance, per-particle trajectories close."""
+    from cylag_gb300.stats import displacement_report
+    case, p = keps_case(20_000)
+    p = dict(p, diffusion_model=diffusion_model, rng_method=rng_method,
+             horizontal_diffusivity=0.05)
+    meta = dict(params=p, nsteps=60, seed=7, pset={})
+    o = run_oracle(case, meta, nthreads=8)
+    s, ps = gpu_run(case, meta, precision="mixed")
+    act = (o.inactive == 0) & (ps.inactive == 0)
+    assert (o.inactive != ps.inactive).sum() <= 5
+    rep = displacement_report(case["position"], ps.position, o.pos, act)
+    assert max(rep["var_rel_err"]) <= VAR_TOL, rep
+    assert max(rep["mean_rel_err"]) <= VAR_TOL, rep
+    assert rep["rms_displacement_diff"] < 1e-2 * np.sqrt(max(rep["var_ref"])), rep
+    s.close()
+
+
 def test_mixed_vs_plain_same_decisions():
     """From identical positions one mixed step and one plain step give the
     same element indices when the displacement is identical (zero
