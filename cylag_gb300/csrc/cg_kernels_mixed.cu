@@ -18,19 +18,22 @@ static int wave_of(K kernel, int bs) {
 }
 
 // the split Euler step compiled for one configuration (diffusion class DC,
-// random number method RM), for the steps without per-call outputs
-template <int DC, int RM>
+// random number method RM): the steps without per-call outputs (aux 0), or
+// (TWO) those with them, on two working velocity arrays
+template <int DC, int RM, bool TWO>
 static void launch_split_conf(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
-                              const DevState& s, const WalkQueue& wq, int step_index, int* stats,
-                              uint32_t* err, int nb, int bs, cudaStream_t st) {
-    static const int w = wave_of(step_mixed2d_kernel<4, true, true, false, DC, RM>, bs);
-    step_mixed2d_kernel<4, true, true, false, DC, RM><<<nb < w ? nb : w, bs, 0, st>>>(
-        m, f, p, s, wq, 0, step_index, stats, err);
+                              const DevState& s, const WalkQueue& wq, int aux, int step_index,
+                              int* stats, uint32_t* err, int nb, int bs, cudaStream_t st) {
+    static const int w = wave_of(step_mixed2d_kernel<4, true, true, TWO, DC, RM>, bs);
+    step_mixed2d_kernel<4, true, true, TWO, DC, RM><<<nb < w ? nb : w, bs, 0, st>>>(
+        m, f, p, s, wq, aux, step_index, stats, err);
 }
 
 using SplitConfLaunch = void (*)(const DevMesh&, const DevFields<float>&, const DevParams&,
-                                 const DevState&, const WalkQueue&, int, int*, uint32_t*, int,
-                                 int, cudaStream_t);
+                                 const DevState&, const WalkQueue&, int, int, int*, uint32_t*,
+                                 int, int, cudaStream_t);
+#define CG_CONF_ROW(DC, TWO) \
+    { launch_split_conf<DC, 1, TWO>, launch_split_conf<DC, 2, TWO>, launch_split_conf<DC, 3, TWO> }
 
 void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
                        const DevState& s, const WalkQueue& wq, int aux, int step_index,
@@ -62,16 +65,17 @@ void launch_step_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p
         const bool eq = p.time_scheme == 1 && wq.e != nullptr;
         const bool split = (s.work & W_SPLIT) != 0;
         // the configuration forms: diffusion off / constant / k-epsilon x
-        // random number methods 1-3, steps without per-call outputs and
-        // without control sections
-        static const SplitConfLaunch conf[3][3] = {
-            {launch_split_conf<0, 1>, launch_split_conf<0, 2>, launch_split_conf<0, 3>},
-            {launch_split_conf<1, 1>, launch_split_conf<1, 2>, launch_split_conf<1, 3>},
-            {launch_split_conf<2, 1>, launch_split_conf<2, 2>, launch_split_conf<2, 3>}};
+        // random number methods 1-3, without and with per-call outputs, for
+        // runs without control sections
+        static const SplitConfLaunch conf[2][3][3] = {
+            {CG_CONF_ROW(0, false), CG_CONF_ROW(1, false), CG_CONF_ROW(2, false)},
+            {CG_CONF_ROW(0, true), CG_CONF_ROW(1, true), CG_CONF_ROW(2, true)}};
+#undef CG_CONF_ROW
         const int dc = p.diffmod == 0 ? 0 : (p.diffmod == 1 ? 1 : 2);
-        if (split && eq && aux == 0 && p.ncsec == 0 && p.rng_method >= 1 && p.rng_method <= 3 &&
+        if (split && eq && p.ncsec == 0 && p.rng_method >= 1 && p.rng_method <= 3 &&
             p.diffmod >= 0 && p.diffmod <= 3)
-            conf[dc][p.rng_method - 1](m, f, p, s, wq, step_index, stats, err, nb, bs, st);
+            conf[aux > 0][dc][p.rng_method - 1](m, f, p, s, wq, aux, step_index, stats, err, nb,
+                                                bs, st);
         else if (split && eq && aux == 0)
             step_mixed2d_kernel<4, true, true><<<grid(w4se), bs, 0, st>>>(m, f, p, s, wq, aux,
                                                                         step_index, stats, err);

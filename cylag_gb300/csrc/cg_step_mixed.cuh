@@ -223,10 +223,10 @@ __device__ __forceinline__ double2 double2_from_bits(float4 r) {
 // TWO: the working copies have two velocity arrays (W_VEL2); a step writes
 // its velocity alone and the write-back gives the fluid velocity seen and the
 // last velocity.  Only the steps with per-call outputs (aux >= 1) differ.
-// DC >= 0: a form compiled for one run configuration, for the steps without
-// per-call outputs (aux 0) and without control sections: DC the diffusion
-// class (0 none, 1 constant diffusivity, 2 k-epsilon: diffusion_model 2 or
-// 3), RM the random number method.  -1: read from the parameters.
+// DC >= 0: a form compiled for one run configuration, for runs without
+// control sections: DC the diffusion class (0 none, 1 constant diffusivity,
+// 2 k-epsilon: diffusion_model 2 or 3), RM the random number method.  -1:
+// read from the parameters.
 template <bool SPLIT, bool EQ = false, bool TWO = false, int DC = -1, int RM = -1>
 __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevFields<float>& f,
                                                     const DevParams& p, DevState& s,
@@ -463,7 +463,9 @@ __device__ __forceinline__ void step_mixed_particle(const DevMesh& m, const DevF
 
 // Persistent grid (one wave of resident blocks) striding over the particles.
 // MINB: resident blocks of 256 per SM the register budget is set for.
-// DC, RM: the form compiled for one run configuration (step_mixed_particle).
+// DC, RM: the form compiled for one run configuration (step_mixed_particle);
+// with DC >= 0 and not TWO, the form of the steps without per-call outputs
+// (aux 0).
 template <int MINB, bool SPLIT = false, bool EQ = false, bool TWO = false, int DC = -1,
           int RM = -1>
 __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevFields<float> f,
@@ -484,9 +486,10 @@ __global__ void __launch_bounds__(256, MINB) step_mixed2d_kernel(DevMesh m, DevF
     }
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        step_mixed_particle<SPLIT, EQ, TWO, DC, RM>(m, f, p, s, wq, DC >= 0 ? 0 : aux,
-                                                    step_index, stats, err_word, z32,
-                                                    load_mixed_in(s, i), i);
+        step_mixed_particle<SPLIT, EQ, TWO, DC, RM>(m, f, p, s, wq,
+                                                    (DC >= 0 && !TWO) ? 0 : aux, step_index,
+                                                    stats, err_word, z32, load_mixed_in(s, i),
+                                                    i);
 }
 
 }  // namespace cg
