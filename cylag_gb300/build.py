@@ -47,6 +47,8 @@ UNITS = {
     "cg_sort.cu": [],
     "cg_snapshot.cpp": ["-Xcompiler", "-pthread"],
 }
+# cg_split3_form.cu: one object per form of the split 3D LSM3 step
+FORM_UNITS = [("cg_split3_form.cu", f"cg_split3_form_{k}", [f"-DCG_FORM={k}"]) for k in range(16)]
 
 
 def nvcc() -> str:
@@ -74,8 +76,8 @@ def build(force: bool = False, verbose: bool = False, debug_bounds: bool = False
     suffix = "_debug.o" if debug_bounds else ".o"
 
     def one(item):
-        src, extra = item
-        obj = OUT_DIR / (Path(src).stem + suffix)
+        src, stem, extra = item
+        obj = OUT_DIR / (stem + suffix)
         cmd = [exe, *ARCH, *COMMON, *flags, *extra, "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -84,8 +86,9 @@ def build(force: bool = False, verbose: bool = False, debug_bounds: bool = False
             print(r.stdout, r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 1)) as ex:
-        objs = list(ex.map(one, UNITS.items()))
+    units = [(src, Path(src).stem, extra) for src, extra in UNITS.items()] + FORM_UNITS
+    with ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(one, units))
     tmp = lib.with_suffix(f".so.{os.getpid()}")
     cmd = [exe, *ARCH, "-shared", *map(str, objs), "-o", str(tmp), "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -32,15 +32,17 @@ __device__ __forceinline__ double drag_almedeij(double Re) {
     return pow(1. / (1. / (phi1 + phi2) + 1. / phi3) + phi4, 1. / 10.);
 }
 
-template <typename R>
+// DRAG >= 0: the drag law compiled in (the run's drag_coefficient_model)
+template <typename R, int DRAG = -1>
 __device__ __forceinline__ R drag_coefficient(const DevParams& p, R U, R dp) {
+    const int dm = DRAG >= 0 ? DRAG : p.drag_model;
     R Re = fmax(R(EPSILON), U * dp / R(NU0));
-    if (p.drag_model == 0) return par<R>(p.drag_coef, p.drag_coef32);
-    if (p.drag_model == 1) {
+    if (dm == 0) return par<R>(p.drag_coef, p.drag_coef32);
+    if (dm == 1) {
         if (Re <= R(1000.)) return (R(24.) / Re) * (R(1.) + R(0.15) * cpow_re(Re, R(0.687)));
         return R(0.44);
     }
-    if (p.drag_model == 2) return R(drag_almedeij((double)Re));
+    if (dm == 2) return R(drag_almedeij((double)Re));
     return R(0.44);
 }
 
@@ -925,9 +927,9 @@ __device__ __forceinline__ void lsm3_cholesky_clipped(const R* q, R* lower) {
 }
 
 // drag rate ((a1c*(1.5/dp))*unorm)*Cd (update_state_lsm3.pyx:728)
-template <typename R>
+template <typename R, int DRAG = -1>
 __device__ __forceinline__ R lsm3_a1(const DevParams& p, R dp, R unorm) {
-    R Cd = drag_coefficient(p, unorm, dp);
+    R Cd = drag_coefficient<R, DRAG>(p, unorm, dp);
     return par<R>(p.a1c, p.a1c32) * (R(1.5) / dp) * unorm * Cd;
 }
 
@@ -996,19 +998,23 @@ __device__ __forceinline__ void euler_maruyama_lsm3(Particle<DIM, FT>& q, double
 // height z0 (in q.ll), the particle velocity up and fluid velocity seen us
 // (both updated) and the displacement dx.  False, with ERR_NONFINITE in
 // q.err and nothing set, when a coefficient or factor is not finite.
-template <int DIM, typename FT>
+// DRAG, KEPS, EDGE2, AM >= 0: the run's drag law, k-epsilon diffusion
+// (diffusion model 2 or 3) or not, lsm3_edge_opt 2 or not and added mass or
+// not compiled in (-1: from the parameters).
+template <int DIM, typename FT, int DRAG = -1, int KEPS = -1, int EDGE2 = -1, int AM = -1>
 __device__ __forceinline__ bool di_lsm3_32(Particle<DIM, FT>& q,
                                            const typename Particle<DIM, FT>::P1f& P0, float z0,
                                            float dp, float* up, float* us, float* dx) {
     const DevParams& p = q.p;
-    const int diffmod = p.diffmod, edge_opt = p.edge_opt;
+    // (a form without k-epsilon diffusion: only "not 2 or 3" matters)
+    const int diffmod = KEPS == 0 ? 1 : p.diffmod, edge_opt = EDGE2 == 1 ? 2 : p.edge_opt;
     float ux, uy, uz, ax, ay, az, ep = 0.f, tml_ke = 0.f;
     mean_fields32(q, P0, q.ll, z0, true, ux, uy, uz, ax, ay, az);
     if (diffmod == 2 || diffmod == 3) tml_ke = keps_tml32p(q, P0, q.ll, z0, ep);
     const float sx = us[0] - up[0], sy = us[1] - up[1], sz = DIM == 3 ? us[2] - up[2] : 0.f;
     const float unorm = fmax(float(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
-    const float a1 = lsm3_a1<float>(p, dp, unorm);
-    const float a2 = p.added_mass ? p.a2c32 : 0.f;
+    const float a1 = lsm3_a1<float, DRAG>(p, dp, unorm);
+    const float a2 = AM == 0 ? 0.f : (AM == 1 || p.added_mass ? p.a2c32 : 0.f);
     float tl_h = p.tl_h32, tl_v = p.tl_v32, sigma_h, sigma_v = 0.f;
     if (diffmod == 2 || diffmod == 3) {
         tl_h = fmax(float(EPSILON_LSM3), tml_ke);

@@ -10,6 +10,41 @@
 
 namespace cg {
 
+// The split 3D step (W_SPLIT3): the LSM3 form compiled for the run's
+// configuration when there is one (launch_lsm3_form), else the general
+// kernels (persistent grid).
+static void launch_split3_kernel(const DevMesh& m, const DevFields<float>& f,
+                                 const DevParams& p, const DevState& s, int aux, int step_index,
+                                 int* stats, uint32_t* err, cudaStream_t st) {
+    using Form = void (*)(const DevMesh&, const DevFields<float>&, const DevParams&,
+                          const DevState&, int, int, int*, uint32_t*, cudaStream_t);
+    static const Form forms[16] = {
+        launch_lsm3_form<0>,  launch_lsm3_form<1>,  launch_lsm3_form<2>,  launch_lsm3_form<3>,
+        launch_lsm3_form<4>,  launch_lsm3_form<5>,  launch_lsm3_form<6>,  launch_lsm3_form<7>,
+        launch_lsm3_form<8>,  launch_lsm3_form<9>,  launch_lsm3_form<10>, launch_lsm3_form<11>,
+        launch_lsm3_form<12>, launch_lsm3_form<13>, launch_lsm3_form<14>, launch_lsm3_form<15>};
+    if (p.model == 3 && p.ncsec == 0 && (p.drag_model == 0 || p.drag_model == 1)) {
+        const int keps = (p.diffmod == 2 || p.diffmod == 3) ? 1 : 0;
+        const int k = 8 * p.drag_model + 4 * keps + 2 * (p.edge_opt == 2 ? 1 : 0) +
+                      (p.added_mass ? 1 : 0);
+        forms[k](m, f, p, s, aux, step_index, stats, err, st);
+        return;
+    }
+    const int bs = 256;
+    const int need = (s.n + bs - 1) / bs;
+    if (need == 0) return;
+    static int wave2 = 0, wave3 = 0;
+    if (p.model == 2) {
+        if (!wave2) wave2 = resident_blocks(step_split3_kernel<2>, bs);
+        step_split3_kernel<2><<<need < wave2 ? need : wave2, bs, 0, st>>>(m, f, p, s, aux,
+                                                                         step_index, stats, err);
+    } else {
+        if (!wave3) wave3 = resident_blocks(step_split3_kernel<3>, bs);
+        step_split3_kernel<3><<<need < wave3 ? need : wave3, bs, 0, st>>>(m, f, p, s, aux,
+                                                                         step_index, stats, err);
+    }
+}
+
 void launch_lsm23_mixed(const DevMesh& m, const FieldView& fv, const DevParams& p,
                         const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
                         cudaStream_t st) {

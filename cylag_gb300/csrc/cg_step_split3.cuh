@@ -23,12 +23,15 @@
 
 namespace cg {
 
-template <int MODEL>
+// DRAG >= 0 (LSM3): the form compiled for one run configuration, without
+// control sections (DRAG, KEPS, EDGE2, AM: di_lsm3_32)
+template <int MODEL, int DRAG = -1, int KEPS = -1, int EDGE2 = -1, int AM = -1>
 __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevFields<float>& f,
                                                 const DevParams& p, DevState& s, int aux,
                                                 int step_index, int* __restrict__ stats,
                                                 uint32_t* __restrict__ err_word,
                                                 const ZigTables& zt, const Zig32& z32, int i) {
+    const int ncsec = DRAG >= 0 ? 0 : p.ncsec;
     const int tri0 = s.tri[i];
     if (tri0 < 0) return;   // inactive (-1) or awaiting initialization (-2)
     // every per-particle array is a working copy (W_VEL, W_FVS for LSM3,
@@ -60,7 +63,8 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
     if constexpr (MODEL == 2)
         di_lsm2_32(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, p.diffmod, p.nuopt, up, us, dx);
     else if (p.dt != 0.)   // update_state_lsm3.pyx: no update for a zero step
-        di_lsm3_32(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, up, us, dx);
+        di_lsm3_32<3, float, DRAG, KEPS, EDGE2, AM>(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, up,
+                                                    us, dx);
     // end position as FP32 pairs
     float2 ex = sx, ey = sy, ez = sz;
     split_add1(ex.x, ex.y, dx[0]);
@@ -143,7 +147,7 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
         s.lowerlayer[i] = 0;
         s.tag[i] = -2 - step_index;
         s.rng[i] = q.rng.state;
-        if (p.ncsec) count_sections(p, stats, 0., 0., 0., 0.);
+        if (ncsec) count_sections(p, stats, 0., 0., 0., 0.);
         return;
     }
     P[0] = ex;
@@ -167,14 +171,14 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
 #pragma unroll
         for (int d = 0; d < 3; ++d) fvs_st(s, 3 * (size_t)i + d, (double)us[d]);
     }
-    if (p.ncsec) count_sections(p, stats, join1(sx), join1(sy), join1(ex), join1(ey));
+    if (ncsec) count_sections(p, stats, join1(sx), join1(sy), join1(ex), join1(ey));
 }
 
 // One step of every particle of a W_SPLIT3 run (persistent grid), MODEL 2 or
 // 3: two resident blocks of 256 per SM for LSM2, as the generic mixed
 // LSM2/LSM3 kernels; three for LSM3 (85 registers, spilling; 2% faster
 // than two on the LSM3 workload, where LSM2 is 8% slower with three).
-template <int MODEL>
+template <int MODEL, int DRAG = -1, int KEPS = -1, int EDGE2 = -1, int AM = -1>
 __global__ void __launch_bounds__(256, MODEL == 3 ? 3 : 2) step_split3_kernel(DevMesh m, DevFields<float> f,
                                                              DevParams p, DevState s, int aux,
                                                              int step_index,
@@ -189,25 +193,20 @@ __global__ void __launch_bounds__(256, MODEL == 3 ? 3 : 2) step_split3_kernel(De
     }
     load_zig(zt);   // ends with __syncthreads
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        split3_particle<MODEL>(m, f, p, s, aux, step_index, stats, err_word, zt, z32, i);
+        split3_particle<MODEL, DRAG, KEPS, EDGE2, AM>(m, f, p, s, aux, step_index, stats,
+                                                      err_word, zt, z32, i);
 }
 
-inline void launch_split3_kernel(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
-                                 const DevState& s, int aux, int step_index, int* stats,
-                                 uint32_t* err, cudaStream_t st) {
-    const int bs = 256;
-    const int need = (s.n + bs - 1) / bs;
-    if (need == 0) return;
-    static int wave2 = 0, wave3 = 0;
-    if (p.model == 2) {
-        if (!wave2) wave2 = resident_blocks(step_split3_kernel<2>, bs);
-        step_split3_kernel<2><<<need < wave2 ? need : wave2, bs, 0, st>>>(m, f, p, s, aux,
-                                                                         step_index, stats, err);
-    } else {
-        if (!wave3) wave3 = resident_blocks(step_split3_kernel<3>, bs);
-        step_split3_kernel<3><<<need < wave3 ? need : wave3, bs, 0, st>>>(m, f, p, s, aux,
-                                                                         step_index, stats, err);
-    }
-}
+// The LSM3 forms compiled for one run configuration: the drag law
+// (drag_coefficient_model 0 or 1), k-epsilon diffusion (diffusion model 2 or
+// 3) or not, lsm3_edge_opt 2 (clipped coefficients) or not, added mass or
+// not, no control sections.  Form K = 8 DRAG + 4 KEPS + 2 EDGE2 + AM is
+// launched by launch_lsm3_form<K>, defined in cg_split3_form.cu, which the
+// build compiles once per form: alone in its unit, the form's kernel gets
+// the inlining decisions of a single call site.
+template <int K>
+void launch_lsm3_form(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
+                      const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
+                      cudaStream_t st);
 
 }  // namespace cg
