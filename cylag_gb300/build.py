@@ -47,8 +47,8 @@ UNITS = {
     "cg_sort.cu": [],
     "cg_snapshot.cpp": ["-Xcompiler", "-pthread"],
 }
-# cg_split3_form.cu: one object per form of the split 3D LSM3 step
-FORM_UNITS = [("cg_split3_form.cu", f"cg_split3_form_{k}", [f"-DCG_FORM={k}"]) for k in range(16)]
+# cg_split3_form.cu: one object per form of the split 3D LSM3 and LSM2 steps
+FORM_UNITS = [("cg_split3_form.cu", f"cg_split3_form_{k}", [f"-DCG_FORM={k}"]) for k in range(32)]
 
 
 def nvcc() -> str:

@@ -373,17 +373,20 @@ __device__ __forceinline__ bool lsm2_direct_coefficients(R a1, R dt, Lsm2Coef<R>
 // and height z0 (in q.ll), the particle velocity up (updated), the fluid
 // velocity seen us (set) and the displacement dx.  False, with ERR_NONFINITE
 // in q.err and nothing set, when the coefficients are not finite.
-template <int DIM, typename FT>
+// DRAG, AM >= 0: the run's drag law and added mass compiled in (-1: from
+// the parameters).
+template <int DIM, typename FT, int DRAG = -1, int AM = -1>
 __device__ __forceinline__ bool di_lsm2_32(Particle<DIM, FT>& q,
                                            const typename Particle<DIM, FT>::P1f& P0, float z0,
                                            float dp, int diffmod, int nuopt, float* up, float* us,
                                            float* dx) {
     const DevParams& p = q.p;
     float ux, uy, uz, ax, ay, az;
-    mean_fields32(q, P0, q.ll, z0, p.added_mass, ux, uy, uz, ax, ay, az);
+    mean_fields32(q, P0, q.ll, z0, AM >= 0 ? AM != 0 : p.added_mass, ux, uy, uz, ax, ay, az);
     const float sx = ux - up[0], sy = uy - up[1], sz = DIM == 3 ? uz - up[2] : 0.f;
     const float unorm = fmax(float(EPSILON_LSM2), sqrt(sx * sx + sy * sy + sz * sz));
-    const float a1 = p.a1c32 * (1.5f / dp) * drag_coefficient<float>(p, unorm, dp) * unorm;
+    const float a1 =
+        p.a1c32 * (1.5f / dp) * drag_coefficient<float, DRAG>(p, unorm, dp) * unorm;
     const float rdt = p.dt32;
     Lsm2Coef<float> c;
     if (!lsm2_direct_coefficients<float>(a1, rdt, c)) { q.err |= ERR_NONFINITE; return false; }

@@ -10,25 +10,33 @@
 
 namespace cg {
 
-// The split 3D step (W_SPLIT3): the LSM3 form compiled for the run's
-// configuration when there is one (launch_lsm3_form), else the general
+// The split 3D step (W_SPLIT3): the form compiled for the run's
+// configuration when there is one (launch_split3_form), else the general
 // kernels (persistent grid).
 static void launch_split3_kernel(const DevMesh& m, const DevFields<float>& f,
                                  const DevParams& p, const DevState& s, int aux, int step_index,
                                  int* stats, uint32_t* err, cudaStream_t st) {
     using Form = void (*)(const DevMesh&, const DevFields<float>&, const DevParams&,
                           const DevState&, int, int, int*, uint32_t*, cudaStream_t);
-    static const Form forms[16] = {
-        launch_lsm3_form<0>,  launch_lsm3_form<1>,  launch_lsm3_form<2>,  launch_lsm3_form<3>,
-        launch_lsm3_form<4>,  launch_lsm3_form<5>,  launch_lsm3_form<6>,  launch_lsm3_form<7>,
-        launch_lsm3_form<8>,  launch_lsm3_form<9>,  launch_lsm3_form<10>, launch_lsm3_form<11>,
-        launch_lsm3_form<12>, launch_lsm3_form<13>, launch_lsm3_form<14>, launch_lsm3_form<15>};
-    if (p.model == 3 && p.ncsec == 0 && (p.drag_model == 0 || p.drag_model == 1)) {
-        const int keps = (p.diffmod == 2 || p.diffmod == 3) ? 1 : 0;
-        const int k = 8 * p.drag_model + 4 * keps + 2 * (p.edge_opt == 2 ? 1 : 0) +
-                      (p.added_mass ? 1 : 0);
-        forms[k](m, f, p, s, aux, step_index, stats, err, st);
-        return;
+#define CG_FORMS8(B)                                                                   \
+    launch_split3_form<B>, launch_split3_form<B + 1>, launch_split3_form<B + 2>,           \
+        launch_split3_form<B + 3>, launch_split3_form<B + 4>, launch_split3_form<B + 5>,   \
+        launch_split3_form<B + 6>, launch_split3_form<B + 7>
+    static const Form forms[32] = {CG_FORMS8(0), CG_FORMS8(8), CG_FORMS8(16), CG_FORMS8(24)};
+#undef CG_FORMS8
+    if (p.ncsec == 0 && (p.drag_model == 0 || p.drag_model == 1)) {
+        const int am = p.added_mass ? 1 : 0;
+        if (p.model == 3) {
+            const int keps = (p.diffmod == 2 || p.diffmod == 3) ? 1 : 0;
+            forms[8 * p.drag_model + 4 * keps + 2 * (p.edge_opt == 2 ? 1 : 0) + am](
+                m, f, p, s, aux, step_index, stats, err, st);
+            return;
+        }
+        if (p.model == 2 && p.diffmod >= 0 && p.diffmod <= 3) {
+            forms[16 + 8 * p.drag_model + 2 * p.diffmod + am](m, f, p, s, aux, step_index, stats,
+                                                              err, st);
+            return;
+        }
     }
     const int bs = 256;
     const int need = (s.n + bs - 1) / bs;

@@ -23,9 +23,11 @@
 
 namespace cg {
 
-// DRAG >= 0 (LSM3): the form compiled for one run configuration, without
-// control sections (DRAG, KEPS, EDGE2, AM: di_lsm3_32)
-template <int MODEL, int DRAG = -1, int KEPS = -1, int EDGE2 = -1, int AM = -1>
+// DRAG >= 0: the form compiled for one run configuration, without control
+// sections: DRAG the drag law, AM added mass or not; DIFF: for LSM3
+// k-epsilon diffusion or not (KEPS of di_lsm3_32, with EDGE2), for LSM2 the
+// diffusion model (0-3).
+template <int MODEL, int DRAG = -1, int DIFF = -1, int EDGE2 = -1, int AM = -1>
 __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevFields<float>& f,
                                                 const DevParams& p, DevState& s, int aux,
                                                 int step_index, int* __restrict__ stats,
@@ -61,9 +63,10 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
     const Bary b0 = bary32_off(t0, r0.x, r0.y);
     float dx[3] = {0.f, 0.f, 0.f};
     if constexpr (MODEL == 2)
-        di_lsm2_32(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, p.diffmod, p.nuopt, up, us, dx);
+        di_lsm2_32<3, float, DRAG, AM>(q, q.p1f_of(t0, b0), sz.x + sz.y, dp,
+                                       DIFF >= 0 ? DIFF : p.diffmod, p.nuopt, up, us, dx);
     else if (p.dt != 0.)   // update_state_lsm3.pyx: no update for a zero step
-        di_lsm3_32<3, float, DRAG, KEPS, EDGE2, AM>(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, up,
+        di_lsm3_32<3, float, DRAG, DIFF, EDGE2, AM>(q, q.p1f_of(t0, b0), sz.x + sz.y, dp, up,
                                                     us, dx);
     // end position as FP32 pairs
     float2 ex = sx, ey = sy, ez = sz;
@@ -178,7 +181,7 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
 // 3: two resident blocks of 256 per SM for LSM2, as the generic mixed
 // LSM2/LSM3 kernels; three for LSM3 (85 registers, spilling; 2% faster
 // than two on the LSM3 workload, where LSM2 is 8% slower with three).
-template <int MODEL, int DRAG = -1, int KEPS = -1, int EDGE2 = -1, int AM = -1>
+template <int MODEL, int DRAG = -1, int DIFF = -1, int EDGE2 = -1, int AM = -1>
 __global__ void __launch_bounds__(256, MODEL == 3 ? 3 : 2) step_split3_kernel(DevMesh m, DevFields<float> f,
                                                              DevParams p, DevState s, int aux,
                                                              int step_index,
@@ -193,19 +196,20 @@ __global__ void __launch_bounds__(256, MODEL == 3 ? 3 : 2) step_split3_kernel(De
     }
     load_zig(zt);   // ends with __syncthreads
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n; i += gridDim.x * blockDim.x)
-        split3_particle<MODEL, DRAG, KEPS, EDGE2, AM>(m, f, p, s, aux, step_index, stats,
+        split3_particle<MODEL, DRAG, DIFF, EDGE2, AM>(m, f, p, s, aux, step_index, stats,
                                                       err_word, zt, z32, i);
 }
 
-// The LSM3 forms compiled for one run configuration: the drag law
-// (drag_coefficient_model 0 or 1), k-epsilon diffusion (diffusion model 2 or
-// 3) or not, lsm3_edge_opt 2 (clipped coefficients) or not, added mass or
-// not, no control sections.  Form K = 8 DRAG + 4 KEPS + 2 EDGE2 + AM is
-// launched by launch_lsm3_form<K>, defined in cg_split3_form.cu, which the
-// build compiles once per form: alone in its unit, the form's kernel gets
-// the inlining decisions of a single call site.
+// The forms compiled for one run configuration, for runs without control
+// sections: the drag law (drag_coefficient_model 0 or 1) and added mass or
+// not, and for LSM3 k-epsilon diffusion (diffusion model 2 or 3) or not and
+// lsm3_edge_opt 2 (clipped coefficients) or not: form K = 8 DRAG + 4 KEPS +
+// 2 EDGE2 + AM (0-15); for LSM2 the diffusion model DM: form K = 16 + 8 DRAG
+// + 2 DM + AM (16-31).  launch_split3_form<K> is defined in
+// cg_split3_form.cu, which the build compiles once per form: alone in its
+// unit, the form's kernel gets the inlining decisions of a single call site.
 template <int K>
-void launch_lsm3_form(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
+void launch_split3_form(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
                       const DevState& s, int aux, int step_index, int* stats, uint32_t* err,
                       cudaStream_t st);
 
