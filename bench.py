@@ -210,17 +210,20 @@ def bytes_per_particle_step(workload, precision):
 # DRAM bytes per particle-step of one step kernel launch, from ncu captures
 # of the same kernel on smaller particle counts (element-sorted; the traffic
 # grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 55.9, ("lsm1_2d", "fp64"): 147.0,
-                                   ("lsm2_3d", "mixed"): 153.6, ("lsm3_3d", "mixed"): 160.9}
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 54.9, ("lsm1_2d", "fp64"): 147.0,
+                                   ("lsm2_3d", "mixed"): 153.4, ("lsm3_3d", "mixed"): 148.9}
 NCU_TRAFFIC_SOURCE = {
-    ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel at "
-                          "4e6 particles, scaled to the launch",
+    ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel's "
+                          "form for the run's configuration at 4e6 particles, scaled to the "
+                          "launch",
     ("lsm1_2d", "fp64"): "ncu dram bytes (read+write) of the element-sorted step and walk "
                          "kernels at 4e6 particles, scaled to the launch",
-    ("lsm2_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel at "
-                          "2e6 particles, scaled to the launch",
-    ("lsm3_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel at "
-                          "2e6 particles, scaled to the launch"}
+    ("lsm2_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel's "
+                          "form for the run's configuration at 2e6 particles, scaled to the "
+                          "launch",
+    ("lsm3_3d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel's "
+                          "form for the run's configuration at 2e6 particles, scaled to the "
+                          "launch"}
 
 
 def field_set_of(c):
