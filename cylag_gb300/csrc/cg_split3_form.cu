@@ -7,7 +7,9 @@
 // and the code of the other branches (the Almedeij drag law in FP64, the
 // k-epsilon time scale, the added-mass acceleration, the other Cholesky
 // factorization), which keeps the kernel's instruction footprint and
-// register use down.  A run steps every step with the same form.
+// register use down.  A run steps every step with the same form.  (The LSM2
+// forms of diffusion model 0 complete the index range; such runs do not
+// take the split kernels, whose LSM2 runs have velocity diffusion.)
 #include "cg_internal.h"
 #include "cg_step_split3.cuh"
 
