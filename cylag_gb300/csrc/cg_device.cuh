@@ -1077,14 +1077,21 @@ __device__ inline void path_walk_mixed(const DevMesh& m, int k, double p0x, doub
     WalkRec t = load_walkrec(m, k);
     for (int niter = 0; niter <= NITER_MAX; ++niter) {
         bool intersects = false;
+        // the element's three vertices relative to the segment's start, once
+        // per element (each edge takes two of them; the FP64 subtraction and
+        // the conversion are the walk's FP64-pipe work)
+        const float2 va = make_float2((float)(t.a.x - p0x), (float)(t.a.y - p0y));
+        const float2 vb = make_float2((float)(t.b.x - p0x), (float)(t.b.y - p0y));
+        const float2 vc = make_float2((float)(t.c.x - p0x), (float)(t.c.y - p0y));
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             int j, kn;
             double2 a, b;
             rec_edge(t, i, k, j, a, b, kn);
             if (j == intersected_edge) continue;
-            const float2 fa = make_float2((float)(a.x - p0x), (float)(a.y - p0y));
-            const float2 fb = make_float2((float)(b.x - p0x), (float)(b.y - p0y));
+            const int la = (t.order >> (4 * i)) & 3, lb = (t.order >> (4 * i + 2)) & 3;
+            const float2 fa = la == 0 ? va : (la == 1 ? vb : vc);
+            const float2 fb = lb == 0 ? va : (lb == 1 ? vb : vc);
             if (intersec2d_filtered(p1, fa, fb, p0x, p0y, x, y, a, b)) {
                 intersects = true;
                 if (kn == -1) { bnd = j; return; }
