@@ -210,7 +210,7 @@ def bytes_per_particle_step(workload, precision):
 # DRAM bytes per particle-step of one step kernel launch, from ncu captures
 # of the same kernel on smaller particle counts (element-sorted; the traffic
 # grows with the particles processed)
-NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 54.9, ("lsm1_2d", "fp64"): 147.0,
+NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 55.8, ("lsm1_2d", "fp64"): 147.0,
                                    ("lsm2_3d", "mixed"): 153.4, ("lsm3_3d", "mixed"): 148.9}
 NCU_TRAFFIC_SOURCE = {
     ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel's "

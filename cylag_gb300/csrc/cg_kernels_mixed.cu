@@ -18,14 +18,16 @@ static int wave_of(K kernel, int bs) {
 }
 
 // the split Euler step compiled for one configuration (diffusion class DC,
-// random number method RM): the steps without per-call outputs (aux 0), or
-// (TWO) those with them, on two working velocity arrays
+// random number method RM): the steps without per-call outputs (aux 0), five
+// blocks of 256 per SM (48 registers), or (TWO) those with them, on two
+// working velocity arrays, four blocks (64 registers)
 template <int DC, int RM, bool TWO>
 static void launch_split_conf(const DevMesh& m, const DevFields<float>& f, const DevParams& p,
                               const DevState& s, const WalkQueue& wq, int aux, int step_index,
                               int* stats, uint32_t* err, int nb, int bs, cudaStream_t st) {
-    static const int w = wave_of(step_mixed2d_kernel<4, true, true, TWO, DC, RM>, bs);
-    step_mixed2d_kernel<4, true, true, TWO, DC, RM><<<nb < w ? nb : w, bs, 0, st>>>(
+    constexpr int MINB = TWO ? 4 : 5;
+    static const int w = wave_of(step_mixed2d_kernel<MINB, true, true, TWO, DC, RM>, bs);
+    step_mixed2d_kernel<MINB, true, true, TWO, DC, RM><<<nb < w ? nb : w, bs, 0, st>>>(
         m, f, p, s, wq, aux, step_index, stats, err);
 }
 
