@@ -180,9 +180,11 @@ __device__ __forceinline__ void split3_particle(const DevMesh& m, const DevField
 // One step of every particle of a W_SPLIT3 run (persistent grid), MODEL 2 or
 // 3: two resident blocks of 256 per SM for LSM2, as the generic mixed
 // LSM2/LSM3 kernels; three for LSM3 (85 registers, spilling; 2% faster
-// than two on the LSM3 workload, where LSM2 is 8% slower with three).
+// than two on the LSM3 workload, where LSM2 is 8% slower with three), four
+// for the LSM3 configuration forms (64 registers, spilling; 3% faster than
+// three).
 template <int MODEL, int DRAG = -1, int DIFF = -1, int EDGE2 = -1, int AM = -1>
-__global__ void __launch_bounds__(256, MODEL == 3 ? 3 : 2) step_split3_kernel(DevMesh m, DevFields<float> f,
+__global__ void __launch_bounds__(256, MODEL == 3 ? (DRAG >= 0 ? 4 : 3) : 2) step_split3_kernel(DevMesh m, DevFields<float> f,
                                                              DevParams p, DevState s, int aux,
                                                              int step_index,
                                                              int* __restrict__ stats,
