@@ -211,7 +211,7 @@ def bytes_per_particle_step(workload, precision):
 # of the same kernel on smaller particle counts (element-sorted; the traffic
 # grows with the particles processed)
 NCU_TRAFFIC_B_PER_PARTICLE_STEP = {("lsm1_2d", "mixed"): 55.8, ("lsm1_2d", "fp64"): 147.0,
-                                   ("lsm2_3d", "mixed"): 153.4, ("lsm3_3d", "mixed"): 148.9}
+                                   ("lsm2_3d", "mixed"): 153.4, ("lsm3_3d", "mixed"): 185.3}
 NCU_TRAFFIC_SOURCE = {
     ("lsm1_2d", "mixed"): "ncu dram bytes (read+write) of the element-sorted step kernel's "
                           "form for the run's configuration at 4e6 particles, scaled to the "
